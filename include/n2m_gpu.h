@@ -1,0 +1,127 @@
+/* n2m_gpu.h — C ABI of the GB300 volume->mesh path (libn2m_gpu.so).
+ *
+ * Two layers:
+ *  1. Drop-in entry points with the reference's exact signatures and semantics
+ *     (same names, argument meaning, 0/1 return codes, malloc'd outputs the
+ *     caller frees with free()).  Link libn2m_gpu.so instead of meshify.o /
+ *     quadric.o / MarchingCubes.o / bwlabel.o / isolevel.o.
+ *  2. n2m_* entry points: explicit status codes, a context (CUDA stream +
+ *     workspace), device-resident variants, the adjoint and the batched atlas.
+ *
+ * All compute runs on the GPU; there is no CPU fallback.  If no CUDA device is
+ * usable every entry point fails with N2M_ERR_NO_DEVICE (drop-in calls return
+ * EXIT_FAILURE and print the reason).
+ */
+#ifndef N2M_GPU_H
+#define N2M_GPU_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef MESHIFY_TYPES_H
+#define MESHIFY_TYPES_H
+/* Same layout as the reference's mesh types (src/meshtypes.h:4-10). */
+typedef struct { double x, y, z; } vec3d;
+typedef struct { int x, y, z; } vec3i;
+#endif
+
+typedef enum {
+    N2M_OK = 0,
+    N2M_ERR_NO_DEVICE = 1,      /* no usable CUDA device / extension not loaded */
+    N2M_ERR_CUDA = 2,           /* a CUDA runtime call failed (see n2m_last_error) */
+    N2M_ERR_OOM = 3,            /* device or host allocation failed */
+    N2M_ERR_BAD_ARGS = 4,       /* null pointer, bad dims, unsupported option */
+    N2M_ERR_NO_VARIABILITY = 5, /* min == max after pre-smooth (src/meshify.c:312) */
+    N2M_ERR_EMPTY = 6,          /* marching cubes found < 3 vertices or no triangle */
+    N2M_ERR_NONFINITE = 7,      /* NaN/Inf in the volume entering the mesher */
+    N2M_ERR_TOO_LARGE = 8,      /* counts exceed the 32-bit index range of vec3i */
+    N2M_ERR_TIMEOUT = 9,        /* a bounded device-side wait gave up */
+    N2M_ERR_INTERNAL = 10
+} n2m_status;
+
+/* cube variants: the reference selects these with -o and the
+ * USE_CLASSIC_CUBES build flag (src/meshify.c:25-29). */
+typedef enum { N2M_CUBES_MC33 = 0, N2M_CUBES_CLASSIC_TABLE = 1, N2M_CUBES_OLDCUBES = 2 } n2m_cubes;
+
+typedef struct n2m_context n2m_context;
+
+typedef struct {
+    int cubes;          /* n2m_cubes */
+    float isolevel;
+    bool pre_smooth;    /* -p */
+    bool only_largest;  /* -l */
+    bool fill_bubbles;  /* -b */
+    int post_smooth;    /* -s: HC iterations (alpha 0.1, beta 0.5, edges locked) */
+    bool verbose;       /* per-stage CUDA-event timings on stdout */
+} n2m_options;
+
+/* Per-call report (optional out-parameter). */
+typedef struct {
+    float isolevel_used;     /* after the out-of-range fallback */
+    float vmin, vmax;        /* range of the (smoothed) volume */
+    int lo[3], hi[3];        /* padded bounding box handed to marching cubes */
+    int64_t nvert_raw, ntri_raw;  /* before weld / degenerate removal */
+    int64_t nvert, ntri;     /* final */
+    int welded;              /* vertices merged by the weld */
+    int degenerate;          /* triangles removed */
+    float ms_total;          /* device time of the call (CUDA events) */
+} n2m_report;
+
+/* ---- context ------------------------------------------------------------ */
+/* A context owns a CUDA stream and a grow-only device workspace.  Contexts are
+ * independent; one context must not be used by two threads at once.  The
+ * drop-in entry points use a per-thread default context. */
+n2m_status n2m_context_create(n2m_context **ctx, int device);
+void n2m_context_destroy(n2m_context *ctx);
+void *n2m_context_stream(n2m_context *ctx);          /* cudaStream_t */
+const char *n2m_last_error(void);                    /* per-thread message */
+const char *n2m_status_string(int status);
+int n2m_device_count(void);
+
+/* ---- drop-in entry points ------------------------------------------------ */
+/* replaces meshify() (src/meshify.h:9).  originalMC: 0 = Lewiner MC33,
+ * 1 = classic case table in the Lewiner framework.  `img` is read only (the
+ * reference smooths it in place; no caller reads it afterwards,
+ * src/nii2mesh.c:573,589).  *t and *p are malloc'd; free() them. */
+int meshify(float *img, short dim[3], int originalMC, float isolevel, vec3i **t, vec3d **p, int *nt, int *np,
+            bool preSmooth, bool onlyLargest, bool fillBubbles, bool verbose);
+/* replaces laplacian_smoothHC() (src/quadric.h:7); verts updated in place. */
+void laplacian_smoothHC(vec3d *verts, vec3i *tris, int nvert, int ntri, double alpha, double beta, int iter,
+                        bool lockEdges);
+/* replaces marchingCubes() (src/MarchingCubes.h:19 / src/oldcubes.h:9). */
+int marchingCubes(float *img, short dim[3], int lo[3], int hi[3], int originalMC, float isolevel, vec3d **vs,
+                  vec3i **ts, int *nv, int *nt);
+/* replaces bwlabel() (src/bwlabel.h:10) for conn 6/18/26; img overwritten. */
+int bwlabel(float *img, int conn, size_t dim[3], bool onlyLargest, bool fillBubbles);
+/* replaces apply_sform() (src/meshify.h:10). */
+void apply_sform(vec3i *t, vec3d *p, int nt, int np, float srow_x[4], float srow_y[4], float srow_z[4]);
+/* replaces setThreshold() (src/isolevel.h:9). */
+float setThreshold(float *img, int nvox, int darkMediumBright123);
+/* Mirrors the USE_CLASSIC_CUBES build flag for the drop-in marchingCubes()
+ * and meshify(): nonzero selects Bourke's oldcubes. Returns the old value. */
+int n2m_set_oldcubes(int enable);
+
+/* ---- explicit-status API -------------------------------------------------- */
+/* Host buffers in/out; meshes malloc'd like meshify(). */
+n2m_status n2m_meshify(n2m_context *ctx, const float *img, const int dim[3], const n2m_options *opt, vec3i **t,
+                       vec3d **p, int *nt, int *np, n2m_report *rep);
+
+/* Device-resident variant: d_img is a device pointer (float32, x fastest).
+ * The mesh stays in context-owned device memory (valid until the next call on
+ * ctx): *d_t (vec3i[*nt]) and *d_p (vec3d[*np]). */
+n2m_status n2m_meshify_device(n2m_context *ctx, const float *d_img, const int dim[3], const n2m_options *opt,
+                              vec3i **d_t, vec3d **d_p, int *nt, int *np, n2m_report *rep);
+
+/* HC smoothing of device-resident meshes (d_verts updated in place). */
+n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,
+                                double alpha, double beta, int iter, bool lock_edges);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* N2M_GPU_H */

@@ -1,0 +1,168 @@
+"""nii2mesh_gb300 — GB300-native volume->mesh path of nii2mesh.
+
+The product is libn2m_gpu.so (C ABI in include/n2m_gpu.h): the reference's own
+entry points (meshify, laplacian_smoothHC, marchingCubes, bwlabel,
+apply_sform) plus n2m_* calls with explicit status codes, device-resident
+variants, the adjoint and the batched atlas.  This module is a thin numpy /
+torch front end over that ABI, mirroring the reference's functions
+(src/meshify.h:9, src/quadric.h:7, src/MarchingCubes.h:19, src/bwlabel.h:10):
+same argument meaning, same failure behaviour (None where the reference
+returns EXIT_FAILURE).
+
+Volumes are numpy float32 arrays shaped (nz, ny, nx) — x fastest, exactly the
+reference's memory layout.  Meshes are (tris int32 (nt,3), pts float64 (np,3)).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import N2MError, Options, Report, vec3d, vec3i
+
+MC33, CLASSIC_TABLE, OLDCUBES = 0, 1, 2
+
+__all__ = ["Context", "meshify", "laplacian_smoothHC", "marching_cubes", "bwlabel", "apply_sform", "N2MError",
+           "MC33", "CLASSIC_TABLE", "OLDCUBES", "lib"]
+
+
+def lib():
+    return _lib.load()
+
+
+def _vol(img):
+    a = np.ascontiguousarray(img, dtype=np.float32)
+    if a.ndim != 3:
+        raise ValueError("volume must be 3-D (nz, ny, nx)")
+    return a
+
+
+def _take(L, tp, pp, nt, np_):
+    t = np.ctypeslib.as_array(C.cast(tp, C.POINTER(C.c_int)), shape=(nt, 3)).copy() if nt else np.zeros((0, 3), np.int32)
+    p = np.ctypeslib.as_array(C.cast(pp, C.POINTER(C.c_double)), shape=(np_, 3)).copy() if np_ else np.zeros((0, 3))
+    L.libc_free(tp)
+    L.libc_free(pp)
+    return t, p
+
+
+class Context:
+    """A CUDA stream + device workspace (n2m_context)."""
+
+    def __init__(self, device=0):
+        L = _lib.load()
+        self._L = L
+        h = C.c_void_p()
+        _lib.check(L.n2m_context_create(C.byref(h), device), "n2m_context_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self._L.n2m_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return self._L.n2m_context_stream(self.h)
+
+    @staticmethod
+    def _opts(iso, cubes, pre_smooth, only_largest, fill_bubbles, post_smooth, verbose):
+        return Options(int(cubes), float(iso), bool(pre_smooth), bool(only_largest), bool(fill_bubbles),
+                       int(post_smooth), bool(verbose))
+
+    def meshify(self, img, iso, cubes=MC33, pre_smooth=True, only_largest=True, fill_bubbles=False, post_smooth=0,
+                verbose=False):
+        """Host volume in, host mesh out (n2m_meshify).  Raises N2MError."""
+        a = _vol(img)
+        nz, ny, nx = a.shape
+        dims = (C.c_int * 3)(nx, ny, nz)
+        o = self._opts(iso, cubes, pre_smooth, only_largest, fill_bubbles, post_smooth, verbose)
+        tp, pp, nt, np_ = C.c_void_p(), C.c_void_p(), C.c_int(), C.c_int()
+        rep = Report()
+        _lib.check(self._L.n2m_meshify(self.h, a.ctypes.data, dims, C.byref(o), C.byref(tp), C.byref(pp), C.byref(nt),
+                                       C.byref(np_), C.byref(rep)), "n2m_meshify")
+        t, p = _take(self._L, tp, pp, nt.value, np_.value)
+        return t, p, rep.as_dict()
+
+    def meshify_device(self, d_img_ptr, dims_xyz, iso, cubes=MC33, pre_smooth=True, only_largest=True,
+                       fill_bubbles=False, post_smooth=0):
+        """Device volume (pointer) in; mesh stays on the device.  Returns
+        (d_tris_ptr, d_pts_ptr, nt, np, report)."""
+        dims = (C.c_int * 3)(*dims_xyz)
+        o = self._opts(iso, cubes, pre_smooth, only_largest, fill_bubbles, post_smooth, False)
+        tp, pp, nt, np_ = C.c_void_p(), C.c_void_p(), C.c_int(), C.c_int()
+        rep = Report()
+        _lib.check(self._L.n2m_meshify_device(self.h, C.c_void_p(d_img_ptr), dims, C.byref(o), C.byref(tp), C.byref(pp),
+                                              C.byref(nt), C.byref(np_), C.byref(rep)), "n2m_meshify_device")
+        return tp.value, pp.value, nt.value, np_.value, rep.as_dict()
+
+
+# ---- the reference's entry points, through the drop-in C symbols -----------------
+def meshify(img, isolevel, original_mc=0, pre_smooth=True, only_largest=True, fill_bubbles=False, verbose=False,
+            oldcubes=False):
+    """meshify() (src/meshify.h:9).  Returns (tris, pts) or None on failure."""
+    L = _lib.load()
+    a = _vol(img)
+    nz, ny, nx = a.shape
+    dims = (C.c_short * 3)(nx, ny, nz)
+    tp, pp, nt, np_ = C.c_void_p(), C.c_void_p(), C.c_int(), C.c_int()
+    prev = L.n2m_set_oldcubes(1 if oldcubes else 0)
+    try:
+        r = L.meshify(a.ctypes.data, dims, int(original_mc), float(isolevel), C.byref(tp), C.byref(pp), C.byref(nt),
+                      C.byref(np_), pre_smooth, only_largest, fill_bubbles, verbose)
+    finally:
+        L.n2m_set_oldcubes(prev)
+    if r != 0:
+        return None
+    return _take(L, tp, pp, nt.value, np_.value)
+
+
+def laplacian_smoothHC(pts, tris, alpha=0.1, beta=0.5, iters=1, lock_edges=True):
+    """laplacian_smoothHC() (src/quadric.h:7); returns the smoothed vertices."""
+    L = _lib.load()
+    p = np.ascontiguousarray(pts, dtype=np.float64).copy()
+    t = np.ascontiguousarray(tris, dtype=np.int32)
+    L.laplacian_smoothHC(p.ctypes.data, t.ctypes.data, len(p), len(t), alpha, beta, iters, lock_edges)
+    return p
+
+
+def marching_cubes(img, lo, hi, isolevel, original_mc=0, oldcubes=False):
+    """marchingCubes() (src/MarchingCubes.h:19): mesh of the padded box lo..hi
+    before any weld.  Returns (tris, pts) or None."""
+    L = _lib.load()
+    a = _vol(img)
+    nz, ny, nx = a.shape
+    dims = (C.c_short * 3)(nx, ny, nz)
+    tp, pp, nv, nt = C.c_void_p(), C.c_void_p(), C.c_int(), C.c_int()
+    prev = L.n2m_set_oldcubes(1 if oldcubes else 0)
+    try:
+        r = L.marchingCubes(a.ctypes.data, dims, (C.c_int * 3)(*lo), (C.c_int * 3)(*hi), int(original_mc),
+                            float(isolevel), C.byref(pp), C.byref(tp), C.byref(nv), C.byref(nt))
+    finally:
+        L.n2m_set_oldcubes(prev)
+    if r != 0:
+        return None
+    return _take(L, tp, pp, nt.value, nv.value)
+
+
+def bwlabel(img, conn=18, only_largest=False, fill_bubbles=False):
+    """bwlabel() (src/bwlabel.h:10): returns (labelled volume, number of labels)."""
+    L = _lib.load()
+    a = _vol(img).copy()
+    nz, ny, nx = a.shape
+    n = L.bwlabel(a.ctypes.data, conn, (C.c_size_t * 3)(nx, ny, nz), only_largest, fill_bubbles)
+    return a, n
+
+
+def apply_sform(pts, tris, srow_x, srow_y, srow_z):
+    """apply_sform() (src/meshify.h:10): returns (tris, pts)."""
+    L = _lib.load()
+    p = np.ascontiguousarray(pts, dtype=np.float64).copy()
+    t = np.ascontiguousarray(tris, dtype=np.int32).copy()
+    f = lambda r: (C.c_float * 4)(*r)
+    L.apply_sform(t.ctypes.data, p.ctypes.data, len(t), len(p), f(srow_x), f(srow_y), f(srow_z))
+    return t, p

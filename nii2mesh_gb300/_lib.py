@@ -1,0 +1,99 @@
+"""ctypes binding of libn2m_gpu.so (C ABI declared in include/n2m_gpu.h).
+
+The library is the product: every call below runs on the GPU.  Loading fails
+loudly (RuntimeError) when the library has not been built — there is no CPU
+fallback.
+"""
+import ctypes as C
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libn2m_gpu.so"
+
+N2M_OK = 0
+STATUS = ["ok", "no CUDA device", "CUDA error", "out of memory", "bad arguments", "no variability", "empty mesh",
+          "non-finite voxels", "too large", "device wait timed out", "internal error"]
+
+# exported symbols (the C-ABI contract; tests check that every one is present)
+SYMBOLS = ["n2m_context_create", "n2m_context_destroy", "n2m_context_stream", "n2m_last_error",
+           "n2m_status_string", "n2m_device_count", "meshify", "laplacian_smoothHC", "marchingCubes", "bwlabel",
+           "apply_sform", "n2m_set_oldcubes", "n2m_meshify", "n2m_meshify_device", "n2m_smooth_hc_device"]
+
+
+class vec3d(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+
+class vec3i(C.Structure):
+    _fields_ = [("x", C.c_int), ("y", C.c_int), ("z", C.c_int)]
+
+
+class Options(C.Structure):
+    _fields_ = [("cubes", C.c_int), ("isolevel", C.c_float), ("pre_smooth", C.c_bool), ("only_largest", C.c_bool),
+                ("fill_bubbles", C.c_bool), ("post_smooth", C.c_int), ("verbose", C.c_bool)]
+
+
+class Report(C.Structure):
+    _fields_ = [("isolevel_used", C.c_float), ("vmin", C.c_float), ("vmax", C.c_float), ("lo", C.c_int * 3),
+                ("hi", C.c_int * 3), ("nvert_raw", C.c_int64), ("ntri_raw", C.c_int64), ("nvert", C.c_int64),
+                ("ntri", C.c_int64), ("welded", C.c_int), ("degenerate", C.c_int), ("ms_total", C.c_float)]
+
+    def as_dict(self):
+        return {f: (list(getattr(self, f)) if f in ("lo", "hi") else getattr(self, f)) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load (once) and return the library with argtypes declared."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build the CUDA extension first (__graft_entry__.build() or "
+                           f"python -m nii2mesh_gb300.build); there is no CPU fallback")
+    L = C.CDLL(str(p))
+    vp, ip = C.c_void_p, C.POINTER(C.c_int)
+    L.n2m_context_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.n2m_context_destroy.argtypes = [vp]
+    L.n2m_context_destroy.restype = None
+    L.n2m_context_stream.argtypes = [vp]
+    L.n2m_context_stream.restype = vp
+    L.n2m_last_error.restype = C.c_char_p
+    L.n2m_status_string.restype = C.c_char_p
+    L.meshify.argtypes = [vp, C.POINTER(C.c_short), C.c_int, C.c_float, C.POINTER(vp), C.POINTER(vp), ip, ip,
+                          C.c_bool, C.c_bool, C.c_bool, C.c_bool]
+    L.laplacian_smoothHC.argtypes = [vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_bool]
+    L.laplacian_smoothHC.restype = None
+    L.marchingCubes.argtypes = [vp, C.POINTER(C.c_short), ip, ip, C.c_int, C.c_float, C.POINTER(vp), C.POINTER(vp),
+                                ip, ip]
+    L.bwlabel.argtypes = [vp, C.c_int, C.POINTER(C.c_size_t), C.c_bool, C.c_bool]
+    L.apply_sform.argtypes = [vp, vp, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                              C.POINTER(C.c_float)]
+    L.apply_sform.restype = None
+    L.n2m_set_oldcubes.argtypes = [C.c_int]
+    L.n2m_meshify.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip, C.POINTER(Report)]
+    L.n2m_meshify_device.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip,
+                                     C.POINTER(Report)]
+    L.n2m_smooth_hc_device.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_bool]
+    libc = C.CDLL(None)
+    libc.free.argtypes = [vp]
+    L.libc_free = libc.free
+    _lib = L
+    return L
+
+
+def check(status, what="n2m call"):
+    if status != N2M_OK:
+        L = load()
+        msg = L.n2m_last_error().decode(errors="replace")
+        name = STATUS[status] if 0 <= status < len(STATUS) else str(status)
+        raise N2MError(status, f"{what}: {name}: {msg}")
+
+
+class N2MError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(msg)
+        self.status = status

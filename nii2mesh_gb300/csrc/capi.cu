@@ -1,0 +1,724 @@
+// capi.cu — host orchestration of the meshify pipeline and the C ABI.
+//
+// meshify (src/meshify.c:286-389) on the GPU, stage by stage:
+//   1. pre-smooth fused with range + bbox (smooth.cu), or a range/bbox pass
+//   2. one readback: range, isolevel fallback, non-finite check
+//   3. optional clustering (label.cu), range/bbox recomputed afterwards
+//   4. marching cubes count pass + scan (mc.cu / oldcubes.cu), readback of
+//      the vertex/triangle totals, emit pass straight into vec3d/vec3i
+//   5. weld: the few near-grid-point candidates are read back and grouped on
+//      the host with the reference's greedy rule; merges applied on device
+//   6. degenerate-triangle removal and compaction (mesh.cu)
+// Edge darkening is applied on the fly by the marching-cubes value fetch.
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "n2m_internal.cuh"
+
+// ---- errors ---------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+void n2m_set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+extern "C" const char *n2m_last_error(void) { return g_err; }
+
+extern "C" const char *n2m_status_string(int s) {
+    static const char *names[] = {"ok",         "no CUDA device",   "CUDA error",      "out of memory",
+                                  "bad arguments", "no variability", "empty mesh",      "non-finite voxels",
+                                  "too large",  "device wait timed out", "internal error"};
+    return (s >= 0 && s <= 10) ? names[s] : "unknown";
+}
+
+n2m_status DevBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return N2M_OK;
+    release();
+    size_t want = bytes + bytes / 8 + 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        cap = 0;
+        n2m_set_error("cudaMalloc(%zu): %s", want, cudaGetErrorString(e));
+        return N2M_ERR_OOM;
+    }
+    cap = want;
+    return N2M_OK;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+}
+
+// ---- context ------------------------------------------------------------------------
+struct n2m_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    DevBuf in, vol, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath, hmesh;
+    McWork mc;
+    ScanWork scan;
+    LabelWork lab;
+    DegWork deg;
+    HcWork hc;
+    void *pinned = nullptr;   // small readbacks
+    // result of the last pipeline run (device pointers into the buffers above)
+    vec3d *res_pts = nullptr;
+    vec3i *res_tris = nullptr;
+    int res_np = 0, res_nt = 0;
+};
+
+extern "C" int n2m_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+extern "C" n2m_status n2m_context_create(n2m_context **out, int device) {
+    if (!out) return N2M_ERR_BAD_ARGS;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || device < 0 || device >= n) {
+        cudaGetLastError();
+        n2m_set_error("no usable CUDA device (count %d, requested %d)", n, device);
+        return N2M_ERR_NO_DEVICE;
+    }
+    n2m_context *c = new n2m_context;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+        cudaMallocHost(&c->pinned, 4096) != cudaSuccess) {
+        n2m_set_error("context creation failed: %s", cudaGetErrorString(cudaGetLastError()));
+        delete c;
+        return N2M_ERR_CUDA;
+    }
+    *out = c;
+    return N2M_OK;
+}
+
+extern "C" void n2m_context_destroy(n2m_context *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    DevBuf *bufs[] = {&c->in, &c->vol, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
+                      &c->tris_raw, &c->pts, &c->tris, &c->ntf, &c->weld, &c->gath, &c->hmesh,
+                      &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->scan.part,
+                      &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
+                      &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
+                      &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb};
+    for (DevBuf *b : bufs) b->release();
+    if (c->pinned) cudaFreeHost(c->pinned);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+extern "C" void *n2m_context_stream(n2m_context *c) { return c ? (void *)c->stream : nullptr; }
+
+namespace {
+// per-thread default context for the drop-in entry points
+struct TlsCtx {
+    n2m_context *c = nullptr;
+    ~TlsCtx() { n2m_context_destroy(c); }
+};
+thread_local TlsCtx g_tls;
+int g_oldcubes = 0;
+
+n2m_status default_ctx(n2m_context **c) {
+    if (!g_tls.c) {
+        const char *d = getenv("N2M_DEVICE");
+        CKS(n2m_context_create(&g_tls.c, d ? atoi(d) : 0));
+    }
+    *c = g_tls.c;
+    return N2M_OK;
+}
+
+template <class T> n2m_status readback(n2m_context *c, T *dst, const void *dsrc, size_t n = 1) {
+    CK(cudaMemcpyAsync(c->pinned, dsrc, n * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    memcpy(dst, c->pinned, n * sizeof(T));
+    return N2M_OK;
+}
+
+__global__ void k_gather(const vec3d *__restrict__ p, const int *__restrict__ ids, int n, vec3d *out,
+                         const long long *__restrict__ lastuse, long long *lout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        out[i] = p[ids[i]];
+        if (lastuse) lout[i] = lastuse[ids[i]];
+    }
+}
+
+__global__ void k_fill_ll(long long *p, size_t n, long long v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+double dist3(const vec3d &a, const vec3d &b) {
+    const double dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+uint32_t key_bits(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Host side of the weld (src/meshify.c:45-106) restricted to the candidates:
+// only vertices within the tolerance of another vertex can merge, and every
+// such vertex is a candidate, so the greedy grouping in key order over the
+// candidates makes exactly the reference's merges.  Outputs the removed ids
+// (sorted), the id each merges into, and position overrides (the group's
+// last writer in the reference's vertex order).
+n2m_status weld_candidates(n2m_context *c, int nv, int ncand, bool oldcubes, std::vector<int> &removed,
+                           std::vector<int> &keep, std::vector<int> &ov_id, std::vector<vec3d> &ov_pos, vec3d v0) {
+    std::vector<int> ids(ncand);
+    CK(cudaMemcpyAsync(ids.data(), c->cand.p, ncand * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::sort(ids.begin(), ids.end());
+    ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+    const int n = (int)ids.size();
+    CKS(c->gath.ensure((size_t)n * (sizeof(vec3d) + sizeof(int) + sizeof(long long))));
+    vec3d *dpos = c->gath.as<vec3d>();
+    int *dids = (int *)(dpos + n);
+    long long *dlu = (long long *)(dids + n + (n & 1));
+    CK(cudaMemcpyAsync(dids, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    k_gather<<<(n + 255) / 256, 256, 0, c->stream>>>(c->pts_raw.as<vec3d>(), dids, n, dpos,
+                                                     oldcubes ? c->lastuse.as<long long>() : nullptr, dlu);
+    CKL();
+    std::vector<vec3d> pos(n);
+    std::vector<long long> order(n);
+    CK(cudaMemcpyAsync(pos.data(), dpos, n * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream));
+    if (oldcubes) CK(cudaMemcpyAsync(order.data(), dlu, n * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!oldcubes)
+        for (int i = 0; i < n; i++) order[i] = ids[i];
+    // sort by (float key, reference order) = the reference's stable radix sort
+    std::vector<float> key(n);
+    std::vector<int> srt(n);
+    for (int i = 0; i < n; i++) {
+        key[i] = (float)dist3(v0, pos[i]);
+        srt[i] = i;
+    }
+    std::sort(srt.begin(), srt.end(), [&](int a, int b) {
+        const uint32_t ka = key_bits(key[a]), kb = key_bits(key[b]);
+        return ka != kb ? ka < kb : order[a] < order[b];
+    });
+    const float tol = 0.00001f;
+    std::vector<int> grp(n, -1);
+    int ng = 0;
+    for (int i = 0; i < n; i++) {
+        const int a = srt[i];
+        if (grp[a] >= 0) continue;
+        for (int j = i; j < n && (key[srt[j]] - key[a]) < tol; j++)
+            if (dist3(pos[a], pos[srt[j]]) < tol) grp[srt[j]] = ng;
+        ng++;
+    }
+    // per group: keep the smallest id, position of the last writer
+    std::vector<int> gkeep(ng, INT32_MAX), glast(ng, -1), gsize(ng, 0);
+    for (int i = 0; i < n; i++) {
+        const int g = grp[i];
+        gsize[g]++;
+        gkeep[g] = std::min(gkeep[g], ids[i]);
+        if (glast[g] < 0 || order[i] > order[glast[g]]) glast[g] = i;
+    }
+    for (int i = 0; i < n; i++) {
+        const int g = grp[i];
+        if (gsize[g] < 2) continue;
+        if (ids[i] != gkeep[g]) {
+            removed.push_back(ids[i]);
+            keep.push_back(gkeep[g]);
+        } else if (glast[g] != i) {
+            ov_id.push_back(ids[i]);
+            ov_pos.push_back(pos[glast[g]]);
+        }
+    }
+    // sort removed (with keep) and overrides by id
+    std::vector<int> ri(removed.size());
+    for (size_t i = 0; i < ri.size(); i++) ri[i] = (int)i;
+    std::sort(ri.begin(), ri.end(), [&](int a, int b) { return removed[a] < removed[b]; });
+    std::vector<int> r2, k2;
+    for (int i : ri) { r2.push_back(removed[i]); k2.push_back(keep[i]); }
+    removed.swap(r2);
+    keep.swap(k2);
+    std::vector<int> oi(ov_id.size());
+    for (size_t i = 0; i < oi.size(); i++) oi[i] = (int)i;
+    std::sort(oi.begin(), oi.end(), [&](int a, int b) { return ov_id[a] < ov_id[b]; });
+    std::vector<int> o2;
+    std::vector<vec3d> p2;
+    for (int i : oi) { o2.push_back(ov_id[i]); p2.push_back(ov_pos[i]); }
+    ov_id.swap(o2);
+    ov_pos.swap(p2);
+    (void)nv;
+    return N2M_OK;
+}
+
+float half_sum(float a, float b) {   // (float)(0.5 * (a + b)) with a float sum, as C evaluates it
+    volatile float s = a + b;
+    return (float)(0.5 * (double)s);
+}
+
+struct Prep {
+    const float *vol;
+    float iso, mn, mnp, edge_max;
+    int lo[3], hi[3];
+};
+
+// stages 1-3: smoothing, range, clustering, bbox
+n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n2m_options &o, bool verbose,
+                   Prep &P, n2m_report *rep) {
+    const int nx = dim[0], ny = dim[1], nz = dim[2];
+    const size_t n = (size_t)nx * ny * nz;
+    const bool smooth = o.pre_smooth && nx >= 5 && ny >= 5 && nz >= 5;
+    const bool label = o.only_largest || o.fill_bubbles;
+    float iso = o.isolevel;
+    CKS(c->stats.ensure(2 * sizeof(VolStats)));
+    VolStats *dst = c->stats.as<VolStats>();
+    VolStats h[2];
+    stats_init_host(&h[0]);
+    stats_init_host(&h[1]);
+    CK(cudaMemcpyAsync(dst, h, 2 * sizeof(VolStats), cudaMemcpyHostToDevice, c->stream));
+    float *vol = nullptr;
+    if (smooth || label) {
+        CKS(c->vol.ensure(n * sizeof(float)));
+        vol = c->vol.as<float>();
+    }
+    if (smooth) {
+        CKS(launch_smooth(d_src, vol, nx, ny, nz, iso, dst, c->stream));
+    } else {
+        if (label) CK(cudaMemcpyAsync(vol, d_src, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+        CKS(launch_stats(label ? vol : d_src, nx, ny, nz, iso, true, dst, c->stream));
+    }
+    const float *v = vol ? vol : d_src;
+    VolStats s0;
+    CKS(readback(c, &s0, dst));
+    if (s0.nonfinite) {
+        n2m_set_error("%u non-finite voxels in the volume", s0.nonfinite);
+        return N2M_ERR_NONFINITE;
+    }
+    const float mn = ord2f(s0.vmin), mx = ord2f(s0.vmax);
+    if (mn == mx) {
+        printf("Error: No variability in image intensity.\n");
+        n2m_set_error("no variability in image intensity");
+        return N2M_ERR_NO_VARIABILITY;
+    }
+    bool stale = false;
+    if (iso <= mn || iso > mx) {
+        iso = half_sum(mn, mx);
+        printf("Suggested isolevel out of range. Intensity range %g..%g, setting isolevel to %g\n", mn, mx, iso);
+        stale = true;
+    }
+    if (verbose) printf("intensity range %g..%g, isolevel %g\n", mn, mx, iso);
+    VolStats s1 = s0;
+    float min_after = mn;
+    if (label) {
+        CKS(run_labelling(vol, nx, ny, nz, iso, mn, o.only_largest, o.fill_bubbles, c->lab, c->stream));
+        CKS(launch_stats(vol, nx, ny, nz, iso, true, dst + 1, c->stream));
+        CKS(readback(c, &s1, dst + 1));
+        min_after = ord2f(s1.vmin);
+    } else if (stale) {
+        CKS(launch_stats(v, nx, ny, nz, iso, false, dst + 1, c->stream));
+        CKS(readback(c, &s1, dst + 1));
+    }
+    if (s1.lo[0] > s1.hi[0]) {
+        n2m_set_error("no voxel at or above the isolevel");
+        return N2M_ERR_EMPTY;
+    }
+    volatile float mi = mn + iso;
+    P.edge_max = (float)(0.75 * (double)mi);
+    P.mnp = fminf(min_after, P.edge_max);
+    P.vol = v;
+    P.iso = iso;
+    P.mn = mn;
+    for (int i = 0; i < 3; i++) {
+        P.lo[i] = std::max(s1.lo[i] - 1, 0);
+        P.hi[i] = std::min(s1.hi[i] + 2, dim[i]);
+    }
+    if (rep) {
+        rep->isolevel_used = iso;
+        rep->vmin = mn;
+        rep->vmax = mx;
+        for (int i = 0; i < 3; i++) { rep->lo[i] = P.lo[i]; rep->hi[i] = P.hi[i]; }
+    }
+    return N2M_OK;
+}
+
+// stage 4: marching cubes into pts_raw / tris_raw
+n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int *nv_out, int *nt_out,
+                 int *ncand_out) {
+    const bool old = cubes == N2M_CUBES_OLDCUBES;
+    McGrid g;
+    g.vol = P.vol;
+    for (int i = 0; i < 3; i++) {
+        g.dim[i] = dim[i];
+        g.lo[i] = P.lo[i];
+        g.n[i] = P.hi[i] - P.lo[i] + 1;
+    }
+    g.iso = P.iso;
+    g.edge_max = P.edge_max;
+    volatile float pv = P.mnp - P.iso;
+    g.pad_val = pv;
+    const double ng = (double)g.n[0] * g.n[1] * g.n[2];
+    if (ng >= 4294967040.0) {
+        n2m_set_error("grid of %.0f points exceeds the 32-bit range", ng);
+        return N2M_ERR_TOO_LARGE;
+    }
+    CKS(c->totals.ensure(sizeof(uint4)));
+    uint4 *dtot = c->totals.as<uint4>();
+    if (old) CKS(oc_count(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->scan, dtot, c->stream));
+    else CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream));
+    uint4 tot;
+    CKS(readback(c, &tot, dtot));
+    const unsigned long long nv = (unsigned long long)tot.x + tot.z, nt = tot.y;
+    if (nv >= 0x7fffffffULL || nt >= 0x7fffffffULL) {
+        n2m_set_error("mesh too large for 32-bit indices");
+        return N2M_ERR_TOO_LARGE;
+    }
+    if ((!old && (nv < 3 || nt < 1)) || (old && nt < 1)) {
+        if (old) printf("marching cubes failed to identify triangles with an isolevel of %g\n", P.iso);
+        n2m_set_error("marching cubes produced no surface");
+        return N2M_ERR_EMPTY;
+    }
+    CKS(c->pts_raw.ensure(nv * sizeof(vec3d)));
+    CKS(c->tris_raw.ensure(nt * sizeof(vec3i)));
+    const int cap = (int)std::min<unsigned long long>(nv / 16 + 65536, 1 << 26);
+    CKS(c->cand.ensure((size_t)2 * cap * sizeof(int)));
+    CKS(c->ncand.ensure(2 * sizeof(unsigned)));
+    CK(cudaMemsetAsync(c->ncand.p, 0, 2 * sizeof(unsigned), c->stream));
+    McCounts mcn{tot.x, tot.y, tot.z};
+    if (old) {
+        CKS(c->lastuse.ensure(nv * sizeof(long long)));
+        k_fill_ll<<<1024, 256, 0, c->stream>>>(c->lastuse.as<long long>(), nv, -1);
+        CKS(oc_emit(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, mcn, c->pts_raw.as<vec3d>(),
+                    c->tris_raw.as<vec3i>(), c->cand.as<int>(), c->ncand.as<unsigned>(), cap,
+                    c->lastuse.as<long long>(), c->stream));
+    } else {
+        CKS(mc_emit(g, cubes, c->mc, mcn, c->pts_raw.as<vec3d>(), c->tris_raw.as<vec3i>(), c->cand.as<int>(),
+                    c->ncand.as<unsigned>(), cap, c->stream));
+    }
+    unsigned nc[2];
+    CKS(readback(c, nc, c->ncand.p, 2));
+    if (nc[0] > (unsigned)cap || nc[1] > (unsigned)cap) {
+        n2m_set_error("weld candidate overflow (%u, %u > %d)", nc[0], nc[1], cap);
+        return N2M_ERR_INTERNAL;
+    }
+    if (nc[1]) {   // c-vertex candidates: collect every vertex near them
+        CK(cudaMemcpyAsync(c->cand.as<int>() + nc[0], c->cand.as<int>() + cap, nc[1] * sizeof(int),
+                           cudaMemcpyDeviceToDevice, c->stream));
+        unsigned tot2 = nc[0] + nc[1];
+        CK(cudaMemcpyAsync(c->ncand.p, &tot2, sizeof(unsigned), cudaMemcpyHostToDevice, c->stream));
+        CKS(mc_ccand_scan(c->pts_raw.as<vec3d>(), (int)nv, c->cand.as<int>() + cap, (int)nc[1], c->cand.as<int>(),
+                          c->ncand.as<unsigned>(), cap, c->stream));
+        CKS(readback(c, nc, c->ncand.p, 1));
+        if (nc[0] > (unsigned)cap) {
+            n2m_set_error("weld candidate overflow");
+            return N2M_ERR_INTERNAL;
+        }
+    }
+    *nv_out = (int)nv;
+    *nt_out = (int)nt;
+    *ncand_out = (int)nc[0];
+    return N2M_OK;
+}
+
+// the whole meshify on device input; result in c->res_*
+n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const n2m_options &o, n2m_report *rep) {
+    if (!d_src || dim[0] <= 0 || dim[1] <= 0 || dim[2] <= 0) {
+        n2m_set_error("bad volume arguments");
+        return N2M_ERR_BAD_ARGS;
+    }
+    if ((double)dim[0] * dim[1] * dim[2] > 2147483647.0) {
+        n2m_set_error("volume exceeds 2^31-1 voxels");
+        return N2M_ERR_TOO_LARGE;
+    }
+    CK(cudaEventRecord(c->ev0, c->stream));
+    Prep P;
+    CKS(prepare(c, d_src, dim, o, o.verbose, P, rep));
+    int nv, nt, ncand;
+    CKS(march(c, P, dim, o.cubes, &nv, &nt, &ncand));
+    vec3d *pts = c->pts_raw.as<vec3d>();
+    int np = nv;
+    int welded = 0;
+    if (ncand > 0) {
+        vec3d v0;
+        if (o.cubes == N2M_CUBES_OLDCUBES) {
+            vec3i t0;
+            CKS(readback(c, &t0, c->tris_raw.p));
+            CKS(readback(c, &v0, pts + t0.x));
+        } else {
+            CKS(readback(c, &v0, pts));
+        }
+        std::vector<int> removed, keep, ov_id;
+        std::vector<vec3d> ov_pos;
+        CKS(weld_candidates(c, nv, ncand, o.cubes == N2M_CUBES_OLDCUBES, removed, keep, ov_id, ov_pos, v0));
+        if (!removed.empty()) {
+            const int nr = (int)removed.size(), no = (int)ov_id.size();
+            CKS(c->weld.ensure((size_t)(2 * nr + no + 1) * sizeof(int) + (size_t)(no + 1) * sizeof(vec3d)));
+            vec3d *dov = c->weld.as<vec3d>();
+            int *drem = (int *)(dov + no + 1);
+            int *dkeep = drem + nr, *dovid = dkeep + nr;
+            if (no) CK(cudaMemcpyAsync(dov, ov_pos.data(), no * sizeof(vec3d), cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(drem, removed.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(dkeep, keep.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            if (no) CK(cudaMemcpyAsync(dovid, ov_id.data(), no * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            np = nv - nr;
+            CKS(c->pts.ensure((size_t)np * sizeof(vec3d)));
+            CKS(mesh_apply_weld(pts, c->tris_raw.as<vec3i>(), nv, nt, drem, dkeep, nr, dovid, dov, no,
+                                c->pts.as<vec3d>(), c->stream));
+            pts = c->pts.as<vec3d>();
+            welded = nr;
+            CK(cudaStreamSynchronize(c->stream));   // host vectors go out of scope
+        }
+    }
+    if (np < 3) {
+        n2m_set_error("fewer than 3 vertices after the weld");
+        return N2M_ERR_EMPTY;
+    }
+    CKS(c->tris.ensure((size_t)nt * sizeof(vec3i)));
+    CKS(c->ntf.ensure(sizeof(unsigned)));
+    CKS(mesh_remove_degenerate(pts, c->tris_raw.as<vec3i>(), nt, c->tris.as<vec3i>(), c->ntf.as<unsigned>(), c->deg,
+                               c->scan, c->stream));
+    CK(cudaEventRecord(c->ev1, c->stream));
+    unsigned ntf;
+    CKS(readback(c, &ntf, c->ntf.p));
+    c->res_pts = pts;
+    c->res_tris = c->tris.as<vec3i>();
+    c->res_np = np;
+    c->res_nt = (int)ntf;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    if (o.verbose) {
+        printf("marching cubes (%dx%dx%d) + weld + degenerate removal on GPU: %.3f ms\n", dim[0], dim[1], dim[2], ms);
+        if (welded) printf("vertex welding %d -> %d\n", nv, np);
+        if ((int)ntf != nt) printf("remove degenerate triangles %d -> %u\n", nt, ntf);
+    }
+    if (rep) {
+        rep->nvert_raw = nv;
+        rep->ntri_raw = nt;
+        rep->nvert = np;
+        rep->ntri = ntf;
+        rep->welded = welded;
+        rep->degenerate = nt - (int)ntf;
+        rep->ms_total = ms;
+    }
+    return N2M_OK;
+}
+
+n2m_status to_host_mesh(n2m_context *c, vec3i **t, vec3d **p, int *nt, int *np) {
+    vec3d *hp = (vec3d *)malloc((size_t)c->res_np * sizeof(vec3d));
+    vec3i *ht = (vec3i *)malloc((size_t)std::max(c->res_nt, 1) * sizeof(vec3i));
+    if (!hp || !ht) {
+        free(hp);
+        free(ht);
+        n2m_set_error("host allocation failed");
+        return N2M_ERR_OOM;
+    }
+    CK(cudaMemcpyAsync(hp, c->res_pts, (size_t)c->res_np * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(ht, c->res_tris, (size_t)c->res_nt * sizeof(vec3i), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *t = ht;
+    *p = hp;
+    *nt = c->res_nt;
+    *np = c->res_np;
+    return N2M_OK;
+}
+
+n2m_status upload(n2m_context *c, const float *img, size_t n) {
+    CKS(c->in.ensure(n * sizeof(float)));
+    CK(cudaMemcpyAsync(c->in.p, img, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    return N2M_OK;
+}
+}  // namespace
+
+// ---- explicit-status API -------------------------------------------------------------
+extern "C" n2m_status n2m_meshify_device(n2m_context *c, const float *d_img, const int dim[3], const n2m_options *opt,
+                                         vec3i **d_t, vec3d **d_p, int *nt, int *np, n2m_report *rep) {
+    if (!c || !opt || !dim) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    CKS(pipeline(c, d_img, dim, *opt, rep));
+    if (opt->post_smooth > 0)
+        CKS(mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc,
+                           c->scan, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (d_t) *d_t = c->res_tris;
+    if (d_p) *d_p = c->res_pts;
+    if (nt) *nt = c->res_nt;
+    if (np) *np = c->res_np;
+    return N2M_OK;
+}
+
+extern "C" n2m_status n2m_meshify(n2m_context *c, const float *img, const int dim[3], const n2m_options *opt,
+                                  vec3i **t, vec3d **p, int *nt, int *np, n2m_report *rep) {
+    if (!c || !opt || !dim || !img || !t || !p || !nt || !np) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    const size_t n = (size_t)dim[0] * dim[1] * dim[2];
+    CKS(upload(c, img, n));
+    CKS(pipeline(c, c->in.as<float>(), dim, *opt, rep));
+    if (opt->post_smooth > 0)
+        CKS(mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc,
+                           c->scan, c->stream));
+    return to_host_mesh(c, t, p, nt, np);
+}
+
+extern "C" n2m_status n2m_smooth_hc_device(n2m_context *c, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,
+                                           double alpha, double beta, int iter, bool lock_edges) {
+    if (!c) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    CKS(mesh_smooth_hc(d_verts, d_tris, nvert, ntri, alpha, beta, iter, lock_edges, c->hc, c->scan, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return N2M_OK;
+}
+
+// ---- drop-in entry points ---------------------------------------------------------------
+static void report_failure(const char *fn, n2m_status s) {
+    if (s == N2M_ERR_NO_VARIABILITY || s == N2M_ERR_EMPTY) return;   // reference prints its own message
+    printf("%s: %s (%s)\n", fn, n2m_status_string(s), n2m_last_error());
+}
+
+extern "C" int n2m_set_oldcubes(int enable) {
+    const int old = g_oldcubes;
+    g_oldcubes = enable;
+    return old;
+}
+
+extern "C" int meshify(float *img, short dim[3], int originalMC, float isolevel, vec3i **t, vec3d **p, int *nt,
+                       int *np, bool preSmooth, bool onlyLargest, bool fillBubbles, bool verbose) {
+    n2m_context *c;
+    n2m_status s = default_ctx(&c);
+    if (s == N2M_OK) {
+        const int d[3] = {dim[0], dim[1], dim[2]};
+        n2m_options o = {g_oldcubes ? (int)N2M_CUBES_OLDCUBES : (originalMC ? (int)N2M_CUBES_CLASSIC_TABLE : (int)N2M_CUBES_MC33),
+                         isolevel, preSmooth, onlyLargest, fillBubbles, 0, verbose};
+        s = n2m_meshify(c, img, d, &o, t, p, nt, np, nullptr);
+    }
+    if (s != N2M_OK) {
+        report_failure("meshify", s);
+        return EXIT_FAILURE;
+    }
+    return EXIT_SUCCESS;
+}
+
+extern "C" void laplacian_smoothHC(vec3d *verts, vec3i *tris, int nvert, int ntri, double alpha, double beta, int iter,
+                                   bool lockEdges) {
+    n2m_context *c;
+    n2m_status s = default_ctx(&c);
+    if (s == N2M_OK && nvert > 0 && iter > 0) {
+        s = N2M_ERR_CUDA;
+        if (c->hmesh.ensure((size_t)nvert * sizeof(vec3d) + (size_t)std::max(ntri, 1) * sizeof(vec3i)) == N2M_OK) {
+            vec3d *dv = c->hmesh.as<vec3d>();
+            vec3i *dt = (vec3i *)(dv + nvert);
+            if (cudaMemcpyAsync(dv, verts, (size_t)nvert * sizeof(vec3d), cudaMemcpyHostToDevice, c->stream) == cudaSuccess &&
+                cudaMemcpyAsync(dt, tris, (size_t)ntri * sizeof(vec3i), cudaMemcpyHostToDevice, c->stream) == cudaSuccess) {
+                s = mesh_smooth_hc(dv, dt, nvert, ntri, alpha, beta, iter, lockEdges, c->hc, c->scan, c->stream);
+                if (s == N2M_OK &&
+                    (cudaMemcpyAsync(verts, dv, (size_t)nvert * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                     cudaStreamSynchronize(c->stream) != cudaSuccess))
+                    s = N2M_ERR_CUDA;
+            }
+        }
+    }
+    if (s != N2M_OK) report_failure("laplacian_smoothHC", s);
+}
+
+extern "C" void apply_sform(vec3i *t, vec3d *p, int nt, int np, float srow_x[4], float srow_y[4], float srow_z[4]) {
+    n2m_context *c;
+    n2m_status s = default_ctx(&c);
+    if (s == N2M_OK && np > 0) {
+        s = N2M_ERR_CUDA;
+        if (c->hmesh.ensure((size_t)np * sizeof(vec3d) + (size_t)std::max(nt, 1) * sizeof(vec3i)) == N2M_OK) {
+            vec3d *dv = c->hmesh.as<vec3d>();
+            vec3i *dt = (vec3i *)(dv + np);
+            if (cudaMemcpyAsync(dv, p, (size_t)np * sizeof(vec3d), cudaMemcpyHostToDevice, c->stream) == cudaSuccess &&
+                cudaMemcpyAsync(dt, t, (size_t)nt * sizeof(vec3i), cudaMemcpyHostToDevice, c->stream) == cudaSuccess) {
+                s = mesh_apply_sform(dv, dt, np, nt, srow_x, srow_y, srow_z, c->stream);
+                if (s == N2M_OK &&
+                    (cudaMemcpyAsync(p, dv, (size_t)np * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                     cudaMemcpyAsync(t, dt, (size_t)nt * sizeof(vec3i), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                     cudaStreamSynchronize(c->stream) != cudaSuccess))
+                    s = N2M_ERR_CUDA;
+            }
+        }
+    }
+    if (s != N2M_OK) report_failure("apply_sform", s);
+}
+
+extern "C" int bwlabel(float *img, int conn, size_t dim[3], bool onlyLargest, bool fillBubbles) {
+    if (conn != 6 && conn != 18 && conn != 26) {
+        fprintf(stderr, "bwlabel: conn must be 6, 18 or 26.\n");
+        return 0;
+    }
+    if (dim[0] < 2 || dim[1] < 2 || dim[2] < 1) {
+        fprintf(stderr, "bwlabel: img must be 2 or 3-dimensional\n");
+        return 0;
+    }
+    n2m_context *c;
+    n2m_status s = default_ctx(&c);
+    int nl = 0;
+    if (s == N2M_OK) {
+        const size_t n = dim[0] * dim[1] * dim[2];
+        s = upload(c, img, n);
+        if (s == N2M_OK) s = c->ntf.ensure(sizeof(int));
+        if (s == N2M_OK)
+            s = run_bwlabel(c->in.as<float>(), (int)dim[0], (int)dim[1], (int)dim[2], conn, onlyLargest, fillBubbles,
+                            c->lab, c->scan, c->ntf.as<int>(), c->stream);
+        if (s == N2M_OK && (cudaMemcpyAsync(img, c->in.p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess))
+            s = N2M_ERR_CUDA;
+        if (s == N2M_OK) s = readback(c, &nl, c->ntf.p);
+    }
+    if (s != N2M_OK) {
+        report_failure("bwlabel", s);
+        return 0;
+    }
+    return nl;
+}
+
+extern "C" int marchingCubes(float *img, short dim[3], int lo[3], int hi[3], int originalMC, float isolevel,
+                             vec3d **vs, vec3i **ts, int *nv, int *nt) {
+    n2m_context *c;
+    n2m_status s = default_ctx(&c);
+    if (s == N2M_OK) {
+        const int d[3] = {dim[0], dim[1], dim[2]};
+        const size_t n = (size_t)d[0] * d[1] * d[2];
+        s = upload(c, img, n);
+        Prep P;
+        P.vol = c->in.as<float>();
+        P.iso = isolevel;
+        P.edge_max = INFINITY;   // the standalone call does not darken edges
+        for (int i = 0; i < 3; i++) { P.lo[i] = lo[i]; P.hi[i] = hi[i]; }
+        if (s == N2M_OK) {   // padding: min of the whole volume (src/MarchingCubes.c:1094-1098)
+            CKS(c->stats.ensure(sizeof(VolStats)));
+            VolStats h;
+            stats_init_host(&h);
+            if (cudaMemcpyAsync(c->stats.p, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) s = N2M_ERR_CUDA;
+            if (s == N2M_OK) s = launch_stats(P.vol, d[0], d[1], d[2], isolevel, true, c->stats.as<VolStats>(), c->stream);
+            if (s == N2M_OK) s = readback(c, &h, c->stats.p);
+            P.mnp = ord2f(h.vmin);
+        }
+        const int cubes = g_oldcubes ? N2M_CUBES_OLDCUBES : (originalMC ? N2M_CUBES_CLASSIC_TABLE : N2M_CUBES_MC33);
+        int v = 0, t = 0, ncand = 0;
+        if (s == N2M_OK) s = march(c, P, d, cubes, &v, &t, &ncand);
+        if (s == N2M_OK) {
+            c->res_pts = c->pts_raw.as<vec3d>();
+            c->res_tris = c->tris_raw.as<vec3i>();
+            c->res_np = v;
+            c->res_nt = t;
+            s = to_host_mesh(c, ts, vs, nt, nv);
+        }
+    }
+    if (s != N2M_OK) {
+        report_failure("marchingCubes", s);
+        return EXIT_FAILURE;
+    }
+    return EXIT_SUCCESS;
+}

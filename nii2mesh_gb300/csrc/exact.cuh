@@ -1,0 +1,125 @@
+// exact.cuh — bit-exact evaluation of the reference's double-precision
+// 5-tap blur tap sum (src/meshify.c:170-216) using FP32 arithmetic.
+//
+// The reference evaluates, per pass and per voxel,
+//     s = ((((a*w2 + b*w1) + c*w0) + d*w1) + e*w2)      in IEEE double
+// (w0 = 0.45, w1 = 0.225, w2 = 0.05 as doubles) and stores (float)s.  GB300's
+// FP64 rate is a small fraction of its FP32 rate, so the fast path computes
+// the exact tap sum in double-float arithmetic (error-free TwoSum/TwoProd
+// transforms, ~2^-40 relative accuracy) and proves that the float rounding of
+// the reference's double result equals the float rounding of this estimate:
+// the estimate T = Th + Tl must be farther than a rigorous error bound from
+// every rounding boundary (midpoint between adjacent floats) of Th.  When the
+// proof fails (about 1 voxel in 10^5, plus zero/tiny/non-finite sums) the
+// voxel is recomputed with the reference's exact double operation sequence.
+// Either way the result equals the reference's float bit pattern.
+//
+// Written for both host and device so the arithmetic can be unit-tested on
+// the CPU (host builds must use -ffp-contract=off).
+#pragma once
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define N2M_HD __host__ __device__ __forceinline__
+#else
+#define N2M_HD static inline
+#endif
+
+#if defined(__CUDA_ARCH__)
+#define FADD(a, b) __fadd_rn((a), (b))
+#define FSUB(a, b) __fsub_rn((a), (b))
+#define FMUL(a, b) __fmul_rn((a), (b))
+#define FFMA(a, b, c) __fmaf_rn((a), (b), (c))
+#define DADD(a, b) __dadd_rn((a), (b))
+#define DMUL(a, b) __dmul_rn((a), (b))
+#define D2F(a) __double2float_rn(a)
+N2M_HD uint32_t f2u(float f) { return __float_as_uint(f); }
+N2M_HD float u2f(uint32_t u) { return __uint_as_float(u); }
+#else
+#define FADD(a, b) ((float)((a) + (b)))
+#define FSUB(a, b) ((float)((a) - (b)))
+#define FMUL(a, b) ((float)((a) * (b)))
+#define FFMA(a, b, c) fmaf((a), (b), (c))
+#define DADD(a, b) ((double)((a) + (b)))
+#define DMUL(a, b) ((double)((a) * (b)))
+#define D2F(a) ((float)(a))
+N2M_HD uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+N2M_HD float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+#endif
+
+// taps as doubles, and their double-float splits w = wH + wL (|err| < 2^-50 w)
+#define N2M_W0D 0.45
+#define N2M_W1D 0.225
+#define N2M_W2D 0.05
+#define N2M_W0H 0x1.cccccc0000000p-2f
+#define N2M_W0L 0x1.99999a0000000p-27f
+#define N2M_W2H 0x1.99999a0000000p-5f
+#define N2M_W2L (-0x1.99999a0000000p-31f)
+
+N2M_HD void two_sum(float a, float b, float &s, float &e) {
+    s = FADD(a, b);
+    float bb = FSUB(s, a);
+    e = FADD(FSUB(a, FSUB(s, bb)), FSUB(b, bb));
+}
+
+// The reference's operation sequence, verbatim in double.
+N2M_HD float tap5_double(float a, float b, float c, float d, float e) {
+    double s = DMUL((double)a, N2M_W2D);
+    s = DADD(s, DMUL((double)b, N2M_W1D));
+    s = DADD(s, DMUL((double)c, N2M_W0D));
+    s = DADD(s, DMUL((double)d, N2M_W1D));
+    s = DADD(s, DMUL((double)e, N2M_W2D));
+    return D2F(s);
+}
+
+// Fast path.  Returns true and writes *out when the float result is proven
+// equal to tap5_double(a..e).
+//   exact value E = w2*(a+e) + w0*(c + (b+d)/2)         (w1 == w0/2 exactly)
+N2M_HD bool tap5_fast(float a, float b, float c, float d, float e, float *out) {
+    float u, ue, v, ve, w, we;
+    two_sum(a, e, u, ue);
+    two_sum(b, d, v, ve);
+    v = FMUL(v, 0.5f);
+    ve = FMUL(ve, 0.5f);
+    two_sum(c, v, w, we);
+    we = FADD(we, ve);
+    const float p1 = FMUL(N2M_W2H, u), e1 = FFMA(N2M_W2H, u, -p1);
+    const float p2 = FMUL(N2M_W0H, w), e2 = FFMA(N2M_W0H, w, -p2);
+    float S, es;
+    two_sum(p1, p2, S, es);
+    float low = FFMA(N2M_W2H, ue, e1);
+    low = FFMA(N2M_W2L, u, low);
+    low = FFMA(N2M_W0H, we, low);
+    low = FFMA(N2M_W0L, w, low);
+    low = FADD(low, e2);
+    low = FADD(low, es);
+    float th, tl;
+    two_sum(S, low, th, tl);
+    // rigorous bound on |(th + tl) - reference double sum| (see header comment)
+    const float m = FFMA(N2M_W2H, FADD(fabsf(a), fabsf(e)),
+                         FMUL(N2M_W0H, FADD(fabsf(c), FMUL(0.5f, FADD(fabsf(b), fabsf(d))))));
+    if (m == 0.0f) {                                             // all taps +-0
+        *out = FADD(FADD(FADD(FADD(a, b), c), d), e);            // same signed zero
+        return true;
+    }
+    const float bound = FMUL(m, 0x1p-39f);
+    const float ath = fabsf(th);
+    if (!(ath >= 0x1p-100f && ath < 0x1p+120f)) return false;   // tiny, zero, huge, NaN
+    const float t = th < 0.0f ? -tl : tl;                        // offset away from zero
+    const uint32_t bits = f2u(ath);
+    const float up = FSUB(u2f(bits + 1u), ath);                  // exact gaps
+    const float dn = FSUB(ath, u2f(bits - 1u));
+    if (FADD(t, bound) < FMUL(0.5f, up) && FSUB(t, bound) > -FMUL(0.5f, dn)) {
+        *out = th;
+        return true;
+    }
+    return false;
+}
+
+N2M_HD float tap5_exact(float a, float b, float c, float d, float e) {
+    float r;
+    if (tap5_fast(a, b, c, d, e, &r)) return r;
+    return tap5_double(a, b, c, d, e);
+}

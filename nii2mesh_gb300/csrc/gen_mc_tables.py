@@ -102,10 +102,12 @@ def main():
         f.write(f"#define N2M_LUT_BLOB_SIZE {len(blob)}\n\n")
 
         def emit(ctype, name, vals, per=24):
-            f.write(f"static const {ctype} {name}[{len(vals)}] = {{\n")
+            # initializer as a macro so host code and __device__ arrays share it
+            f.write(f"#define {name.upper()}_INIT {{ \\\n")
             for i in range(0, len(vals), per):
-                f.write("  " + ",".join(str(v) for v in vals[i:i + per]) + ",\n")
-            f.write("};\n\n")
+                f.write("  " + ",".join(str(v) for v in vals[i:i + per]) + ", \\\n")
+            f.write("}\n")
+            f.write(f"static const {ctype} {name}[{len(vals)}] = {name.upper()}_INIT;\n\n")
         emit("signed char", "n2m_lut_blob", blob)
         emit("unsigned short", "n2m_classic_edge", edge, 16)
         emit("signed char", "n2m_classic_tri", tri, 16)

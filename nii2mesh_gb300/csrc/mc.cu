@@ -1,0 +1,512 @@
+// mc.cu — Lewiner MC33 marching cubes (src/MarchingCubes.c:116-1143) as two
+// passes over the padded bounding-box grid, plus the classic case table of
+// the same framework (-o 1).
+//
+// Numbering is the reference's: the edge vertices of grid point p (its +x,
+// +y, +z edges, in that order) come after those of every point before p in
+// raster order; c-vertices follow all edge vertices in cube raster order;
+// triangles are in cube raster order, tiling order within a cube.  So the
+// mesh is the reference's mesh before its weld, vertex for vertex.
+//
+// count pass: one thread per grid point; a warp covers 32 consecutive points
+//   (a "word").  Edge crossings are ballots (three 32-bit masks per word);
+//   triangle and c-vertex counts come from the cube's MC33 decision.
+// scan: exclusive scan over words -> vertex/triangle/c-vertex offsets.
+// emit pass: only words that own output recompute their cubes; an edge
+//   vertex id anywhere in the grid is offset(word) + popcounts of the word's
+//   masks below the lane, so every edge is emitted exactly once (this replaces
+//   the reference's vertex weld for shared edges).
+// Vertices whose final coordinates sit within 1.5e-5 of a grid point (edge
+// vertices) or of a grid plane (c-vertices) are recorded as weld candidates:
+// only such vertices can lie within the weld tolerance (1e-5) of another.
+#include <float.h>
+
+#include "mc_tables.h"
+#include "n2m_internal.cuh"
+
+namespace {
+__device__ const signed char d_lut[N2M_LUT_BLOB_SIZE] = N2M_LUT_BLOB_INIT;
+
+#define L1(T, a) ((int)d_lut[N2M_##T##_OFF + (a)])
+#define L2(T, a, b) ((int)d_lut[N2M_##T##_OFF + (a)*N2M_##T##_S0 + (b)])
+#define L3(T, a, b, c) ((int)d_lut[N2M_##T##_OFF + (a)*N2M_##T##_S0 + (b)*N2M_##T##_S1 + (c)])
+#define O2(T, a) (N2M_##T##_OFF + (a)*N2M_##T##_S0)
+#define O3(T, a, b) (N2M_##T##_OFF + (a)*N2M_##T##_S0 + (b)*N2M_##T##_S1)
+
+struct GV {  // device view of the padded grid
+    const float *vol;
+    int dx, dy, dz;
+    long long nvox, dxy;
+    int lo0, lo1, lo2, NX, NY, NZ;
+    unsigned NXY, NG;
+    float iso, edge_max, pad;
+};
+
+// value of grid point (x,y,z) minus isolevel, as marchingCubes() builds it
+// (src/MarchingCubes.c:1097-1115, incl. the row wrap past x = dim0-1), with
+// meshify's edge darkening (src/meshify.c:348-369) applied on the fly and
+// run()'s FLT_EPSILON clamp (src/MarchingCubes.c:131-132).
+__device__ __forceinline__ float gval(const GV &g, int x, int y, int z) {
+    const long long j = (long long)(g.lo0 + x) + (long long)(y + g.lo1) * g.dx + (long long)(z + g.lo2) * g.dxy;
+    float v;
+    if (j < g.nvox) {
+        v = __ldg(g.vol + j);
+        int vx = g.lo0 + x, vy = y + g.lo1, vz = z + g.lo2;
+        if (vx >= g.dx || vy >= g.dy) {
+            vz = (int)(j / g.dxy);
+            const long long r = j - (long long)vz * g.dxy;
+            vy = (int)(r / g.dx);
+            vx = (int)(r - (long long)vy * g.dx);
+        }
+        if (vx == 0 || vy == 0 || vz == 0 || vx == g.dx - 1 || vy == g.dy - 1 || vz == g.dz - 1)
+            v = fminf(g.edge_max, v);
+        v = __fsub_rn(v, g.iso);
+    } else {
+        v = g.pad;
+    }
+    if (fabsf(v) < N2M_FLT_EPS) v = N2M_FLT_EPS;
+    return v;
+}
+
+// ---- MC33 decisions (src/MarchingCubes.c:276-795) ---------------------------
+__device__ __forceinline__ bool test_face(const float *c, int face) {
+    float A = 0.f, B = 0.f, C = 0.f, D = 0.f;
+    switch (face < 0 ? -face : face) {
+    case 1: A = c[0]; B = c[4]; C = c[5]; D = c[1]; break;
+    case 2: A = c[1]; B = c[5]; C = c[6]; D = c[2]; break;
+    case 3: A = c[2]; B = c[6]; C = c[7]; D = c[3]; break;
+    case 4: A = c[3]; B = c[7]; C = c[4]; D = c[0]; break;
+    case 5: A = c[0]; B = c[3]; C = c[2]; D = c[1]; break;
+    case 6: A = c[4]; B = c[7]; C = c[6]; D = c[5]; break;
+    default: break;
+    }
+    const float det = __fsub_rn(__fmul_rn(A, C), __fmul_rn(B, D));
+    if (fabsf(det) < N2M_FLT_EPS) return face >= 0;
+    return __fmul_rn(__fmul_rn((float)face, A), det) >= 0.f;
+}
+
+__device__ __forceinline__ float lerp_t(const float *c, int a, int b, float t) {
+    return __fadd_rn(c[a], __fmul_rn(__fsub_rn(c[b], c[a]), t));
+}
+
+// reference edge of the interior test: t = c[p]/(c[p]-c[q]); Bt, Ct, Dt
+// interpolate three corner pairs (src/MarchingCubes.c:337-431)
+__constant__ signed char k_ie[12][8] = {
+    {0, 1, 3, 2, 7, 6, 4, 5}, {1, 2, 0, 3, 4, 7, 5, 6}, {2, 3, 1, 0, 5, 4, 6, 7}, {3, 0, 2, 1, 6, 5, 7, 4},
+    {4, 5, 7, 6, 3, 2, 0, 1}, {5, 6, 4, 7, 0, 3, 1, 2}, {6, 7, 5, 4, 1, 0, 2, 3}, {7, 4, 6, 5, 2, 1, 3, 0},
+    {0, 4, 3, 7, 2, 6, 1, 5}, {1, 5, 0, 4, 3, 7, 2, 6}, {2, 6, 1, 5, 0, 4, 3, 7}, {3, 7, 2, 6, 1, 5, 0, 4}};
+
+__device__ bool test_interior(const float *c, int kase, int config, int subconfig, int s) {
+    float At = 0.f, Bt = 0.f, Ct = 0.f, Dt = 0.f;
+    if (kase == 4 || kase == 10) {
+        const float d40 = __fsub_rn(c[4], c[0]), d62 = __fsub_rn(c[6], c[2]);
+        const float d73 = __fsub_rn(c[7], c[3]), d51 = __fsub_rn(c[5], c[1]);
+        const float a = __fsub_rn(__fmul_rn(d40, d62), __fmul_rn(d73, d51));
+        const float b = __fsub_rn(__fsub_rn(__fadd_rn(__fmul_rn(c[2], d40), __fmul_rn(c[0], d62)), __fmul_rn(c[1], d73)),
+                                  __fmul_rn(c[3], d51));
+        const float t = __fdiv_rn(-b, __fmul_rn(2.f, a));
+        if (t < 0.f || t > 1.f) return s > 0;
+        At = __fadd_rn(c[0], __fmul_rn(d40, t));
+        Bt = __fadd_rn(c[3], __fmul_rn(d73, t));
+        Ct = __fadd_rn(c[2], __fmul_rn(d62, t));
+        Dt = __fadd_rn(c[1], __fmul_rn(d51, t));
+    } else {
+        int edge = -1;
+        switch (kase) {
+        case 6: edge = L2(TEST6, config, 2); break;
+        case 7: edge = L2(TEST7, config, 4); break;
+        case 12: edge = L2(TEST12, config, 3); break;
+        case 13: edge = L3(TILING13_5_1, config, subconfig, 0); break;
+        default: break;
+        }
+        if (edge >= 0 && edge < 12) {
+            const signed char *e = k_ie[edge];
+            const float t = __fdiv_rn(c[e[0]], __fsub_rn(c[e[0]], c[e[1]]));
+            Bt = lerp_t(c, e[2], e[3], t);
+            Ct = lerp_t(c, e[4], e[5], t);
+            Dt = lerp_t(c, e[6], e[7], t);
+        }
+    }
+    const int test = (At >= 0.f) + 2 * (Bt >= 0.f) + 4 * (Ct >= 0.f) + 8 * (Dt >= 0.f);
+    const float det = __fsub_rn(__fmul_rn(At, Ct), __fmul_rn(Bt, Dt));
+    switch (test) {
+    case 5: if (det < N2M_FLT_EPS) return s > 0; break;
+    case 10: if (det >= N2M_FLT_EPS) return s > 0; break;
+    case 7: case 11: case 13: case 14: case 15: return s < 0;
+    default: return s > 0;
+    }
+    return s < 0;
+}
+
+struct Tiling {
+    int off;    // blob offset of 3*n edge codes
+    int n;      // triangles
+    bool cv;    // needs the c-vertex (code 12)
+};
+
+// process_cube's decision tree (src/MarchingCubes.c:458-795)
+__device__ Tiling select_tiling(const float *c, int lut, bool classic) {
+    Tiling T = {0, 0, false};
+    if (classic) {
+        T.off = O2(CASESCLASSIC, lut);
+        int n = 0;
+        while (n < 5 && d_lut[T.off + 3 * n] != -1) n++;
+        T.n = n;
+        return T;
+    }
+    const int kase = L2(CASES, lut, 0), cf = L2(CASES, lut, 1);
+    int sub = 0;
+    switch (kase) {
+    case 1: T = {O2(TILING1, cf), 1, false}; break;
+    case 2: T = {O2(TILING2, cf), 2, false}; break;
+    case 3:
+        T = test_face(c, L1(TEST3, cf)) ? Tiling{O2(TILING3_2, cf), 4, false} : Tiling{O2(TILING3_1, cf), 2, false};
+        break;
+    case 4:
+        T = test_interior(c, 4, cf, 0, L1(TEST4, cf)) ? Tiling{O2(TILING4_1, cf), 2, false}
+                                                       : Tiling{O2(TILING4_2, cf), 6, false};
+        break;
+    case 5: T = {O2(TILING5, cf), 3, false}; break;
+    case 6:
+        if (test_face(c, L2(TEST6, cf, 0))) T = {O2(TILING6_2, cf), 5, false};
+        else if (test_interior(c, 6, cf, 0, L2(TEST6, cf, 1))) T = {O2(TILING6_1_1, cf), 3, false};
+        else T = {O2(TILING6_1_2, cf), 9, true};
+        break;
+    case 7:
+        if (test_face(c, L2(TEST7, cf, 0))) sub += 1;
+        if (test_face(c, L2(TEST7, cf, 1))) sub += 2;
+        if (test_face(c, L2(TEST7, cf, 2))) sub += 4;
+        switch (sub) {
+        case 0: T = {O2(TILING7_1, cf), 3, false}; break;
+        case 1: T = {O3(TILING7_2, cf, 0), 5, false}; break;
+        case 2: T = {O3(TILING7_2, cf, 1), 5, false}; break;
+        case 3: T = {O3(TILING7_3, cf, 0), 9, true}; break;
+        case 4: T = {O3(TILING7_2, cf, 2), 5, false}; break;
+        case 5: T = {O3(TILING7_3, cf, 1), 9, true}; break;
+        case 6: T = {O3(TILING7_3, cf, 2), 9, true}; break;
+        default:
+            T = test_interior(c, 7, cf, 0, L2(TEST7, cf, 3)) ? Tiling{O2(TILING7_4_2, cf), 9, false}
+                                                              : Tiling{O2(TILING7_4_1, cf), 5, false};
+        }
+        break;
+    case 8: T = {O2(TILING8, cf), 2, false}; break;
+    case 9: T = {O2(TILING9, cf), 4, false}; break;
+    case 10:
+        if (test_face(c, L2(TEST10, cf, 0))) {
+            T = test_face(c, L2(TEST10, cf, 1)) ? Tiling{O2(TILING10_1_1_B, cf), 4, false}
+                                                : Tiling{O2(TILING10_2, cf), 8, true};
+        } else if (test_face(c, L2(TEST10, cf, 1))) {
+            T = {O2(TILING10_2_B, cf), 8, true};
+        } else {
+            T = test_interior(c, 10, cf, 0, L2(TEST10, cf, 2)) ? Tiling{O2(TILING10_1_1, cf), 4, false}
+                                                               : Tiling{O2(TILING10_1_2, cf), 8, false};
+        }
+        break;
+    case 11: T = {O2(TILING11, cf), 4, false}; break;
+    case 12:
+        if (test_face(c, L2(TEST12, cf, 0))) {
+            T = test_face(c, L2(TEST12, cf, 1)) ? Tiling{O2(TILING12_1_1_B, cf), 4, false}
+                                                : Tiling{O2(TILING12_2, cf), 8, true};
+        } else if (test_face(c, L2(TEST12, cf, 1))) {
+            T = {O2(TILING12_2_B, cf), 8, true};
+        } else {
+            T = test_interior(c, 12, cf, 0, L2(TEST12, cf, 2)) ? Tiling{O2(TILING12_1_1, cf), 4, false}
+                                                               : Tiling{O2(TILING12_1_2, cf), 8, false};
+        }
+        break;
+    case 13: {
+        for (int f = 0; f < 6; f++)
+            if (test_face(c, L2(TEST13, cf, f))) sub += 1 << f;
+        const int sc = L1(SUBCONFIG13, sub);
+        if (sc == 0) T = {O2(TILING13_1, cf), 4, false};
+        else if (sc >= 1 && sc <= 6) T = {O3(TILING13_2, cf, sc - 1), 6, false};
+        else if (sc >= 7 && sc <= 18) T = {O3(TILING13_3, cf, sc - 7), 10, true};
+        else if (sc >= 19 && sc <= 22) T = {O3(TILING13_4, cf, sc - 19), 12, true};
+        else if (sc >= 23 && sc <= 26)
+            T = test_interior(c, 13, cf, sc - 23, L2(TEST13, cf, 6)) ? Tiling{O3(TILING13_5_1, cf, sc - 23), 6, false}
+                                                                    : Tiling{O3(TILING13_5_2, cf, sc - 23), 10, false};
+        else if (sc >= 27 && sc <= 38) T = {O3(TILING13_3_B, cf, sc - 27), 10, true};
+        else if (sc >= 39 && sc <= 44) T = {O3(TILING13_2_B, cf, sc - 39), 6, false};
+        else if (sc == 45) T = {O2(TILING13_1_B, cf), 4, false};
+        break;
+    }
+    case 14: T = {O2(TILING14, cf), 4, false}; break;
+    default: break;
+    }
+    return T;
+}
+
+__device__ __forceinline__ void unravel(const GV &g, unsigned p, int &x, int &y, int &z) {
+    z = (int)(p / g.NXY);
+    const unsigned r = p - (unsigned)z * g.NXY;
+    y = (int)(r / (unsigned)g.NX);
+    x = (int)(r - (unsigned)y * (unsigned)g.NX);
+}
+
+// corner p of cube (x,y,z): x + ((p^(p>>1))&1), y + ((p>>1)&1), z + ((p>>2)&1)
+__device__ __forceinline__ void load_cube(const GV &g, int x, int y, int z, float *c) {
+    c[0] = gval(g, x, y, z);         c[1] = gval(g, x + 1, y, z);
+    c[2] = gval(g, x + 1, y + 1, z); c[3] = gval(g, x, y + 1, z);
+    c[4] = gval(g, x, y, z + 1);     c[5] = gval(g, x + 1, y, z + 1);
+    c[6] = gval(g, x + 1, y + 1, z + 1); c[7] = gval(g, x, y + 1, z + 1);
+}
+
+__device__ __forceinline__ int cube_lut(const float *c) {
+    int lut = 0;
+    for (int p = 0; p < 8; p++) lut |= (c[p] > 0.f) << p;
+    return lut;
+}
+
+// per-point classification shared by both passes
+struct PointInfo {
+    bool in, ex, ey, ez, cube;
+    int x, y, z;
+    float c[8];
+};
+
+__device__ __forceinline__ void classify(const GV &g, unsigned p, PointInfo &pi) {
+    pi.in = p < g.NG;
+    pi.ex = pi.ey = pi.ez = pi.cube = false;
+    if (!pi.in) return;
+    unravel(g, p, pi.x, pi.y, pi.z);
+    const bool hx = pi.x < g.NX - 1, hy = pi.y < g.NY - 1, hz = pi.z < g.NZ - 1;
+    pi.c[0] = gval(g, pi.x, pi.y, pi.z);
+    if (hx && hy && hz) {
+        pi.cube = true;
+        pi.c[1] = gval(g, pi.x + 1, pi.y, pi.z);
+        pi.c[2] = gval(g, pi.x + 1, pi.y + 1, pi.z);
+        pi.c[3] = gval(g, pi.x, pi.y + 1, pi.z);
+        pi.c[4] = gval(g, pi.x, pi.y, pi.z + 1);
+        pi.c[5] = gval(g, pi.x + 1, pi.y, pi.z + 1);
+        pi.c[6] = gval(g, pi.x + 1, pi.y + 1, pi.z + 1);
+        pi.c[7] = gval(g, pi.x, pi.y + 1, pi.z + 1);
+    } else {
+        pi.c[1] = hx ? gval(g, pi.x + 1, pi.y, pi.z) : pi.c[0];
+        pi.c[3] = hy ? gval(g, pi.x, pi.y + 1, pi.z) : pi.c[0];
+        pi.c[4] = hz ? gval(g, pi.x, pi.y, pi.z + 1) : pi.c[0];
+    }
+    const bool s0 = pi.c[0] > 0.f;
+    pi.ex = hx && ((pi.c[1] > 0.f) != s0);
+    pi.ey = hy && ((pi.c[3] > 0.f) != s0);
+    pi.ez = hz && ((pi.c[4] > 0.f) != s0);
+}
+
+__global__ void __launch_bounds__(256) k_count(GV g, bool classic, uint4 *words, uint4 *counts) {
+    const unsigned p = blockIdx.x * 256u + threadIdx.x;
+    PointInfo pi;
+    classify(g, p, pi);
+    int nt = 0, nc = 0;
+    if (pi.cube) {
+        const int lut = cube_lut(pi.c);
+        if (lut != 0 && lut != 255) {
+            const Tiling T = select_tiling(pi.c, lut, classic);
+            nt = T.n;
+            nc = T.cv;
+        }
+    }
+    const unsigned xm = __ballot_sync(0xffffffffu, pi.ex), ym = __ballot_sync(0xffffffffu, pi.ey),
+                   zm = __ballot_sync(0xffffffffu, pi.ez);
+    for (int o = 16; o; o >>= 1) {
+        nt += __shfl_xor_sync(0xffffffffu, nt, o);
+        nc += __shfl_xor_sync(0xffffffffu, nc, o);
+    }
+    const unsigned w = p >> 5;
+    if ((threadIdx.x & 31) == 0 && w * 32u < g.NG) {
+        words[w] = make_uint4(xm, ym, zm, 0u);
+        counts[w] = make_uint4(__popc(xm) + __popc(ym) + __popc(zm), (unsigned)nt, (unsigned)nc, 0u);
+    }
+}
+
+// id of the vertex on the `axis` edge of grid point q (must exist)
+__device__ __forceinline__ int vid(const uint4 *__restrict__ words, const uint4 *__restrict__ offs, unsigned q,
+                                   int axis) {
+    const unsigned w = q >> 5, l = q & 31u;
+    const uint4 m = words[w];
+    const unsigned lt = (1u << l) - 1u;
+    unsigned id = offs[w].x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt);
+    if (axis >= 1) id += (m.x >> l) & 1u;
+    if (axis == 2) id += (m.y >> l) & 1u;
+    return (int)id;
+}
+
+__device__ __forceinline__ float frac_dist(float f) { return fabsf(f - rintf(f)); }
+
+// local position of cube edge e (edge numbering of the tiling tables):
+// owner corner, axis, and the two corners it interpolates
+__constant__ signed char k_edge[12][4] = {{0, 0, 0, 1}, {1, 1, 1, 2}, {3, 0, 3, 2}, {0, 1, 0, 3},
+                                         {4, 0, 4, 5}, {5, 1, 5, 6}, {7, 0, 7, 6}, {4, 1, 4, 7},
+                                         {0, 2, 0, 4}, {1, 2, 1, 5}, {2, 2, 2, 6}, {3, 2, 3, 7}};
+
+__device__ __forceinline__ float edge_u(float c0, float c1) {
+    const float den = __fsub_rn(c0, c1);
+    return den != 0.f ? __fdiv_rn(c0, den) : 0.5f;
+}
+
+__global__ void __launch_bounds__(256) k_emit(GV g, bool classic, const uint4 *__restrict__ words,
+                                              const uint4 *__restrict__ offs, uint4 totals, vec3d *pts,
+                                              vec3i *tris, int *cand, unsigned *ncand, int *ccand,
+                                              unsigned *nccand, int cap) {
+    const unsigned p = blockIdx.x * 256u + threadIdx.x;
+    const unsigned w = p >> 5, lane = threadIdx.x & 31u;
+    const unsigned nwords = (g.NG + 31u) >> 5;
+    if (w >= nwords) return;  // whole warp
+    const uint4 o = offs[w];
+    const uint4 on = (w + 1 < nwords) ? offs[w + 1] : totals;
+    const uint4 m = words[w];
+    if ((m.x | m.y | m.z) == 0u && on.y == o.y && on.z == o.z) return;  // whole warp: nothing to emit
+    PointInfo pi;
+    classify(g, p, pi);
+    const float flo0 = (float)g.lo0, flo1 = (float)g.lo1, flo2 = (float)g.lo2;
+    // ---- edge vertices owned by this point (src/MarchingCubes.c:935-1026)
+    if (pi.ex | pi.ey | pi.ez) {
+        const unsigned lt = (1u << lane) - 1u;
+        int id = (int)(o.x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt));
+        const float fx = (float)pi.x, fy = (float)pi.y, fz = (float)pi.z;
+        if (pi.ex) {
+            const float X = __fadd_rn(__fadd_rn(fx, edge_u(pi.c[0], pi.c[1])), flo0);
+            pts[id] = {(double)X, (double)__fadd_rn(fy, flo1), (double)__fadd_rn(fz, flo2)};
+            if (frac_dist(X) < 1.5e-5f) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
+            id++;
+        }
+        if (pi.ey) {
+            const float Y = __fadd_rn(__fadd_rn(fy, edge_u(pi.c[0], pi.c[3])), flo1);
+            pts[id] = {(double)__fadd_rn(fx, flo0), (double)Y, (double)__fadd_rn(fz, flo2)};
+            if (frac_dist(Y) < 1.5e-5f) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
+            id++;
+        }
+        if (pi.ez) {
+            const float Z = __fadd_rn(__fadd_rn(fz, edge_u(pi.c[0], pi.c[4])), flo2);
+            pts[id] = {(double)__fadd_rn(fx, flo0), (double)__fadd_rn(fy, flo1), (double)Z};
+            if (frac_dist(Z) < 1.5e-5f) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
+        }
+    }
+    // ---- cube triangles
+    Tiling T = {0, 0, false};
+    if (pi.cube) {
+        const int lut = cube_lut(pi.c);
+        if (lut != 0 && lut != 255) T = select_tiling(pi.c, lut, classic);
+    }
+    int tb = T.n, cb = T.cv;  // warp exclusive scans
+    for (int d = 1; d < 32; d <<= 1) {
+        const int a = __shfl_up_sync(0xffffffffu, tb, d), b = __shfl_up_sync(0xffffffffu, cb, d);
+        if ((int)lane >= d) { tb += a; cb += b; }
+    }
+    tb -= T.n;
+    cb -= T.cv;
+    if (T.n == 0) return;
+    int v12 = -1;
+    if (T.cv) {  // c-vertex: mean of the cube's edge vertices (src/MarchingCubes.c:1029-1082)
+        v12 = (int)(totals.x + o.z + cb);
+        float n = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+        for (int e = 0; e < 12; e++) {
+            const int own = k_edge[e][0], ax = k_edge[e][1], ca = k_edge[e][2], cbn = k_edge[e][3];
+            if ((pi.c[ca] > 0.f) == (pi.c[cbn] > 0.f)) continue;
+            const float u = edge_u(pi.c[ca], pi.c[cbn]);
+            float px = (float)(pi.x + ((own ^ (own >> 1)) & 1)), py = (float)(pi.y + ((own >> 1) & 1)),
+                  pz = (float)(pi.z + ((own >> 2) & 1));
+            if (ax == 0) px = __fadd_rn(px, u);
+            else if (ax == 1) py = __fadd_rn(py, u);
+            else pz = __fadd_rn(pz, u);
+            n = __fadd_rn(n, 1.f);
+            sx = __fadd_rn(sx, px); sy = __fadd_rn(sy, py); sz = __fadd_rn(sz, pz);
+        }
+        if (n > 0.f) { sx = __fdiv_rn(sx, n); sy = __fdiv_rn(sy, n); sz = __fdiv_rn(sz, n); }
+        const float X = __fadd_rn(sx, flo0), Y = __fadd_rn(sy, flo1), Z = __fadd_rn(sz, flo2);
+        pts[v12] = {(double)X, (double)Y, (double)Z};
+        if (fminf(frac_dist(X), fminf(frac_dist(Y), frac_dist(Z))) < 1.5e-5f) {
+            unsigned k = atomicAdd(nccand, 1u);
+            if (k < (unsigned)cap) ccand[k] = v12;
+        }
+    }
+    // ---- triangles, stored reversed (v3,v2,v1) as marchingCubes() returns them
+    const unsigned NX = (unsigned)g.NX, NXY = g.NXY;
+    int tv[3];
+    for (int t = 0; t < 3 * T.n; t++) {
+        const int code = d_lut[T.off + t];
+        int v;
+        switch (code) {
+        case 0: v = vid(words, offs, p, 0); break;
+        case 1: v = vid(words, offs, p + 1, 1); break;
+        case 2: v = vid(words, offs, p + NX, 0); break;
+        case 3: v = vid(words, offs, p, 1); break;
+        case 4: v = vid(words, offs, p + NXY, 0); break;
+        case 5: v = vid(words, offs, p + NXY + 1, 1); break;
+        case 6: v = vid(words, offs, p + NXY + NX, 0); break;
+        case 7: v = vid(words, offs, p + NXY, 1); break;
+        case 8: v = vid(words, offs, p, 2); break;
+        case 9: v = vid(words, offs, p + 1, 2); break;
+        case 10: v = vid(words, offs, p + NX + 1, 2); break;
+        case 11: v = vid(words, offs, p + NX, 2); break;
+        case 12: v = v12; break;
+        default: v = -1; break;
+        }
+        tv[t % 3] = v;
+        if (t % 3 == 2) tris[o.y + tb + t / 3] = {tv[2], tv[1], tv[0]};
+    }
+}
+
+// vertices within 1.5e-5 of a c-vertex candidate become weld candidates too
+__global__ void k_ccand(const vec3d *__restrict__ pts, int np, const int *__restrict__ cc, int ncc, int *cand,
+                        unsigned *ncand, int cap) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const vec3d a = pts[i];
+        for (int k = 0; k < ncc; k++) {
+            const int j = cc[k];
+            if (j == i) continue;
+            const vec3d b = pts[j];
+            const double dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+            if (fabs(dx) < 1.5e-5 && fabs(dy) < 1.5e-5 && fabs(dz) < 1.5e-5) {
+                unsigned q = atomicAdd(ncand, 1u);
+                if (q < (unsigned)cap) cand[q] = i;
+                break;
+            }
+        }
+    }
+}
+
+GV make_gv(const McGrid &g) {
+    GV v;
+    v.vol = g.vol;
+    v.dx = g.dim[0]; v.dy = g.dim[1]; v.dz = g.dim[2];
+    v.dxy = (long long)g.dim[0] * g.dim[1];
+    v.nvox = v.dxy * g.dim[2];
+    v.lo0 = g.lo[0]; v.lo1 = g.lo[1]; v.lo2 = g.lo[2];
+    v.NX = g.n[0]; v.NY = g.n[1]; v.NZ = g.n[2];
+    v.NXY = (unsigned)g.n[0] * (unsigned)g.n[1];
+    v.NG = v.NXY * (unsigned)g.n[2];
+    v.iso = g.iso; v.edge_max = g.edge_max; v.pad = g.pad_val;
+    return v;
+}
+}  // namespace
+
+n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s) {
+    const GV v = make_gv(g);
+    const size_t nwords = ((size_t)v.NG + 31) / 32;
+    CKS(w.words.ensure(nwords * sizeof(uint4)));
+    CKS(w.counts.ensure(nwords * sizeof(uint4)));
+    const unsigned blocks = (unsigned)(((size_t)v.NG + 255) / 256);
+    k_count<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, w.words.as<uint4>(), w.counts.as<uint4>());
+    CKL();
+    return scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s);
+}
+
+n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,
+                   int *d_cand, unsigned *d_ncand, int cand_cap, cudaStream_t s) {
+    const GV v = make_gv(g);
+    const unsigned blocks = (unsigned)(((size_t)v.NG + 255) / 256);
+    // c-vertex candidates live after the edge candidates' slot range
+    k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, w.words.as<uint4>(), w.counts.as<uint4>(),
+                                  make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand,
+                                  d_cand + cand_cap, d_ncand + 1, cand_cap);
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status mc_ccand_scan(const vec3d *d_pts, int np, const int *d_ccand, int nccand, int *d_cand,
+                         unsigned *d_ncand, int cand_cap, cudaStream_t s) {
+    if (nccand <= 0) return N2M_OK;
+    const int blocks = (np + 255) / 256 < 4096 ? (np + 255) / 256 : 4096;
+    k_ccand<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(d_pts, np, d_ccand, nccand, d_cand, d_ncand, cand_cap);
+    CKL();
+    return N2M_OK;
+}

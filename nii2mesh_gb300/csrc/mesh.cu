@@ -1,0 +1,347 @@
+// mesh.cu — per-mesh stages after marching cubes:
+//   * weld fix-up (src/meshify.c:45-106): applies the merges the host decided
+//     for the few near-grid-point candidates (vertex compaction + remap);
+//   * remove_degenerate_triangles (src/meshify.c:113-168): FP32 area filter
+//     with a rigorous error margin, the reference's FP64 predicate for the
+//     rest, stable compaction;
+//   * laplacian_smoothHC (src/quadric.c:316-394): CSR gather kernels in FP32
+//     on displacements from the original positions (HC is affine-equivariant);
+//     border vertices (update_mesh(0), src/quadric.c:184-212) keep their input;
+//   * apply_sform (src/meshify.c:1021-1045).
+#include <float.h>
+
+#include "n2m_internal.cuh"
+
+namespace {
+// ---- weld -------------------------------------------------------------------
+__device__ __forceinline__ int lower_bound(const int *a, int n, int v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int m = (lo + hi) >> 1;
+        if (a[m] < v) lo = m + 1;
+        else hi = m;
+    }
+    return lo;
+}
+
+// removed[k] (sorted) merges into keep[k]; override ids (sorted) take pos.
+__global__ void k_weld_verts(const vec3d *__restrict__ in, int np, const int *__restrict__ removed, int nrem,
+                             const int *__restrict__ ov_id, const vec3d *__restrict__ ov_pos, int nov,
+                             vec3d *__restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int r = lower_bound(removed, nrem, i);
+        if (r < nrem && removed[r] == i) continue;
+        const int o = lower_bound(ov_id, nov, i);
+        out[i - r] = (o < nov && ov_id[o] == i) ? ov_pos[o] : in[i];
+    }
+}
+
+__global__ void k_weld_tris(vec3i *t, int nt, const int *__restrict__ removed, const int *__restrict__ keep,
+                            int nrem) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+        int v[3] = {t[i].x, t[i].y, t[i].z};
+        for (int k = 0; k < 3; k++) {
+            int r = lower_bound(removed, nrem, v[k]);
+            if (r < nrem && removed[r] == v[k]) {
+                v[k] = keep[r];
+                r = lower_bound(removed, nrem, v[k]);
+            }
+            v[k] -= r;
+        }
+        t[i] = {v[0], v[1], v[2]};
+    }
+}
+
+// ---- degenerate triangles --------------------------------------------------------
+__device__ __forceinline__ double dist_d(vec3d a, vec3d b) {
+    const double dx = __dsub_rn(a.x, b.x), dy = __dsub_rn(a.y, b.y), dz = __dsub_rn(a.z, b.z);
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+}
+
+// the reference predicate, operation for operation (src/meshify.c:119-144)
+__device__ bool degenerate_ref(vec3d A, vec3d B, vec3d C) {
+    const double l = dist_d(A, B), m = dist_d(A, C), n = dist_d(B, C);
+    const double c = fmin(fmin(l, m), n), a = fmax(fmax(l, m), n);
+    const double b = __dsub_rn(__dsub_rn(__dadd_rn(__dadd_rn(l, m), n), a), c);
+    const double cab = __dsub_rn(c, __dsub_rn(a, b));
+    if (cab <= 0.0) return true;
+    const double q = __dmul_rn(__dmul_rn(__dmul_rn(__dadd_rn(a, __dadd_rn(b, c)), cab), __dadd_rn(c, __dsub_rn(a, b))),
+                               __dadd_rn(a, __dsub_rn(b, c)));
+    return __dmul_rn(0.25, __dsqrt_rn(q)) < (double)FLT_EPSILON;
+}
+
+// True iff the triangle is degenerate under the reference predicate.  Fast
+// path: the area from an FP32 cross product of (double) edge vectors, minus a
+// bound on its rounding error, exceeding 4e-7 (> 3x FLT_EPSILON) proves the
+// triangle is kept.
+__device__ __forceinline__ bool degenerate(vec3d A, vec3d B, vec3d C) {
+    const float ux = (float)(B.x - A.x), uy = (float)(B.y - A.y), uz = (float)(B.z - A.z);
+    const float vx = (float)(C.x - A.x), vy = (float)(C.y - A.y), vz = (float)(C.z - A.z);
+    const float cx = uy * vz - uz * vy, cy = uz * vx - ux * vz, cz = ux * vy - uy * vx;
+    const float cr = sqrtf(cx * cx + cy * cy + cz * cz);
+    const float nu = sqrtf(ux * ux + uy * uy + uz * uz), nv = sqrtf(vx * vx + vy * vy + vz * vz);
+    if (0.5f * (cr - 1e-6f * nu * nv) > 4e-7f && isfinite(cr)) return false;
+    return degenerate_ref(A, B, C);
+}
+
+constexpr int CB = 256;   // compaction tile = one CTA
+
+__global__ void __launch_bounds__(CB) k_deg_count(const vec3d *__restrict__ p, const vec3i *__restrict__ t, int nt,
+                                                  unsigned *keep, unsigned *tile_cnt) {
+    const int i = blockIdx.x * CB + threadIdx.x;
+    unsigned k = 0;
+    if (i < nt) {
+        const vec3i T = t[i];
+        k = !degenerate(p[T.x], p[T.y], p[T.z]);
+        keep[i] = k;
+    }
+    k = __syncthreads_count(k);
+    if (threadIdx.x == 0) tile_cnt[blockIdx.x] = k;
+}
+
+__global__ void __launch_bounds__(CB) k_deg_compact(const vec3i *__restrict__ t, int nt, const unsigned *keep,
+                                                    const unsigned *tile_off, vec3i *out) {
+    __shared__ unsigned wcnt[CB / 32];
+    const int i = blockIdx.x * CB + threadIdx.x;
+    const unsigned k = i < nt ? keep[i] : 0u;
+    const unsigned b = __ballot_sync(0xffffffffu, k);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) wcnt[wid] = __popc(b);
+    __syncthreads();
+    unsigned off = tile_off[blockIdx.x];
+    for (int w = 0; w < wid; w++) off += wcnt[w];
+    if (k) out[off + __popc(b & ((1u << lane) - 1u))] = t[i];
+}
+
+// ---- HC smoothing ----------------------------------------------------------------
+__global__ void k_degree(const vec3i *__restrict__ t, int nt, unsigned *deg) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+        atomicAdd(&deg[t[i].x], 1u);
+        atomicAdd(&deg[t[i].y], 1u);
+        atomicAdd(&deg[t[i].z], 1u);
+    }
+}
+
+__global__ void k_fill_refs(const vec3i *__restrict__ t, int nt, const unsigned *__restrict__ start, unsigned *fill,
+                            int *refs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+        const int v[3] = {t[i].x, t[i].y, t[i].z};
+        for (int s = 0; s < 3; s++) refs[start[v[s]] + atomicAdd(&fill[v[s]], 1u)] = 3 * i + s;
+    }
+}
+
+// order each vertex's (triangle, slot) references as the reference visits them
+__global__ void k_sort_refs(const unsigned *__restrict__ start, int np, int *refs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int a = (int)start[i], b = (int)start[i + 1];
+        for (int k = a + 1; k < b; k++) {
+            const int v = refs[k];
+            int j = k - 1;
+            while (j >= a && refs[j] > v) { refs[j + 1] = refs[j]; j--; }
+            refs[j + 1] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ void others(const vec3i *t, int ref, int &a, int &b) {
+    const vec3i T = t[ref / 3];
+    const int s = ref % 3;
+    a = s == 0 ? T.y : T.x;
+    b = s == 2 ? T.y : T.z;
+}
+
+// Lo = L(o) - o in double (once), original positions o kept in double
+__global__ void k_hc_init(const vec3d *__restrict__ o, const vec3i *__restrict__ t, const unsigned *__restrict__ start,
+                          const int *__restrict__ refs, int np, float3 *Lo, float3 *P, unsigned char *hasnb) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int a0 = (int)start[i], a1 = (int)start[i + 1];
+        P[i] = make_float3(0.f, 0.f, 0.f);
+        hasnb[i] = a1 > a0;
+        if (a1 == a0) { Lo[i] = make_float3(0.f, 0.f, 0.f); continue; }
+        double sx = 0, sy = 0, sz = 0;
+        for (int k = a0; k < a1; k++) {
+            int a, b;
+            others(t, refs[k], a, b);
+            sx += o[a].x + o[b].x; sy += o[a].y + o[b].y; sz += o[a].z + o[b].z;
+        }
+        const double n = 2.0 * (a1 - a0);
+        Lo[i] = make_float3((float)(sx / n - o[i].x), (float)(sy / n - o[i].y), (float)(sz / n - o[i].z));
+    }
+}
+
+__device__ __forceinline__ float3 lap(const float3 *__restrict__ X, const vec3i *__restrict__ t,
+                                      const int *__restrict__ refs, int a0, int a1) {
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int k = a0; k < a1; k++) {
+        int a, b;
+        others(t, refs[k], a, b);
+        const float3 A = X[a], B = X[b];
+        sx += A.x + B.x; sy += A.y + B.y; sz += A.z + B.z;
+    }
+    const float inv = 1.f / (2.f * (float)(a1 - a0));
+    return make_float3(sx * inv, sy * inv, sz * inv);
+}
+
+// first half of an HC iteration: Pn = L(p) - o, B = Pn - (1-alpha) Q
+__global__ void k_hc_a(const float3 *__restrict__ P, const float3 *__restrict__ Lo, const vec3i *__restrict__ t,
+                       const unsigned *__restrict__ start, const int *__restrict__ refs,
+                       const unsigned char *__restrict__ hasnb, int np, float alpha1, float3 *Pn, float3 *B) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const float3 q = P[i];
+        float3 pn = q;
+        if (hasnb[i]) {
+            const float3 l = lap(P, t, refs, (int)start[i], (int)start[i + 1]);
+            const float3 lo = Lo[i];
+            pn = make_float3(lo.x + l.x, lo.y + l.y, lo.z + l.z);
+        }
+        Pn[i] = pn;
+        B[i] = make_float3(pn.x - alpha1 * q.x, pn.y - alpha1 * q.y, pn.z - alpha1 * q.z);
+    }
+}
+
+// second half: P = Pn - (beta B + (1-beta) L(B))
+__global__ void k_hc_b(const float3 *__restrict__ Pn, const float3 *__restrict__ B, const vec3i *__restrict__ t,
+                       const unsigned *__restrict__ start, const int *__restrict__ refs,
+                       const unsigned char *__restrict__ hasnb, int np, float beta, float beta1, float3 *P) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const float3 b = B[i];
+        float3 lb = b;
+        if (hasnb[i]) lb = lap(B, t, refs, (int)start[i], (int)start[i + 1]);
+        const float3 pn = Pn[i];
+        P[i] = make_float3(pn.x - (beta * b.x + beta1 * lb.x), pn.y - (beta * b.y + beta1 * lb.y),
+                           pn.z - (beta * b.z + beta1 * lb.z));
+    }
+}
+
+// border flags: an id seen exactly once among a vertex's incident triangles
+__global__ void k_border(const vec3i *__restrict__ t, const unsigned *__restrict__ start, const int *__restrict__ refs,
+                         int np, unsigned char *border) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int a0 = (int)start[i], a1 = (int)start[i + 1];
+        for (int k = a0; k < a1; k++) {
+            const vec3i T = t[refs[k] / 3];
+            const int cand[3] = {T.x, T.y, T.z};
+            for (int c = 0; c < 3; c++) {
+                const int id = cand[c];
+                int cnt = 0;
+                for (int k2 = a0; k2 < a1 && cnt < 2; k2++) {
+                    const vec3i U = t[refs[k2] / 3];
+                    cnt += (U.x == id) + (U.y == id) + (U.z == id);
+                }
+                if (cnt == 1) border[id] = 1;
+            }
+        }
+    }
+}
+
+__global__ void k_hc_out(vec3d *o, const float3 *__restrict__ P, const unsigned char *__restrict__ border, int np,
+                         bool lock) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        if (lock && border[i]) continue;
+        const float3 d = P[i];
+        o[i].x += (double)d.x; o[i].y += (double)d.y; o[i].z += (double)d.z;
+    }
+}
+
+__global__ void k_sform(vec3d *p, int np, double a0, double a1, double a2, double a3, double b0, double b1, double b2,
+                        double b3, double c0, double c1, double c2, double c3) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const vec3d v = p[i];
+        p[i].x = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v.x, a0), __dmul_rn(v.y, a1)), __dmul_rn(v.z, a2)), a3);
+        p[i].y = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v.x, b0), __dmul_rn(v.y, b1)), __dmul_rn(v.z, b2)), b3);
+        p[i].z = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v.x, c0), __dmul_rn(v.y, c1)), __dmul_rn(v.z, c2)), c3);
+    }
+}
+
+__global__ void k_flip(vec3i *t, int nt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+        const int x = t[i].x;
+        t[i].x = t[i].y;
+        t[i].y = x;
+    }
+}
+
+inline unsigned gs(size_t n) {
+    size_t b = (n + 255) / 256;
+    if (b > 152 * 32) b = 152 * 32;
+    return b ? (unsigned)b : 1u;
+}
+}  // namespace
+
+n2m_status mesh_apply_weld(vec3d *d_pts, vec3i *d_tris, int np, int nt, const int *d_removed, const int *d_keep,
+                           int nrem, const int *d_ov_id, const vec3d *d_ov_pos, int nov, vec3d *d_out,
+                           cudaStream_t s) {
+    k_weld_verts<<<gs(np), 256, 0, s>>>(d_pts, np, d_removed, nrem, d_ov_id, d_ov_pos, nov, d_out);
+    k_weld_tris<<<gs(nt), 256, 0, s>>>(d_tris, nt, d_removed, d_keep, nrem);
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status mesh_remove_degenerate(const vec3d *d_pts, const vec3i *d_tris_in, int nt, vec3i *d_tris_out,
+                                  unsigned *d_nt_out, DegWork &w, ScanWork &sw, cudaStream_t s) {
+    const int tiles = (nt + CB - 1) / CB;
+    if (nt == 0) {
+        CK(cudaMemsetAsync(d_nt_out, 0, sizeof(unsigned), s));
+        return N2M_OK;
+    }
+    CKS(w.flags.ensure((size_t)nt * sizeof(unsigned)));
+    CKS(w.tmp.ensure((size_t)tiles * sizeof(unsigned)));
+    k_deg_count<<<tiles, CB, 0, s>>>(d_pts, d_tris_in, nt, w.flags.as<unsigned>(), w.tmp.as<unsigned>());
+    CKL();
+    CKS(scan_u32(w.tmp.as<unsigned>(), tiles, d_nt_out, sw, s));
+    k_deg_compact<<<tiles, CB, 0, s>>>(d_tris_in, nt, w.flags.as<unsigned>(), w.tmp.as<unsigned>(), d_tris_out);
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status mesh_smooth_hc(vec3d *d_pts, const vec3i *d_tris, int np, int nt, double alpha, double beta, int iter,
+                          bool lock_edges, HcWork &w, ScanWork &sw, cudaStream_t s) {
+    if (np <= 0 || iter <= 0) return N2M_OK;
+    CKS(w.start.ensure(((size_t)np + 1) * sizeof(unsigned)));
+    CKS(w.fill.ensure((size_t)np * sizeof(unsigned)));
+    CKS(w.refs.ensure((size_t)3 * (nt > 0 ? nt : 1) * sizeof(int)));
+    CKS(w.P.ensure((size_t)np * sizeof(float3)));
+    CKS(w.Q.ensure((size_t)np * sizeof(float3)));
+    CKS(w.B.ensure((size_t)np * sizeof(float3)));
+    CKS(w.Lo.ensure((size_t)np * sizeof(float3)));
+    CKS(w.hasnb.ensure((size_t)np));
+    CKS(w.border.ensure((size_t)np));
+    unsigned *start = w.start.as<unsigned>();
+    CK(cudaMemsetAsync(start, 0, ((size_t)np + 1) * sizeof(unsigned), s));
+    CK(cudaMemsetAsync(w.fill.p, 0, (size_t)np * sizeof(unsigned), s));
+    k_degree<<<gs(nt), 256, 0, s>>>(d_tris, nt, start);
+    CKL();
+    CKS(scan_u32(start, (size_t)np + 1, start + np + 0, sw, s));  // start[np] receives the total as well
+    k_fill_refs<<<gs(nt), 256, 0, s>>>(d_tris, nt, start, w.fill.as<unsigned>(), w.refs.as<int>());
+    k_sort_refs<<<gs(np), 256, 0, s>>>(start, np, w.refs.as<int>());
+    k_hc_init<<<gs(np), 256, 0, s>>>(d_pts, d_tris, start, w.refs.as<int>(), np, w.Lo.as<float3>(), w.P.as<float3>(),
+                                     w.hasnb.as<unsigned char>());
+    CKL();
+    const float a1 = (float)(1.0 - alpha), b = (float)beta, b1 = (float)(1.0 - beta);
+    for (int it = 0; it < iter; it++) {
+        k_hc_a<<<gs(np), 256, 0, s>>>(w.P.as<float3>(), w.Lo.as<float3>(), d_tris, start, w.refs.as<int>(),
+                                      w.hasnb.as<unsigned char>(), np, a1, w.Q.as<float3>(), w.B.as<float3>());
+        k_hc_b<<<gs(np), 256, 0, s>>>(w.Q.as<float3>(), w.B.as<float3>(), d_tris, start, w.refs.as<int>(),
+                                      w.hasnb.as<unsigned char>(), np, b, b1, w.P.as<float3>());
+    }
+    CKL();
+    if (lock_edges) {
+        CK(cudaMemsetAsync(w.border.p, 0, (size_t)np, s));
+        k_border<<<gs(np), 256, 0, s>>>(d_tris, start, w.refs.as<int>(), np, w.border.as<unsigned char>());
+    }
+    k_hc_out<<<gs(np), 256, 0, s>>>(d_pts, w.P.as<float3>(), w.border.as<unsigned char>(), np, lock_edges);
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status mesh_apply_sform(vec3d *d_pts, vec3i *d_tris, int np, int nt, const float sx[4], const float sy[4],
+                            const float sz[4], cudaStream_t s) {
+    k_sform<<<gs(np), 256, 0, s>>>(d_pts, np, sx[0], sx[1], sx[2], sx[3], sy[0], sy[1], sy[2], sy[3], sz[0], sz[1],
+                                   sz[2], sz[3]);
+    const double px = (double)(sx[0] + sx[1] + sx[2]), py = (double)(sy[0] + sy[1] + sy[2]),
+                 pz = (double)(sz[0] + sz[1] + sz[2]);
+    const float det = (float)(px * py * pz);
+    if (det < 0.0) k_flip<<<gs(nt), 256, 0, s>>>(d_tris, nt);
+    CKL();
+    return N2M_OK;
+}

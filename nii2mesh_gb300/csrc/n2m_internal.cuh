@@ -1,0 +1,130 @@
+// n2m_internal.cuh — shared declarations of the CUDA implementation.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "../../include/n2m_gpu.h"
+
+#define N2M_FLT_EPS 1.19209290e-07f
+
+// ---- error plumbing ---------------------------------------------------------
+void n2m_set_error(const char *fmt, ...);
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            n2m_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return e_ == cudaErrorMemoryAllocation ? N2M_ERR_OOM : N2M_ERR_CUDA;          \
+        }                                                                                 \
+    } while (0)
+#define CKS(st)                                   \
+    do {                                          \
+        n2m_status s_ = (st);                     \
+        if (s_ != N2M_OK) return s_;              \
+    } while (0)
+#define CKL()  CK(cudaGetLastError())
+
+// ---- grow-only device buffers -----------------------------------------------
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    n2m_status ensure(size_t bytes);
+    void release();
+    template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+// ---- ordered-int encoding of floats for atomicMin/atomicMax ------------------
+__device__ __forceinline__ int f2ord(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__host__ __device__ __forceinline__ float ord2f(int i) {
+    int j = i >= 0 ? i : i ^ 0x7fffffff;
+#ifdef __CUDA_ARCH__
+    return __int_as_float(j);
+#else
+    float f;
+    memcpy(&f, &j, 4);
+    return f;
+#endif
+}
+
+// Reductions produced by the volume passes (device-resident, read back once).
+struct VolStats {
+    int vmin, vmax;          // ordered-int min/max of the volume
+    int lo[3], hi[3];        // bbox of voxels >= iso (unpadded, inclusive)
+    unsigned nonfinite;      // NaN/Inf voxels
+    unsigned pad;
+};
+
+// ---- kernels' host launchers (stream-ordered, no syncs) ----------------------
+// smooth.cu
+n2m_status launch_smooth(const float *in, float *out, int nx, int ny, int nz, float iso, VolStats *st,
+                         cudaStream_t s);
+n2m_status launch_stats(const float *vol, int nx, int ny, int nz, float iso, bool minmax, VolStats *st,
+                        cudaStream_t s);
+void stats_init_host(VolStats *h);
+
+// scan.cu: exclusive scan of uint4 (component-wise) in place; total -> *d_total
+struct ScanWork {
+    DevBuf part;
+};
+n2m_status scan_uint4(uint4 *d, size_t n, uint4 *d_total, ScanWork &w, cudaStream_t s);
+n2m_status scan_u32(unsigned *d, size_t n, unsigned *d_total, ScanWork &w, cudaStream_t s);
+
+// label.cu
+struct LabelWork {
+    DevBuf lab, mask, keep, cnt, edge, misc;
+};
+n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn, bool only_largest,
+                         bool fill_bubbles, LabelWork &w, cudaStream_t s);
+// bwlabel() semantics on a float volume (nonzero = foreground); *d_nl gets the label count
+n2m_status run_bwlabel(float *vol, int nx, int ny, int nz, int conn, bool only_largest, bool fill_bubbles,
+                       LabelWork &w, ScanWork &sw, int *d_nl, cudaStream_t s);
+
+// mc.cu
+struct McGrid {
+    const float *vol;        // processed volume (before edge darkening)
+    int dim[3];              // volume dims
+    int lo[3];               // grid origin in the volume
+    int n[3];                // grid size (NX, NY, NZ)
+    float iso, edge_max, pad_val;   // pad_val = float(min' - iso)
+};
+struct McWork {
+    DevBuf words, counts, cand, verts_tmp, tris_tmp;
+};
+struct McCounts {
+    unsigned nv_edge, nt, nc;
+};
+n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s);
+n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,
+                   int *d_cand, unsigned *d_ncand, int cand_cap, cudaStream_t s);
+n2m_status mc_ccand_scan(const vec3d *d_pts, int np, const int *d_ccand, int nccand, int *d_cand,
+                         unsigned *d_ncand, int cand_cap, cudaStream_t s);
+
+// oldcubes.cu
+n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
+                    McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s);
+n2m_status oc_emit(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
+                   McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris, int *d_cand, unsigned *d_ncand,
+                   int cand_cap, long long *d_lastuse, cudaStream_t s);
+
+// mesh.cu
+n2m_status mesh_apply_weld(vec3d *d_pts, vec3i *d_tris, int np, int nt, const int *d_removed, const int *d_keep,
+                           int nrem, const int *d_ov_id, const vec3d *d_ov_pos, int nov, vec3d *d_out,
+                           cudaStream_t s);
+struct DegWork {
+    DevBuf flags, tmp;
+};
+n2m_status mesh_remove_degenerate(const vec3d *d_pts, const vec3i *d_tris_in, int nt, vec3i *d_tris_out,
+                                  unsigned *d_nt_out, DegWork &w, ScanWork &sw, cudaStream_t s);
+struct HcWork {
+    DevBuf start, refs, fill, P, Q, B, Lo, border, hasnb;
+};
+n2m_status mesh_smooth_hc(vec3d *d_pts, const vec3i *d_tris, int np, int nt, double alpha, double beta, int iter,
+                          bool lock_edges, HcWork &w, ScanWork &sw, cudaStream_t s);
+n2m_status mesh_apply_sform(vec3d *d_pts, vec3i *d_tris, int np, int nt, const float sx[4], const float sy[4],
+                            const float sz[4], cudaStream_t s);

@@ -1,0 +1,124 @@
+"""GPU parity of meshify (src/meshify.c:286-389) against the oracle.
+
+Every case runs the CUDA path through the C ABI and the CPU oracle on the same
+seeded input.  The bar: identical vertex and triangle counts, identical
+triangle connectivity after canonical sorting, vertex positions bit-identical
+(tolerance 0.0; the path reproduces the reference's float arithmetic).
+"""
+import numpy as np
+import pytest
+
+from nii2mesh_gb300 import synth
+from oracle.oracle import MC33, MC_CLASSIC_TABLE, OLDCUBES, mesh_equal
+
+pytestmark = pytest.mark.gpu
+
+POS_TOL = 0.0   # raw vertices are bit-exact (spec bar: 1e-5 voxels)
+
+
+def small_spheres(seed=10, n=48):
+    return synth.spheres(n=n, count=6, rmin=5, rmax=11, cmin=10, cmax=n - 10, seed=seed)
+
+
+def run_both(gpu, oracle, vol, iso, variant, smooth, largest, bubbles):
+    got = gpu.meshify(vol, iso, original_mc=1 if variant == MC_CLASSIC_TABLE else 0, pre_smooth=smooth,
+                      only_largest=largest, fill_bubbles=bubbles, oldcubes=variant == OLDCUBES)
+    want = oracle.meshify(vol, iso, variant, smooth, largest, bubbles)
+    return got, want
+
+
+@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE, OLDCUBES])
+@pytest.mark.parametrize("flags", [(True, True, False), (True, False, False), (False, False, False),
+                                   (True, True, True), (False, True, True), (True, False, True)])
+def test_spheres_all_options(gpu, oracle, variant, flags):
+    vol = small_spheres()
+    got, want = run_both(gpu, oracle, vol, 50.0, variant, *flags)
+    assert want is not None and got is not None
+    ok, d, msg = mesh_equal(got, want, POS_TOL)
+    assert ok, msg
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_sphere64_config(gpu, oracle, seed):
+    """the 64^3 workload (-p 1 -l 1 -b 0 -o 0)"""
+    vol = synth.spheres(seed=seed)
+    got, want = run_both(gpu, oracle, vol, 50.0, MC33, True, True, False)
+    ok, d, msg = mesh_equal(got, want, POS_TOL)
+    assert ok, msg
+
+
+@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE])
+def test_ct_like(gpu, oracle, variant):
+    """CT-like values (negative background, salt noise), iso 300, no clustering"""
+    vol = synth.ct512(seed=5, n=96, count=12)
+    got, want = run_both(gpu, oracle, vol, 300.0, variant, True, False, False)
+    ok, d, msg = mesh_equal(got, want, POS_TOL)
+    assert ok, msg
+
+
+def test_brain_u8(gpu, oracle):
+    """brain-sized u8 volume, Otsu iso, -p 1 -l 1 -b 1, both cube tables"""
+    vol = synth.brain().astype(np.float32)
+    iso = oracle.set_threshold(vol, 2)
+    for variant in (MC33, MC_CLASSIC_TABLE):
+        got, want = run_both(gpu, oracle, vol, iso, variant, True, True, True)
+        ok, d, msg = mesh_equal(got, want, POS_TOL)
+        assert ok, msg
+
+
+def test_selftest_fields_meshify(gpu, oracle):
+    """the reference's analytic self-test fields through the whole pipeline"""
+    for obj in range(10):
+        f = oracle.selftest_field(obj)
+        for variant in (MC33, MC_CLASSIC_TABLE):
+            got, want = run_both(gpu, oracle, f, 0.001, variant, False, False, False)
+            if want is None:
+                assert got is None
+                continue
+            ok, d, msg = mesh_equal(got, want, POS_TOL)
+            assert ok, f"object {obj} variant {variant}: {msg}"
+
+
+def test_iso_out_of_range(gpu, oracle):
+    vol = small_spheres()
+    for iso in (-1e6, 1e6, float(vol.max()) + 1):
+        got, want = run_both(gpu, oracle, vol, iso, MC33, True, True, False)
+        ok, d, msg = mesh_equal(got, want, POS_TOL)
+        assert ok, msg
+
+
+def test_failures(gpu, oracle):
+    flat = np.full((16, 16, 16), 3.0, np.float32)
+    assert gpu.meshify(flat, 1.0) is None
+    assert oracle.meshify(flat, 1.0) is None
+
+
+def test_small_dims_skip_smoothing(gpu, oracle):
+    vol = small_spheres()[:4, :, :].copy()   # nz < 5: the reference skips the pre-smooth
+    got, want = run_both(gpu, oracle, vol, 50.0, MC33, True, False, False)
+    ok, d, msg = mesh_equal(got, want, POS_TOL)
+    assert ok, msg
+
+
+def test_ragged_dims(gpu, oracle):
+    rng = np.random.default_rng(7)
+    for shape in ((37, 5, 61), (5, 33, 7), (70, 19, 33)):
+        vol = (rng.random(shape) * 100).astype(np.float32)
+        got, want = run_both(gpu, oracle, vol, 50.0, MC33, True, False, False)
+        if want is None:
+            assert got is None
+            continue
+        ok, d, msg = mesh_equal(got, want, POS_TOL)
+        assert ok, f"{shape}: {msg}"
+
+
+def test_bbox_touches_volume_faces(gpu, oracle):
+    """bright voxels on the faces exercise the padded grid and its row wrap"""
+    rng = np.random.default_rng(3)
+    vol = rng.normal(0, 1, (20, 24, 28)).astype(np.float32)
+    vol[:, :, -3:] += 10
+    vol[-2:, :, :] += 10
+    for variant in (MC33, OLDCUBES):
+        got, want = run_both(gpu, oracle, vol, 4.0, variant, True, False, False)
+        ok, d, msg = mesh_equal(got, want, POS_TOL)
+        assert ok, msg
