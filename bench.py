@@ -1,0 +1,249 @@
+#!/usr/bin/env python3
+"""Benchmark: meshify (smooth + marching cubes + weld) of the 512^3 CT-like
+workload on GB300, in Gvox/s.
+
+Workload: 512^3 float32, background N(-1000,20), 300 ellipsoidal structures,
+1% salt noise at +2000, iso 300, -p 1 -l 0 -b 0 -o 0 (Lewiner MC33) -r 1 -s 0.
+A step = one full meshify of that volume (pre-smooth, range, bbox, marching
+cubes count + emit, weld, degenerate removal) with the volume resident in HBM
+(537 MB > 129 MB L2, so no L2 flush is needed between steps).  `e2e` measures
+the same through the C ABI with host buffers: the volume is copied from pinned
+host memory and the mesh (vec3d/vec3i) copied back every step.
+
+--impl reference times the reference algorithm on the host cores: the CPU
+oracle port (the reference's C path restated), or the reference itself when
+oracle/_ref was built on this machine.
+
+Multi-GPU: the path does not shard across GPUs in this build (replicas only):
+each rank meshes its own copy and `value` counts the voxels of all ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gvox/s smooth+MC+weld at 512³; atlas meshes/s batched vs loop; fwd+bwd ms @128³"
+WORKLOAD = "ct512: 512^3 f32 CT-like, iso 300, -p 1 -l 0 -b 0 -o 0 -r 1 -s 0 (Lewiner MC33)"
+ISO = 300.0
+# DRAM bytes per launch of the dominant kernel from the committed ncu capture
+# (profiles/ summary of the same workload); None until captured.
+NCU_TRAFFIC = {}
+# algorithmic bytes per stage (per unit): see DESIGN.md "Roofline"
+STAGE_NAMES = ("smooth", "cluster", "count", "emit", "weld", "degenerate", "hc")
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.proc, self.file = index, None, None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for n, v in zip(names, r[4:8]):
+                    if "Active" in v and "Not" not in v:
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n):
+    import torch
+    if n <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl", init_method="env://")
+    return rank, world, dist
+
+
+def cpu_reference(vol, steps, warmup):
+    """Time the reference algorithm on the host (one thread: meshify is serial)."""
+    from oracle.oracle import Oracle, Reference, reference_available
+    if reference_available():
+        impl, kind = Reference(False), "reference"
+    else:
+        impl, kind = Oracle(), "port"
+    times = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        m = impl.meshify(vol, ISO, 0, True, False, False)
+        t1 = time.perf_counter()
+        if i >= warmup:
+            times.append(t1 - t0)
+    assert m is not None
+    nvox = vol.size
+    return nvox / statistics.median(times) / 1e9, kind, times, len(m[0])
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    a = ap.parse_args()
+    warmup = max(a.warmup, 3)
+    import numpy as np
+    from nii2mesh_gb300 import synth
+
+    rank, world, dist = (0, 1, None)
+    if a.impl == "reference":
+        if a.gpus > 1 and int(os.environ.get("RANK", "0")) != 0:
+            return
+        vol = synth.ct512()
+        steps = max(1, min(a.steps, 3))
+        gv, kind, times, nt = cpu_reference(vol, steps, 1)
+        line = {"metric": METRIC, "value": round(gv, 6), "unit": "Gvox/s", "n_gpus": a.gpus, "steps": steps,
+                "warmup": 1, "ms_per_step": round(1e3 * statistics.median(times), 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+                "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"}, "impl": "reference",
+                "cpu_baseline": {"value": round(gv, 6), "unit": "Gvox/s", "cores": 1, "kind": kind,
+                                 "sample": "full 512^3 volume per step (meshify is single-threaded)"},
+                "e2e": {"value": round(gv, 6), "unit": "Gvox/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    import nii2mesh_gb300 as n2m
+    rank, world, dist = dist_setup(a.gpus)
+    dev = torch.cuda.current_device()
+    vol = synth.ct512()
+    nx = ny = nz = 512
+    nvox = vol.size
+    d_vol = torch.from_numpy(vol).to(f"cuda:{dev}")
+    ctx = n2m.Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+
+    def step():
+        return ctx.meshify_device(d_vol.data_ptr(), (nx, ny, nz), ISO, n2m.MC33, True, False, False)
+
+    for _ in range(warmup):
+        step()
+    reps = []
+    clocks = Clocks(dev)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(a.steps):
+        reps.append(step()[4])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    if dist:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nvox / (ms * 1e-3) / 1e9
+    nt, nv = reps[-1]["ntri"], reps[-1]["nvert"]
+    launches = sum(r["kernel_launches"] for r in reps)
+    stage_ms = [statistics.mean(r["ms_stage"][i] for r in reps) for i in range(7)]
+
+    # roofline of the dominant stage (algorithmic bytes / CUDA-event duration)
+    lo, hi = reps[-1]["lo"], reps[-1]["hi"]
+    ngrid = (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1)
+    algo = {"smooth": 8.0 * nvox, "count": 4.0 * ngrid,
+            "emit": 24.0 * reps[-1]["nvert_raw"] + 12.0 * reps[-1]["ntri_raw"],
+            "degenerate": 24.0 * reps[-1]["ntri_raw"]}
+    top = max(range(7), key=lambda i: stage_ms[i])
+    name = STAGE_NAMES[top]
+    peak, peak_kind = peaks()
+    roof = None
+    if name in algo:
+        ach = algo[name] / (stage_ms[top] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel_stage": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                "algorithmic_bytes": algo[name], "traffic": NCU_TRAFFIC.get(name)}
+
+    # e2e through the C ABI with host buffers (pinned input, mesh copied back)
+    pinned = torch.from_numpy(vol).pin_memory().numpy()
+    for _ in range(2):
+        ctx.meshify(pinned, ISO, n2m.MC33, True, False, False)
+    e2e_t = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        tris, pts, _ = ctx.meshify(pinned, ISO, n2m.MC33, True, False, False)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = statistics.median(e2e_t) * 1e3
+    if dist:
+        t = torch.tensor([e2e_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": round(world * nvox / (e2e_ms * 1e-3) / 1e9, 4), "unit": "Gvox/s",
+           "h2d_bytes_per_step": 4 * nvox, "d2h_bytes_per_step": 24 * len(pts) + 12 * len(tris),
+           "ms_per_step": round(e2e_ms, 3)}
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1:
+        gv, kind, times, _ = cpu_reference(vol, 1, 0)
+        cpu = {"value": round(gv, 6), "unit": "Gvox/s", "cores": 1, "kind": kind,
+               "sample": f"one full 512^3 meshify ({times[0]:.1f} s)"}
+    line = {"metric": METRIC, "value": round(value, 4), "unit": "Gvox/s", "n_gpus": world, "steps": a.steps,
+            "warmup": warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD, "l2": "inputs larger than L2 (537 MB volume)",
+                       "parallelism": "replicas" if world > 1 else "single GPU", "triangles": nt, "vertices": nv},
+            "stage_ms": {n: round(v, 4) for n, v in zip(STAGE_NAMES, stage_ms)},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

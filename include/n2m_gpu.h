@@ -70,6 +70,12 @@ typedef struct {
     int welded;              /* vertices merged by the weld */
     int degenerate;          /* triangles removed */
     float ms_total;          /* device time of the call (CUDA events) */
+    /* device time per stage (CUDA events on the context stream):
+     * [0] pre-smooth kernel (or the range pass), [1] clustering + range/bbox,
+     * [2] marching-cubes count pass + scan, [3] emit pass, [4] weld,
+     * [5] degenerate removal, [6] HC post-smoothing, [7] unused */
+    float ms_stage[8];
+    int64_t kernel_launches; /* kernels this call launched */
 } n2m_report;
 
 /* ---- context ------------------------------------------------------------ */
@@ -82,6 +88,7 @@ void *n2m_context_stream(n2m_context *ctx);          /* cudaStream_t */
 const char *n2m_last_error(void);                    /* per-thread message */
 const char *n2m_status_string(int status);
 int n2m_device_count(void);
+long long n2m_kernel_launches(void);                 /* process-wide kernel launch counter */
 
 /* ---- drop-in entry points ------------------------------------------------ */
 /* replaces meshify() (src/meshify.h:9).  originalMC: 0 = Lewiner MC33,
@@ -100,8 +107,6 @@ int marchingCubes(float *img, short dim[3], int lo[3], int hi[3], int originalMC
 int bwlabel(float *img, int conn, size_t dim[3], bool onlyLargest, bool fillBubbles);
 /* replaces apply_sform() (src/meshify.h:10). */
 void apply_sform(vec3i *t, vec3d *p, int nt, int np, float srow_x[4], float srow_y[4], float srow_z[4]);
-/* replaces setThreshold() (src/isolevel.h:9). */
-float setThreshold(float *img, int nvox, int darkMediumBright123);
 /* Mirrors the USE_CLASSIC_CUBES build flag for the drop-in marchingCubes()
  * and meshify(): nonzero selects Bourke's oldcubes. Returns the old value. */
 int n2m_set_oldcubes(int enable);

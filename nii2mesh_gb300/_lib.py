@@ -17,7 +17,8 @@ STATUS = ["ok", "no CUDA device", "CUDA error", "out of memory", "bad arguments"
 # exported symbols (the C-ABI contract; tests check that every one is present)
 SYMBOLS = ["n2m_context_create", "n2m_context_destroy", "n2m_context_stream", "n2m_last_error",
            "n2m_status_string", "n2m_device_count", "meshify", "laplacian_smoothHC", "marchingCubes", "bwlabel",
-           "apply_sform", "n2m_set_oldcubes", "n2m_meshify", "n2m_meshify_device", "n2m_smooth_hc_device"]
+           "apply_sform", "n2m_set_oldcubes", "n2m_meshify", "n2m_meshify_device", "n2m_smooth_hc_device",
+           "n2m_kernel_launches"]
 
 
 class vec3d(C.Structure):
@@ -36,10 +37,13 @@ class Options(C.Structure):
 class Report(C.Structure):
     _fields_ = [("isolevel_used", C.c_float), ("vmin", C.c_float), ("vmax", C.c_float), ("lo", C.c_int * 3),
                 ("hi", C.c_int * 3), ("nvert_raw", C.c_int64), ("ntri_raw", C.c_int64), ("nvert", C.c_int64),
-                ("ntri", C.c_int64), ("welded", C.c_int), ("degenerate", C.c_int), ("ms_total", C.c_float)]
+                ("ntri", C.c_int64), ("welded", C.c_int), ("degenerate", C.c_int), ("ms_total", C.c_float),
+                ("ms_stage", C.c_float * 8), ("kernel_launches", C.c_int64)]
+    STAGES = ("smooth", "cluster", "count", "emit", "weld", "degenerate", "hc", "unused")
 
     def as_dict(self):
-        return {f: (list(getattr(self, f)) if f in ("lo", "hi") else getattr(self, f)) for f, _ in self._fields_}
+        return {f: (list(getattr(self, f)) if f in ("lo", "hi", "ms_stage") else getattr(self, f))
+                for f, _ in self._fields_}
 
 
 _lib = None
@@ -77,6 +81,7 @@ def load(path=None):
     L.n2m_meshify.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip, C.POINTER(Report)]
     L.n2m_meshify_device.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip,
                                      C.POINTER(Report)]
+    L.n2m_kernel_launches.restype = C.c_longlong
     L.n2m_smooth_hc_device.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_bool]
     libc = C.CDLL(None)
     libc.free.argtypes = [vp]

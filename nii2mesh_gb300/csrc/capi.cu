@@ -20,8 +20,11 @@
 
 #include "n2m_internal.cuh"
 
-// ---- errors ---------------------------------------------------------------------
+// ---- errors, counters -------------------------------------------------------------
 static thread_local char g_err[512] = "";
+std::atomic<long long> g_n2m_launches{0};
+
+extern "C" long long n2m_kernel_launches(void) { return g_n2m_launches.load(); }
 
 void n2m_set_error(const char *fmt, ...) {
     va_list ap;
@@ -65,6 +68,7 @@ struct n2m_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t evs[8] = {};   // stage boundaries of the last pipeline run
     DevBuf in, vol, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath, hmesh;
     McWork mc;
     ScanWork scan;
@@ -102,6 +106,11 @@ extern "C" n2m_status n2m_context_create(n2m_context **out, int device) {
         delete c;
         return N2M_ERR_CUDA;
     }
+    for (int i = 0; i < 8; i++)
+        if (cudaEventCreate(&c->evs[i]) != cudaSuccess) {
+            n2m_set_error("event creation failed");
+            return N2M_ERR_CUDA;
+        }
     *out = c;
     return N2M_OK;
 }
@@ -118,6 +127,8 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb};
     for (DevBuf *b : bufs) b->release();
     if (c->pinned) cudaFreeHost(c->pinned);
+    for (int i = 0; i < 8; i++)
+        if (c->evs[i]) cudaEventDestroy(c->evs[i]);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -194,8 +205,8 @@ n2m_status weld_candidates(n2m_context *c, int nv, int ncand, bool oldcubes, std
     int *dids = (int *)(dpos + n);
     long long *dlu = (long long *)(dids + n + (n & 1));
     CK(cudaMemcpyAsync(dids, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    k_gather<<<(n + 255) / 256, 256, 0, c->stream>>>(c->pts_raw.as<vec3d>(), dids, n, dpos,
-                                                     oldcubes ? c->lastuse.as<long long>() : nullptr, dlu);
+    { k_gather<<<(n + 255) / 256, 256, 0, c->stream>>>(c->pts_raw.as<vec3d>(), dids, n, dpos,
+                                                     oldcubes ? c->lastuse.as<long long>() : nullptr, dlu); N2M_COUNT(); }
     CKL();
     std::vector<vec3d> pos(n);
     std::vector<long long> order(n);
@@ -294,12 +305,11 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
         CKS(c->vol.ensure(n * sizeof(float)));
         vol = c->vol.as<float>();
     }
-    if (smooth) {
-        CKS(launch_smooth(d_src, vol, nx, ny, nz, iso, dst, c->stream));
-    } else {
-        if (label) CK(cudaMemcpyAsync(vol, d_src, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
-        CKS(launch_stats(label ? vol : d_src, nx, ny, nz, iso, true, dst, c->stream));
-    }
+    if (!smooth && label) CK(cudaMemcpyAsync(vol, d_src, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaEventRecord(c->evs[0], c->stream));
+    if (smooth) CKS(launch_smooth(d_src, vol, nx, ny, nz, iso, dst, c->stream));
+    else CKS(launch_stats(label ? vol : d_src, nx, ny, nz, iso, true, dst, c->stream));
+    CK(cudaEventRecord(c->evs[1], c->stream));
     const float *v = vol ? vol : d_src;
     VolStats s0;
     CKS(readback(c, &s0, dst));
@@ -331,6 +341,7 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
         CKS(launch_stats(v, nx, ny, nz, iso, false, dst + 1, c->stream));
         CKS(readback(c, &s1, dst + 1));
     }
+    CK(cudaEventRecord(c->evs[2], c->stream));
     if (s1.lo[0] > s1.hi[0]) {
         n2m_set_error("no voxel at or above the isolevel");
         return N2M_ERR_EMPTY;
@@ -378,6 +389,7 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
     uint4 *dtot = c->totals.as<uint4>();
     if (old) CKS(oc_count(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->scan, dtot, c->stream));
     else CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream));
+    CK(cudaEventRecord(c->evs[3], c->stream));
     uint4 tot;
     CKS(readback(c, &tot, dtot));
     const unsigned long long nv = (unsigned long long)tot.x + tot.z, nt = tot.y;
@@ -399,7 +411,7 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
     McCounts mcn{tot.x, tot.y, tot.z};
     if (old) {
         CKS(c->lastuse.ensure(nv * sizeof(long long)));
-        k_fill_ll<<<1024, 256, 0, c->stream>>>(c->lastuse.as<long long>(), nv, -1);
+        { k_fill_ll<<<1024, 256, 0, c->stream>>>(c->lastuse.as<long long>(), nv, -1); N2M_COUNT(); }
         CKS(oc_emit(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, mcn, c->pts_raw.as<vec3d>(),
                     c->tris_raw.as<vec3i>(), c->cand.as<int>(), c->ncand.as<unsigned>(), cap,
                     c->lastuse.as<long long>(), c->stream));
@@ -426,6 +438,7 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
             return N2M_ERR_INTERNAL;
         }
     }
+    CK(cudaEventRecord(c->evs[4], c->stream));
     *nv_out = (int)nv;
     *nt_out = (int)nt;
     *ncand_out = (int)nc[0];
@@ -442,6 +455,7 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
         n2m_set_error("volume exceeds 2^31-1 voxels");
         return N2M_ERR_TOO_LARGE;
     }
+    const long long launches0 = g_n2m_launches.load();
     CK(cudaEventRecord(c->ev0, c->stream));
     Prep P;
     CKS(prepare(c, d_src, dim, o, o.verbose, P, rep));
@@ -481,6 +495,7 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
             CK(cudaStreamSynchronize(c->stream));   // host vectors go out of scope
         }
     }
+    CK(cudaEventRecord(c->evs[5], c->stream));
     if (np < 3) {
         n2m_set_error("fewer than 3 vertices after the weld");
         return N2M_ERR_EMPTY;
@@ -489,6 +504,7 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     CKS(c->ntf.ensure(sizeof(unsigned)));
     CKS(mesh_remove_degenerate(pts, c->tris_raw.as<vec3i>(), nt, c->tris.as<vec3i>(), c->ntf.as<unsigned>(), c->deg,
                                c->scan, c->stream));
+    CK(cudaEventRecord(c->evs[6], c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
     unsigned ntf;
     CKS(readback(c, &ntf, c->ntf.p));
@@ -511,6 +527,12 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
         rep->welded = welded;
         rep->degenerate = nt - (int)ntf;
         rep->ms_total = ms;
+        for (int i = 0; i < 6; i++) {
+            rep->ms_stage[i] = 0.f;
+            cudaEventElapsedTime(&rep->ms_stage[i], c->evs[i], c->evs[i + 1]);
+        }
+        rep->ms_stage[6] = rep->ms_stage[7] = 0.f;
+        rep->kernel_launches = g_n2m_launches.load() - launches0;
     }
     return N2M_OK;
 }
@@ -547,9 +569,18 @@ extern "C" n2m_status n2m_meshify_device(n2m_context *c, const float *d_img, con
     if (!c || !opt || !dim) return N2M_ERR_BAD_ARGS;
     CK(cudaSetDevice(c->device));
     CKS(pipeline(c, d_img, dim, *opt, rep));
-    if (opt->post_smooth > 0)
+    if (opt->post_smooth > 0) {
+        const long long l0 = g_n2m_launches.load();
+        CK(cudaEventRecord(c->evs[6], c->stream));
         CKS(mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc,
                            c->scan, c->stream));
+        CK(cudaEventRecord(c->evs[7], c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (rep) {
+            cudaEventElapsedTime(&rep->ms_stage[6], c->evs[6], c->evs[7]);
+            rep->kernel_launches += g_n2m_launches.load() - l0;
+        }
+    }
     CK(cudaStreamSynchronize(c->stream));
     if (d_t) *d_t = c->res_tris;
     if (d_p) *d_p = c->res_pts;

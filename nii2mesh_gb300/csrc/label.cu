@@ -194,10 +194,10 @@ inline unsigned gsz(long long n) {
 
 n2m_status components(LabelWork &w, Dims d, unsigned char want, int conn, unsigned *d_nroots, cudaStream_t s) {
     int *L = w.lab.as<int>();
-    k_uf_init<<<gsz(d.n), 256, 0, s>>>(w.mask.as<unsigned char>(), d.n, want, L);
-    k_uf_merge<<<gsz(d.n), 256, 0, s>>>(L, d, conn == 6 ? 3 : conn == 18 ? 9 : 13);
+    { k_uf_init<<<gsz(d.n), 256, 0, s>>>(w.mask.as<unsigned char>(), d.n, want, L); N2M_COUNT(); }
+    { k_uf_merge<<<gsz(d.n), 256, 0, s>>>(L, d, conn == 6 ? 3 : conn == 18 ? 9 : 13); N2M_COUNT(); }
     if (d_nroots) CK(cudaMemsetAsync(d_nroots, 0, sizeof(unsigned), s));
-    k_uf_flatten<<<gsz(d.n), 256, 0, s>>>(L, d.n, d_nroots);
+    { k_uf_flatten<<<gsz(d.n), 256, 0, s>>>(L, d.n, d_nroots); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
@@ -219,22 +219,22 @@ n2m_status label_core(LabelWork &w, Dims d, int conn, bool only_largest, bool fi
         CKS(w.edge.ensure((size_t)d.n));
         CKS(components(w, d, 0, 6, &misc->nbg, s));
         CK(cudaMemsetAsync(w.edge.p, 0, (size_t)d.n, s));
-        k_edge_roots<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d, w.edge.as<unsigned char>());
-        k_fill_bubbles<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, w.edge.as<unsigned char>(), &misc->nbg,
-                                                w.mask.as<unsigned char>());
+        { k_edge_roots<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d, w.edge.as<unsigned char>()); N2M_COUNT(); }
+        { k_fill_bubbles<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, w.edge.as<unsigned char>(), &misc->nbg,
+                                                w.mask.as<unsigned char>()); N2M_COUNT(); }
         CKL();
     }
     CKS(components(w, d, 1, conn, &misc->nfg, s));
     if (only_largest) {
         CKS(w.cnt.ensure((size_t)d.n * sizeof(unsigned)));
         CK(cudaMemsetAsync(w.cnt.p, 0, (size_t)d.n * sizeof(unsigned), s));
-        k_sizes<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, w.cnt.as<unsigned>());
-        k_best<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), w.cnt.as<unsigned>(), d.n, &misc->best);
-        k_keep_best<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, &misc->best, w.keep.as<unsigned char>());
+        { k_sizes<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, w.cnt.as<unsigned>()); N2M_COUNT(); }
+        { k_best<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), w.cnt.as<unsigned>(), d.n, &misc->best); N2M_COUNT(); }
+        { k_keep_best<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, &misc->best, w.keep.as<unsigned char>()); N2M_COUNT(); }
     } else {
         CK(cudaMemcpyAsync(w.keep.p, w.mask.p, (size_t)d.n, cudaMemcpyDeviceToDevice, s));
     }
-    k_nl_from<<<1, 1, 0, s>>>(&misc->nfg, &misc->best, only_largest, &misc->nl);
+    { k_nl_from<<<1, 1, 0, s>>>(&misc->nfg, &misc->best, only_largest, &misc->nl); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
@@ -248,11 +248,11 @@ n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn
         return N2M_ERR_TOO_LARGE;
     }
     CKS(w.mask.ensure((size_t)d.n));
-    k_mask<<<gsz(d.n), 256, 0, s>>>(vol, d.n, iso, w.mask.as<unsigned char>());
+    { k_mask<<<gsz(d.n), 256, 0, s>>>(vol, d.n, iso, w.mask.as<unsigned char>()); N2M_COUNT(); }
     CKL();
     CKS(label_core(w, d, 18, only_largest, fill_bubbles, s));
-    if (fill_bubbles) k_fill_iso<<<gsz(d.n), 256, 0, s>>>(vol, d.n, w.keep.as<unsigned char>(), iso);
-    if (only_largest) k_dilate_maskout<<<gsz(d.n), 256, 0, s>>>(w.keep.as<unsigned char>(), d, vol, mn);
+    if (fill_bubbles) { k_fill_iso<<<gsz(d.n), 256, 0, s>>>(vol, d.n, w.keep.as<unsigned char>(), iso); N2M_COUNT(); }
+    if (only_largest) { k_dilate_maskout<<<gsz(d.n), 256, 0, s>>>(w.keep.as<unsigned char>(), d, vol, mn); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
@@ -265,19 +265,19 @@ n2m_status run_bwlabel(float *vol, int nx, int ny, int nz, int conn, bool only_l
         return N2M_ERR_TOO_LARGE;
     }
     CKS(w.mask.ensure((size_t)d.n));
-    k_nonzero<<<gsz(d.n), 256, 0, s>>>(vol, d.n, w.mask.as<unsigned char>());
+    { k_nonzero<<<gsz(d.n), 256, 0, s>>>(vol, d.n, w.mask.as<unsigned char>()); N2M_COUNT(); }
     CKL();
     CKS(label_core(w, d, conn, only_largest, fill_bubbles, s));
     if (only_largest) {
-        k_write_keep<<<gsz(d.n), 256, 0, s>>>(w.keep.as<unsigned char>(), d.n, vol);
+        { k_write_keep<<<gsz(d.n), 256, 0, s>>>(w.keep.as<unsigned char>(), d.n, vol); N2M_COUNT(); }
     } else {
         CKS(w.cnt.ensure(((size_t)d.n + 1) * sizeof(unsigned)));
         unsigned *rank = w.cnt.as<unsigned>();
         CK(cudaMemsetAsync(rank + d.n, 0, sizeof(unsigned), s));
-        k_root_flags<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, rank);
+        { k_root_flags<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, rank); N2M_COUNT(); }
         CKL();
         CKS(scan_u32(rank, (size_t)d.n + 1, rank + d.n, sw, s));
-        k_write_labels<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, rank, vol);
+        { k_write_labels<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, rank, vol); N2M_COUNT(); }
     }
     CK(cudaMemcpyAsync(d_nl, &w.misc.as<Misc>()->nl, sizeof(int), cudaMemcpyDeviceToDevice, s));
     CKL();

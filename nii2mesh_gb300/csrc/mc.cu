@@ -485,7 +485,7 @@ n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4
     CKS(w.words.ensure(nwords * sizeof(uint4)));
     CKS(w.counts.ensure(nwords * sizeof(uint4)));
     const unsigned blocks = (unsigned)(((size_t)v.NG + 255) / 256);
-    k_count<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, w.words.as<uint4>(), w.counts.as<uint4>());
+    { k_count<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, w.words.as<uint4>(), w.counts.as<uint4>()); N2M_COUNT(); }
     CKL();
     return scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s);
 }
@@ -495,9 +495,9 @@ n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, v
     const GV v = make_gv(g);
     const unsigned blocks = (unsigned)(((size_t)v.NG + 255) / 256);
     // c-vertex candidates live after the edge candidates' slot range
-    k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, w.words.as<uint4>(), w.counts.as<uint4>(),
+    { k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, w.words.as<uint4>(), w.counts.as<uint4>(),
                                   make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand,
-                                  d_cand + cand_cap, d_ncand + 1, cand_cap);
+                                  d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
@@ -506,7 +506,7 @@ n2m_status mc_ccand_scan(const vec3d *d_pts, int np, const int *d_ccand, int ncc
                          unsigned *d_ncand, int cand_cap, cudaStream_t s) {
     if (nccand <= 0) return N2M_OK;
     const int blocks = (np + 255) / 256 < 4096 ? (np + 255) / 256 : 4096;
-    k_ccand<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(d_pts, np, d_ccand, nccand, d_cand, d_ncand, cand_cap);
+    { k_ccand<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(d_pts, np, d_ccand, nccand, d_cand, d_ncand, cand_cap); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

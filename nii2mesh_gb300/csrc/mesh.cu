@@ -271,8 +271,8 @@ inline unsigned gs(size_t n) {
 n2m_status mesh_apply_weld(vec3d *d_pts, vec3i *d_tris, int np, int nt, const int *d_removed, const int *d_keep,
                            int nrem, const int *d_ov_id, const vec3d *d_ov_pos, int nov, vec3d *d_out,
                            cudaStream_t s) {
-    k_weld_verts<<<gs(np), 256, 0, s>>>(d_pts, np, d_removed, nrem, d_ov_id, d_ov_pos, nov, d_out);
-    k_weld_tris<<<gs(nt), 256, 0, s>>>(d_tris, nt, d_removed, d_keep, nrem);
+    { k_weld_verts<<<gs(np), 256, 0, s>>>(d_pts, np, d_removed, nrem, d_ov_id, d_ov_pos, nov, d_out); N2M_COUNT(); }
+    { k_weld_tris<<<gs(nt), 256, 0, s>>>(d_tris, nt, d_removed, d_keep, nrem); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
@@ -286,10 +286,10 @@ n2m_status mesh_remove_degenerate(const vec3d *d_pts, const vec3i *d_tris_in, in
     }
     CKS(w.flags.ensure((size_t)nt * sizeof(unsigned)));
     CKS(w.tmp.ensure((size_t)tiles * sizeof(unsigned)));
-    k_deg_count<<<tiles, CB, 0, s>>>(d_pts, d_tris_in, nt, w.flags.as<unsigned>(), w.tmp.as<unsigned>());
+    { k_deg_count<<<tiles, CB, 0, s>>>(d_pts, d_tris_in, nt, w.flags.as<unsigned>(), w.tmp.as<unsigned>()); N2M_COUNT(); }
     CKL();
     CKS(scan_u32(w.tmp.as<unsigned>(), tiles, d_nt_out, sw, s));
-    k_deg_compact<<<tiles, CB, 0, s>>>(d_tris_in, nt, w.flags.as<unsigned>(), w.tmp.as<unsigned>(), d_tris_out);
+    { k_deg_compact<<<tiles, CB, 0, s>>>(d_tris_in, nt, w.flags.as<unsigned>(), w.tmp.as<unsigned>(), d_tris_out); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
@@ -309,39 +309,39 @@ n2m_status mesh_smooth_hc(vec3d *d_pts, const vec3i *d_tris, int np, int nt, dou
     unsigned *start = w.start.as<unsigned>();
     CK(cudaMemsetAsync(start, 0, ((size_t)np + 1) * sizeof(unsigned), s));
     CK(cudaMemsetAsync(w.fill.p, 0, (size_t)np * sizeof(unsigned), s));
-    k_degree<<<gs(nt), 256, 0, s>>>(d_tris, nt, start);
+    { k_degree<<<gs(nt), 256, 0, s>>>(d_tris, nt, start); N2M_COUNT(); }
     CKL();
     CKS(scan_u32(start, (size_t)np + 1, start + np + 0, sw, s));  // start[np] receives the total as well
-    k_fill_refs<<<gs(nt), 256, 0, s>>>(d_tris, nt, start, w.fill.as<unsigned>(), w.refs.as<int>());
-    k_sort_refs<<<gs(np), 256, 0, s>>>(start, np, w.refs.as<int>());
-    k_hc_init<<<gs(np), 256, 0, s>>>(d_pts, d_tris, start, w.refs.as<int>(), np, w.Lo.as<float3>(), w.P.as<float3>(),
-                                     w.hasnb.as<unsigned char>());
+    { k_fill_refs<<<gs(nt), 256, 0, s>>>(d_tris, nt, start, w.fill.as<unsigned>(), w.refs.as<int>()); N2M_COUNT(); }
+    { k_sort_refs<<<gs(np), 256, 0, s>>>(start, np, w.refs.as<int>()); N2M_COUNT(); }
+    { k_hc_init<<<gs(np), 256, 0, s>>>(d_pts, d_tris, start, w.refs.as<int>(), np, w.Lo.as<float3>(), w.P.as<float3>(),
+                                     w.hasnb.as<unsigned char>()); N2M_COUNT(); }
     CKL();
     const float a1 = (float)(1.0 - alpha), b = (float)beta, b1 = (float)(1.0 - beta);
     for (int it = 0; it < iter; it++) {
-        k_hc_a<<<gs(np), 256, 0, s>>>(w.P.as<float3>(), w.Lo.as<float3>(), d_tris, start, w.refs.as<int>(),
-                                      w.hasnb.as<unsigned char>(), np, a1, w.Q.as<float3>(), w.B.as<float3>());
-        k_hc_b<<<gs(np), 256, 0, s>>>(w.Q.as<float3>(), w.B.as<float3>(), d_tris, start, w.refs.as<int>(),
-                                      w.hasnb.as<unsigned char>(), np, b, b1, w.P.as<float3>());
+        { k_hc_a<<<gs(np), 256, 0, s>>>(w.P.as<float3>(), w.Lo.as<float3>(), d_tris, start, w.refs.as<int>(),
+                                      w.hasnb.as<unsigned char>(), np, a1, w.Q.as<float3>(), w.B.as<float3>()); N2M_COUNT(); }
+        { k_hc_b<<<gs(np), 256, 0, s>>>(w.Q.as<float3>(), w.B.as<float3>(), d_tris, start, w.refs.as<int>(),
+                                      w.hasnb.as<unsigned char>(), np, b, b1, w.P.as<float3>()); N2M_COUNT(); }
     }
     CKL();
     if (lock_edges) {
         CK(cudaMemsetAsync(w.border.p, 0, (size_t)np, s));
-        k_border<<<gs(np), 256, 0, s>>>(d_tris, start, w.refs.as<int>(), np, w.border.as<unsigned char>());
+        { k_border<<<gs(np), 256, 0, s>>>(d_tris, start, w.refs.as<int>(), np, w.border.as<unsigned char>()); N2M_COUNT(); }
     }
-    k_hc_out<<<gs(np), 256, 0, s>>>(d_pts, w.P.as<float3>(), w.border.as<unsigned char>(), np, lock_edges);
+    { k_hc_out<<<gs(np), 256, 0, s>>>(d_pts, w.P.as<float3>(), w.border.as<unsigned char>(), np, lock_edges); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
 
 n2m_status mesh_apply_sform(vec3d *d_pts, vec3i *d_tris, int np, int nt, const float sx[4], const float sy[4],
                             const float sz[4], cudaStream_t s) {
-    k_sform<<<gs(np), 256, 0, s>>>(d_pts, np, sx[0], sx[1], sx[2], sx[3], sy[0], sy[1], sy[2], sy[3], sz[0], sz[1],
-                                   sz[2], sz[3]);
+    { k_sform<<<gs(np), 256, 0, s>>>(d_pts, np, sx[0], sx[1], sx[2], sx[3], sy[0], sy[1], sy[2], sy[3], sz[0], sz[1],
+                                   sz[2], sz[3]); N2M_COUNT(); }
     const double px = (double)(sx[0] + sx[1] + sx[2]), py = (double)(sy[0] + sy[1] + sy[2]),
                  pz = (double)(sz[0] + sz[1] + sz[2]);
     const float det = (float)(px * py * pz);
-    if (det < 0.0) k_flip<<<gs(nt), 256, 0, s>>>(d_tris, nt);
+    if (det < 0.0) { k_flip<<<gs(nt), 256, 0, s>>>(d_tris, nt); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

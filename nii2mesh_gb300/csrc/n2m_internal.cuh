@@ -4,6 +4,7 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/n2m_gpu.h"
@@ -26,6 +27,10 @@ void n2m_set_error(const char *fmt, ...);
         if (s_ != N2M_OK) return s_;              \
     } while (0)
 #define CKL()  CK(cudaGetLastError())
+
+// process-wide count of kernel launches (reported by n2m_kernel_launches)
+extern std::atomic<long long> g_n2m_launches;
+#define N2M_COUNT() g_n2m_launches.fetch_add(1, std::memory_order_relaxed)
 
 // ---- grow-only device buffers -----------------------------------------------
 struct DevBuf {

@@ -226,7 +226,7 @@ n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const i
     const size_t nwords = ((size_t)g.NG + 31) / 32;
     CKS(w.words.ensure(nwords * sizeof(uint4)));
     CKS(w.counts.ensure(nwords * sizeof(uint4)));
-    k_oc_count<<<(unsigned)(((size_t)g.NG + 255) / 256), 256, 0, s>>>(g, w.words.as<uint4>(), w.counts.as<uint4>());
+    { k_oc_count<<<(unsigned)(((size_t)g.NG + 255) / 256), 256, 0, s>>>(g, w.words.as<uint4>(), w.counts.as<uint4>()); N2M_COUNT(); }
     CKL();
     return scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s);
 }
@@ -235,9 +235,9 @@ n2m_status oc_emit(const float *vol, const int dim[3], const int lo[3], const in
                     McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris, int *d_cand, unsigned *d_ncand,
                     int cand_cap, long long *d_lastuse, cudaStream_t s) {
     const OV g = make_ov(vol, dim, lo, hi, iso, edge_max);
-    k_oc_emit<<<(unsigned)(((size_t)g.NG + 255) / 256), 256, 0, s>>>(g, w.words.as<uint4>(), w.counts.as<uint4>(),
+    { k_oc_emit<<<(unsigned)(((size_t)g.NG + 255) / 256), 256, 0, s>>>(g, w.words.as<uint4>(), w.counts.as<uint4>(),
                                                                      make_uint4(c.nv_edge, c.nt, 0, 0), d_pts, d_tris,
-                                                                     d_cand, d_ncand, cand_cap, d_lastuse);
+                                                                     d_cand, d_ncand, cand_cap, d_lastuse); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

@@ -97,9 +97,9 @@ n2m_status scan_uint4(uint4 *d, size_t n, uint4 *d_total, ScanWork &w, cudaStrea
     }
     const size_t tiles = (n + TILE - 1) / TILE;
     CKS(w.part.ensure(tiles * sizeof(uint4)));
-    k_tile_sums<<<(unsigned)tiles, SB, 0, s>>>(d, n, w.part.as<uint4>());
-    k_scan_parts<<<1, SB, 0, s>>>(w.part.as<uint4>(), tiles, d_total);
-    k_tile_scan<<<(unsigned)tiles, SB, 0, s>>>(d, n, w.part.as<uint4>());
+    { k_tile_sums<<<(unsigned)tiles, SB, 0, s>>>(d, n, w.part.as<uint4>()); N2M_COUNT(); }
+    { k_scan_parts<<<1, SB, 0, s>>>(w.part.as<uint4>(), tiles, d_total); N2M_COUNT(); }
+    { k_tile_scan<<<(unsigned)tiles, SB, 0, s>>>(d, n, w.part.as<uint4>()); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
@@ -182,9 +182,9 @@ n2m_status scan_u32(unsigned *d, size_t n, unsigned *d_total, ScanWork &w, cudaS
     }
     const size_t tiles = (n + TILE - 1) / TILE;
     CKS(w.part.ensure(tiles * sizeof(unsigned)));
-    k_tile_sums_u32<<<(unsigned)tiles, SB, 0, s>>>(d, n, w.part.as<unsigned>());
-    k_scan_parts_u32<<<1, SB, 0, s>>>(w.part.as<unsigned>(), tiles, d_total);
-    k_tile_scan_u32<<<(unsigned)tiles, SB, 0, s>>>(d, n, w.part.as<unsigned>());
+    { k_tile_sums_u32<<<(unsigned)tiles, SB, 0, s>>>(d, n, w.part.as<unsigned>()); N2M_COUNT(); }
+    { k_scan_parts_u32<<<1, SB, 0, s>>>(w.part.as<unsigned>(), tiles, d_total); N2M_COUNT(); }
+    { k_tile_scan_u32<<<(unsigned)tiles, SB, 0, s>>>(d, n, w.part.as<unsigned>()); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

@@ -157,7 +157,7 @@ void stats_init_host(VolStats *h) {
 n2m_status launch_smooth(const float *in, float *out, int nx, int ny, int nz, float iso, VolStats *st,
                          cudaStream_t s) {
     dim3 grid((nx + STX - 1) / STX, (ny + STY - 1) / STY, (nz + SZC - 1) / SZC);
-    k_smooth<<<grid, dim3(STX, STY), 0, s>>>(in, out, nx, ny, nz, iso, st);
+    { k_smooth<<<grid, dim3(STX, STY), 0, s>>>(in, out, nx, ny, nz, iso, st); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
@@ -165,7 +165,7 @@ n2m_status launch_smooth(const float *in, float *out, int nx, int ny, int nz, fl
 n2m_status launch_stats(const float *vol, int nx, int ny, int nz, float iso, bool minmax, VolStats *st,
                         cudaStream_t s) {
     dim3 grid((nx + 255) / 256 > 4 ? 4 : (nx + 255) / 256, ny, nz);
-    k_stats<<<grid, 256, 0, s>>>(vol, nx, ny, nz, iso, st, minmax);
+    { k_stats<<<grid, 256, 0, s>>>(vol, nx, ny, nz, iso, st, minmax); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
