@@ -408,7 +408,7 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
     CKS(c->cand.ensure((size_t)2 * cap * sizeof(int)));
     CKS(c->ncand.ensure(2 * sizeof(unsigned)));
     CK(cudaMemsetAsync(c->ncand.p, 0, 2 * sizeof(unsigned), c->stream));
-    McCounts mcn{tot.x, tot.y, tot.z};
+    McCounts mcn{tot.x, tot.y, tot.z, tot.w};
     if (old) {
         CKS(c->lastuse.ensure(nv * sizeof(long long)));
         { k_fill_ll<<<1024, 256, 0, c->stream>>>(c->lastuse.as<long long>(), nv, -1); N2M_COUNT(); }

@@ -21,6 +21,8 @@
 // only such vertices can lie within the weld tolerance (1e-5) of another.
 #include <float.h>
 
+#include <algorithm>
+
 #include "mc_tables.h"
 #include "n2m_internal.cuh"
 
@@ -236,91 +238,86 @@ __device__ Tiling select_tiling(const float *c, int lut, bool classic) {
     return T;
 }
 
-__device__ __forceinline__ void unravel(const GV &g, unsigned p, int &x, int &y, int &z) {
-    z = (int)(p / g.NXY);
-    const unsigned r = p - (unsigned)z * g.NXY;
-    y = (int)(r / (unsigned)g.NX);
-    x = (int)(r - (unsigned)y * (unsigned)g.NX);
-}
-
-// corner p of cube (x,y,z): x + ((p^(p>>1))&1), y + ((p>>1)&1), z + ((p>>2)&1)
-__device__ __forceinline__ void load_cube(const GV &g, int x, int y, int z, float *c) {
-    c[0] = gval(g, x, y, z);         c[1] = gval(g, x + 1, y, z);
-    c[2] = gval(g, x + 1, y + 1, z); c[3] = gval(g, x, y + 1, z);
-    c[4] = gval(g, x, y, z + 1);     c[5] = gval(g, x + 1, y, z + 1);
-    c[6] = gval(g, x + 1, y + 1, z + 1); c[7] = gval(g, x, y + 1, z + 1);
-}
-
 __device__ __forceinline__ int cube_lut(const float *c) {
     int lut = 0;
     for (int p = 0; p < 8; p++) lut |= (c[p] > 0.f) << p;
     return lut;
 }
 
-// per-point classification shared by both passes
-struct PointInfo {
-    bool in, ex, ey, ez, cube;
-    int x, y, z;
-    float c[8];
-};
+// ---- count pass ---------------------------------------------------------------
+// Words are row-aligned: word (z*NY + y)*WX + xw holds grid points
+// x = 32*xw + lane of row (y, z); WX = ceil(NX/32).  Word order is raster
+// order, so numbering by an exclusive scan over words is the reference's.
+constexpr int TY = 8, TZ = 8;          // a CTA covers one word column x 8 rows x 8 slices
 
-__device__ __forceinline__ void classify(const GV &g, unsigned p, PointInfo &pi) {
-    pi.in = p < g.NG;
-    pi.ex = pi.ey = pi.ez = pi.cube = false;
-    if (!pi.in) return;
-    unravel(g, p, pi.x, pi.y, pi.z);
-    const bool hx = pi.x < g.NX - 1, hy = pi.y < g.NY - 1, hz = pi.z < g.NZ - 1;
-    pi.c[0] = gval(g, pi.x, pi.y, pi.z);
-    if (hx && hy && hz) {
-        pi.cube = true;
-        pi.c[1] = gval(g, pi.x + 1, pi.y, pi.z);
-        pi.c[2] = gval(g, pi.x + 1, pi.y + 1, pi.z);
-        pi.c[3] = gval(g, pi.x, pi.y + 1, pi.z);
-        pi.c[4] = gval(g, pi.x, pi.y, pi.z + 1);
-        pi.c[5] = gval(g, pi.x + 1, pi.y, pi.z + 1);
-        pi.c[6] = gval(g, pi.x + 1, pi.y + 1, pi.z + 1);
-        pi.c[7] = gval(g, pi.x, pi.y + 1, pi.z + 1);
-    } else {
-        pi.c[1] = hx ? gval(g, pi.x + 1, pi.y, pi.z) : pi.c[0];
-        pi.c[3] = hy ? gval(g, pi.x, pi.y + 1, pi.z) : pi.c[0];
-        pi.c[4] = hz ? gval(g, pi.x, pi.y, pi.z + 1) : pi.c[0];
+__global__ void __launch_bounds__(256) k_count(GV g, bool classic, unsigned WX, uint4 *words, uint4 *counts,
+                                               unsigned *active, unsigned *nactive) {
+    __shared__ float sv[TZ + 1][TY + 1][33];
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+    // tile and halo strictly inside the volume: no darkening, wrap or padding
+    const bool simple = g.lo0 + x0 >= 1 && g.lo0 + x0 + 32 <= g.dx - 2 && g.lo1 + y0 >= 1 &&
+                        g.lo1 + y0 + TY <= g.dy - 2 && g.lo2 + z0 >= 1 && g.lo2 + z0 + TZ <= g.dz - 2;
+    for (int i = threadIdx.x; i < (TZ + 1) * (TY + 1) * 33; i += 256) {
+        const int xx = i % 33, r = i / 33, yy = r % (TY + 1), zz = r / (TY + 1);
+        float v;
+        if (simple) {
+            const unsigned j = (unsigned)(g.lo0 + x0 + xx) + (unsigned)(y0 + yy + g.lo1) * (unsigned)g.dx +
+                               (unsigned)(z0 + zz + g.lo2) * (unsigned)g.dxy;
+            v = __fsub_rn(__ldg(g.vol + j), g.iso);
+            if (fabsf(v) < N2M_FLT_EPS) v = N2M_FLT_EPS;
+        } else {
+            v = gval(g, x0 + xx, y0 + yy, z0 + zz);
+        }
+        sv[zz][yy][xx] = v;
     }
-    const bool s0 = pi.c[0] > 0.f;
-    pi.ex = hx && ((pi.c[1] > 0.f) != s0);
-    pi.ey = hy && ((pi.c[3] > 0.f) != s0);
-    pi.ez = hz && ((pi.c[4] > 0.f) != s0);
-}
-
-__global__ void __launch_bounds__(256) k_count(GV g, bool classic, uint4 *words, uint4 *counts) {
-    const unsigned p = blockIdx.x * 256u + threadIdx.x;
-    PointInfo pi;
-    classify(g, p, pi);
-    int nt = 0, nc = 0;
-    if (pi.cube) {
-        const int lut = cube_lut(pi.c);
-        if (lut != 0 && lut != 255) {
-            const Tiling T = select_tiling(pi.c, lut, classic);
-            nt = T.n;
-            nc = T.cv;
+    __syncthreads();
+    const int wy = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y = y0 + wy, x = x0 + lane;
+    if (y >= g.NY) return;                           // whole warp
+    for (int zz = 0; zz < TZ; zz++) {
+        const int z = z0 + zz;
+        if (z >= g.NZ) break;                        // whole warp
+        const bool in = x < g.NX;
+        const bool hx = in && x < g.NX - 1, hy = in && y < g.NY - 1, hz = in && z < g.NZ - 1;
+        const float c0 = sv[zz][wy][lane];
+        const bool s0 = c0 > 0.f;
+        const bool ex = hx && ((sv[zz][wy][lane + 1] > 0.f) != s0);
+        const bool ey = hy && ((sv[zz][wy + 1][lane] > 0.f) != s0);
+        const bool ez = hz && ((sv[zz + 1][wy][lane] > 0.f) != s0);
+        int nt = 0, nc = 0;
+        if (hx && hy && hz) {
+            float c[8] = {c0, sv[zz][wy][lane + 1], sv[zz][wy + 1][lane + 1], sv[zz][wy + 1][lane],
+                          sv[zz + 1][wy][lane], sv[zz + 1][wy][lane + 1], sv[zz + 1][wy + 1][lane + 1],
+                          sv[zz + 1][wy + 1][lane]};
+            const int lut = cube_lut(c);
+            if (lut != 0 && lut != 255) {
+                const Tiling T = select_tiling(c, lut, classic);
+                nt = T.n;
+                nc = T.cv;
+            }
+        }
+        const unsigned xm = __ballot_sync(0xffffffffu, ex), ym = __ballot_sync(0xffffffffu, ey),
+                       zm = __ballot_sync(0xffffffffu, ez);
+        for (int o = 16; o; o >>= 1) {
+            nt += __shfl_xor_sync(0xffffffffu, nt, o);
+            nc += __shfl_xor_sync(0xffffffffu, nc, o);
+        }
+        if (lane == 0) {
+            const unsigned w = ((unsigned)z * (unsigned)g.NY + (unsigned)y) * WX + blockIdx.x;
+            const unsigned nv = __popc(xm) + __popc(ym) + __popc(zm);
+            const bool act = nv | nt | nc;
+            words[w] = make_uint4(xm, ym, zm, 0u);
+            counts[w] = make_uint4(nv, (unsigned)nt, (unsigned)nc, act);
+            if (act) active[atomicAdd(nactive, 1u)] = w;
         }
     }
-    const unsigned xm = __ballot_sync(0xffffffffu, pi.ex), ym = __ballot_sync(0xffffffffu, pi.ey),
-                   zm = __ballot_sync(0xffffffffu, pi.ez);
-    for (int o = 16; o; o >>= 1) {
-        nt += __shfl_xor_sync(0xffffffffu, nt, o);
-        nc += __shfl_xor_sync(0xffffffffu, nc, o);
-    }
-    const unsigned w = p >> 5;
-    if ((threadIdx.x & 31) == 0 && w * 32u < g.NG) {
-        words[w] = make_uint4(xm, ym, zm, 0u);
-        counts[w] = make_uint4(__popc(xm) + __popc(ym) + __popc(zm), (unsigned)nt, (unsigned)nc, 0u);
-    }
 }
 
-// id of the vertex on the `axis` edge of grid point q (must exist)
-__device__ __forceinline__ int vid(const uint4 *__restrict__ words, const uint4 *__restrict__ offs, unsigned q,
-                                   int axis) {
-    const unsigned w = q >> 5, l = q & 31u;
+// ---- emit pass -------------------------------------------------------------------
+// id of the vertex on the `axis` edge of grid point (x,y,z) (the edge must cross)
+__device__ __forceinline__ int vid(const uint4 *__restrict__ words, const uint4 *__restrict__ offs, unsigned NY,
+                                   unsigned WX, int x, int y, int z, int axis) {
+    const unsigned w = ((unsigned)z * NY + (unsigned)y) * WX + ((unsigned)x >> 5), l = (unsigned)x & 31u;
     const uint4 m = words[w];
     const unsigned lt = (1u << l) - 1u;
     unsigned id = offs[w].x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt);
@@ -331,8 +328,8 @@ __device__ __forceinline__ int vid(const uint4 *__restrict__ words, const uint4 
 
 __device__ __forceinline__ float frac_dist(float f) { return fabsf(f - rintf(f)); }
 
-// local position of cube edge e (edge numbering of the tiling tables):
-// owner corner, axis, and the two corners it interpolates
+// cube edge e of the tiling tables: owner corner, axis, the two corners it
+// interpolates (owner first)
 __constant__ signed char k_edge[12][4] = {{0, 0, 0, 1}, {1, 1, 1, 2}, {3, 0, 3, 2}, {0, 1, 0, 3},
                                          {4, 0, 4, 5}, {5, 1, 5, 6}, {7, 0, 7, 6}, {4, 1, 4, 7},
                                          {0, 2, 0, 4}, {1, 2, 1, 5}, {2, 2, 2, 6}, {3, 2, 3, 7}};
@@ -342,107 +339,127 @@ __device__ __forceinline__ float edge_u(float c0, float c1) {
     return den != 0.f ? __fdiv_rn(c0, den) : 0.5f;
 }
 
-__global__ void __launch_bounds__(256) k_emit(GV g, bool classic, const uint4 *__restrict__ words,
-                                              const uint4 *__restrict__ offs, uint4 totals, vec3d *pts,
-                                              vec3i *tris, int *cand, unsigned *ncand, int *ccand,
-                                              unsigned *nccand, int cap) {
-    const unsigned p = blockIdx.x * 256u + threadIdx.x;
-    const unsigned w = p >> 5, lane = threadIdx.x & 31u;
-    const unsigned nwords = (g.NG + 31u) >> 5;
-    if (w >= nwords) return;  // whole warp
-    const uint4 o = offs[w];
-    const uint4 on = (w + 1 < nwords) ? offs[w + 1] : totals;
-    const uint4 m = words[w];
-    if ((m.x | m.y | m.z) == 0u && on.y == o.y && on.z == o.z) return;  // whole warp: nothing to emit
-    PointInfo pi;
-    classify(g, p, pi);
+__device__ __forceinline__ void add_cand(int *cand, unsigned *n, int cap, int id) {
+    const unsigned k = atomicAdd(n, 1u);
+    if (k < (unsigned)cap) cand[k] = id;
+}
+
+// one warp per active word
+__global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, const uint4 *__restrict__ words,
+                                              const uint4 *__restrict__ offs, const unsigned *__restrict__ active,
+                                              unsigned nactive, unsigned nwords, uint4 totals, vec3d *pts,
+                                              vec3i *tris, int *cand, unsigned *ncand, int *ccand, unsigned *nccand,
+                                              int cap) {
+    const unsigned lane = threadIdx.x & 31u;
     const float flo0 = (float)g.lo0, flo1 = (float)g.lo1, flo2 = (float)g.lo2;
-    // ---- edge vertices owned by this point (src/MarchingCubes.c:935-1026)
-    if (pi.ex | pi.ey | pi.ez) {
-        const unsigned lt = (1u << lane) - 1u;
-        int id = (int)(o.x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt));
-        const float fx = (float)pi.x, fy = (float)pi.y, fz = (float)pi.z;
-        if (pi.ex) {
-            const float X = __fadd_rn(__fadd_rn(fx, edge_u(pi.c[0], pi.c[1])), flo0);
-            pts[id] = {(double)X, (double)__fadd_rn(fy, flo1), (double)__fadd_rn(fz, flo2)};
-            if (frac_dist(X) < 1.5e-5f) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
-            id++;
+    for (unsigned aw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; aw < nactive; aw += (gridDim.x * blockDim.x) >> 5) {
+        const unsigned w = active[aw];
+        const unsigned row = w / WX, xw = w - row * WX;
+        const int z = (int)(row / (unsigned)g.NY), y = (int)(row - (unsigned)z * (unsigned)g.NY);
+        const int x = (int)(xw * 32u + lane);
+        const uint4 o = offs[w];
+        const uint4 m = words[w];
+        const bool in = x < g.NX;
+        const bool hx = in && x < g.NX - 1, hy = in && y < g.NY - 1, hz = in && z < g.NZ - 1;
+        const bool cube = hx && hy && hz;
+        const bool ex = (m.x >> lane) & 1u, ey = (m.y >> lane) & 1u, ez = (m.z >> lane) & 1u;
+        float c[8];
+        if (in) {
+            c[0] = gval(g, x, y, z);
+            c[1] = hx ? gval(g, x + 1, y, z) : c[0];
+            c[3] = hy ? gval(g, x, y + 1, z) : c[0];
+            c[4] = hz ? gval(g, x, y, z + 1) : c[0];
+            if (cube) {
+                c[2] = gval(g, x + 1, y + 1, z);
+                c[5] = gval(g, x + 1, y, z + 1);
+                c[6] = gval(g, x + 1, y + 1, z + 1);
+                c[7] = gval(g, x, y + 1, z + 1);
+            }
         }
-        if (pi.ey) {
-            const float Y = __fadd_rn(__fadd_rn(fy, edge_u(pi.c[0], pi.c[3])), flo1);
-            pts[id] = {(double)__fadd_rn(fx, flo0), (double)Y, (double)__fadd_rn(fz, flo2)};
-            if (frac_dist(Y) < 1.5e-5f) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
-            id++;
+        // edge vertices owned by this point (src/MarchingCubes.c:935-1026)
+        if (ex | ey | ez) {
+            const unsigned lt = (1u << lane) - 1u;
+            int id = (int)(o.x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt));
+            const float fx = (float)x, fy = (float)y, fz = (float)z;
+            if (ex) {
+                const float X = __fadd_rn(__fadd_rn(fx, edge_u(c[0], c[1])), flo0);
+                pts[id] = {(double)X, (double)__fadd_rn(fy, flo1), (double)__fadd_rn(fz, flo2)};
+                if (frac_dist(X) < 1.5e-5f) add_cand(cand, ncand, cap, id);
+                id++;
+            }
+            if (ey) {
+                const float Y = __fadd_rn(__fadd_rn(fy, edge_u(c[0], c[3])), flo1);
+                pts[id] = {(double)__fadd_rn(fx, flo0), (double)Y, (double)__fadd_rn(fz, flo2)};
+                if (frac_dist(Y) < 1.5e-5f) add_cand(cand, ncand, cap, id);
+                id++;
+            }
+            if (ez) {
+                const float Z = __fadd_rn(__fadd_rn(fz, edge_u(c[0], c[4])), flo2);
+                pts[id] = {(double)__fadd_rn(fx, flo0), (double)__fadd_rn(fy, flo1), (double)Z};
+                if (frac_dist(Z) < 1.5e-5f) add_cand(cand, ncand, cap, id);
+            }
         }
-        if (pi.ez) {
-            const float Z = __fadd_rn(__fadd_rn(fz, edge_u(pi.c[0], pi.c[4])), flo2);
-            pts[id] = {(double)__fadd_rn(fx, flo0), (double)__fadd_rn(fy, flo1), (double)Z};
-            if (frac_dist(Z) < 1.5e-5f) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
+        Tiling T = {0, 0, false};
+        if (cube) {
+            const int lut = cube_lut(c);
+            if (lut != 0 && lut != 255) T = select_tiling(c, lut, classic);
+        }
+        int tb = T.n, cb = T.cv;   // warp exclusive scans
+        for (int d = 1; d < 32; d <<= 1) {
+            const int a = __shfl_up_sync(0xffffffffu, tb, d), b = __shfl_up_sync(0xffffffffu, cb, d);
+            if ((int)lane >= d) { tb += a; cb += b; }
+        }
+        tb -= T.n;
+        cb -= T.cv;
+        if (T.n == 0) continue;
+        int v12 = -1;
+        if (T.cv) {   // c-vertex: mean of the cube's edge vertices (src/MarchingCubes.c:1029-1082)
+            v12 = (int)(totals.x + o.z + cb);
+            float n = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+            for (int e = 0; e < 12; e++) {
+                const int own = k_edge[e][0], ax = k_edge[e][1], ca = k_edge[e][2], cbn = k_edge[e][3];
+                if ((c[ca] > 0.f) == (c[cbn] > 0.f)) continue;
+                const float u = edge_u(c[ca], c[cbn]);
+                float px = (float)(x + ((own ^ (own >> 1)) & 1)), py = (float)(y + ((own >> 1) & 1)),
+                      pz = (float)(z + ((own >> 2) & 1));
+                if (ax == 0) px = __fadd_rn(px, u);
+                else if (ax == 1) py = __fadd_rn(py, u);
+                else pz = __fadd_rn(pz, u);
+                n = __fadd_rn(n, 1.f);
+                sx = __fadd_rn(sx, px); sy = __fadd_rn(sy, py); sz = __fadd_rn(sz, pz);
+            }
+            if (n > 0.f) { sx = __fdiv_rn(sx, n); sy = __fdiv_rn(sy, n); sz = __fdiv_rn(sz, n); }
+            const float X = __fadd_rn(sx, flo0), Y = __fadd_rn(sy, flo1), Z = __fadd_rn(sz, flo2);
+            pts[v12] = {(double)X, (double)Y, (double)Z};
+            if (fminf(frac_dist(X), fminf(frac_dist(Y), frac_dist(Z))) < 1.5e-5f) add_cand(ccand, nccand, cap, v12);
+        }
+        // triangles, stored reversed (v3,v2,v1) as marchingCubes() returns them
+        const unsigned NY = (unsigned)g.NY;
+        int tv[3];
+        for (int t = 0; t < 3 * T.n; t++) {
+            const int code = d_lut[T.off + t];
+            int v;
+            switch (code) {
+            case 0: v = vid(words, offs, NY, WX, x, y, z, 0); break;
+            case 1: v = vid(words, offs, NY, WX, x + 1, y, z, 1); break;
+            case 2: v = vid(words, offs, NY, WX, x, y + 1, z, 0); break;
+            case 3: v = vid(words, offs, NY, WX, x, y, z, 1); break;
+            case 4: v = vid(words, offs, NY, WX, x, y, z + 1, 0); break;
+            case 5: v = vid(words, offs, NY, WX, x + 1, y, z + 1, 1); break;
+            case 6: v = vid(words, offs, NY, WX, x, y + 1, z + 1, 0); break;
+            case 7: v = vid(words, offs, NY, WX, x, y, z + 1, 1); break;
+            case 8: v = vid(words, offs, NY, WX, x, y, z, 2); break;
+            case 9: v = vid(words, offs, NY, WX, x + 1, y, z, 2); break;
+            case 10: v = vid(words, offs, NY, WX, x + 1, y + 1, z, 2); break;
+            case 11: v = vid(words, offs, NY, WX, x, y + 1, z, 2); break;
+            case 12: v = v12; break;
+            default: v = -1; break;
+            }
+            tv[t % 3] = v;
+            if (t % 3 == 2) tris[o.y + tb + t / 3] = {tv[2], tv[1], tv[0]};
         }
     }
-    // ---- cube triangles
-    Tiling T = {0, 0, false};
-    if (pi.cube) {
-        const int lut = cube_lut(pi.c);
-        if (lut != 0 && lut != 255) T = select_tiling(pi.c, lut, classic);
-    }
-    int tb = T.n, cb = T.cv;  // warp exclusive scans
-    for (int d = 1; d < 32; d <<= 1) {
-        const int a = __shfl_up_sync(0xffffffffu, tb, d), b = __shfl_up_sync(0xffffffffu, cb, d);
-        if ((int)lane >= d) { tb += a; cb += b; }
-    }
-    tb -= T.n;
-    cb -= T.cv;
-    if (T.n == 0) return;
-    int v12 = -1;
-    if (T.cv) {  // c-vertex: mean of the cube's edge vertices (src/MarchingCubes.c:1029-1082)
-        v12 = (int)(totals.x + o.z + cb);
-        float n = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
-        for (int e = 0; e < 12; e++) {
-            const int own = k_edge[e][0], ax = k_edge[e][1], ca = k_edge[e][2], cbn = k_edge[e][3];
-            if ((pi.c[ca] > 0.f) == (pi.c[cbn] > 0.f)) continue;
-            const float u = edge_u(pi.c[ca], pi.c[cbn]);
-            float px = (float)(pi.x + ((own ^ (own >> 1)) & 1)), py = (float)(pi.y + ((own >> 1) & 1)),
-                  pz = (float)(pi.z + ((own >> 2) & 1));
-            if (ax == 0) px = __fadd_rn(px, u);
-            else if (ax == 1) py = __fadd_rn(py, u);
-            else pz = __fadd_rn(pz, u);
-            n = __fadd_rn(n, 1.f);
-            sx = __fadd_rn(sx, px); sy = __fadd_rn(sy, py); sz = __fadd_rn(sz, pz);
-        }
-        if (n > 0.f) { sx = __fdiv_rn(sx, n); sy = __fdiv_rn(sy, n); sz = __fdiv_rn(sz, n); }
-        const float X = __fadd_rn(sx, flo0), Y = __fadd_rn(sy, flo1), Z = __fadd_rn(sz, flo2);
-        pts[v12] = {(double)X, (double)Y, (double)Z};
-        if (fminf(frac_dist(X), fminf(frac_dist(Y), frac_dist(Z))) < 1.5e-5f) {
-            unsigned k = atomicAdd(nccand, 1u);
-            if (k < (unsigned)cap) ccand[k] = v12;
-        }
-    }
-    // ---- triangles, stored reversed (v3,v2,v1) as marchingCubes() returns them
-    const unsigned NX = (unsigned)g.NX, NXY = g.NXY;
-    int tv[3];
-    for (int t = 0; t < 3 * T.n; t++) {
-        const int code = d_lut[T.off + t];
-        int v;
-        switch (code) {
-        case 0: v = vid(words, offs, p, 0); break;
-        case 1: v = vid(words, offs, p + 1, 1); break;
-        case 2: v = vid(words, offs, p + NX, 0); break;
-        case 3: v = vid(words, offs, p, 1); break;
-        case 4: v = vid(words, offs, p + NXY, 0); break;
-        case 5: v = vid(words, offs, p + NXY + 1, 1); break;
-        case 6: v = vid(words, offs, p + NXY + NX, 0); break;
-        case 7: v = vid(words, offs, p + NXY, 1); break;
-        case 8: v = vid(words, offs, p, 2); break;
-        case 9: v = vid(words, offs, p + 1, 2); break;
-        case 10: v = vid(words, offs, p + NX + 1, 2); break;
-        case 11: v = vid(words, offs, p + NX, 2); break;
-        case 12: v = v12; break;
-        default: v = -1; break;
-        }
-        tv[t % 3] = v;
-        if (t % 3 == 2) tris[o.y + tb + t / 3] = {tv[2], tv[1], tv[0]};
-    }
+    (void)nwords;
 }
 
 // vertices within 1.5e-5 of a c-vertex candidate become weld candidates too
@@ -479,13 +496,23 @@ GV make_gv(const McGrid &g) {
 }
 }  // namespace
 
+// counts: per word {vertices, triangles, c-vertices, active}; after the scan,
+// exclusive offsets; totals.w = number of active words (listed in w.cand)
 n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s) {
     const GV v = make_gv(g);
-    const size_t nwords = ((size_t)v.NG + 31) / 32;
+    const unsigned WX = (unsigned)((g.n[0] + 31) / 32);
+    const size_t nwords = (size_t)WX * g.n[1] * g.n[2];
+    if (nwords >= 0xffffffffULL) {
+        n2m_set_error("grid too large");
+        return N2M_ERR_TOO_LARGE;
+    }
     CKS(w.words.ensure(nwords * sizeof(uint4)));
     CKS(w.counts.ensure(nwords * sizeof(uint4)));
-    const unsigned blocks = (unsigned)(((size_t)v.NG + 255) / 256);
-    { k_count<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, w.words.as<uint4>(), w.counts.as<uint4>()); N2M_COUNT(); }
+    CKS(w.cand.ensure((nwords + 1) * sizeof(unsigned)));
+    unsigned *active = w.cand.as<unsigned>();
+    CK(cudaMemsetAsync(active + nwords, 0, sizeof(unsigned), s));
+    dim3 grid(WX, (g.n[1] + TY - 1) / TY, (g.n[2] + TZ - 1) / TZ);
+    { k_count<<<grid, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), active, active + nwords); N2M_COUNT(); }
     CKL();
     return scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s);
 }
@@ -493,11 +520,12 @@ n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4
 n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,
                    int *d_cand, unsigned *d_ncand, int cand_cap, cudaStream_t s) {
     const GV v = make_gv(g);
-    const unsigned blocks = (unsigned)(((size_t)v.NG + 255) / 256);
-    // c-vertex candidates live after the edge candidates' slot range
-    { k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, w.words.as<uint4>(), w.counts.as<uint4>(),
-                                  make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand,
-                                  d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
+    const unsigned WX = (unsigned)((g.n[0] + 31) / 32);
+    const size_t nwords = (size_t)WX * g.n[1] * g.n[2];
+    const unsigned nact = c.nactive;
+    if (nact == 0) return N2M_OK;
+    const unsigned blocks = std::min<unsigned>((nact + 7) / 8, 152u * 16u);
+    { k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.cand.as<unsigned>(), nact, (unsigned)nwords, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand, d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

@@ -102,7 +102,7 @@ struct McWork {
     DevBuf words, counts, cand, verts_tmp, tris_tmp;
 };
 struct McCounts {
-    unsigned nv_edge, nt, nc;
+    unsigned nv_edge, nt, nc, nactive;
 };
 n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s);
 n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,

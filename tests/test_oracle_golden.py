@@ -1,0 +1,103 @@
+"""Pin the CPU oracle against the reference (CPU only).
+
+The golden fixtures in tests/golden/ were produced by the reference nii2mesh
+itself (tests/golden/make_golden.py).  The oracle must reproduce every one of
+them bit for bit; where the reference build (oracle/_ref) is present, the
+oracle is also compared with it directly on further seeded inputs.
+"""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle.oracle import MC33, MC_CLASSIC_TABLE, OLDCUBES, Reference, canonical, mesh_equal, reference_available
+
+GOLD = Path(__file__).resolve().parent / "golden"
+G = json.loads((GOLD / "golden.json").read_text())
+INPUTS = dict(np.load(GOLD / "inputs.npz"))
+
+# MC self-test known answers (vertices, triangles) of the reference's ten
+# analytic 60^3 fields (src/MarchingCubes.c:1282-1405), Lewiner, iso 0
+KNOWN_SELFTEST = {0: (302, 600), 1: (792, 1572), 2: (7038, 13720), 3: (554, 1104), 4: (2168, 4352),
+                  5: (5304, 10616), 6: (13196, 25834), 7: (11333, 22620), 8: (10800, 20886), 9: (5789, 11298)}
+
+
+def mesh_hash(tris, pts):
+    ct, cp = canonical(tris, pts)
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(ct, np.int64).tobytes())
+    h.update(np.ascontiguousarray(cp, np.float64).tobytes())
+    return h.hexdigest()
+
+
+def raw_hash(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("e", G["meshify"], ids=lambda e: f"{e['input']}-v{e['variant']}-"
+                         f"{int(e['pre_smooth'])}{int(e['only_largest'])}{int(e['fill_bubbles'])}")
+def test_meshify_matches_reference(oracle, e):
+    m = oracle.meshify(INPUTS[e["input"]], e["iso"], e["variant"], e["pre_smooth"], e["only_largest"],
+                       e["fill_bubbles"])
+    if e.get("result", 1) is None:
+        assert m is None
+        return
+    assert (len(m[1]), len(m[0])) == (e["nvert"], e["ntri"])
+    assert mesh_hash(*m) == e["sha256"]
+
+
+def test_selftest_known_answers(oracle):
+    for obj, (nv, nt) in KNOWN_SELFTEST.items():
+        f = oracle.selftest_field(obj)
+        assert raw_hash(f) == G["selftest"][str(obj)]["field_sha256"]
+        t, v = oracle.mc_raw(f, 0)
+        assert (len(v), len(t)) == (nv, nt) == (G["selftest"][str(obj)]["nvert"], G["selftest"][str(obj)]["ntri"])
+
+
+def test_thresholds(oracle):
+    for key, val in G["threshold"].items():
+        name, mode = key.split(":")
+        assert oracle.set_threshold(INPUTS[name], int(mode)) == pytest.approx(val, abs=0, rel=0)
+
+
+def test_bwlabel(oracle):
+    for e in G["bwlabel"]:
+        lab, n = oracle.bwlabel(INPUTS["blobs40"], e["conn"], e["only_largest"], e["fill_bubbles"])
+        assert n == e["n"]
+        assert raw_hash(lab.astype(np.float32)) == e["sha256"]
+
+
+def test_marching_cubes_order(oracle):
+    v = INPUTS["sphere48"]
+    for e in G["marching_cubes"]:
+        t, p = oracle.marching_cubes(v, e["lo"], e["hi"], e["original_mc"], 50.0)
+        assert raw_hash(t.astype(np.int32), p.astype(np.float64)) == e["sha256"]
+
+
+def test_hc_and_sform(oracle):
+    hc = np.load(GOLD / "hc.npz")
+    t, p = hc["tris"], hc["pts"]
+    for it in (1, 5, 20):
+        assert np.array_equal(oracle.laplacian_smoothHC(p, t, 0.1, 0.5, it, True), hc[f"smoothed_{it}"])
+    assert np.array_equal(oracle.laplacian_smoothHC(p, hc["open_tris"], 0.1, 0.5, 5, True), hc["open_smoothed_5"])
+    for e in G["sform"]:
+        tt, pp = oracle.apply_sform(p, t, *e["rows"])
+        assert raw_hash(tt.astype(np.int32), pp.astype(np.float64)) == e["sha256"]
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference build (oracle/_ref) not present")
+@pytest.mark.parametrize("seed", [21, 22, 23])
+def test_oracle_vs_reference_random(oracle, seed):
+    from nii2mesh_gb300 import synth
+    rl, rc = Reference(False), Reference(True)
+    vol = synth.spheres(n=40, count=5, rmin=3, rmax=9, cmin=8, cmax=32, noise=12.0, seed=seed)
+    for variant, ref in ((MC33, rl), (MC_CLASSIC_TABLE, rl), (OLDCUBES, rc)):
+        for flags in ((True, True, True), (False, False, False), (True, False, True)):
+            a, b = oracle.meshify(vol, 50.0, variant, *flags), ref.meshify(vol, 50.0, variant, *flags)
+            ok, d, msg = mesh_equal(a, b, 0.0)
+            assert ok, msg
