@@ -126,6 +126,25 @@ n2m_status n2m_meshify_device(n2m_context *ctx, const float *d_img, const int di
 n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,
                                 double alpha, double beta, int iter, bool lock_edges);
 
+/* ---- allocation-free entry point -----------------------------------------------
+ * No counterpart in the reference.  HC smoothing (same semantics as
+ * n2m_smooth_hc_device) for callers that cannot call cudaMalloc: code inside
+ * another framework's captured or allocation-controlled region, or programs
+ * whose device memory all comes from their own pool.  All scratch lives in one
+ * fixed device array inside the library (about 11 MB, held by every GPU that
+ * loads the library until the process exits), so meshes are limited to
+ * N2M_NOALLOC_MAX_VERTS vertices and N2M_NOALLOC_MAX_TRIS triangles; larger
+ * meshes fail with N2M_ERR_TOO_LARGE before any work is queued.  d_verts and
+ * d_tris are device pointers; the work is queued on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) and the call returns without waiting.  The
+ * first call on each device looks up the array's device address (make it
+ * before any stream capture).  Every call shares the one array: calls whose
+ * work overlaps on the GPU race and corrupt each other's results. */
+#define N2M_NOALLOC_MAX_VERTS 131072
+#define N2M_NOALLOC_MAX_TRIS 262144
+n2m_status n2m_smooth_hc_noalloc(vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri, double alpha,
+                                 double beta, int iter, bool lock_edges, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

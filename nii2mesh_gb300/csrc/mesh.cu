@@ -10,6 +10,8 @@
 //   * apply_sform (src/meshify.c:1021-1045).
 #include <float.h>
 
+#include <mutex>
+
 #include "n2m_internal.cuh"
 
 namespace {
@@ -342,6 +344,113 @@ n2m_status mesh_apply_sform(vec3d *d_pts, vec3i *d_tris, int np, int nt, const f
                  pz = (double)(sz[0] + sz[1] + sz[2]);
     const float det = (float)(px * py * pz);
     if (det < 0.0) { k_flip<<<gs(nt), 256, 0, s>>>(d_tris, nt); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
+}
+
+// ---- allocation-free HC smoothing ---------------------------------------------------
+// For callers that cannot call cudaMalloc: code running inside another
+// framework's captured or allocation-controlled region, or a host program that
+// owns all device memory through its own pool.  The scratch of the HC
+// smoothing (CSR incidence, displacement buffers, flags) lives in one
+// file-scope device array of fixed size, so the entry point allocates nothing.
+// Limits: N2M_NOALLOC_MAX_VERTS vertices and N2M_NOALLOC_MAX_TRIS triangles
+// (about 11 MB, held by every GPU that loads the library until exit).
+namespace {
+constexpr size_t NA_V = N2M_NOALLOC_MAX_VERTS, NA_T = N2M_NOALLOC_MAX_TRIS;
+constexpr size_t na_align(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr size_t NA_START = 0;
+constexpr size_t NA_FILL = NA_START + na_align((NA_V + 1) * 4);
+constexpr size_t NA_REFS = NA_FILL + na_align(NA_V * 4);
+constexpr size_t NA_P = NA_REFS + na_align(NA_T * 3 * 4);
+constexpr size_t NA_Q = NA_P + na_align(NA_V * 12);
+constexpr size_t NA_B = NA_Q + na_align(NA_V * 12);
+constexpr size_t NA_LO = NA_B + na_align(NA_V * 12);
+constexpr size_t NA_HASNB = NA_LO + na_align(NA_V * 12);
+constexpr size_t NA_BORDER = NA_HASNB + na_align(NA_V);
+constexpr size_t NA_TOTAL = NA_BORDER + na_align(NA_V);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_TOTAL];
+
+void *g_noalloc_addr[128];     // device address of g_noalloc_scratch, per device
+std::mutex g_noalloc_mu;
+
+// exclusive scan of n <= NA_V + 1 counts in one CTA (n is small by construction)
+__global__ void __launch_bounds__(1024) k_scan_small(unsigned *d, int n) {
+    __shared__ unsigned part[1024];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 1024) {
+        const int i = base + threadIdx.x;
+        const unsigned v = i < n ? d[i] : 0u;
+        part[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            const unsigned t = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+            __syncthreads();
+            part[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < n) d[i] = carry + part[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += part[1023];
+        __syncthreads();
+    }
+}
+}  // namespace
+
+// First call on each device looks up the device address of the scratch array
+// with that device current; make that first call before any stream capture.
+extern "C" n2m_status n2m_smooth_hc_noalloc(vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri, double alpha,
+                                            double beta, int iter, bool lock_edges, void *stream) {
+    if (nvert < 0 || ntri < 0 || (nvert > 0 && !d_verts) || (ntri > 0 && !d_tris)) {
+        n2m_set_error("n2m_smooth_hc_noalloc: bad arguments");
+        return N2M_ERR_BAD_ARGS;
+    }
+    if ((size_t)nvert > NA_V || (size_t)ntri > NA_T) {
+        n2m_set_error("n2m_smooth_hc_noalloc: mesh of %d vertices / %d triangles exceeds the fixed scratch "
+                      "(max %d vertices, %d triangles)", nvert, ntri, N2M_NOALLOC_MAX_VERTS, N2M_NOALLOC_MAX_TRIS);
+        return N2M_ERR_TOO_LARGE;
+    }
+    if (nvert == 0 || iter <= 0) return N2M_OK;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return N2M_ERR_BAD_ARGS;
+    unsigned char *base;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            g_noalloc_addr[dev] = p;
+        }
+        base = (unsigned char *)g_noalloc_addr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned *start = (unsigned *)(base + NA_START), *fill = (unsigned *)(base + NA_FILL);
+    int *refs = (int *)(base + NA_REFS);
+    float3 *P = (float3 *)(base + NA_P), *Q = (float3 *)(base + NA_Q), *B = (float3 *)(base + NA_B),
+           *Lo = (float3 *)(base + NA_LO);
+    unsigned char *hasnb = base + NA_HASNB, *border = base + NA_BORDER;
+    // the array keeps the previous call's contents: clear what must start at zero
+    CK(cudaMemsetAsync(start, 0, ((size_t)nvert + 1) * sizeof(unsigned), s));
+    CK(cudaMemsetAsync(fill, 0, (size_t)nvert * sizeof(unsigned), s));
+    { k_degree<<<gs(ntri), 256, 0, s>>>(d_tris, ntri, start); N2M_COUNT(); }
+    { k_scan_small<<<1, 1024, 0, s>>>(start, nvert + 1); N2M_COUNT(); }
+    { k_fill_refs<<<gs(ntri), 256, 0, s>>>(d_tris, ntri, start, fill, refs); N2M_COUNT(); }
+    { k_sort_refs<<<gs(nvert), 256, 0, s>>>(start, nvert, refs); N2M_COUNT(); }
+    { k_hc_init<<<gs(nvert), 256, 0, s>>>(d_verts, d_tris, start, refs, nvert, Lo, P, hasnb); N2M_COUNT(); }
+    const float a1 = (float)(1.0 - alpha), b = (float)beta, b1 = (float)(1.0 - beta);
+    for (int it = 0; it < iter; it++) {
+        { k_hc_a<<<gs(nvert), 256, 0, s>>>(P, Lo, d_tris, start, refs, hasnb, nvert, a1, Q, B); N2M_COUNT(); }
+        { k_hc_b<<<gs(nvert), 256, 0, s>>>(Q, B, d_tris, start, refs, hasnb, nvert, b, b1, P); N2M_COUNT(); }
+    }
+    if (lock_edges) {
+        CK(cudaMemsetAsync(border, 0, (size_t)nvert, s));
+        { k_border<<<gs(nvert), 256, 0, s>>>(d_tris, start, refs, nvert, border); N2M_COUNT(); }
+    }
+    { k_hc_out<<<gs(nvert), 256, 0, s>>>(d_verts, P, border, nvert, lock_edges); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
