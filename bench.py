@@ -123,6 +123,61 @@ def cpu_reference(vol, steps, warmup):
     return nvox / statistics.median(times) / 1e9, kind, times, len(m[0])
 
 
+def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
+    """fwd and fwd+bwd ms on the 128^3 differentiation workload (pre-smooth,
+    Lewiner MC, 10 HC iterations; loss = sum(|v - c| - 40)^2), and the time of
+    200 gradient-descent steps of shape fitting."""
+    from nii2mesh_gb300 import synth
+    from nii2mesh_gb300.autograd import MeshifyFunction, sphere_loss
+    ctx = n2m.Context(torch.cuda.current_device())
+    img = torch.from_numpy(synth.sphere128()).cuda()
+    center, radius = (63.5, 63.5, 63.5), 40.0
+
+    def fwd(v):
+        pts, _ = MeshifyFunction.apply(v, ctx, 50.0, 10)
+        return sphere_loss(pts, center, radius)
+
+    def timed(fn, n):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / n * 1e3
+
+    def f_only():
+        with torch.no_grad():
+            float(fwd(img))
+
+    def f_b():
+        v = img.clone().requires_grad_(True)
+        fwd(v).backward()
+
+    t_f = timed(f_only, steps)
+    t_fb = timed(f_b, steps)
+    v = img.clone()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    first = last = None
+    for it in range(gd_steps):
+        v.requires_grad_(True)
+        loss = fwd(v)
+        loss.backward()
+        with torch.no_grad():
+            v = v - 0.05 * v.grad / (v.grad.abs().max() + 1e-12)
+        first = float(loss) if first is None else first
+        last = float(loss)
+    torch.cuda.synchronize()
+    t_gd = time.perf_counter() - t0
+    ctx.close()
+    return {"workload": "sphere128: 128^3 f32, spheres r 12-28, iso 50, -p 1, Lewiner, 10 HC iterations",
+            "fwd_ms": round(t_f, 3), "fwd_bwd_ms": round(t_fb, 3), "ratio": round(t_fb / t_f, 3),
+            "gd200_s": round(t_gd, 3), "gd_loss_first_last": [round(first, 2), round(last, 2)],
+            "timing": "wall clock per step incl. host syncs (forward reads back counts)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -233,13 +288,15 @@ def main():
         gv, kind, times, _ = cpu_reference(vol, 1, 0)
         cpu = {"value": round(gv, 6), "unit": "Gvox/s", "cores": 1, "kind": kind,
                "sample": f"one full 512^3 meshify ({times[0]:.1f} s)"}
+    adj = adjoint_metric(n2m, torch) if world == 1 else None
     line = {"metric": METRIC, "value": round(value, 4), "unit": "Gvox/s", "n_gpus": world, "steps": a.steps,
             "warmup": warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
             "config": {"workload": WORKLOAD, "l2": "inputs larger than L2 (537 MB volume)",
                        "parallelism": "replicas" if world > 1 else "single GPU", "triangles": nt, "vertices": nv},
             "stage_ms": {n: round(v, 4) for n, v in zip(STAGE_NAMES, stage_ms)},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck}
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck,
+            "adjoint": adj}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

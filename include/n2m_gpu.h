@@ -122,6 +122,18 @@ n2m_status n2m_meshify(n2m_context *ctx, const float *img, const int dim[3], con
 n2m_status n2m_meshify_device(n2m_context *ctx, const float *d_img, const int dim[3], const n2m_options *opt,
                               vec3i **d_t, vec3d **d_p, int *nt, int *np, n2m_report *rep);
 
+/* Adjoint (no counterpart in the reference; the spec differentiation
+ * path).  After an n2m_meshify_device / n2m_meshify call on ctx with Lewiner
+ * cubes and no clustering (only_largest = fill_bubbles = false), maps
+ * dL/d(vertex) (device float32, np x 3, the mesh of that call) to dL/d(voxel)
+ * (device float32, one per input voxel) for the fixed topology of that call:
+ * through the HC post-smoothing iterations (recomputed adjoint recursion),
+ * the weld, the edge interpolation u = c0/(c0-c1) and c-vertex means, and the
+ * transposed pre-smooth stencil.  Values clamped to FLT_EPSILON, padding and
+ * darkened edge voxels are constants of the forward pass (zero gradient).  If
+ * pre_smooth was false the forward's input buffer must still be valid. */
+n2m_status n2m_meshify_backward(n2m_context *ctx, const float *d_grad_pts, float *d_grad_img);
+
 /* HC smoothing of device-resident meshes (d_verts updated in place). */
 n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,
                                 double alpha, double beta, int iter, bool lock_edges);

@@ -18,7 +18,7 @@ STATUS = ["ok", "no CUDA device", "CUDA error", "out of memory", "bad arguments"
 SYMBOLS = ["n2m_context_create", "n2m_context_destroy", "n2m_context_stream", "n2m_last_error",
            "n2m_status_string", "n2m_device_count", "meshify", "laplacian_smoothHC", "marchingCubes", "bwlabel",
            "apply_sform", "n2m_set_oldcubes", "n2m_meshify", "n2m_meshify_device", "n2m_smooth_hc_device",
-           "n2m_kernel_launches"]
+           "n2m_kernel_launches", "n2m_meshify_backward", "n2m_smooth_hc_noalloc"]
 
 
 class vec3d(C.Structure):
@@ -82,6 +82,7 @@ def load(path=None):
     L.n2m_meshify_device.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip,
                                      C.POINTER(Report)]
     L.n2m_kernel_launches.restype = C.c_longlong
+    L.n2m_meshify_backward.argtypes = [vp, vp, vp]
     L.n2m_smooth_hc_device.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_bool]
     libc = C.CDLL(None)
     libc.free.argtypes = [vp]

@@ -76,6 +76,16 @@ struct n2m_context {
     DegWork deg;
     HcWork hc;
     void *pinned = nullptr;   // small readbacks
+    DevBuf gA, gB, gs, gtmp;   // adjoint scratch
+    // state of the last forward run that the adjoint needs
+    struct {
+        bool valid = false, smoothed = false, clustered = false;
+        int cubes = 0, nv_raw = 0, post_smooth = 0, nrem = 0, nov = 0;
+        int dim[3] = {0, 0, 0};
+        McGrid g;
+        McCounts mcn;
+        const int *removed = nullptr, *ov_id = nullptr, *ov_src = nullptr;
+    } fwd;
     // result of the last pipeline run (device pointers into the buffers above)
     vec3d *res_pts = nullptr;
     vec3i *res_tris = nullptr;
@@ -119,7 +129,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    DevBuf *bufs[] = {&c->in, &c->vol, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
+    DevBuf *bufs[] = {&c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->vol, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
                       &c->tris_raw, &c->pts, &c->tris, &c->ntf, &c->weld, &c->gath, &c->hmesh,
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
@@ -193,7 +203,8 @@ uint32_t key_bits(float f) {
 // (sorted), the id each merges into, and position overrides (the group's
 // last writer in the reference's vertex order).
 n2m_status weld_candidates(n2m_context *c, int nv, int ncand, bool oldcubes, std::vector<int> &removed,
-                           std::vector<int> &keep, std::vector<int> &ov_id, std::vector<vec3d> &ov_pos, vec3d v0) {
+                           std::vector<int> &keep, std::vector<int> &ov_id, std::vector<vec3d> &ov_pos,
+                           std::vector<int> &ov_src, vec3d v0) {
     std::vector<int> ids(ncand);
     CK(cudaMemcpyAsync(ids.data(), c->cand.p, ncand * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -253,6 +264,7 @@ n2m_status weld_candidates(n2m_context *c, int nv, int ncand, bool oldcubes, std
         } else if (glast[g] != i) {
             ov_id.push_back(ids[i]);
             ov_pos.push_back(pos[glast[g]]);
+            ov_src.push_back(ids[glast[g]]);
         }
     }
     // sort removed (with keep) and overrides by id
@@ -266,11 +278,12 @@ n2m_status weld_candidates(n2m_context *c, int nv, int ncand, bool oldcubes, std
     std::vector<int> oi(ov_id.size());
     for (size_t i = 0; i < oi.size(); i++) oi[i] = (int)i;
     std::sort(oi.begin(), oi.end(), [&](int a, int b) { return ov_id[a] < ov_id[b]; });
-    std::vector<int> o2;
+    std::vector<int> o2, s2;
     std::vector<vec3d> p2;
-    for (int i : oi) { o2.push_back(ov_id[i]); p2.push_back(ov_pos[i]); }
+    for (int i : oi) { o2.push_back(ov_id[i]); p2.push_back(ov_pos[i]); s2.push_back(ov_src[i]); }
     ov_id.swap(o2);
     ov_pos.swap(p2);
+    ov_src.swap(s2);
     (void)nv;
     return N2M_OK;
 }
@@ -368,6 +381,7 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
 // stage 4: marching cubes into pts_raw / tris_raw
 n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int *nv_out, int *nt_out,
                  int *ncand_out) {
+    c->fwd.valid = false;
     const bool old = cubes == N2M_CUBES_OLDCUBES;
     McGrid g;
     g.vol = P.vol;
@@ -439,6 +453,10 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
         }
     }
     CK(cudaEventRecord(c->evs[4], c->stream));
+    c->fwd.g = g;
+    c->fwd.mcn = mcn;
+    c->fwd.cubes = cubes;
+    c->fwd.nv_raw = (int)nv;
     *nv_out = (int)nv;
     *nt_out = (int)nt;
     *ncand_out = (int)nc[0];
@@ -464,6 +482,7 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     vec3d *pts = c->pts_raw.as<vec3d>();
     int np = nv;
     int welded = 0;
+    c->fwd.nrem = c->fwd.nov = 0;
     if (ncand > 0) {
         vec3d v0;
         if (o.cubes == N2M_CUBES_OLDCUBES) {
@@ -473,19 +492,25 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
         } else {
             CKS(readback(c, &v0, pts));
         }
-        std::vector<int> removed, keep, ov_id;
+        std::vector<int> removed, keep, ov_id, ov_src;
         std::vector<vec3d> ov_pos;
-        CKS(weld_candidates(c, nv, ncand, o.cubes == N2M_CUBES_OLDCUBES, removed, keep, ov_id, ov_pos, v0));
+        CKS(weld_candidates(c, nv, ncand, o.cubes == N2M_CUBES_OLDCUBES, removed, keep, ov_id, ov_pos, ov_src, v0));
         if (!removed.empty()) {
             const int nr = (int)removed.size(), no = (int)ov_id.size();
-            CKS(c->weld.ensure((size_t)(2 * nr + no + 1) * sizeof(int) + (size_t)(no + 1) * sizeof(vec3d)));
+            CKS(c->weld.ensure((size_t)(2 * nr + 2 * no + 2) * sizeof(int) + (size_t)(no + 1) * sizeof(vec3d)));
             vec3d *dov = c->weld.as<vec3d>();
             int *drem = (int *)(dov + no + 1);
-            int *dkeep = drem + nr, *dovid = dkeep + nr;
+            int *dkeep = drem + nr, *dovid = dkeep + nr, *dovsrc = dovid + no + 1;
             if (no) CK(cudaMemcpyAsync(dov, ov_pos.data(), no * sizeof(vec3d), cudaMemcpyHostToDevice, c->stream));
             CK(cudaMemcpyAsync(drem, removed.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
             CK(cudaMemcpyAsync(dkeep, keep.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
             if (no) CK(cudaMemcpyAsync(dovid, ov_id.data(), no * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            if (no) CK(cudaMemcpyAsync(dovsrc, ov_src.data(), no * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            c->fwd.removed = drem;
+            c->fwd.ov_id = dovid;
+            c->fwd.ov_src = dovsrc;
+            c->fwd.nrem = nr;
+            c->fwd.nov = no;
             np = nv - nr;
             CKS(c->pts.ensure((size_t)np * sizeof(vec3d)));
             CKS(mesh_apply_weld(pts, c->tris_raw.as<vec3i>(), nv, nt, drem, dkeep, nr, dovid, dov, no,
@@ -512,6 +537,11 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     c->res_tris = c->tris.as<vec3i>();
     c->res_np = np;
     c->res_nt = (int)ntf;
+    c->fwd.valid = true;
+    c->fwd.smoothed = o.pre_smooth && dim[0] >= 5 && dim[1] >= 5 && dim[2] >= 5;
+    c->fwd.clustered = o.only_largest || o.fill_bubbles;
+    c->fwd.post_smooth = 0;
+    for (int i = 0; i < 3; i++) c->fwd.dim[i] = dim[i];
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     if (o.verbose) {
@@ -569,6 +599,7 @@ extern "C" n2m_status n2m_meshify_device(n2m_context *c, const float *d_img, con
     if (!c || !opt || !dim) return N2M_ERR_BAD_ARGS;
     CK(cudaSetDevice(c->device));
     CKS(pipeline(c, d_img, dim, *opt, rep));
+    c->fwd.post_smooth = opt->post_smooth > 0 ? opt->post_smooth : 0;
     if (opt->post_smooth > 0) {
         const long long l0 = g_n2m_launches.load();
         CK(cudaEventRecord(c->evs[6], c->stream));
@@ -596,10 +627,55 @@ extern "C" n2m_status n2m_meshify(n2m_context *c, const float *img, const int di
     const size_t n = (size_t)dim[0] * dim[1] * dim[2];
     CKS(upload(c, img, n));
     CKS(pipeline(c, c->in.as<float>(), dim, *opt, rep));
+    c->fwd.post_smooth = opt->post_smooth > 0 ? opt->post_smooth : 0;
     if (opt->post_smooth > 0)
         CKS(mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc,
                            c->scan, c->stream));
     return to_host_mesh(c, t, p, nt, np);
+}
+
+// Adjoint of the last n2m_meshify_device / n2m_meshify call on ctx with fixed
+// topology: dL/d(final vertex) -> dL/d(input voxel), through the HC
+// iterations, the weld, the marching-cubes edge interpolation and c-vertex
+// means, and the transposed pre-smooth stencil.
+extern "C" n2m_status n2m_meshify_backward(n2m_context *c, const float *d_grad_pts, float *d_grad_img) {
+    if (!c || !d_grad_pts || !d_grad_img) return N2M_ERR_BAD_ARGS;
+    if (!c->fwd.valid) {
+        n2m_set_error("n2m_meshify_backward: no forward pass on this context");
+        return N2M_ERR_BAD_ARGS;
+    }
+    if (c->fwd.clustered || c->fwd.cubes == N2M_CUBES_OLDCUBES) {
+        n2m_set_error("n2m_meshify_backward: supported for the Lewiner cubes without clustering (-l 0 -b 0)");
+        return N2M_ERR_BAD_ARGS;
+    }
+    CK(cudaSetDevice(c->device));
+    const int np = c->res_np, nvr = c->fwd.nv_raw;
+    const size_t nvox = (size_t)c->fwd.dim[0] * c->fwd.dim[1] * c->fwd.dim[2];
+    CKS(c->gA.ensure((size_t)np * sizeof(float3)));
+    CKS(c->gB.ensure((size_t)nvr * sizeof(float3)));
+    CKS(c->gs.ensure(nvox * sizeof(float)));
+    const float3 *go = (const float3 *)d_grad_pts;
+    if (c->fwd.post_smooth > 0) {
+        CKS(mesh_smooth_hc_backward(c->res_tris, np, 0.1, 0.5, c->fwd.post_smooth, true, c->hc, go, c->gA.as<float3>(),
+                                    c->stream));
+        go = c->gA.as<float3>();
+    }
+    const float3 *graw = go;
+    if (c->fwd.nrem > 0) {
+        CKS(mesh_weld_backward(go, np, nvr, c->fwd.removed, c->fwd.nrem, c->fwd.ov_id, c->fwd.ov_src, c->fwd.nov,
+                               c->gB.as<float3>(), c->stream));
+        graw = c->gB.as<float3>();
+    }
+    float *gs = c->fwd.smoothed ? c->gs.as<float>() : d_grad_img;
+    CK(cudaMemsetAsync(gs, 0, nvox * sizeof(float), c->stream));
+    CKS(mc_backward(c->fwd.g, c->fwd.cubes, c->mc, c->fwd.mcn, graw, gs, c->stream));
+    if (c->fwd.smoothed) {
+        CKS(c->gtmp.ensure(nvox * sizeof(float)));
+        CKS(launch_smooth_adjoint(gs, c->gtmp.as<float>(), d_grad_img, c->fwd.dim[0], c->fwd.dim[1], c->fwd.dim[2],
+                                  c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return N2M_OK;
 }
 
 extern "C" n2m_status n2m_smooth_hc_device(n2m_context *c, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,

@@ -462,6 +462,114 @@ __global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, c
     (void)nwords;
 }
 
+// ---- adjoint of the vertex positions w.r.t. the processed volume -----------------
+// Same value fetch as gval, also returning the voxel the value depends on (-1
+// for padding, a darkened boundary voxel clamped to edge_max, or a value
+// clamped to FLT_EPSILON: those are constant in the forward pass).
+__device__ __forceinline__ float gval_src(const GV &g, int x, int y, int z, long long &src) {
+    const long long j = (long long)(g.lo0 + x) + (long long)(y + g.lo1) * g.dx + (long long)(z + g.lo2) * g.dxy;
+    float v;
+    src = -1;
+    if (j < g.nvox) {
+        v = __ldg(g.vol + j);
+        src = j;
+        int vx = g.lo0 + x, vy = y + g.lo1, vz = z + g.lo2;
+        if (vx >= g.dx || vy >= g.dy) {
+            vz = (int)(j / g.dxy);
+            const long long r = j - (long long)vz * g.dxy;
+            vy = (int)(r / g.dx);
+            vx = (int)(r - (long long)vy * g.dx);
+        }
+        if ((vx == 0 || vy == 0 || vz == 0 || vx == g.dx - 1 || vy == g.dy - 1 || vz == g.dz - 1) && !(v <= g.edge_max)) {
+            v = g.edge_max;
+            src = -1;
+        }
+        v = __fsub_rn(v, g.iso);
+    } else {
+        v = g.pad;
+    }
+    if (fabsf(v) < N2M_FLT_EPS) {
+        v = N2M_FLT_EPS;
+        src = -1;
+    }
+    return v;
+}
+
+// u = c0/(c0-c1): du/dc0 = -c1/(c0-c1)^2, du/dc1 = c0/(c0-c1)^2
+__device__ __forceinline__ void edge_adjoint(float gax, float c0, float c1, long long s0, long long s1, float *gs) {
+    const float den = c0 - c1;
+    if (den == 0.f || gax == 0.f) return;
+    const float inv2 = 1.f / (den * den);
+    if (s0 >= 0) atomicAdd(gs + s0, -gax * c1 * inv2);
+    if (s1 >= 0) atomicAdd(gs + s1, gax * c0 * inv2);
+}
+
+__device__ __forceinline__ float comp(const float3 &v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+
+// one warp per active word, mirroring k_emit; gv = dL/d(raw vertex position)
+__global__ void __launch_bounds__(256) k_mc_backward(GV g, bool classic, unsigned WX, const uint4 *__restrict__ words,
+                                                     const uint4 *__restrict__ offs, const unsigned *__restrict__ active,
+                                                     unsigned nactive, uint4 totals, const float3 *__restrict__ gv,
+                                                     float *gs) {
+    const unsigned lane = threadIdx.x & 31u;
+    for (unsigned aw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; aw < nactive; aw += (gridDim.x * blockDim.x) >> 5) {
+        const unsigned w = active[aw];
+        const unsigned row = w / WX, xw = w - row * WX;
+        const int z = (int)(row / (unsigned)g.NY), y = (int)(row - (unsigned)z * (unsigned)g.NY);
+        const int x = (int)(xw * 32u + lane);
+        const uint4 o = offs[w];
+        const uint4 m = words[w];
+        const bool in = x < g.NX;
+        const bool hx = in && x < g.NX - 1, hy = in && y < g.NY - 1, hz = in && z < g.NZ - 1;
+        const bool cube = hx && hy && hz;
+        const bool ex = (m.x >> lane) & 1u, ey = (m.y >> lane) & 1u, ez = (m.z >> lane) & 1u;
+        float c[8];
+        long long sr[8];
+        if (in) {
+            c[0] = gval_src(g, x, y, z, sr[0]);
+            c[1] = hx ? gval_src(g, x + 1, y, z, sr[1]) : c[0];
+            c[3] = hy ? gval_src(g, x, y + 1, z, sr[3]) : c[0];
+            c[4] = hz ? gval_src(g, x, y, z + 1, sr[4]) : c[0];
+            if (cube) {
+                c[2] = gval_src(g, x + 1, y + 1, z, sr[2]);
+                c[5] = gval_src(g, x + 1, y, z + 1, sr[5]);
+                c[6] = gval_src(g, x + 1, y + 1, z + 1, sr[6]);
+                c[7] = gval_src(g, x, y + 1, z + 1, sr[7]);
+            }
+        }
+        if (ex | ey | ez) {
+            const unsigned lt = (1u << lane) - 1u;
+            int id = (int)(o.x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt));
+            if (ex) { edge_adjoint(gv[id].x, c[0], c[1], sr[0], sr[1], gs); id++; }
+            if (ey) { edge_adjoint(gv[id].y, c[0], c[3], sr[0], sr[3], gs); id++; }
+            if (ez) edge_adjoint(gv[id].z, c[0], c[4], sr[0], sr[4], gs);
+        }
+        Tiling T = {0, 0, false};
+        if (cube) {
+            const int lut = cube_lut(c);
+            if (lut != 0 && lut != 255) T = select_tiling(c, lut, classic);
+        }
+        int cb = T.cv;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int b = __shfl_up_sync(0xffffffffu, cb, d);
+            if ((int)lane >= d) cb += b;
+        }
+        cb -= T.cv;
+        if (!T.cv) continue;
+        // c-vertex = mean of the cube's crossing edge vertices
+        const float3 gc = gv[totals.x + o.z + cb];
+        int n = 0;
+        for (int e = 0; e < 12; e++) n += (c[k_edge[e][2]] > 0.f) != (c[k_edge[e][3]] > 0.f);
+        if (!n) continue;
+        const float inv = 1.f / (float)n;
+        for (int e = 0; e < 12; e++) {
+            const int ax = k_edge[e][1], ca = k_edge[e][2], cbn = k_edge[e][3];
+            if ((c[ca] > 0.f) == (c[cbn] > 0.f)) continue;
+            edge_adjoint(comp(gc, ax) * inv, c[ca], c[cbn], sr[ca], sr[cbn], gs);
+        }
+    }
+}
+
 // vertices within 1.5e-5 of a c-vertex candidate become weld candidates too
 __global__ void k_ccand(const vec3d *__restrict__ pts, int np, const int *__restrict__ cc, int ncc, int *cand,
                         unsigned *ncand, int cap) {
@@ -526,6 +634,17 @@ n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, v
     if (nact == 0) return N2M_OK;
     const unsigned blocks = std::min<unsigned>((nact + 7) / 8, 152u * 16u);
     { k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.cand.as<unsigned>(), nact, (unsigned)nwords, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand, d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status mc_backward(const McGrid &g, int variant, McWork &w, const McCounts &c, const float3 *d_gv, float *d_gs,
+                       cudaStream_t s) {
+    const GV v = make_gv(g);
+    const unsigned WX = (unsigned)((g.n[0] + 31) / 32);
+    if (c.nactive == 0) return N2M_OK;
+    const unsigned blocks = std::min<unsigned>((c.nactive + 7) / 8, 152u * 16u);
+    { k_mc_backward<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.cand.as<unsigned>(), c.nactive, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_gv, d_gs); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

@@ -245,6 +245,82 @@ __global__ void k_hc_out(vec3d *o, const float3 *__restrict__ P, const unsigned 
     }
 }
 
+// ---- HC adjoint ------------------------------------------------------------------------
+// One iteration is p' = A p + B o with L the (row-normalised) neighbour mean:
+//   A = beta(1-alpha) I + (1-beta)(2-alpha) L - (1-beta) L^2,  B = alpha beta I + alpha(1-beta) L.
+// Backward: lambda = dL/dp_K; per iteration g_o += B^T lambda, lambda = A^T lambda; finally
+// g_o += lambda (p_0 = o).  L^T y at j sums y_i / num_i over the same (triangle, slot)
+// references (the neighbour relation is symmetric); isolated vertices are identity rows.
+__global__ void k_scale_inv(const float3 *__restrict__ Y, const unsigned *__restrict__ start, int np, float3 *Ys) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int d = (int)(start[i + 1] - start[i]);
+        const float s = d ? 1.f / (2.f * (float)d) : 0.f;
+        const float3 y = Y[i];
+        Ys[i] = make_float3(y.x * s, y.y * s, y.z * s);
+    }
+}
+
+__global__ void k_lapT(const float3 *__restrict__ Ys, const float3 *__restrict__ Y, const vec3i *__restrict__ t,
+                       const unsigned *__restrict__ start, const int *__restrict__ refs, int np, float3 *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int a0 = (int)start[i], a1 = (int)start[i + 1];
+        if (a0 == a1) { out[i] = Y[i]; continue; }
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        for (int k = a0; k < a1; k++) {
+            int a, b;
+            others(t, refs[k], a, b);
+            const float3 A = Ys[a], B = Ys[b];
+            sx += A.x + B.x; sy += A.y + B.y; sz += A.z + B.z;
+        }
+        out[i] = make_float3(sx, sy, sz);
+    }
+}
+
+__global__ void k_hcT_init(const float3 *__restrict__ g, const unsigned char *__restrict__ border, int np, bool lock,
+                           float3 *lam, float3 *go) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const bool b = lock && border[i];
+        lam[i] = b ? make_float3(0.f, 0.f, 0.f) : g[i];
+        go[i] = b ? g[i] : make_float3(0.f, 0.f, 0.f);
+    }
+}
+
+// go += ab*lam + a1b*t1 ; lam = c0*lam + c1*t1 - c2*t2
+__global__ void k_hcT_step(float3 *lam, const float3 *__restrict__ t1, const float3 *__restrict__ t2, float3 *go, int np,
+                           float ab, float a1b, float c0, float c1, float c2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const float3 l = lam[i], u = t1[i], v = t2[i];
+        float3 o = go[i];
+        o.x += ab * l.x + a1b * u.x; o.y += ab * l.y + a1b * u.y; o.z += ab * l.z + a1b * u.z;
+        go[i] = o;
+        lam[i] = make_float3(c0 * l.x + c1 * u.x - c2 * v.x, c0 * l.y + c1 * u.y - c2 * v.y, c0 * l.z + c1 * u.z - c2 * v.z);
+    }
+}
+
+__global__ void k_add3(float3 *go, const float3 *__restrict__ lam, int np) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const float3 l = lam[i];
+        go[i].x += l.x; go[i].y += l.y; go[i].z += l.z;
+    }
+}
+
+// raw vertex gradient: every kept raw vertex receives its welded vertex's
+// gradient, except that a merged group's gradient goes to the member whose
+// position it kept
+__global__ void k_weld_back(const float3 *__restrict__ go, int nv_raw, const int *__restrict__ removed, int nrem,
+                            const int *__restrict__ ov_id, const int *__restrict__ ov_src, int nov, float3 *graw) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv_raw; i += gridDim.x * blockDim.x) {
+        const int r = lower_bound(removed, nrem, i);
+        if (r < nrem && removed[r] == i) continue;
+        const int o = lower_bound(ov_id, nov, i);
+        const int src = (o < nov && ov_id[o] == i) ? ov_src[o] : i;
+        const float3 g = go[i - r];
+        atomicAdd(&graw[src].x, g.x);
+        atomicAdd(&graw[src].y, g.y);
+        atomicAdd(&graw[src].z, g.z);
+    }
+}
+
 __global__ void k_sform(vec3d *p, int np, double a0, double a1, double a2, double a3, double b0, double b1, double b2,
                         double b3, double c0, double c1, double c2, double c3) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
@@ -333,6 +409,37 @@ n2m_status mesh_smooth_hc(vec3d *d_pts, const vec3i *d_tris, int np, int nt, dou
     }
     { k_hc_out<<<gs(np), 256, 0, s>>>(d_pts, w.P.as<float3>(), w.border.as<unsigned char>(), np, lock_edges); N2M_COUNT(); }
     CKL();
+    return N2M_OK;
+}
+
+n2m_status mesh_smooth_hc_backward(const vec3i *d_tris, int np, double alpha, double beta, int iter, bool lock_edges,
+                                   HcWork &w, const float3 *d_g, float3 *d_go, cudaStream_t s) {
+    // buffers of the forward: start, refs, border; scratch: P (lambda), Q (t1), B (t2), Lo (scaled)
+    const unsigned *start = w.start.as<unsigned>();
+    const int *refs = w.refs.as<int>();
+    float3 *lam = w.P.as<float3>(), *t1 = w.Q.as<float3>(), *t2 = w.B.as<float3>(), *ys = w.Lo.as<float3>();
+    { k_hcT_init<<<gs(np), 256, 0, s>>>(d_g, w.border.as<unsigned char>(), np, lock_edges, lam, d_go); N2M_COUNT(); }
+    const float al = (float)alpha, be = (float)beta;
+    const float ab = al * be, a1b = al * (1.f - be);
+    const float c0 = be * (1.f - al), c1 = (1.f - be) * (2.f - al), c2 = 1.f - be;
+    for (int it = 0; it < iter; it++) {
+        { k_scale_inv<<<gs(np), 256, 0, s>>>(lam, start, np, ys); N2M_COUNT(); }
+        { k_lapT<<<gs(np), 256, 0, s>>>(ys, lam, d_tris, start, refs, np, t1); N2M_COUNT(); }
+        { k_scale_inv<<<gs(np), 256, 0, s>>>(t1, start, np, ys); N2M_COUNT(); }
+        { k_lapT<<<gs(np), 256, 0, s>>>(ys, t1, d_tris, start, refs, np, t2); N2M_COUNT(); }
+        { k_hcT_step<<<gs(np), 256, 0, s>>>(lam, t1, t2, d_go, np, ab, a1b, c0, c1, c2); N2M_COUNT(); }
+    }
+    { k_add3<<<gs(np), 256, 0, s>>>(d_go, lam, np); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status mesh_weld_backward(const float3 *d_go, int np_final, int nv_raw, const int *d_removed, int nrem,
+                              const int *d_ov_id, const int *d_ov_src, int nov, float3 *d_graw, cudaStream_t s) {
+    CK(cudaMemsetAsync(d_graw, 0, (size_t)nv_raw * sizeof(float3), s));
+    { k_weld_back<<<gs(nv_raw), 256, 0, s>>>(d_go, nv_raw, d_removed, nrem, d_ov_id, d_ov_src, nov, d_graw); N2M_COUNT(); }
+    CKL();
+    (void)np_final;
     return N2M_OK;
 }
 

@@ -69,6 +69,8 @@ struct VolStats {
 // smooth.cu
 n2m_status launch_smooth(const float *in, float *out, int nx, int ny, int nz, float iso, VolStats *st,
                          cudaStream_t s);
+// transposed pre-smooth: g_img = Sx^T Sy^T Sz^T g (tmp: one volume of scratch)
+n2m_status launch_smooth_adjoint(const float *g, float *tmp, float *out, int nx, int ny, int nz, cudaStream_t s);
 n2m_status launch_stats(const float *vol, int nx, int ny, int nz, float iso, bool minmax, VolStats *st,
                         cudaStream_t s);
 void stats_init_host(VolStats *h);
@@ -107,6 +109,8 @@ struct McCounts {
 n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s);
 n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,
                    int *d_cand, unsigned *d_ncand, int cand_cap, cudaStream_t s);
+n2m_status mc_backward(const McGrid &g, int variant, McWork &w, const McCounts &c, const float3 *d_gv, float *d_gs,
+                       cudaStream_t s);
 n2m_status mc_ccand_scan(const vec3d *d_pts, int np, const int *d_ccand, int nccand, int *d_cand,
                          unsigned *d_ncand, int cand_cap, cudaStream_t s);
 
@@ -131,5 +135,11 @@ struct HcWork {
 };
 n2m_status mesh_smooth_hc(vec3d *d_pts, const vec3i *d_tris, int np, int nt, double alpha, double beta, int iter,
                           bool lock_edges, HcWork &w, ScanWork &sw, cudaStream_t s);
+// adjoint of mesh_smooth_hc (uses the CSR and border flags the forward left in w)
+n2m_status mesh_smooth_hc_backward(const vec3i *d_tris, int np, double alpha, double beta, int iter, bool lock_edges,
+                                   HcWork &w, const float3 *d_g, float3 *d_go, cudaStream_t s);
+// grad of raw (pre-weld) vertices from grad of welded vertices
+n2m_status mesh_weld_backward(const float3 *d_go, int np_final, int nv_raw, const int *d_removed, int nrem,
+                              const int *d_ov_id, const int *d_ov_src, int nov, float3 *d_graw, cudaStream_t s);
 n2m_status mesh_apply_sform(vec3d *d_pts, vec3i *d_tris, int np, int nt, const float sx[4], const float sy[4],
                             const float sz[4], cudaStream_t s);

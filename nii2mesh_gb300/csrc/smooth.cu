@@ -13,6 +13,8 @@
 // pass.  Algorithmic traffic: 4 B read + 4 B written per voxel.
 #include <float.h>
 
+#include <algorithm>
+
 #include "exact.cuh"
 #include "n2m_internal.cuh"
 
@@ -219,6 +221,37 @@ n2m_status launch_smooth(const float *in, float *out, int nx, int ny, int nz, fl
                          cudaStream_t s) {
     dim3 grid((nx + STX - 1) / STX, (ny + STY - 1) / STY, (nz + SZC - 1) / SZC);
     { k_smooth<<<grid, dim3(STX, STY), 0, s>>>(in, out, nx, ny, nz, iso, st); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
+}
+
+namespace {
+// transposed 5-tap pass along one axis: out_j = sum over interior rows i with
+// |i-j| <= 2 of w_|i-j| g_i, plus g_j where j itself is a row left unfiltered
+__global__ void k_smooth_T(const float *__restrict__ g, float *__restrict__ out, int nx, int ny, int nz, int axis) {
+    const long long n = (long long)nx * ny * nz;
+    const long long stride = axis == 0 ? 1 : (axis == 1 ? nx : (long long)nx * ny);
+    const int len = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    const float w[3] = {0.45f, 0.225f, 0.05f};
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const long long q = v / stride;
+        const int j = (int)(axis == 0 ? q % nx : (axis == 1 ? q % ny : q));
+        float acc = (j < 2 || j > len - 3) ? g[v] : 0.f;
+        for (int d = -2; d <= 2; d++) {
+            const int i = j + d;
+            if (i >= 2 && i <= len - 3) acc += w[d < 0 ? -d : d] * g[v + d * stride];
+        }
+        out[v] = acc;
+    }
+}
+}  // namespace
+
+n2m_status launch_smooth_adjoint(const float *g, float *tmp, float *out, int nx, int ny, int nz, cudaStream_t s) {
+    const long long n = (long long)nx * ny * nz;
+    const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 152 * 64);
+    { k_smooth_T<<<blocks, 256, 0, s>>>(g, out, nx, ny, nz, 2); N2M_COUNT(); }
+    { k_smooth_T<<<blocks, 256, 0, s>>>(out, tmp, nx, ny, nz, 1); N2M_COUNT(); }
+    { k_smooth_T<<<blocks, 256, 0, s>>>(tmp, out, nx, ny, nz, 0); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

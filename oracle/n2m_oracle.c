@@ -289,6 +289,8 @@ typedef struct {
     int nv, capv;
     int *tr;                     /* triangles (v1,v2,v3) in emission order */
     int nt, capt;
+    int *src;                    /* optional: per vertex (kind, grid index, axis); kind 1 = c-vertex */
+    int cur_kind, cur_index, cur_axis;
     int i, j, k, kase, config, subconfig;
     float cube[8];
 } mcx;
@@ -301,7 +303,9 @@ static int push_vertex(mcx *m, float x, float y, float z) {
     if (m->nv >= m->capv) {
         m->capv = m->capv ? 2 * m->capv : 65536;
         m->vp = (float *)realloc(m->vp, (size_t)m->capv * 3 * sizeof(float));
+        m->src = (int *)realloc(m->src, (size_t)m->capv * 3 * sizeof(int));
     }
+    m->src[3 * m->nv] = m->cur_kind; m->src[3 * m->nv + 1] = m->cur_index; m->src[3 * m->nv + 2] = m->cur_axis;
     m->vp[3 * m->nv] = x; m->vp[3 * m->nv + 1] = y; m->vp[3 * m->nv + 2] = z;
     return m->nv++;
 }
@@ -324,14 +328,18 @@ static void mc_edge_vertices(mcx *m) {
                 if (c0 < 0) { ex = c1 > 0; ey = c3 > 0; ez = c4 > 0; }
                 else { ex = c1 < 0; ey = c3 < 0; ez = c4 < 0; }
                 size_t g = gi(m, i, j, k);
+                m->cur_kind = 0; m->cur_index = (int)g;
+                m->cur_axis = 0;
                 if (ex) {
                     float den = c0 - c1, u = den != 0.0f ? c0 / den : 0.5f;
                     m->xv[g] = push_vertex(m, (float)i + u, (float)j, (float)k);
                 }
+                m->cur_axis = 1;
                 if (ey) {
                     float den = c0 - c3, u = den != 0.0f ? c0 / den : 0.5f;
                     m->yv[g] = push_vertex(m, (float)i, (float)j + u, (float)k);
                 }
+                m->cur_axis = 2;
                 if (ez) {
                     float den = c0 - c4, u = den != 0.0f ? c0 / den : 0.5f;
                     m->zv[g] = push_vertex(m, (float)i, (float)j, (float)k + u);
@@ -415,6 +423,7 @@ static int mc_test_interior(const mcx *m, int s) {
  * existing edge vertices, visited in edge order 0..11. */
 static int mc_c_vertex(mcx *m) {
     const int i = m->i, j = m->j, k = m->k;
+    m->cur_kind = 1; m->cur_index = (int)gi(m, i, j, k); m->cur_axis = -1;
     const int *ids[12] = {&m->xv[gi(m, i, j, k)],         &m->yv[gi(m, i + 1, j, k)],
                           &m->xv[gi(m, i, j + 1, k)],     &m->yv[gi(m, i, j, k)],
                           &m->xv[gi(m, i, j, k + 1)],     &m->yv[gi(m, i + 1, j, k + 1)],
@@ -589,6 +598,7 @@ int or_mc_raw(const float *data, int nx, int ny, int nz, int originalMC, float *
     m.nx = nx; m.ny = ny; m.nz = nz; m.original = originalMC; m.d = data;
     mc_run(&m);
     *verts = m.vp; *tris = m.tr; *nv = m.nv; *nt = m.nt;
+    free(m.src);
     return 0;
 }
 
@@ -596,6 +606,9 @@ int or_mc_raw(const float *data, int nx, int ny, int nz, int originalMC, float *
  * spans the padded bbox; a grid point maps to linear voxel index
  * lo0+x + (y+lo1)*dim0 + (z+lo2)*dim0*dim1 (so x past the row end reads the
  * next row), and indices past the volume hold min-minus-isolevel. */
+/* when set, mc_lewiner hands out the per-vertex sources (test use only) */
+static int **mc_sources_out = NULL;
+
 static int mc_lewiner(float *img, const short dim[3], const int lo[3], const int hi[3], int originalMC, float iso,
                       or_vec3d **vs, or_vec3i **ts, int *nv, int *nt) {
     const int NX = hi[0] - lo[0] + 1, NY = hi[1] - lo[1] + 1, NZ = hi[2] - lo[2] + 1;
@@ -618,7 +631,7 @@ static int mc_lewiner(float *img, const short dim[3], const int lo[3], const int
     m.nx = NX; m.ny = NY; m.nz = NZ; m.original = originalMC; m.d = g;
     mc_run(&m);
     free(g);
-    if (m.nv < 3 || m.nt < 1) { free(m.vp); free(m.tr); return 1; }
+    if (m.nv < 3 || m.nt < 1) { free(m.vp); free(m.tr); free(m.src); return 1; }
     *vs = (or_vec3d *)malloc((size_t)m.nv * sizeof(or_vec3d));
     for (int i = 0; i < m.nv; i++) {
         (*vs)[i].x = m.vp[3 * i] + lo[0];
@@ -632,7 +645,8 @@ static int mc_lewiner(float *img, const short dim[3], const int lo[3], const int
         (*ts)[i].z = m.tr[3 * i];
     }
     *nv = m.nv; *nt = m.nt;
-    free(m.vp); free(m.tr);
+    if (mc_sources_out) { *mc_sources_out = m.src; m.src = NULL; }
+    free(m.vp); free(m.tr); free(m.src);
     return 0;
 }
 
@@ -684,6 +698,17 @@ static int mc_oldcubes(const float *img, const short dim[3], const int lo[3], co
     for (int i = 0; i < ntri; i++) { (*ts)[i].x = 3 * i; (*ts)[i].y = 3 * i + 1; (*ts)[i].z = 3 * i + 2; }
     *nv = (int)n; *nt = ntri;
     return 0;
+}
+
+/* Lewiner marching cubes that also reports, per vertex, where it comes from:
+ * (0, grid point, axis) for edge vertices, (1, cube, -1) for c-vertices,
+ * grid indices over the padded box (hi-lo+1 points per axis). */
+int or_marching_cubes_sources(float *img, const short dim[3], const int lo[3], const int hi[3], int originalMC,
+                              float isolevel, or_vec3d **vs, or_vec3i **ts, int *nv, int *nt, int **src) {
+    mc_sources_out = src;
+    int r = mc_lewiner(img, dim, lo, hi, originalMC, isolevel, vs, ts, nv, nt);
+    mc_sources_out = NULL;
+    return r;
 }
 
 int or_marching_cubes(float *img, const short dim[3], const int lo[3], const int hi[3], int variant, float isolevel,

@@ -37,6 +37,8 @@ int or_prepare_volume(float *img, const short dim[3], float *isolevel, bool preS
 
 int or_marching_cubes(float *img, const short dim[3], const int lo[3], const int hi[3], int variant,
                       float isolevel, or_vec3d **vs, or_vec3i **ts, int *nv, int *nt);
+int or_marching_cubes_sources(float *img, const short dim[3], const int lo[3], const int hi[3], int originalMC,
+                              float isolevel, or_vec3d **vs, or_vec3i **ts, int *nv, int *nt, int **src);
 /* Raw Lewiner run() on an already iso-subtracted grid (the MC self-test,
  * src/MarchingCubes.c:1374-1405): vertices in grid coordinates (float). */
 int or_mc_raw(const float *data, int nx, int ny, int nz, int originalMC, float **verts, int **tris,

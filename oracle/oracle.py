@@ -73,6 +73,9 @@ class Oracle:
                                         C.POINTER(C.c_int)]
         L.or_meshify.argtypes = [_f32p, C.POINTER(C.c_short), C.c_int, C.c_float, C.POINTER(C.c_void_p),
                                  C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_bool, C.c_bool, C.c_bool]
+        L.or_marching_cubes_sources.argtypes = [_f32p, C.POINTER(C.c_short), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                C.c_int, C.c_float, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                                C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_void_p)]
         L.or_mc_raw.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.or_laplacian_smoothHC.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_bool]
@@ -117,6 +120,19 @@ class Oracle:
         if r:
             return None
         return _take_mesh(self.lib, tp, pp, nt.value, nv.value)
+
+    def marching_cubes_sources(self, img, lo, hi, iso, original_mc=0):
+        """(tris, pts, src): src[i] = (kind, grid index, axis) for raw vertex i"""
+        a = _as_vol(img)
+        tp, pp, nv, nt, sp = C.c_void_p(), C.c_void_p(), C.c_int(), C.c_int(), C.c_void_p()
+        r = self.lib.or_marching_cubes_sources(a, _dims(a), (C.c_int * 3)(*lo), (C.c_int * 3)(*hi), original_mc, iso,
+                                               C.byref(pp), C.byref(tp), C.byref(nv), C.byref(nt), C.byref(sp))
+        if r:
+            return None
+        src = np.ctypeslib.as_array(C.cast(sp, C.POINTER(C.c_int)), shape=(nv.value, 3)).copy()
+        self.lib.or_free(sp)
+        t, p = _take_mesh(self.lib, tp, pp, nt.value, nv.value)
+        return t, p, src
 
     def mc_raw(self, data, original_mc=0):
         a = _as_vol(data)
