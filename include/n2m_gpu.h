@@ -134,6 +134,32 @@ n2m_status n2m_meshify_device(n2m_context *ctx, const float *d_img, const int di
  * pre_smooth was false the forward's input buffer must still be valid. */
 n2m_status n2m_meshify_backward(n2m_context *ctx, const float *d_grad_pts, float *d_grad_img);
 
+/* ---- atlas (src/nii2mesh.c:492-583) ---------------------------------------------
+ * Meshes every label 1..max of a label volume as its own binary mask (the
+ * reference's `lo < v < hi` window around each integer label) at isolevel
+ * 0.5, with opt's pre-smooth / largest-cluster / bubble-fill / post-smooth
+ * options (opt->isolevel is ignored).  N2M_ATLAS_BATCHED runs all labels
+ * together on per-label sub-boxes (one launch per stage over a shared work
+ * queue); N2M_ATLAS_LOOP runs the full single-volume pipeline once per label.
+ * Both give the same meshes.  Labels without voxels are skipped, as in the
+ * reference.  Results are concatenated; triangle indices are local to their
+ * mesh. */
+typedef enum { N2M_ATLAS_BATCHED = 0, N2M_ATLAS_LOOP = 1 } n2m_atlas_mode;
+typedef struct {
+    int label;
+    int status;                      /* N2M_OK, or why this label has no mesh */
+    int nvert, ntri;
+    int64_t vert_offset, tri_offset; /* into the concatenated vertex / triangle arrays */
+} n2m_atlas_mesh;
+/* d_labels: device int16 volume (x fastest).  Meshes stay in context-owned
+ * device memory until the next call on ctx; *meshes points into the context. */
+n2m_status n2m_atlas_device(n2m_context *ctx, const int16_t *d_labels, const int dim[3], const n2m_options *opt,
+                            int mode, int *nmesh, const n2m_atlas_mesh **meshes, vec3d **d_pts, vec3i **d_tris,
+                            int64_t *npts, int64_t *ntris, n2m_report *rep);
+/* Host volume in; everything malloc'd (free() each array). */
+n2m_status n2m_atlas(n2m_context *ctx, const int16_t *labels, const int dim[3], const n2m_options *opt, int mode,
+                     int *nmesh, n2m_atlas_mesh **meshes, vec3d **pts, vec3i **tris, int64_t *npts, int64_t *ntris);
+
 /* HC smoothing of device-resident meshes (d_verts updated in place). */
 n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,
                                 double alpha, double beta, int iter, bool lock_edges);

@@ -17,9 +17,10 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import N2MError, Options, Report, vec3d, vec3i
+from ._lib import AtlasMesh, N2MError, Options, Report, vec3d, vec3i
 
 MC33, CLASSIC_TABLE, OLDCUBES = 0, 1, 2
+ATLAS_BATCHED, ATLAS_LOOP = 0, 1
 
 __all__ = ["Context", "meshify", "laplacian_smoothHC", "marching_cubes", "bwlabel", "apply_sform", "N2MError",
            "MC33", "CLASSIC_TABLE", "OLDCUBES", "lib"]
@@ -99,6 +100,48 @@ class Context:
         _lib.check(self._L.n2m_meshify_device(self.h, C.c_void_p(d_img_ptr), dims, C.byref(o), C.byref(tp), C.byref(pp),
                                               C.byref(nt), C.byref(np_), C.byref(rep)), "n2m_meshify_device")
         return tp.value, pp.value, nt.value, np_.value, rep.as_dict()
+
+
+    def atlas(self, labels, cubes=MC33, pre_smooth=True, only_largest=True, fill_bubbles=True, post_smooth=5,
+              mode=ATLAS_BATCHED):
+        """Mesh every label of an int16 label volume (n2m_atlas).  Returns a
+        list of (label, status, tris, pts) — tris local to each mesh."""
+        a = np.ascontiguousarray(labels, dtype=np.int16)
+        nz, ny, nx = a.shape
+        o = self._opts(0.5, cubes, pre_smooth, only_largest, fill_bubbles, post_smooth, False)
+        nm = C.c_int()
+        mp, pp, tp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        npts, ntri = C.c_int64(), C.c_int64()
+        _lib.check(self._L.n2m_atlas(self.h, a.ctypes.data, (C.c_int * 3)(nx, ny, nz), C.byref(o), int(mode),
+                                     C.byref(nm), C.byref(mp), C.byref(pp), C.byref(tp), C.byref(npts),
+                                     C.byref(ntri)), "n2m_atlas")
+        ms = C.cast(mp, C.POINTER(AtlasMesh))
+        pts = np.ctypeslib.as_array(C.cast(pp, C.POINTER(C.c_double)), shape=(max(npts.value, 1), 3))[:npts.value].copy()
+        tri = np.ctypeslib.as_array(C.cast(tp, C.POINTER(C.c_int)), shape=(max(ntri.value, 1), 3))[:ntri.value].copy()
+        out = []
+        for i in range(nm.value):
+            m = ms[i]
+            out.append((m.label, m.status, tri[m.tri_offset:m.tri_offset + m.ntri],
+                        pts[m.vert_offset:m.vert_offset + m.nvert]))
+        for ptr in (mp, pp, tp):
+            self._L.libc_free(ptr)
+        return out
+
+    def atlas_device(self, d_labels_ptr, dims_xyz, cubes=MC33, pre_smooth=True, only_largest=True, fill_bubbles=True,
+                     post_smooth=5, mode=ATLAS_BATCHED):
+        """Device label volume in; meshes stay on the device.  Returns
+        (number of meshes, total vertices, total triangles, report)."""
+        o = self._opts(0.5, cubes, pre_smooth, only_largest, fill_bubbles, post_smooth, False)
+        nm = C.c_int()
+        mp = C.POINTER(AtlasMesh)()
+        pp, tp = C.c_void_p(), C.c_void_p()
+        npts, ntri = C.c_int64(), C.c_int64()
+        rep = Report()
+        _lib.check(self._L.n2m_atlas_device(self.h, C.c_void_p(d_labels_ptr), (C.c_int * 3)(*dims_xyz), C.byref(o),
+                                            int(mode), C.byref(nm), C.byref(mp), C.byref(pp), C.byref(tp),
+                                            C.byref(npts), C.byref(ntri), C.byref(rep)), "n2m_atlas_device")
+        ok = sum(1 for i in range(nm.value) if mp[i].status == 0)
+        return nm.value, ok, npts.value, ntri.value, rep.as_dict()
 
 
 # ---- the reference's entry points, through the drop-in C symbols -----------------

@@ -18,7 +18,7 @@ STATUS = ["ok", "no CUDA device", "CUDA error", "out of memory", "bad arguments"
 SYMBOLS = ["n2m_context_create", "n2m_context_destroy", "n2m_context_stream", "n2m_last_error",
            "n2m_status_string", "n2m_device_count", "meshify", "laplacian_smoothHC", "marchingCubes", "bwlabel",
            "apply_sform", "n2m_set_oldcubes", "n2m_meshify", "n2m_meshify_device", "n2m_smooth_hc_device",
-           "n2m_kernel_launches", "n2m_meshify_backward", "n2m_smooth_hc_noalloc"]
+           "n2m_kernel_launches", "n2m_meshify_backward", "n2m_smooth_hc_noalloc", "n2m_atlas", "n2m_atlas_device"]
 
 
 class vec3d(C.Structure):
@@ -32,6 +32,11 @@ class vec3i(C.Structure):
 class Options(C.Structure):
     _fields_ = [("cubes", C.c_int), ("isolevel", C.c_float), ("pre_smooth", C.c_bool), ("only_largest", C.c_bool),
                 ("fill_bubbles", C.c_bool), ("post_smooth", C.c_int), ("verbose", C.c_bool)]
+
+
+class AtlasMesh(C.Structure):
+    _fields_ = [("label", C.c_int), ("status", C.c_int), ("nvert", C.c_int), ("ntri", C.c_int),
+                ("vert_offset", C.c_int64), ("tri_offset", C.c_int64)]
 
 
 class Report(C.Structure):
@@ -83,6 +88,11 @@ def load(path=None):
                                      C.POINTER(Report)]
     L.n2m_kernel_launches.restype = C.c_longlong
     L.n2m_meshify_backward.argtypes = [vp, vp, vp]
+    i64p = C.POINTER(C.c_int64)
+    L.n2m_atlas.argtypes = [vp, vp, ip, C.POINTER(Options), C.c_int, ip, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
+                            i64p, i64p]
+    L.n2m_atlas_device.argtypes = [vp, vp, ip, C.POINTER(Options), C.c_int, ip, C.POINTER(C.POINTER(AtlasMesh)),
+                                   C.POINTER(vp), C.POINTER(vp), i64p, i64p, C.POINTER(Report)]
     L.n2m_smooth_hc_device.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_bool]
     libc = C.CDLL(None)
     libc.free.argtypes = [vp]

@@ -77,6 +77,9 @@ struct n2m_context {
     HcWork hc;
     void *pinned = nullptr;   // small readbacks
     DevBuf gA, gB, gs, gtmp;   // adjoint scratch
+    AtlasWork aw;
+    DevBuf alab, lpts, ltris;   // atlas input copy, per-label-loop output
+    std::vector<n2m_atlas_mesh> atlas_meshes;
     // state of the last forward run that the adjoint needs
     struct {
         bool valid = false, smoothed = false, clustered = false;
@@ -129,7 +132,10 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    DevBuf *bufs[] = {&c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->vol, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
+    DevBuf *bufs[] = {&c->aw.cnt, &c->aw.bb, &c->aw.boxes, &c->aw.queue, &c->aw.arena, &c->aw.mask, &c->aw.keep,
+                      &c->aw.lab, &c->aw.edge, &c->aw.ucnt, &c->aw.words, &c->aw.counts, &c->aw.active, &c->aw.tot,
+                      &c->aw.pts, &c->aw.pts2, &c->aw.tris, &c->aw.tris2, &c->aw.cand, &c->aw.gath, &c->aw.weld,
+                      &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->vol, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
                       &c->tris_raw, &c->pts, &c->tris, &c->ntf, &c->weld, &c->gath, &c->hmesh,
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
@@ -155,6 +161,7 @@ struct TlsCtx {
 };
 thread_local TlsCtx g_tls;
 int g_oldcubes = 0;
+thread_local bool g_quiet = false;   // atlas runs do not print per-label messages
 
 n2m_status default_ctx(n2m_context **c) {
     if (!g_tls.c) {
@@ -332,14 +339,15 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     }
     const float mn = ord2f(s0.vmin), mx = ord2f(s0.vmax);
     if (mn == mx) {
-        printf("Error: No variability in image intensity.\n");
+        if (!g_quiet) printf("Error: No variability in image intensity.\n");
         n2m_set_error("no variability in image intensity");
         return N2M_ERR_NO_VARIABILITY;
     }
     bool stale = false;
     if (iso <= mn || iso > mx) {
         iso = half_sum(mn, mx);
-        printf("Suggested isolevel out of range. Intensity range %g..%g, setting isolevel to %g\n", mn, mx, iso);
+        if (!g_quiet)
+            printf("Suggested isolevel out of range. Intensity range %g..%g, setting isolevel to %g\n", mn, mx, iso);
         stale = true;
     }
     if (verbose) printf("intensity range %g..%g, isolevel %g\n", mn, mx, iso);
@@ -412,7 +420,7 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
         return N2M_ERR_TOO_LARGE;
     }
     if ((!old && (nv < 3 || nt < 1)) || (old && nt < 1)) {
-        if (old) printf("marching cubes failed to identify triangles with an isolevel of %g\n", P.iso);
+        if (old && !g_quiet) printf("marching cubes failed to identify triangles with an isolevel of %g\n", P.iso);
         n2m_set_error("marching cubes produced no surface");
         return N2M_ERR_EMPTY;
     }
@@ -683,6 +691,146 @@ extern "C" n2m_status n2m_smooth_hc_device(n2m_context *c, vec3d *d_verts, const
     if (!c) return N2M_ERR_BAD_ARGS;
     CK(cudaSetDevice(c->device));
     CKS(mesh_smooth_hc(d_verts, d_tris, nvert, ntri, alpha, beta, iter, lock_edges, c->hc, c->scan, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return N2M_OK;
+}
+
+
+// ---- atlas ---------------------------------------------------------------------------
+namespace {
+n2m_status atlas_loop(n2m_context *c, const int16_t *d_lab, const int dim[3], const n2m_options &opt,
+                      int64_t *npts, int64_t *ntris) {
+    int maxlab = 0;
+    std::vector<unsigned> cnt;
+    std::vector<int> bb;
+    CKS(atlas_hist((const short *)d_lab, dim, c->aw, c->stream, &maxlab, cnt, bb));
+    if (maxlab < 1) {
+        n2m_set_error("intensity range not consistent with an indexed atlas");
+        return N2M_ERR_BAD_ARGS;
+    }
+    const long long n = (long long)dim[0] * dim[1] * dim[2];
+    CKS(c->in.ensure((size_t)n * sizeof(float)));
+    n2m_options o = opt;
+    o.isolevel = 0.5f;
+    o.verbose = false;
+    int64_t vp = 0, tp = 0;
+    for (int l = 1; l <= maxlab; l++) {
+        if (!cnt[l]) continue;   // "Skipping %d: no voxels with this intensity" (src/nii2mesh.c:565)
+        CKS(atlas_binarize((const short *)d_lab, n, l, c->in.as<float>(), c->stream));
+        n2m_atlas_mesh d = {l, N2M_OK, 0, 0, vp, tp};
+        const n2m_status st = pipeline(c, c->in.as<float>(), dim, o, nullptr);
+        if (st == N2M_ERR_NO_VARIABILITY || st == N2M_ERR_EMPTY) {
+            d.status = st;
+            c->atlas_meshes.push_back(d);
+            continue;
+        }
+        CKS(st);
+        if (o.post_smooth > 0)
+            CKS(mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, o.post_smooth, true, c->hc,
+                               c->scan, c->stream));
+        const size_t needp = (size_t)(vp + c->res_np) * sizeof(vec3d), needt = (size_t)(tp + c->res_nt) * sizeof(vec3i);
+        for (int k = 0; k < 2; k++) {   // grow the concatenated outputs, keeping what they hold
+            DevBuf &B = k ? c->ltris : c->lpts;
+            const size_t need = k ? needt : needp, used = k ? (size_t)tp * sizeof(vec3i) : (size_t)vp * sizeof(vec3d);
+            if (need > B.cap) {
+                DevBuf nb;
+                CKS(nb.ensure(std::max(need, 2 * B.cap)));
+                if (used) CK(cudaMemcpyAsync(nb.p, B.p, used, cudaMemcpyDeviceToDevice, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+                B.release();
+                B = nb;
+            }
+        }
+        CK(cudaMemcpyAsync(c->lpts.as<vec3d>() + vp, c->res_pts, (size_t)c->res_np * sizeof(vec3d),
+                           cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->ltris.as<vec3i>() + tp, c->res_tris, (size_t)c->res_nt * sizeof(vec3i),
+                           cudaMemcpyDeviceToDevice, c->stream));
+        d.nvert = c->res_np;
+        d.ntri = c->res_nt;
+        c->atlas_meshes.push_back(d);
+        vp += c->res_np;
+        tp += c->res_nt;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    *npts = vp;
+    *ntris = tp;
+    return N2M_OK;
+}
+}  // namespace
+
+extern "C" n2m_status n2m_atlas_device(n2m_context *c, const int16_t *d_labels, const int dim[3], const n2m_options *opt,
+                                       int mode, int *nmesh, const n2m_atlas_mesh **meshes, vec3d **d_pts,
+                                       vec3i **d_tris, int64_t *npts, int64_t *ntris, n2m_report *rep) {
+    if (!c || !d_labels || !dim || !opt || dim[0] <= 0 || dim[1] <= 0 || dim[2] <= 0) return N2M_ERR_BAD_ARGS;
+    if (opt->cubes == N2M_CUBES_OLDCUBES) {
+        n2m_set_error("n2m_atlas: the batched atlas supports the Lewiner cubes");
+        return N2M_ERR_BAD_ARGS;
+    }
+    CK(cudaSetDevice(c->device));
+    struct Quiet {
+        Quiet() { g_quiet = true; }
+        ~Quiet() { g_quiet = false; }
+    } quiet;
+    c->fwd.valid = false;
+    c->atlas_meshes.clear();
+    const long long l0 = g_n2m_launches.load();
+    CK(cudaEventRecord(c->ev0, c->stream));
+    int64_t np = 0, nt = 0;
+    vec3d *pp = nullptr;
+    vec3i *tt = nullptr;
+    float stage[8] = {0};
+    if (mode == N2M_ATLAS_LOOP) {
+        CKS(atlas_loop(c, d_labels, dim, *opt, &np, &nt));
+        pp = c->lpts.as<vec3d>();
+        tt = c->ltris.as<vec3i>();
+    } else {
+        CKS(atlas_batched((const short *)d_labels, dim, *opt, c->aw, c->scan, c->deg, c->hc, c->stream, c->atlas_meshes,
+                          &pp, &tt, &np, &nt, stage));
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    if (rep) {
+        memset(rep, 0, sizeof(*rep));
+        cudaEventElapsedTime(&rep->ms_total, c->ev0, c->ev1);
+        for (int i = 0; i < 8; i++) rep->ms_stage[i] = stage[i];
+        rep->nvert = np;
+        rep->ntri = nt;
+        rep->kernel_launches = g_n2m_launches.load() - l0;
+    }
+    if (nmesh) *nmesh = (int)c->atlas_meshes.size();
+    if (meshes) *meshes = c->atlas_meshes.data();
+    if (d_pts) *d_pts = pp;
+    if (d_tris) *d_tris = tt;
+    if (npts) *npts = np;
+    if (ntris) *ntris = nt;
+    return N2M_OK;
+}
+
+extern "C" n2m_status n2m_atlas(n2m_context *c, const int16_t *labels, const int dim[3], const n2m_options *opt, int mode,
+                                int *nmesh, n2m_atlas_mesh **meshes, vec3d **pts, vec3i **tris, int64_t *npts,
+                                int64_t *ntris) {
+    if (!c || !labels || !dim || !nmesh || !meshes || !pts || !tris || !npts || !ntris) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    const size_t n = (size_t)dim[0] * dim[1] * dim[2];
+    CKS(c->alab.ensure(n * sizeof(int16_t)));
+    CK(cudaMemcpyAsync(c->alab.p, labels, n * sizeof(int16_t), cudaMemcpyHostToDevice, c->stream));
+    const n2m_atlas_mesh *dm;
+    vec3d *dp;
+    vec3i *dt;
+    int nm;
+    CKS(n2m_atlas_device(c, c->alab.as<int16_t>(), dim, opt, mode, &nm, &dm, &dp, &dt, npts, ntris, nullptr));
+    *meshes = (n2m_atlas_mesh *)malloc(std::max(nm, 1) * sizeof(n2m_atlas_mesh));
+    *pts = (vec3d *)malloc(std::max<int64_t>(*npts, 1) * sizeof(vec3d));
+    *tris = (vec3i *)malloc(std::max<int64_t>(*ntris, 1) * sizeof(vec3i));
+    if (!*meshes || !*pts || !*tris) {
+        free(*meshes); free(*pts); free(*tris);
+        n2m_set_error("host allocation failed");
+        return N2M_ERR_OOM;
+    }
+    memcpy(*meshes, dm, nm * sizeof(n2m_atlas_mesh));
+    *nmesh = nm;
+    CK(cudaMemcpyAsync(*pts, dp, (size_t)*npts * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(*tris, dt, (size_t)*ntris * sizeof(vec3i), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return N2M_OK;
 }

@@ -9,33 +9,14 @@
 // exactly how the reference numbers labels (first appearance) and breaks
 // size ties (lowest label wins).
 #include "n2m_internal.cuh"
+#include "uf.cuh"
 
 namespace {
+using namespace uf;
 struct Dims {
     int nx, ny, nz;
     long long nxy, n;
 };
-
-__device__ __forceinline__ int find_root(const int *L, int i) {
-    int p = ((volatile const int *)L)[i];
-    while (p != i) {
-        i = p;
-        p = ((volatile const int *)L)[i];
-    }
-    return i;
-}
-
-__device__ __forceinline__ void unite(int *L, int a, int b) {
-    for (;;) {
-        a = find_root(L, a);
-        b = find_root(L, b);
-        if (a == b) return;
-        if (a < b) { const int t = a; a = b; b = t; }
-        const int old = atomicCAS(&L[a], a, b);
-        if (old == a) return;
-        a = old;
-    }
-}
 
 __global__ void k_mask(const float *__restrict__ vol, long long n, float iso, unsigned char *m) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)

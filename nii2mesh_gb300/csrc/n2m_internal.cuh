@@ -143,3 +143,17 @@ n2m_status mesh_weld_backward(const float3 *d_go, int np_final, int nv_raw, cons
                               const int *d_ov_id, const int *d_ov_src, int nov, float3 *d_graw, cudaStream_t s);
 n2m_status mesh_apply_sform(vec3d *d_pts, vec3i *d_tris, int np, int nt, const float sx[4], const float sy[4],
                             const float sz[4], cudaStream_t s);
+
+// atlas.cu
+#include <vector>
+struct AtlasWork {
+    DevBuf cnt, bb, boxes, queue, arena, mask, keep, lab, edge, ucnt, words, counts, active, tot, pts, pts2, tris, tris2,
+        cand, gath, weld, ranges;
+};
+n2m_status atlas_hist(const short *d_lab, const int dim[3], AtlasWork &w, cudaStream_t s, int *maxlab,
+                      std::vector<unsigned> &cnt, std::vector<int> &bb);
+n2m_status atlas_binarize(const short *d_lab, long long n, int label, float *out, cudaStream_t s);
+n2m_status atlas_offset_tris(vec3i *t, int n, int off, cudaStream_t s);
+n2m_status atlas_batched(const short *d_lab, const int dim[3], const n2m_options &o, AtlasWork &w, ScanWork &sw,
+                         DegWork &dw, HcWork &hw, cudaStream_t s, std::vector<n2m_atlas_mesh> &out, vec3d **d_pts,
+                         vec3i **d_tris, int64_t *npts, int64_t *ntris, float *ms_stage);

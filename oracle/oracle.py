@@ -299,3 +299,20 @@ def mesh_equal(a, b, pos_tol=0.0):
         n = int(np.sum(np.any(ta != tb, axis=1)))
         return False, d, f"{n} triangles differ after canonical sort"
     return True, d, "ok"
+
+
+def smoothed_equal(a_raw, a_smooth, b_raw, b_smooth, tol):
+    """Compare two post-smoothed meshes whose un-smoothed meshes must match
+    exactly: the vertex correspondence comes from the raw positions (a
+    canonical sort of smoothed positions is unstable under tiny differences),
+    then smoothed positions must agree within tol.  a_raw/b_raw = (tris, pts)."""
+    ok, d, msg = mesh_equal(a_raw, b_raw, 0.0)
+    if not ok:
+        return False, d, "raw meshes differ: " + msg
+    pa, pb = np.asarray(a_raw[1]), np.asarray(b_raw[1])
+    oa = np.lexsort((pa[:, 2], pa[:, 1], pa[:, 0]))
+    ob = np.lexsort((pb[:, 2], pb[:, 1], pb[:, 0]))
+    d = float(np.abs(np.asarray(a_smooth)[oa] - np.asarray(b_smooth)[ob]).max()) if len(oa) else 0.0
+    if d > tol:
+        return False, d, f"max smoothed position difference {d:g} > {tol:g}"
+    return True, d, "ok"
