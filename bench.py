@@ -19,6 +19,8 @@ each rank meshes its own copy and `value` counts the voxels of all ranks.
 """
 import argparse
 import json
+
+import numpy as np
 import os
 import statistics
 import subprocess
@@ -178,6 +180,50 @@ def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
             "timing": "wall clock per step incl. host syncs (forward reads back counts)"}
 
 
+def atlas_metric(n2m, torch, reps=3):
+    """meshes/s on the 256^3 int16 atlas (~250 labels, -p 1 -l 1 -b 1 -s 5):
+    batched all-labels path vs the per-label GPU loop, and the CPU oracle on
+    a sample of labels (one core, the reference's per-label work)."""
+    from nii2mesh_gb300 import synth
+    lab = synth.atlas256()
+    d = torch.from_numpy(lab).cuda()
+    ctx = n2m.Context(torch.cuda.current_device())
+    out = {"workload": "atlas256: 256^3 int16, power-law Voronoi labels, iso 0.5, -p 1 -l 1 -b 1 -s 5, Lewiner"}
+    for mode, name in ((n2m.ATLAS_BATCHED, "batched"), (n2m.ATLAS_LOOP, "loop")):
+        ctx.atlas_device(d.data_ptr(), (256, 256, 256), mode=mode)
+        ts = []
+        for _ in range(reps if mode == n2m.ATLAS_BATCHED else 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            nm, ok, nv, nt, rep = ctx.atlas_device(d.data_ptr(), (256, 256, 256), mode=mode)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        t = statistics.median(ts)
+        out[f"{name}_ms"] = round(1e3 * t, 2)
+        out[f"{name}_meshes_per_s"] = round(ok / t, 1)
+        out["meshes"] = ok
+        if mode == n2m.ATLAS_BATCHED:
+            out["batched_launches"] = rep["kernel_launches"]
+            out["batched_stage_ms"] = [round(x, 3) for x in rep["ms_stage"][:5]]
+    out["speedup_batched_vs_loop"] = round(out["batched_meshes_per_s"] / out["loop_meshes_per_s"], 2)
+    ctx.close()
+    # CPU: the reference's per-label work (binarise the whole volume, meshify, 5 HC iterations)
+    from oracle.oracle import Oracle
+    o = Oracle()
+    img = lab.astype(np.float32)
+    labels = [l for l in np.unique(lab) if l > 0][::max(1, len(np.unique(lab)) // 4)][:4]
+    t0 = time.perf_counter()
+    for l in labels:
+        b, _ = o.binarize_label(img, int(l))
+        m = o.meshify(b, 0.5, 0, True, True, True)
+        if m is not None:
+            o.laplacian_smoothHC(m[1], m[0], 0.1, 0.5, 5, True)
+    tc = time.perf_counter() - t0
+    out["cpu_baseline"] = {"meshes_per_s": round(len(labels) / tc, 4), "cores": 1, "kind": "port",
+                           "sample": f"{len(labels)} labels through the full-volume per-label path ({tc:.1f} s)"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -289,6 +335,7 @@ def main():
         cpu = {"value": round(gv, 6), "unit": "Gvox/s", "cores": 1, "kind": kind,
                "sample": f"one full 512^3 meshify ({times[0]:.1f} s)"}
     adj = adjoint_metric(n2m, torch) if world == 1 else None
+    atl = atlas_metric(n2m, torch) if world == 1 else None
     line = {"metric": METRIC, "value": round(value, 4), "unit": "Gvox/s", "n_gpus": world, "steps": a.steps,
             "warmup": warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
@@ -296,7 +343,7 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU", "triangles": nt, "vertices": nv},
             "stage_ms": {n: round(v, 4) for n, v in zip(STAGE_NAMES, stage_ms)},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck,
-            "adjoint": adj}
+            "adjoint": adj, "atlas": atl}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -65,19 +65,42 @@ __device__ __forceinline__ int find_item(const ABox *b, int nb, unsigned item, u
 }
 
 // ---- S0: per-label voxel count, bounding box and the largest label ---------------
+// A thread scans 32 consecutive voxels of a row and issues its atomics once per
+// run of equal labels (labels are spatially coherent, so runs are long).
+__device__ __forceinline__ void hist_flush(int l, int maxlab, unsigned c, int x0, int x1, int y, int z, unsigned *cnt,
+                                           int *bb) {
+    if (l < 1 || l > maxlab || !c) return;
+    atomicAdd(&cnt[l], c);
+    int *b = bb + 6 * l;
+    atomicMin(b + 0, x0); atomicMin(b + 1, y); atomicMin(b + 2, z);
+    atomicMax(b + 3, x1); atomicMax(b + 4, y); atomicMax(b + 5, z);
+}
+
 __global__ void k_a_hist(AtlasVol v, int maxlab, unsigned *cnt, int *bb, int *vmax) {
     int mx = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < v.nvox; i += (long long)gridDim.x * blockDim.x) {
-        const int l = v.lab[i];
-        mx = max(mx, l);
-        if (l < 1 || l > maxlab) continue;
-        const int z = (int)(i / v.nxy);
-        const long long r = i - (long long)z * v.nxy;
-        const int y = (int)(r / v.nx), x = (int)(r - (long long)y * v.nx);
-        atomicAdd(&cnt[l], 1u);
-        int *b = bb + 6 * l;
-        atomicMin(b + 0, x); atomicMin(b + 1, y); atomicMin(b + 2, z);
-        atomicMax(b + 3, x); atomicMax(b + 4, y); atomicMax(b + 5, z);
+    const unsigned spr = (unsigned)(v.nx + 31) / 32;
+    const long long nseg = (long long)spr * v.ny * v.nz;
+    for (long long sg = blockIdx.x * (long long)blockDim.x + threadIdx.x; sg < nseg; sg += (long long)gridDim.x * blockDim.x) {
+        const long long row = sg / spr;
+        const int xs = (int)(sg - row * spr) * 32;
+        const int z = (int)(row / v.ny), y = (int)(row - (long long)z * v.ny);
+        const short *p = v.lab + row * v.nx;
+        int cur = -1, x0 = 0, x1 = 0;
+        unsigned c = 0;
+        const int xe = min(xs + 32, v.nx);
+        for (int x = xs; x < xe; x++) {
+            const int l = p[x];
+            mx = max(mx, l);
+            if (l != cur) {
+                hist_flush(cur, maxlab, c, x0, x1, y, z, cnt, bb);
+                cur = l;
+                c = 0;
+                x0 = x;
+            }
+            c++;
+            x1 = x;
+        }
+        hist_flush(cur, maxlab, c, x0, x1, y, z, cnt, bb);
     }
     for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) atomicMax(vmax, mx);
@@ -177,7 +200,7 @@ struct VoxCtx {
 };
 
 template <class F>
-__device__ __forceinline__ void for_chunks(const ABox *boxes, int nb, unsigned nchunks, unsigned *queue, F f) {
+__device__ __forceinline__ void for_chunks(const ABox *boxes, int nb, unsigned nchunks, unsigned *queue, unsigned ch, F f) {
     __shared__ unsigned item;
     __shared__ int bi;
     for (;;) {
@@ -193,8 +216,8 @@ __device__ __forceinline__ void for_chunks(const ABox *boxes, int nb, unsigned n
         const ABox &B = boxes[b];
         const unsigned n0 = (unsigned)B.n[0], n01 = (unsigned)B.n[0] * (unsigned)B.n[1];
         const unsigned nvb = n01 * (unsigned)B.n[2];
-        for (int k = threadIdx.x; k < CH; k += blockDim.x) {
-            const unsigned loc = (it - B.chunk0) * (unsigned)CH + (unsigned)k;
+        for (unsigned k = threadIdx.x; k < ch; k += blockDim.x) {
+            const unsigned loc = (it - B.chunk0) * ch + k;
             if (loc >= nvb) break;
             const unsigned z = loc / n01, r = loc - z * n01;
             const unsigned y = r / n0, x = r - y * n0;
@@ -209,29 +232,30 @@ __constant__ signed char k_half[13][3] = {{-1, 0, 0},  {0, -1, 0}, {0, 0, -1},  
 
 __device__ __forceinline__ bool skip_box(const ABox &B) { return B.fail != 0; }
 
-__global__ void k_a_mask(const ABox *boxes, int nb, unsigned nch, unsigned *q, const float *arena, unsigned char *m) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) { m[c.i] = arena[c.i] >= B.iso; });
+__global__ void k_a_mask(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const float *arena, unsigned char *m) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) { m[c.i] = arena[c.i] >= B.iso; });
 }
 
-__global__ void k_a_uf_init(const ABox *boxes, int nb, unsigned nch, unsigned *q, const unsigned char *m,
+__global__ void k_a_uf_init(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const unsigned char *m,
                             unsigned char want, int *L) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) { L[c.i] = m[c.i] == want ? (int)c.i : -1; });
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) { L[c.i] = m[c.i] == want ? (int)c.i : -1; });
 }
 
-__global__ void k_a_uf_merge(const ABox *boxes, int nb, unsigned nch, unsigned *q, int *L, int nnb) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+__global__ void k_a_uf_merge(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, int *L, int nnb) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         if (L[c.i] < 0 || skip_box(B)) return;
         for (int k = 0; k < nnb; k++) {
             const int xx = c.x + k_half[k][0], yy = c.y + k_half[k][1], zz = c.z + k_half[k][2];
             if (xx < 0 || yy < 0 || zz < 0 || xx >= B.n[0] || yy >= B.n[1]) continue;
             const long long j = B.arena + ((long long)zz * B.n[1] + yy) * B.n[0] + xx;
-            if (L[j] >= 0) uf::unite(L, (int)c.i, (int)j);
+            const int lj = L[j];
+            if (lj >= 0 && lj != L[c.i]) uf::unite(L, (int)c.i, (int)j);
         }
     });
 }
 
-__global__ void k_a_uf_flatten(ABox *boxes, int nb, unsigned nch, unsigned *q, int *L, bool fg) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+__global__ void k_a_uf_flatten(ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, int *L, bool fg) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         const int p = L[c.i];
         if (p < 0) return;
         if (p == (int)c.i) atomicAdd(fg ? &boxes[c.b].nfg : &boxes[c.b].nbg, 1u);
@@ -240,32 +264,34 @@ __global__ void k_a_uf_flatten(ABox *boxes, int nb, unsigned nch, unsigned *q, i
 }
 
 // background components touching the sub-box boundary reach a face of the volume
-__global__ void k_a_edge_roots(const ABox *boxes, int nb, unsigned nch, unsigned *q, const int *L, unsigned char *edge) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+__global__ void k_a_edge_roots(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L, unsigned char *edge) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         const int r = L[c.i];
         if (r < 0) return;
         if (c.x == 0 || c.y == 0 || c.z == 0 || c.x == B.n[0] - 1 || c.y == B.n[1] - 1 || c.z == B.n[2] - 1) edge[r] = 1;
     });
 }
 
-__global__ void k_a_fill_bubbles(const ABox *boxes, int nb, unsigned nch, unsigned *q, const int *L,
+__global__ void k_a_fill_bubbles(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L,
                                  const unsigned char *edge, unsigned char *m) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         if (B.nbg <= 1) return;
         const int r = L[c.i];
         if (r >= 0 && !edge[r]) m[c.i] = 1;
     });
 }
 
-__global__ void k_a_sizes(const ABox *boxes, int nb, unsigned nch, unsigned *q, const int *L, unsigned *cnt) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+// component sizes; lanes of a warp that share a root add together
+__global__ void k_a_sizes(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L, unsigned *cnt) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         const int r = L[c.i];
-        if (r >= 0) atomicAdd(&cnt[r], 1u);
+        const unsigned grp = __match_any_sync(__activemask(), r);
+        if (r >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&cnt[r], __popc(grp));
     });
 }
 
-__global__ void k_a_best(ABox *boxes, int nb, unsigned nch, unsigned *q, const int *L, const unsigned *cnt) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+__global__ void k_a_best(ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L, const unsigned *cnt) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         if (L[c.i] == (int)c.i) {
             const unsigned loc = (unsigned)(c.i - B.arena);
             atomicMax(&boxes[c.b].best, ((unsigned long long)cnt[c.i] << 32) | (0xffffffffu - loc));
@@ -273,9 +299,9 @@ __global__ void k_a_best(ABox *boxes, int nb, unsigned nch, unsigned *q, const i
     });
 }
 
-__global__ void k_a_keep(const ABox *boxes, int nb, unsigned nch, unsigned *q, const int *L, const unsigned char *m,
+__global__ void k_a_keep(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L, const unsigned char *m,
                          bool only_largest, unsigned char *keep) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         if (only_largest) {
             const long long root = B.best ? B.arena + (0xffffffffu - (unsigned)(B.best & 0xffffffffu)) : -2;
             keep[c.i] = L[c.i] == root;
@@ -287,15 +313,15 @@ __global__ void k_a_keep(const ABox *boxes, int nb, unsigned nch, unsigned *q, c
 
 // fill (img = max(img, iso) where kept), then dilate (interior voxels of the
 // volume, 25 neighbours) + mask-out (img = mn) — src/meshify.c:332-342
-__global__ void k_a_fill(const ABox *boxes, int nb, unsigned nch, unsigned *q, const unsigned char *keep, float *arena) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+__global__ void k_a_fill(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const unsigned char *keep, float *arena) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         if (keep[c.i]) arena[c.i] = fmaxf(arena[c.i], B.iso);
     });
 }
 
-__global__ void k_a_dilate(const ABox *boxes, int nb, unsigned nch, unsigned *q, const unsigned char *keep, float *arena,
+__global__ void k_a_dilate(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const unsigned char *keep, float *arena,
                            int nx, int ny, int nz) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         bool on = keep[c.i];
         const int gx = B.o[0] + c.x, gy = B.o[1] + c.y, gz = B.o[2] + c.z;
         if (!on && gx > 0 && gy > 0 && gz > 0 && gx < nx - 1 && gy < ny - 1 && gz < nz - 1) {
@@ -313,16 +339,56 @@ __global__ void k_a_dilate(const ABox *boxes, int nb, unsigned nch, unsigned *q,
 }
 
 // ---- S4: bbox of voxels >= iso and the range after clustering -------------------------
-__global__ void k_a_stats(ABox *boxes, int nb, unsigned nch, unsigned *q, const float *arena) {
-    for_chunks(boxes, nb, nch, q, [&](VoxCtx c, const ABox &B) {
-        const float v = arena[c.i];
-        ABox &W = boxes[c.b];
-        atomicMin(&W.amin, f2ord(v));
-        if (v >= B.iso) {
-            atomicMin(&W.blo[0], B.o[0] + c.x); atomicMin(&W.blo[1], B.o[1] + c.y); atomicMin(&W.blo[2], B.o[2] + c.z);
-            atomicMax(&W.bhi[0], B.o[0] + c.x); atomicMax(&W.bhi[1], B.o[1] + c.y); atomicMax(&W.bhi[2], B.o[2] + c.z);
+// reduced per chunk (all its voxels belong to one box): one set of atomics per chunk
+__global__ void __launch_bounds__(256) k_a_stats(ABox *boxes, int nb, unsigned nch, unsigned *queue, unsigned ch,
+                                                 const float *arena) {
+    __shared__ unsigned item;
+    __shared__ int bi;
+    __shared__ int red[8][7];
+    for (;;) {
+        if (threadIdx.x == 0) {
+            item = atomicAdd(queue, 1u);
+            bi = item < nch ? find_item(boxes, nb, item, &ABox::chunk0) : 0;
         }
-    });
+        __syncthreads();
+        const unsigned it = item;
+        const int b = bi;
+        __syncthreads();
+        if (it >= nch) return;
+        const ABox &B = boxes[b];
+        const unsigned n0 = (unsigned)B.n[0], n01 = (unsigned)B.n[0] * (unsigned)B.n[1], nvb = n01 * (unsigned)B.n[2];
+        int v[7] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};   // amin, lo xyz, hi xyz
+        for (unsigned k = threadIdx.x; k < ch; k += blockDim.x) {
+            const unsigned loc = (it - B.chunk0) * ch + k;
+            if (loc >= nvb) break;
+            const float f = arena[B.arena + loc];
+            v[0] = min(v[0], f2ord(f));
+            if (f >= B.iso) {
+                const unsigned z = loc / n01, r = loc - z * n01, y = r / n0, x = r - y * n0;
+                v[1] = min(v[1], (int)x); v[2] = min(v[2], (int)y); v[3] = min(v[3], (int)z);
+                v[4] = max(v[4], (int)x); v[5] = max(v[5], (int)y); v[6] = max(v[6], (int)z);
+            }
+        }
+        for (int o = 16; o; o >>= 1)
+            for (int j = 0; j < 7; j++) {
+                const int t = __shfl_xor_sync(0xffffffffu, v[j], o);
+                v[j] = j < 4 ? min(v[j], t) : max(v[j], t);
+            }
+        if ((threadIdx.x & 31) == 0)
+            for (int j = 0; j < 7; j++) red[threadIdx.x >> 5][j] = v[j];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+                for (int j = 0; j < 7; j++) v[j] = j < 4 ? min(v[j], red[w][j]) : max(v[j], red[w][j]);
+            ABox &W = boxes[b];
+            atomicMin(&W.amin, v[0]);
+            if (v[1] != INT_MAX) {
+                atomicMin(&W.blo[0], B.o[0] + v[1]); atomicMin(&W.blo[1], B.o[1] + v[2]); atomicMin(&W.blo[2], B.o[2] + v[3]);
+                atomicMax(&W.bhi[0], B.o[0] + v[4]); atomicMax(&W.bhi[1], B.o[1] + v[5]); atomicMax(&W.bhi[2], B.o[2] + v[6]);
+            }
+        }
+        __syncthreads();
+    }
 }
 
 __global__ void k_a_pad(ABox *boxes, int nb) {
@@ -654,6 +720,78 @@ __global__ void k_a_localize(vec3i *t, unsigned nt, const unsigned *tri_start, c
 }
 }  // namespace
 
+namespace {
+unsigned set_chunks(std::vector<ABox> &boxes, unsigned ch) {
+    unsigned chunks = 0;
+    for (auto &B : boxes) {
+        B.chunk0 = chunks;
+        chunks += (unsigned)(((long long)B.n[0] * B.n[1] * B.n[2] + ch - 1) / ch);
+    }
+    return chunks;
+}
+
+// smoothing, isolevel, clustering and range/bbox: device-only work (no host
+// synchronisation), enqueued for timing by the autotuner or captured as a graph
+struct Segment {
+    AtlasVol v;
+    ABox *db;
+    int nb;
+    unsigned tiles;
+    float *ar;
+    bool smooth_on, only_largest, fill_bubbles;
+    int nx, ny, nz;
+    unsigned *q;
+    long long arena;
+
+    n2m_status ensure(AtlasWork &w) {
+        if (only_largest || fill_bubbles) {
+            CKS(w.mask.ensure((size_t)arena));
+            CKS(w.keep.ensure((size_t)arena));
+            CKS(w.lab.ensure((size_t)arena * sizeof(int)));
+            if (fill_bubbles) CKS(w.edge.ensure((size_t)arena));
+            if (only_largest) CKS(w.ucnt.ensure((size_t)arena * sizeof(unsigned)));
+        }
+        return N2M_OK;
+    }
+
+    n2m_status enqueue(AtlasWork &w, unsigned ch, unsigned per_sm, unsigned chunks, cudaStream_t s) {
+        int qi = 0;
+        CK(cudaMemsetAsync(q, 0, 32 * sizeof(unsigned), s));
+        { k_a_smooth<<<pgrid(tiles, 2), dim3(smooth::STX, smooth::STY), 0, s>>>(v, db, nb, tiles, q + qi++, ar, smooth_on); N2M_COUNT(); }
+        { k_a_iso<<<(nb + 127) / 128, 128, 0, s>>>(db, nb); N2M_COUNT(); }
+        const unsigned g = pgrid(chunks, per_sm);
+        if (only_largest || fill_bubbles) {
+            unsigned char *m = w.mask.as<unsigned char>(), *keep = w.keep.as<unsigned char>();
+            int *L = w.lab.as<int>();
+            { k_a_mask<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, ar, m); N2M_COUNT(); }
+            if (fill_bubbles) {
+                { k_a_uf_init<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 0, L); N2M_COUNT(); }
+                { k_a_uf_merge<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, 3); N2M_COUNT(); }
+                { k_a_uf_flatten<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, false); N2M_COUNT(); }
+                CK(cudaMemsetAsync(w.edge.p, 0, (size_t)arena, s));
+                { k_a_edge_roots<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.edge.as<unsigned char>()); N2M_COUNT(); }
+                { k_a_fill_bubbles<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.edge.as<unsigned char>(), m); N2M_COUNT(); }
+            }
+            { k_a_uf_init<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 1, L); N2M_COUNT(); }
+            { k_a_uf_merge<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, 9); N2M_COUNT(); }
+            { k_a_uf_flatten<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, true); N2M_COUNT(); }
+            if (only_largest) {
+                CK(cudaMemsetAsync(w.ucnt.p, 0, (size_t)arena * sizeof(unsigned), s));
+                { k_a_sizes<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.ucnt.as<unsigned>()); N2M_COUNT(); }
+                { k_a_best<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.ucnt.as<unsigned>()); N2M_COUNT(); }
+            }
+            { k_a_keep<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, m, only_largest, keep); N2M_COUNT(); }
+            if (fill_bubbles) { k_a_fill<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, keep, ar); N2M_COUNT(); }
+            if (only_largest) { k_a_dilate<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, keep, ar, nx, ny, nz); N2M_COUNT(); }
+        }
+        { k_a_stats<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, ar); N2M_COUNT(); }
+        { k_a_pad<<<(nb + 127) / 128, 128, 0, s>>>(db, nb); N2M_COUNT(); }
+        CKL();
+        return N2M_OK;
+    }
+};
+}  // namespace
+
 n2m_status atlas_hist(const short *d_lab, const int dim[3], AtlasWork &w, cudaStream_t s, int *maxlab,
                       std::vector<unsigned> &cnt, std::vector<int> &bb) {
     const int ML = 32767;
@@ -714,7 +852,7 @@ n2m_status atlas_batched(const short *d_lab, const int dim[3], const n2m_options
     // ---- sub-boxes
     std::vector<ABox> boxes;
     long long arena = 0;
-    unsigned tiles = 0, chunks = 0;
+    unsigned tiles = 0;
     for (int l = 1; l <= maxlab; l++) {
         if (!cnt[l]) continue;
         ABox B;
@@ -733,8 +871,7 @@ n2m_status atlas_batched(const short *d_lab, const int dim[3], const n2m_options
         B.tile0 = tiles;
         tiles += (unsigned)(((B.n[0] + smooth::STX - 1) / smooth::STX) * ((B.n[1] + smooth::STY - 1) / smooth::STY) *
                             ((B.n[2] + smooth::SZC - 1) / smooth::SZC));
-        B.chunk0 = chunks;
-        chunks += (unsigned)(((long long)B.n[0] * B.n[1] * B.n[2] + CH - 1) / CH);
+        B.chunk0 = 0;   // set per chunk size below
         B.vmin = INT_MAX;
         B.vmax = INT_MIN;
         for (int a = 0; a < 3; a++) { B.blo[a] = INT_MAX; B.bhi[a] = INT_MIN; }
@@ -746,53 +883,68 @@ n2m_status atlas_batched(const short *d_lab, const int dim[3], const n2m_options
         return N2M_ERR_TOO_LARGE;
     }
     CKS(w.boxes.ensure((size_t)nb * sizeof(ABox)));
-    CKS(w.queue.ensure(64 * sizeof(unsigned)));
+    CKS(w.queue.ensure(96 * sizeof(unsigned)));
     CKS(w.arena.ensure((size_t)arena * sizeof(float)));
     ABox *db = w.boxes.as<ABox>();
     unsigned *q = w.queue.as<unsigned>();
     CK(cudaMemcpyAsync(db, boxes.data(), nb * sizeof(ABox), cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(q, 0, 64 * sizeof(unsigned), s));
+    CK(cudaMemsetAsync(q, 0, 96 * sizeof(unsigned), s));
     float *ar = w.arena.as<float>();
     const bool smooth_on = o.pre_smooth && dim[0] >= 5 && dim[1] >= 5 && dim[2] >= 5;
-    int qi = 0;
-    CK(cudaEventRecord(ev[1], s));
-    { k_a_smooth<<<pgrid(tiles, 2), dim3(smooth::STX, smooth::STY), 0, s>>>(v, db, nb, tiles, q + qi++, ar, smooth_on); N2M_COUNT(); }
-    { k_a_iso<<<(nb + 127) / 128, 128, 0, s>>>(db, nb); N2M_COUNT(); }
-    CKL();
-    CK(cudaEventRecord(ev[2], s));
-    const unsigned gch = pgrid(chunks, 8);
-    if (o.only_largest || o.fill_bubbles) {
-        CKS(w.mask.ensure((size_t)arena));
-        CKS(w.keep.ensure((size_t)arena));
-        CKS(w.lab.ensure((size_t)arena * sizeof(int)));
-        unsigned char *m = w.mask.as<unsigned char>(), *keep = w.keep.as<unsigned char>();
-        int *L = w.lab.as<int>();
-        { k_a_mask<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, ar, m); N2M_COUNT(); }
-        if (o.fill_bubbles) {
-            CKS(w.edge.ensure((size_t)arena));
-            { k_a_uf_init<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, m, 0, L); N2M_COUNT(); }
-            { k_a_uf_merge<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, 3); N2M_COUNT(); }
-            { k_a_uf_flatten<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, false); N2M_COUNT(); }
-            CK(cudaMemsetAsync(w.edge.p, 0, (size_t)arena, s));
-            { k_a_edge_roots<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, w.edge.as<unsigned char>()); N2M_COUNT(); }
-            { k_a_fill_bubbles<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, w.edge.as<unsigned char>(), m); N2M_COUNT(); }
+    Segment seg{v, db, nb, tiles, ar, smooth_on, o.only_largest, o.fill_bubbles, dim[0], dim[1], dim[2], q, arena};
+    CKS(seg.ensure(w));
+    // pick chunk size and persistent-grid width once per context (autotuner)
+    if (!w.tuned) {
+        float best = 1e30f;
+        const unsigned cands[][2] = {{512, 4}, {1024, 8}, {1024, 16}, {2048, 8}, {4096, 8}, {4096, 16}};
+        for (const auto &cd : cands) {
+            std::vector<ABox> bx(boxes);
+            const unsigned nch = set_chunks(bx, cd[0]);
+            CK(cudaMemcpyAsync(db, bx.data(), nb * sizeof(ABox), cudaMemcpyHostToDevice, s));
+            CK(cudaEventRecord(ev[1], s));
+            CKS(seg.enqueue(w, cd[0], cd[1], nch, s));
+            CK(cudaEventRecord(ev[2], s));
+            CK(cudaEventSynchronize(ev[2]));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[1], ev[2]);
+            if (ms < best) { best = ms; w.chunk = cd[0]; w.per_sm = cd[1]; }
         }
-        { k_a_uf_init<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, m, 1, L); N2M_COUNT(); }
-        { k_a_uf_merge<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, 9); N2M_COUNT(); }
-        { k_a_uf_flatten<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, true); N2M_COUNT(); }
-        if (o.only_largest) {
-            CKS(w.ucnt.ensure((size_t)arena * sizeof(unsigned)));
-            CK(cudaMemsetAsync(w.ucnt.p, 0, (size_t)arena * sizeof(unsigned), s));
-            { k_a_sizes<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, w.ucnt.as<unsigned>()); N2M_COUNT(); }
-            { k_a_best<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, w.ucnt.as<unsigned>()); N2M_COUNT(); }
-        }
-        { k_a_keep<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, L, m, o.only_largest, keep); N2M_COUNT(); }
-        if (o.fill_bubbles) { k_a_fill<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, keep, ar); N2M_COUNT(); }
-        if (o.only_largest) { k_a_dilate<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, keep, ar, dim[0], dim[1], dim[2]); N2M_COUNT(); }
+        w.tuned = true;
+        w.tuned_ms = best;
     }
-    { k_a_stats<<<gch, 256, 0, s>>>(db, nb, chunks, q + qi++, ar); N2M_COUNT(); }
-    { k_a_pad<<<(nb + 127) / 128, 128, 0, s>>>(db, nb); N2M_COUNT(); }
-    CKL();
+    const unsigned chunks = set_chunks(boxes, w.chunk);
+    CK(cudaMemcpyAsync(db, boxes.data(), nb * sizeof(ABox), cudaMemcpyHostToDevice, s));
+    CK(cudaEventRecord(ev[1], s));
+    // the smoothing + clustering + range/bbox segment runs as one CUDA graph
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const n2m_status cst = seg.enqueue(w, w.chunk, w.per_sm, chunks, s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    CKS(cst);
+    CK(ce);
+    cudaGraphExec_t exec = (cudaGraphExec_t)w.exec;
+    bool updated = false;
+    if (exec) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(exec, graph, &info) == cudaSuccess;
+        if (!updated) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+    }
+    if (!exec) {
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        if (ie != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            CK(ie);
+        }
+    }
+    w.exec = exec;
+    cudaGraphDestroy(graph);
+    CK(cudaGraphLaunch(exec, s));
+    CK(cudaEventRecord(ev[2], s));
+    int qi = 32;
     CK(cudaMemcpyAsync(boxes.data(), db, nb * sizeof(ABox), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     CK(cudaEventRecord(ev[3], s));

@@ -142,6 +142,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
                       &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb};
     for (DevBuf *b : bufs) b->release();
+    if (c->aw.exec) cudaGraphExecDestroy((cudaGraphExec_t)c->aw.exec);
     if (c->pinned) cudaFreeHost(c->pinned);
     for (int i = 0; i < 8; i++)
         if (c->evs[i]) cudaEventDestroy(c->evs[i]);

@@ -48,7 +48,8 @@ __global__ void k_uf_merge(int *L, Dims d, int nnb) {
             const int xx = x + k_half[k][0], yy = y + k_half[k][1], zz = z + k_half[k][2];
             if (xx < 0 || yy < 0 || zz < 0 || xx >= d.nx || yy >= d.ny) continue;
             const long long j = zz * d.nxy + (long long)yy * d.nx + xx;
-            if (L[j] >= 0) unite(L, (int)i, (int)j);
+            const int lj = L[j];
+            if (lj >= 0 && lj != L[i]) unite(L, (int)i, (int)j);
         }
     }
 }
@@ -90,7 +91,8 @@ __global__ void k_fill_bubbles(const int *__restrict__ L, long long n, const uns
 __global__ void k_sizes(const int *__restrict__ L, long long n, unsigned *cnt) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int r = L[i];
-        if (r >= 0) atomicAdd(&cnt[r], 1u);
+        const unsigned grp = __match_any_sync(__activemask(), r);   // lanes sharing a root add together
+        if (r >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&cnt[r], __popc(grp));
     }
 }
 

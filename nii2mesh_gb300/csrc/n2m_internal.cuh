@@ -149,6 +149,10 @@ n2m_status mesh_apply_sform(vec3d *d_pts, vec3i *d_tris, int np, int nt, const f
 struct AtlasWork {
     DevBuf cnt, bb, boxes, queue, arena, mask, keep, lab, edge, ucnt, words, counts, active, tot, pts, pts2, tris, tris2,
         cand, gath, weld, ranges;
+    void *exec = nullptr;            // cudaGraphExec_t of the smoothing + clustering segment
+    bool tuned = false;              // autotuned work-item size and grid width
+    unsigned chunk = 1024, per_sm = 8;
+    float tuned_ms = 0.f;
 };
 n2m_status atlas_hist(const short *d_lab, const int dim[3], AtlasWork &w, cudaStream_t s, int *maxlab,
                       std::vector<unsigned> &cnt, std::vector<int> &bb);
