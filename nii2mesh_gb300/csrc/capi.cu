@@ -69,7 +69,7 @@ struct n2m_context {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evs[8] = {};   // stage boundaries of the last pipeline run
-    DevBuf in, vol, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath, hmesh;
+    DevBuf in, vol, stmp, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath, hmesh;
     McWork mc;
     ScanWork scan;
     LabelWork lab;
@@ -135,7 +135,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
     DevBuf *bufs[] = {&c->aw.cnt, &c->aw.bb, &c->aw.boxes, &c->aw.queue, &c->aw.arena, &c->aw.mask, &c->aw.keep,
                       &c->aw.lab, &c->aw.edge, &c->aw.ucnt, &c->aw.words, &c->aw.counts, &c->aw.active, &c->aw.tot,
                       &c->aw.pts, &c->aw.pts2, &c->aw.tris, &c->aw.tris2, &c->aw.cand, &c->aw.gath, &c->aw.weld,
-                      &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->vol, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
+                      &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->vol, &c->stmp, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
                       &c->tris_raw, &c->pts, &c->tris, &c->ntf, &c->weld, &c->gath, &c->hmesh,
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
@@ -328,7 +328,10 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     }
     if (!smooth && label) CK(cudaMemcpyAsync(vol, d_src, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaEventRecord(c->evs[0], c->stream));
-    if (smooth) CKS(launch_smooth(d_src, vol, nx, ny, nz, iso, dst, c->stream));
+    if (smooth) {
+        CKS(c->stmp.ensure(n * sizeof(float)));
+        CKS(launch_smooth(d_src, vol, c->stmp.as<float>(), nx, ny, nz, iso, dst, c->stream));
+    }
     else CKS(launch_stats(label ? vol : d_src, nx, ny, nz, iso, true, dst, c->stream));
     CK(cudaEventRecord(c->evs[1], c->stream));
     const float *v = vol ? vol : d_src;

@@ -77,6 +77,14 @@ N2M_HD float tap5_double(float a, float b, float c, float d, float e) {
 // Fast path.  Returns true and writes *out when the float result is proven
 // equal to tap5_double(a..e).
 //   exact value E = w2*(a+e) + w0*(c + (b+d)/2)         (w1 == w0/2 exactly)
+// th + tl approximates E to within M * 2^-40 (M = max |input|; products
+// and sums are error-free except the final compensation terms, each
+// relatively 2^-24 of a term below M * 2^-24), and the reference's double
+// result lies within M * 2^-50 of E, so M * 2^-38 bounds |th + tl - D| with
+// room to spare.  If |tl| plus that bound stays below half the gap under |th|
+// (the smaller of th's two neighbour gaps), D rounds to th.  Zero, tiny,
+// huge and non-finite inputs (M outside [2^-90, 2^120)) are left to the slow
+// path, except all-zero taps, whose signed-zero sum is exact in float.
 N2M_HD bool tap5_fast(float a, float b, float c, float d, float e, float *out) {
     float u, ue, v, ve, w, we;
     two_sum(a, e, u, ue);
@@ -97,29 +105,19 @@ N2M_HD bool tap5_fast(float a, float b, float c, float d, float e, float *out) {
     low = FADD(low, es);
     float th, tl;
     two_sum(S, low, th, tl);
-    // rigorous bound on |(th + tl) - reference double sum| (see header comment)
-    const float m = FFMA(N2M_W2H, FADD(fabsf(a), fabsf(e)),
-                         FMUL(N2M_W0H, FADD(fabsf(c), FMUL(0.5f, FADD(fabsf(b), fabsf(d))))));
-    if (m == 0.0f) {                                             // all taps +-0
-        *out = FADD(FADD(FADD(FADD(a, b), c), d), e);            // same signed zero
-        return true;
+    const float M = fmaxf(fmaxf(fmaxf(fabsf(a), fabsf(e)), fmaxf(fabsf(b), fabsf(d))), fabsf(c));
+    if (!(M >= 0x1p-90f && M < 0x1p+120f)) {
+        if (M == 0.0f) {                                         // all taps +-0
+            *out = FADD(FADD(FADD(FADD(a, b), c), d), e);        // same signed zero
+            return true;
+        }
+        return false;                                            // tiny, huge, NaN, Inf
     }
-    const float bound = FMUL(m, 0x1p-39f);
     const float ath = fabsf(th);
-    if (!(ath >= 0x1p-100f && ath < 0x1p+120f)) return false;   // tiny, zero, huge, NaN
-    const float t = th < 0.0f ? -tl : tl;                        // offset away from zero
-    const uint32_t bits = f2u(ath);
-    const float up = FSUB(u2f(bits + 1u), ath);                  // exact gaps
-    const float dn = FSUB(ath, u2f(bits - 1u));
-    if (FADD(t, bound) < FMUL(0.5f, up) && FSUB(t, bound) > -FMUL(0.5f, dn)) {
+    const float dn = FSUB(ath, u2f(f2u(ath) - 1u));              // gap below |th|; NaN for th == 0
+    if (FFMA(2.0f, fabsf(tl), FMUL(M, 0x1p-37f)) < dn) {         // |tl| + M 2^-38 < dn / 2
         *out = th;
         return true;
     }
     return false;
-}
-
-N2M_HD float tap5_exact(float a, float b, float c, float d, float e) {
-    float r;
-    if (tap5_fast(a, b, c, d, e, &r)) return r;
-    return tap5_double(a, b, c, d, e);
 }

@@ -67,7 +67,8 @@ struct VolStats {
 
 // ---- kernels' host launchers (stream-ordered, no syncs) ----------------------
 // smooth.cu
-n2m_status launch_smooth(const float *in, float *out, int nx, int ny, int nz, float iso, VolStats *st,
+// tmp: one volume of scratch
+n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny, int nz, float iso, VolStats *st,
                          cudaStream_t s);
 // transposed pre-smooth: g_img = Sx^T Sy^T Sz^T g (tmp: one volume of scratch)
 n2m_status launch_smooth_adjoint(const float *g, float *tmp, float *out, int nx, int ny, int nz, cudaStream_t s);

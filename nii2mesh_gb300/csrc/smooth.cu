@@ -1,17 +1,25 @@
 // smooth.cu — pre-smooth (src/meshify.c:170-216) and the volume reductions of
 // meshify (range, bbox; src/meshify.c:305-371).
 //
-// k_smooth: one fused pass for all three separable blur passes.  A CTA owns a
-// 32x16 column of output voxels and streams along z over a chunk of slices:
-// per input slice it stages the raw slice (+2 halo in x and y) in shared
-// memory, runs the x pass for the 16+4 rows it needs, the y pass for its own
-// 16 rows, and keeps the last five y-pass results of each column in registers,
-// so the z pass needs no further memory traffic.  Every tap sum is rounded
-// exactly as the reference's double arithmetic rounds it (exact.cuh), so the
-// output is bit-identical to quick_smooth().  The range (min/max), the count
-// of non-finite voxels and the bbox of voxels >= iso are reduced in the same
-// pass.  Algorithmic traffic: 4 B read + 4 B written per voxel.
+// The blur is three separable 5-tap passes (x, then y, then z) whose every
+// tap sum is rounded exactly as the reference's double arithmetic rounds it
+// (exact.cuh), so the output is bit-identical to quick_smooth().  Volumes
+// below 2^32 voxels run one streaming kernel per pass (k_pass_x,
+// k_pass_axis): a fast FP32 proof decides ~97 % of the taps, the rest are
+// batched per warp and recomputed in FP64 by full warps; the z pass also
+// reduces the range (min/max), the count of non-finite voxels and the bbox
+// of voxels >= iso.  Traffic: 8 B per voxel per pass, three passes.
+//
+// k_smooth (larger volumes, and the column routine the batched atlas uses):
+// one fused pass for all three blur passes.  A CTA owns a 32x16 column of
+// output voxels and streams along z over a chunk of slices: per input slice
+// it stages the raw slice (+2 halo in x and y) in shared memory, runs the x
+// pass for the 16+4 rows it needs, the y pass for its own 16 rows, and keeps
+// the last five y-pass results of each column in registers, so the z pass
+// needs no further memory traffic (4 B read + 4 B written per voxel).
 #include <float.h>
+
+#include <stdlib.h>
 
 #include <algorithm>
 
@@ -68,8 +76,204 @@ void stats_init_host(VolStats *h) {
     h->pad = 0;
 }
 
-n2m_status launch_smooth(const float *in, float *out, int nx, int ny, int nz, float iso, VolStats *st,
+// ---- three separable passes with batched exact fix-ups -------------------------
+// x pass in -> out, y pass out -> tmp, z pass tmp -> out (with the range and
+// bbox reductions).  Each pass evaluates every tap with the fast path; the
+// voxels whose rounding the fast path cannot prove (about 2.5 % on data whose
+// voxels share an exponent) are staged per warp in shared memory and, 32 at a
+// time, recomputed with the reference's double sequence by the full warp, so
+// each FP64 instruction serves 32 voxels.  A pass never reads its own
+// outputs, so fix-ups can run whenever a batch is full.  Passes run at full
+// occupancy with no redundant taps and no block-wide waits.
+namespace {
+constexpr unsigned FULL = 0xffffffffu;
+
+// The pass being run: input, output, tap stride (1, nx or nx*ny) and, for
+// the z pass, the reductions.
+struct Pass {
+    const float *in;
+    float *out;
+    unsigned stride;
+    int nx, ny;
+    unsigned nxy;
+    float iso;
+    VolStats *st;
+};
+
+// Per-warp stack of failed voxels in shared memory (sized by the kernel for
+// 31 leftover entries plus what its steps push between drains).  All 32 lanes
+// call push, drain and finish together; push adds at most 32 entries, drain
+// recomputes full batches of 32.
+template <bool STATS>
+struct FixStage {
+    unsigned *buf;
+    int n;   // warp-uniform fill
+    __device__ __forceinline__ void run(const Pass &P, Acc &acc, int lo, int cnt, int lane) {
+        __syncwarp();
+        if (lane < cnt) {
+            const unsigned v = buf[lo + lane];
+            const float *p = P.in + v;
+            const long long s = P.stride;
+            const float r = tap5_double(p[-2 * s], p[-s], p[0], p[s], p[2 * s]);
+            P.out[v] = r;
+            if (STATS) acc.add(r, (int)(v % (unsigned)P.nx), (int)((v / (unsigned)P.nx) % (unsigned)P.ny), (int)(v / P.nxy), P.iso);
+        }
+        __syncwarp();
+    }
+    __device__ __forceinline__ void push(bool fail, unsigned vox, int lane) {
+        const unsigned m = __ballot_sync(FULL, fail);
+        if (fail) buf[n + __popc(m & ((1u << lane) - 1u))] = vox;
+        n += __popc(m);
+    }
+    __device__ __forceinline__ void drain(const Pass &P, Acc &acc, int lane) {
+        while (n >= 32) {
+            n -= 32;
+            run(P, acc, n, 32, lane);
+        }
+    }
+    __device__ __forceinline__ void finish(const Pass &P, Acc &acc, int lane) {
+        drain(P, acc, lane);
+        if (n) run(P, acc, 0, n, lane);
+        n = 0;
+    }
+};
+
+// x pass: each warp takes whole rows.
+__global__ void __launch_bounds__(256) k_pass_x(Pass P, unsigned nrows) {
+    __shared__ unsigned stage_buf[8][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    FixStage<false> F{stage_buf[w], 0};   // < 32 entries between steps, + 32
+    Acc acc;   // unused by the x pass
+    const int nx = P.nx;
+    const unsigned nwarps = gridDim.x * (blockDim.x / 32);
+    for (unsigned row = blockIdx.x * (blockDim.x / 32) + w; row < nrows; row += nwarps) {
+        const unsigned r0 = row * (unsigned)nx;
+        for (int x0 = 0; x0 < nx; x0 += 32) {
+            const int x = x0 + lane;
+            const unsigned v = r0 + (unsigned)x;
+            bool fail = false;
+            if (x < nx) {
+                float o;
+                if (x >= 2 && x <= nx - 3) {
+                    const float *p = P.in + v;
+                    fail = !tap5_fast(__ldg(p - 2), __ldg(p - 1), __ldg(p), __ldg(p + 1), __ldg(p + 2), &o);
+                } else {
+                    o = __ldg(P.in + v);
+                }
+                if (!fail) P.out[v] = o;
+            }
+            F.push(fail, v, lane);
+            F.drain(P, acc, lane);
+        }
+    }
+    F.finish(P, acc, lane);
+}
+
+// y and z passes: the volume is viewed as (outer, len, inner) with the pass
+// axis of length len and stride inner.  A task is SEGS consecutive groups of
+// 32 inner positions and a run of K positions along the axis; each lane
+// slides a register window along the axis.  STATS: the z pass, which also
+// reduces range and bbox.
+template <int K, int SEGS, bool STATS>
+__global__ void __launch_bounds__(256, 4) k_pass_axis(Pass P, int len, unsigned nouter) {
+    __shared__ unsigned stage_buf[8][32 * (K + 1)];   // < 32 entries between runs, + 32 per step
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    FixStage<STATS> F{stage_buf[wid], 0};
+    const unsigned inner = P.stride;
+    const unsigned nseg = (inner + 31) / 32, nchunk = (nseg + SEGS - 1) / SEGS;
+    const unsigned nrun = (unsigned)(len + K - 1) / K;
+    const unsigned ntask = nchunk * nrun * nouter;
+    const unsigned nwarps = gridDim.x * (blockDim.x / 32);
+    Acc acc;
+    acc.init();
+    for (unsigned t = blockIdx.x * (blockDim.x / 32) + wid; t < ntask; t += nwarps) {
+        const unsigned chunk = t % nchunk, rest = t / nchunk;
+        const int p0 = (int)(rest % nrun) * K;
+        const unsigned o = rest / nrun;
+        const unsigned sbeg = chunk * SEGS, send = min(sbeg + SEGS, nseg);
+        const bool interior = p0 >= 2 && p0 + K <= len - 2;   // no face rows, whole run inside
+        for (unsigned seg = sbeg; seg < send; seg++) {
+            const unsigned i = seg * 32 + lane;
+            const bool act = i < inner;
+            const unsigned base = o * (unsigned)len * inner + i;
+            float w[K + 4];
+            int gx = 0, gy = 0;
+            if (STATS) { gx = (int)(i % (unsigned)P.nx); gy = (int)(i / (unsigned)P.nx); }
+            if (interior) {
+                const float *q = P.in + base + (unsigned)(p0 - 2) * inner;
+#pragma unroll
+                for (int k = 0; k < K + 4; k++) w[k] = act ? __ldg(q + (unsigned)k * inner) : 0.f;
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    float r;
+                    const bool fail = act && !tap5_fast(w[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], &r);
+                    const unsigned v = base + (unsigned)(p0 + k) * inner;
+                    if (act && !fail) {
+                        P.out[v] = r;
+                        if (STATS) acc.add(r, gx, gy, p0 + k, P.iso);
+                    }
+                    F.push(fail, v, lane);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < K + 4; k++) {
+                    const int pos = p0 - 2 + k;
+                    w[k] = (act && pos >= 0 && pos < len) ? __ldg(P.in + base + (unsigned)pos * inner) : 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const int pos = p0 + k;
+                    bool fail = false;
+                    const unsigned v = base + (unsigned)pos * inner;
+                    if (act && pos < len) {
+                        float r = w[k + 2];
+                        if (pos >= 2 && pos <= len - 3) fail = !tap5_fast(w[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], &r);
+                        if (!fail) {
+                            P.out[v] = r;
+                            if (STATS) acc.add(r, gx, gy, pos, P.iso);
+                        }
+                    }
+                    F.push(fail, v, lane);
+                }
+            }
+            F.drain(P, acc, lane);
+        }
+    }
+    F.finish(P, acc, lane);
+    if (STATS) acc.flush(P.st, true);
+}
+
+int resident_blocks(const void *fn, int threads) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess)
+        return 152 * 4;
+    return sms * std::max(per_sm, 1);
+}
+
+constexpr int KRUN = 8, KSEG = 8;
+}  // namespace
+
+// nx*ny*nz < 2^32: three passes; larger volumes: the fused CTA-column kernel.
+n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny, int nz, float iso, VolStats *st,
                          cudaStream_t s) {
+    const size_t n = (size_t)nx * ny * nz;
+    if (n < ((size_t)1 << 32)) {
+        static int gx = 0, ga = 0, gz = 0;
+        if (!gx) {
+            gx = resident_blocks((const void *)k_pass_x, 256);
+            ga = resident_blocks((const void *)k_pass_axis<KRUN, KSEG, false>, 256);
+            gz = resident_blocks((const void *)k_pass_axis<KRUN, KSEG, true>, 256);
+        }
+        const unsigned nxy = (unsigned)nx * ny;
+        const Pass px{in, out, 1u, nx, ny, nxy, iso, st}, py{out, tmp, (unsigned)nx, nx, ny, nxy, iso, st},
+            pz{tmp, out, nxy, nx, ny, nxy, iso, st};
+        { k_pass_x<<<gx, 256, 0, s>>>(px, (unsigned)ny * nz); N2M_COUNT(); }
+        { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, (unsigned)nz); N2M_COUNT(); }
+        { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 1u); N2M_COUNT(); }
+        CKL();
+        return N2M_OK;
+    }
     dim3 grid((nx + STX - 1) / STX, (ny + STY - 1) / STY, (nz + SZC - 1) / SZC);
     { k_smooth<<<grid, dim3(STX, STY), 0, s>>>(in, out, nx, ny, nz, iso, st); N2M_COUNT(); }
     CKL();

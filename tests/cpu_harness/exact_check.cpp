@@ -1,6 +1,6 @@
 // Host-side check of the double-float smoothing tap (nii2mesh_gb300/csrc/exact.cuh):
 // tap5_exact must equal the reference's double sequence bit-for-bit.
-// Usage: exact_check <samples> <seed>; prints "<mismatches> <fast-path fraction>".
+// Usage: exact_check <samples> <seed>; prints "<mismatches> <fast-path fraction on ordinary data>".
 #include "../../nii2mesh_gb300/csrc/exact.cuh"
 #include <cstdio>
 #include <cstdlib>
@@ -11,10 +11,10 @@ int main(int argc, char **argv) {
     std::mt19937_64 rng(argc > 2 ? atol(argv[2]) : 1);
     std::normal_distribution<float> nd(0.f, 1.f);
     std::uniform_real_distribution<float> ud(0.f, 1.f);
-    long bad = 0, fast = 0;
+    long bad = 0, fast = 0, fm[12] = {0}, nm[12] = {0};
     for (long i = 0; i < n; i++) {
         float v[5];
-        int mode = (int)(i % 8);
+        int mode = (int)(i % 12);
         for (int k = 0; k < 5; k++) {
             switch (mode) {
             case 0: v[k] = nd(rng) * 1000.f; break;                                   // mixed sign
@@ -24,18 +24,30 @@ int main(int argc, char **argv) {
             case 4: v[k] = ldexpf(1.f + ud(rng), (int)(ud(rng) * 60) - 30); break;     // wide exponents
             case 5: v[k] = 100.f + nd(rng) * 1e-3f; break;                             // near-constant
             case 6: v[k] = (ud(rng) < 0.5f ? 1.f : -1.f) * ldexpf(1.f, (int)(ud(rng) * 8)); break;  // powers of 2
-            default: v[k] = (ud(rng) < 0.02f) ? 0.f : nd(rng); break;
+            case 7: v[k] = (ud(rng) < 0.02f) ? 0.f : nd(rng); break;
+            case 8: { uint32_t b = (uint32_t)rng(); v[k] = u2f(b); if (!isfinite(v[k])) v[k] = 0.f; break; }   // any finite bits
+            case 9: v[k] = (ud(rng) < 0.5f ? 0.f : -0.f) + ((ud(rng) < 0.2f) ? ldexpf(nd(rng), -140) : 0.f); break;  // zeros, subnormals
+            case 10: v[k] = ldexpf(nd(rng), (int)(ud(rng) * 40) + 85); break;          // near the upper cut
+            default: v[k] = -1000.f + nd(rng) * 20.f; break;                           // one binade: many exact midpoints
+
             }
         }
         float r;
+        nm[mode]++;
         if (tap5_fast(v[0], v[1], v[2], v[3], v[4], &r)) {
             fast++;
+            fm[mode]++;
             if (f2u(r) != f2u(tap5_double(v[0], v[1], v[2], v[3], v[4]))) {
                 if (bad < 10) printf("mismatch %a %a %a %a %a\n", v[0], v[1], v[2], v[3], v[4]);
                 bad++;
             }
         }
     }
-    printf("%ld %.6f\n", bad, (double)fast / n);
+    if (getenv("EXACT_CHECK_MODES"))
+        for (int k = 0; k < 12; k++) printf("family %d: fast %.5f\n", k, nm[k] ? (double)fm[k] / nm[k] : 0.0);
+    long fo = 0, no = 0;   // ordinary data: every family but random bits, zeros/subnormals and huge values
+    for (int k = 0; k < 12; k++)
+        if (k < 8 || k == 11) { fo += fm[k]; no += nm[k]; }
+    printf("%ld %.6f\n", bad, no ? (double)fo / no : 0.0);
     return bad != 0;
 }

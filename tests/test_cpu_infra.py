@@ -13,7 +13,9 @@ ROOT = Path(__file__).resolve().parents[1]
 
 def test_exact_tap_sum_matches_double(tmp_path):
     """tap5_fast (nii2mesh_gb300/csrc/exact.cuh) never disagrees with the
-    reference's double sequence, over 4M random taps of 8 value families."""
+    reference's double sequence, over 4M random taps of 12 value families
+    (arbitrary finite bit patterns, signed zeros and subnormals included), and
+    decides more than 95 % of the taps on ordinary data by itself."""
     cxx = shutil.which("g++") or shutil.which("c++")
     if not cxx:
         pytest.skip("no C++ compiler")
