@@ -8,9 +8,10 @@
 // triangles are in cube raster order, tiling order within a cube.  So the
 // mesh is the reference's mesh before its weld, vertex for vertex.
 //
-// count pass: one thread per grid point; a warp covers 32 consecutive points
-//   (a "word").  Edge crossings are ballots (three 32-bit masks per word);
-//   triangle and c-vertex counts come from the cube's MC33 decision.
+// count pass: the sign bit of every grid point, packed in 32-point "words"
+//   (ballots); then one thread per word derives its three edge-crossing masks
+//   and the triangle and c-vertex counts of its 32 cubes with bit operations
+//   and the MC33 decision of the few cubes that cross the surface.
 // scan: exclusive scan over words -> vertex/triangle/c-vertex offsets.
 // emit pass: only words that own output recompute their cubes; an edge
 //   vertex id anywhere in the grid is offset(word) + popcounts of the word's
@@ -66,72 +67,154 @@ __device__ __forceinline__ float gval(const GV &g, int x, int y, int z) {
 // Words are row-aligned: word (z*NY + y)*WX + xw holds grid points
 // x = 32*xw + lane of row (y, z); WX = ceil(NX/32).  Word order is raster
 // order, so numbering by an exclusive scan over words is the reference's.
-constexpr int TY = 8, TZ = 8;          // a CTA covers one word column x 8 rows x 8 slices
 
-__global__ void __launch_bounds__(256) k_count(GV g, bool classic, unsigned WX, uint4 *words, uint4 *counts,
-                                               unsigned *active, unsigned *nactive) {
-    __shared__ float sv[TZ + 1][TY + 1][33];
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-    // tile and halo strictly inside the volume: no darkening, wrap or padding
-    const bool simple = g.lo0 + x0 >= 1 && g.lo0 + x0 + 32 <= g.dx - 2 && g.lo1 + y0 >= 1 &&
-                        g.lo1 + y0 + TY <= g.dy - 2 && g.lo2 + z0 >= 1 && g.lo2 + z0 + TZ <= g.dz - 2;
-    for (int i = threadIdx.x; i < (TZ + 1) * (TY + 1) * 33; i += 256) {
-        const int xx = i % 33, r = i / 33, yy = r % (TY + 1), zz = r / (TY + 1);
-        float v;
-        if (simple) {
-            const unsigned j = (unsigned)(g.lo0 + x0 + xx) + (unsigned)(y0 + yy + g.lo1) * (unsigned)g.dx +
-                               (unsigned)(z0 + zz + g.lo2) * (unsigned)g.dxy;
-            v = __fsub_rn(__ldg(g.vol + j), g.iso);
-            if (fabsf(v) < N2M_FLT_EPS) v = N2M_FLT_EPS;
-        } else {
-            v = gval(g, x0 + xx, y0 + yy, z0 + zz);
-        }
-        sv[zz][yy][xx] = v;
+// Triangle count of each cube configuration whose MC33 tiling needs no face
+// or interior test (Lewiner cases 0, 1, 2, 5, 8, 9, 11, 14; every
+// configuration of the classic table); 0x80 marks the ambiguous ones.
+__device__ __forceinline__ unsigned char quick_count(int lut, bool classic) {
+    if (classic) {
+        const int off = O2(CASESCLASSIC, lut);
+        int n = 0;
+        while (n < 5 && d_lut[off + 3 * n] != -1) n++;
+        return (unsigned char)n;
     }
+    switch (L2(CASES, lut, 0)) {
+    case 0: return 0;
+    case 1: return 1;
+    case 2: case 8: return 2;
+    case 5: return 3;
+    case 9: case 11: case 14: return 4;
+    default: return 0x80;
+    }
+}
+
+// triangles | c-vertices << 16 of a cube whose tiling needs face/interior tests
+__device__ __noinline__ unsigned ambiguous_count(const GV &g, int x, int y, int z, int lut, bool classic) {
+    const float c[8] = {gval(g, x, y, z),         gval(g, x + 1, y, z),         gval(g, x + 1, y + 1, z),
+                        gval(g, x, y + 1, z),     gval(g, x, y, z + 1),         gval(g, x + 1, y, z + 1),
+                        gval(g, x + 1, y + 1, z + 1), gval(g, x, y + 1, z + 1)};
+    const Tiling T = select_tiling(c, lut, classic);
+    return (unsigned)T.n | (T.cv ? 1u << 16 : 0u);
+}
+
+// Count pass, part 1: the sign (grid value > 0) of every grid point as one
+// bit, word-aligned like the counts (bit x&31 of signs[(z*NY + y)*WX + x/32]);
+// one warp per word.  Rows strictly inside the volume (no darkening, wrap or
+// padding) read the volume directly, the others go through gval.
+__global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nwords, unsigned *signs) {
+    const int lane = threadIdx.x & 31;
+    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += (gridDim.x * blockDim.x) >> 5) {
+        const unsigned xw = w % WX, row = w / WX;
+        const int y = (int)(row % (unsigned)g.NY), z = (int)(row / (unsigned)g.NY);
+        const int x0 = (int)xw * 32, x = x0 + lane;
+        const int vy = g.lo1 + y, vz = g.lo2 + z;
+        bool s;
+        if (g.lo0 + x0 >= 1 && g.lo0 + x0 + 31 <= g.dx - 2 && vy >= 1 && vy <= g.dy - 2 && vz >= 1 && vz <= g.dz - 2) {
+            const float raw = __ldg(g.vol + ((long long)(g.lo0 + x) + (long long)vy * g.dx + (long long)vz * g.dxy));
+            s = x < g.NX && __fsub_rn(raw, g.iso) > -N2M_FLT_EPS;   // the FLT_EPSILON clamp maps (-eps, eps) to +eps
+        } else {
+            s = x < g.NX && gval(g, x, y, z) > 0.f;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, s);
+        if (lane == 0) signs[w] = m;
+    }
+}
+
+// Count pass, part 2: one thread per word, 32 cubes at a time as bit masks.
+// Corner k of the word's 32 cubes is a mask of the sign bits: the +x corners
+// are the row shifted down by one with bit 0 of the next word on top.  Edge
+// crossings are XORs; a cube needs a table lookup only if its corners are
+// not all equal (about 3 % of them), and a value fetch only if its MC33 tiling
+// needs a face or interior test.
+__global__ void __launch_bounds__(256) k_words(GV g, bool classic, unsigned WX, unsigned nwords,
+                                               const unsigned *__restrict__ signs, uint4 *words, uint4 *counts) {
+    __shared__ unsigned char quick[256];
+    quick[threadIdx.x] = quick_count(threadIdx.x, classic);
     __syncthreads();
-    const int wy = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int y = y0 + wy, x = x0 + lane;
-    if (y >= g.NY) return;                           // whole warp
-    for (int zz = 0; zz < TZ; zz++) {
-        const int z = z0 + zz;
-        if (z >= g.NZ) break;                        // whole warp
-        const bool in = x < g.NX;
-        const bool hx = in && x < g.NX - 1, hy = in && y < g.NY - 1, hz = in && z < g.NZ - 1;
-        const float c0 = sv[zz][wy][lane];
-        const bool s0 = c0 > 0.f;
-        const bool ex = hx && ((sv[zz][wy][lane + 1] > 0.f) != s0);
-        const bool ey = hy && ((sv[zz][wy + 1][lane] > 0.f) != s0);
-        const bool ez = hz && ((sv[zz + 1][wy][lane] > 0.f) != s0);
-        int nt = 0, nc = 0;
-        if (hx && hy && hz) {
-            float c[8] = {c0, sv[zz][wy][lane + 1], sv[zz][wy + 1][lane + 1], sv[zz][wy + 1][lane],
-                          sv[zz + 1][wy][lane], sv[zz + 1][wy][lane + 1], sv[zz + 1][wy + 1][lane + 1],
-                          sv[zz + 1][wy + 1][lane]};
-            const int lut = cube_lut(c);
-            if (lut != 0 && lut != 255) {
-                const Tiling T = select_tiling(c, lut, classic);
-                nt = T.n;
-                nc = T.cv;
+    const unsigned rowstride = WX, slicestride = WX * (unsigned)g.NY;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const unsigned xw = w % WX, row = w / WX;
+        const int y = (int)(row % (unsigned)g.NY), z = (int)(row / (unsigned)g.NY);
+        const int x0 = (int)xw * 32;
+        const bool hy = y < g.NY - 1, hz = z < g.NZ - 1, nx = xw + 1 < WX;
+        const unsigned inm = x0 + 32 <= g.NX ? 0xffffffffu : (1u << (g.NX - x0)) - 1u;   // x < NX
+        const unsigned hxm = x0 + 33 <= g.NX ? 0xffffffffu : (g.NX - 1 - x0 > 0 ? (1u << (g.NX - 1 - x0)) - 1u : 0u);
+        // corners: a = (y, z), b = (y+1, z), c = (y, z+1), d = (y+1, z+1); "1" = the +x neighbours
+        const unsigned a0 = __ldg(signs + w);
+        const unsigned a1 = __funnelshift_r(a0, nx ? __ldg(signs + w + 1) : 0u, 1);
+        unsigned b0 = 0, b1 = 0, c0 = 0, c1 = 0, d0 = 0, d1 = 0;
+        if (hy) {
+            b0 = __ldg(signs + w + rowstride);
+            b1 = __funnelshift_r(b0, nx ? __ldg(signs + w + rowstride + 1) : 0u, 1);
+        }
+        if (hz) {
+            c0 = __ldg(signs + w + slicestride);
+            c1 = __funnelshift_r(c0, nx ? __ldg(signs + w + slicestride + 1) : 0u, 1);
+        }
+        if (hy && hz) {
+            d0 = __ldg(signs + w + slicestride + rowstride);
+            d1 = __funnelshift_r(d0, nx ? __ldg(signs + w + slicestride + rowstride + 1) : 0u, 1);
+        }
+        const unsigned xm = (a0 ^ a1) & hxm;
+        const unsigned ym = hy ? (a0 ^ b0) & inm : 0u;
+        const unsigned zm = hz ? (a0 ^ c0) & inm : 0u;
+        unsigned cnt = 0;
+        if (hy && hz) {
+            const unsigned any = a0 | a1 | b0 | b1 | c0 | c1 | d0 | d1, all = a0 & a1 & b0 & b1 & c0 & c1 & d0 & d1;
+            unsigned mix = any & ~all & hxm;
+            while (mix) {
+                const int i = __ffs(mix) - 1;
+                mix &= mix - 1;
+                // corners 0..7 of the tables: (x,y,z) (x+1,y,z) (x+1,y+1,z) (x,y+1,z) and the same at z+1
+                const int lut = (int)((a0 >> i) & 1u) | (int)((a1 >> i) & 1u) << 1 | (int)((b1 >> i) & 1u) << 2 |
+                                (int)((b0 >> i) & 1u) << 3 | (int)((c0 >> i) & 1u) << 4 | (int)((c1 >> i) & 1u) << 5 |
+                                (int)((d1 >> i) & 1u) << 6 | (int)((d0 >> i) & 1u) << 7;
+                const unsigned q = quick[lut];
+                cnt += (q & 0x80u) ? ambiguous_count(g, x0 + i, y, z, lut, classic) : q;
             }
         }
-        const unsigned xm = __ballot_sync(0xffffffffu, ex), ym = __ballot_sync(0xffffffffu, ey),
-                       zm = __ballot_sync(0xffffffffu, ez);
-        for (int o = 16; o; o >>= 1) {
-            nt += __shfl_xor_sync(0xffffffffu, nt, o);
-            nc += __shfl_xor_sync(0xffffffffu, nc, o);
-        }
-        if (lane == 0) {
-            const unsigned w = ((unsigned)z * (unsigned)g.NY + (unsigned)y) * WX + blockIdx.x;
-            const unsigned nv = __popc(xm) + __popc(ym) + __popc(zm);
-            const bool act = nv | nt | nc;
-            words[w] = make_uint4(xm, ym, zm, 0u);
-            counts[w] = make_uint4(nv, (unsigned)nt, (unsigned)nc, act);
-            if (act) active[atomicAdd(nactive, 1u)] = w;
-        }
+        const unsigned nv = __popc(xm) + __popc(ym) + __popc(zm);
+        words[w] = make_uint4(xm, ym, zm, 0u);
+        counts[w] = make_uint4(nv, cnt & 0xffffu, cnt >> 16, (nv | cnt) ? 1u : 0u);
+    }
+}
+
+// active word list from the scanned counts (counts.w: exclusive count of
+// active words before w), in word order
+__global__ void k_active(const uint4 *__restrict__ offs, const uint4 *__restrict__ total, unsigned nwords,
+                         unsigned *active) {
+    const unsigned tot = total->w;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const unsigned a = offs[w].w, b = w + 1 < nwords ? offs[w + 1].w : tot;
+        if (b != a) active[a] = w;
     }
 }
 
 // ---- emit pass -------------------------------------------------------------------
+// grid value at p (strictly inside the volume: no darkening, wrap or padding)
+__device__ __forceinline__ float ival(const GV &g, const float *p) {
+    const float v = __fsub_rn(__ldg(p), g.iso);
+    return fabsf(v) < N2M_FLT_EPS ? N2M_FLT_EPS : v;
+}
+
+// exact float -> double by assembling the bits (the F2F conversion issues on
+// the FP64 pipe, a small fraction of the integer rate on this part)
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    if (e == 0xffu || (e == 0u && m)) return (double)f;   // non-finite, subnormal
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0u) return __longlong_as_double((long long)sign);
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29)));
+}
+
+// tiling edge code 0..11 -> owner offset (bit 0: +x, 1: +y, 2: +z) and axis (bits 3-4)
+__device__ __forceinline__ unsigned edge_code(int code) {
+    constexpr unsigned long long k = (0x00ull << 0) | (0x09ull << 5) | (0x02ull << 10) | (0x08ull << 15) | (0x04ull << 20) |
+                                     (0x0dull << 25) | (0x06ull << 30) | (0x0cull << 35) | (0x10ull << 40) |
+                                     (0x11ull << 45) | (0x13ull << 50) | (0x12ull << 55);
+    return (unsigned)(k >> (5 * code)) & 31u;
+}
+
 // id of the vertex on the `axis` edge of grid point (x,y,z) (the edge must cross)
 __device__ __forceinline__ int vid(const uint4 *__restrict__ words, const uint4 *__restrict__ offs, unsigned NY,
                                    unsigned WX, int x, int y, int z, int axis) {
@@ -169,7 +252,27 @@ __global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, c
         const bool cube = hx && hy && hz;
         const bool ex = (m.x >> lane) & 1u, ey = (m.y >> lane) & 1u, ez = (m.z >> lane) & 1u;
         float c[8];
-        if (in) {
+        // the word's cubes strictly inside the volume: no darkening, wrap or padding
+        const int x0 = (int)(xw * 32u);
+        const bool simple = g.lo0 + x0 >= 1 && g.lo0 + x0 + 32 <= g.dx - 2 && g.lo1 + y >= 1 && g.lo1 + y + 1 <= g.dy - 2 &&
+                            g.lo2 + z >= 1 && g.lo2 + z + 1 <= g.dz - 2;
+        if (simple) {
+            if (in) {
+                const float *p = g.vol + ((unsigned)(g.lo0 + x) + (unsigned)(y + g.lo1) * (unsigned)g.dx +
+                                          (unsigned)(z + g.lo2) * (unsigned)g.dxy);
+                const unsigned sy = (unsigned)g.dx, sz = (unsigned)g.dxy;
+                c[0] = ival(g, p);
+                c[1] = hx ? ival(g, p + 1) : c[0];
+                c[3] = hy ? ival(g, p + sy) : c[0];
+                c[4] = hz ? ival(g, p + sz) : c[0];
+                if (cube) {
+                    c[2] = ival(g, p + 1 + sy);
+                    c[5] = ival(g, p + 1 + sz);
+                    c[6] = ival(g, p + 1 + sy + sz);
+                    c[7] = ival(g, p + sy + sz);
+                }
+            }
+        } else if (in) {
             c[0] = gval(g, x, y, z);
             c[1] = hx ? gval(g, x + 1, y, z) : c[0];
             c[3] = hy ? gval(g, x, y + 1, z) : c[0];
@@ -186,36 +289,43 @@ __global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, c
             const unsigned lt = (1u << lane) - 1u;
             int id = (int)(o.x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt));
             const float fx = (float)x, fy = (float)y, fz = (float)z;
+            const double gx = f2d(__fadd_rn(fx, flo0)), gy = f2d(__fadd_rn(fy, flo1)), gz = f2d(__fadd_rn(fz, flo2));
             if (ex) {
                 const float X = __fadd_rn(__fadd_rn(fx, edge_u(c[0], c[1])), flo0);
-                pts[id] = {(double)X, (double)__fadd_rn(fy, flo1), (double)__fadd_rn(fz, flo2)};
+                pts[id] = {f2d(X), gy, gz};
                 if (frac_dist(X) < 1.5e-5f) add_cand(cand, ncand, cap, id);
                 id++;
             }
             if (ey) {
                 const float Y = __fadd_rn(__fadd_rn(fy, edge_u(c[0], c[3])), flo1);
-                pts[id] = {(double)__fadd_rn(fx, flo0), (double)Y, (double)__fadd_rn(fz, flo2)};
+                pts[id] = {gx, f2d(Y), gz};
                 if (frac_dist(Y) < 1.5e-5f) add_cand(cand, ncand, cap, id);
                 id++;
             }
             if (ez) {
                 const float Z = __fadd_rn(__fadd_rn(fz, edge_u(c[0], c[4])), flo2);
-                pts[id] = {(double)__fadd_rn(fx, flo0), (double)__fadd_rn(fy, flo1), (double)Z};
+                pts[id] = {gx, gy, f2d(Z)};
                 if (frac_dist(Z) < 1.5e-5f) add_cand(cand, ncand, cap, id);
             }
         }
         Tiling T = {0, 0, false};
+        float cl[8];   // corner array for the face/interior tests and the c-vertex only
         if (cube) {
             const int lut = cube_lut(c);
-            if (lut != 0 && lut != 255) T = select_tiling(c, lut, classic);
+            if (lut != 0 && lut != 255 && !quick_tiling(lut, classic, T)) {
+#pragma unroll
+                for (int k = 0; k < 8; k++) cl[k] = c[k];
+                T = select_tiling(cl, lut, classic);
+            }
         }
-        int tb = T.n, cb = T.cv;   // warp exclusive scans
+        const int cnt = T.n | ((int)T.cv << 16);
+        int sc = cnt;   // warp exclusive scan of (triangles, c-vertices)
         for (int d = 1; d < 32; d <<= 1) {
-            const int a = __shfl_up_sync(0xffffffffu, tb, d), b = __shfl_up_sync(0xffffffffu, cb, d);
-            if ((int)lane >= d) { tb += a; cb += b; }
+            const int a = __shfl_up_sync(0xffffffffu, sc, d);
+            if ((int)lane >= d) sc += a;
         }
-        tb -= T.n;
-        cb -= T.cv;
+        sc -= cnt;
+        const int tb = sc & 0xffff, cb = sc >> 16;
         if (T.n == 0) continue;
         int v12 = -1;
         if (T.cv) {   // c-vertex: mean of the cube's edge vertices (src/MarchingCubes.c:1029-1082)
@@ -223,8 +333,8 @@ __global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, c
             float n = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
             for (int e = 0; e < 12; e++) {
                 const int own = k_edge[e][0], ax = k_edge[e][1], ca = k_edge[e][2], cbn = k_edge[e][3];
-                if ((c[ca] > 0.f) == (c[cbn] > 0.f)) continue;
-                const float u = edge_u(c[ca], c[cbn]);
+                if ((cl[ca] > 0.f) == (cl[cbn] > 0.f)) continue;
+                const float u = edge_u(cl[ca], cl[cbn]);
                 float px = (float)(x + ((own ^ (own >> 1)) & 1)), py = (float)(y + ((own >> 1) & 1)),
                       pz = (float)(z + ((own >> 2) & 1));
                 if (ax == 0) px = __fadd_rn(px, u);
@@ -235,7 +345,7 @@ __global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, c
             }
             if (n > 0.f) { sx = __fdiv_rn(sx, n); sy = __fdiv_rn(sy, n); sz = __fdiv_rn(sz, n); }
             const float X = __fadd_rn(sx, flo0), Y = __fadd_rn(sy, flo1), Z = __fadd_rn(sz, flo2);
-            pts[v12] = {(double)X, (double)Y, (double)Z};
+            pts[v12] = {f2d(X), f2d(Y), f2d(Z)};
             if (fminf(frac_dist(X), fminf(frac_dist(Y), frac_dist(Z))) < 1.5e-5f) add_cand(ccand, nccand, cap, v12);
         }
         // triangles, stored reversed (v3,v2,v1) as marchingCubes() returns them
@@ -243,22 +353,13 @@ __global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, c
         int tv[3];
         for (int t = 0; t < 3 * T.n; t++) {
             const int code = d_lut[T.off + t];
-            int v;
-            switch (code) {
-            case 0: v = vid(words, offs, NY, WX, x, y, z, 0); break;
-            case 1: v = vid(words, offs, NY, WX, x + 1, y, z, 1); break;
-            case 2: v = vid(words, offs, NY, WX, x, y + 1, z, 0); break;
-            case 3: v = vid(words, offs, NY, WX, x, y, z, 1); break;
-            case 4: v = vid(words, offs, NY, WX, x, y, z + 1, 0); break;
-            case 5: v = vid(words, offs, NY, WX, x + 1, y, z + 1, 1); break;
-            case 6: v = vid(words, offs, NY, WX, x, y + 1, z + 1, 0); break;
-            case 7: v = vid(words, offs, NY, WX, x, y, z + 1, 1); break;
-            case 8: v = vid(words, offs, NY, WX, x, y, z, 2); break;
-            case 9: v = vid(words, offs, NY, WX, x + 1, y, z, 2); break;
-            case 10: v = vid(words, offs, NY, WX, x + 1, y + 1, z, 2); break;
-            case 11: v = vid(words, offs, NY, WX, x, y + 1, z, 2); break;
-            case 12: v = v12; break;
-            default: v = -1; break;
+            int v = v12;
+            if (code >= 0 && code < 12) {
+                const unsigned e = edge_code(code);
+                v = vid(words, offs, NY, WX, x + (int)(e & 1u), y + (int)((e >> 1) & 1u), z + (int)((e >> 2) & 1u),
+                        (int)(e >> 3));
+            } else if (code != 12) {
+                v = -1;
             }
             tv[t % 3] = v;
             if (t % 3 == 2) tris[o.y + tb + t / 3] = {tv[2], tv[1], tv[0]};
@@ -422,12 +523,24 @@ n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4
     CKS(w.words.ensure(nwords * sizeof(uint4)));
     CKS(w.counts.ensure(nwords * sizeof(uint4)));
     CKS(w.cand.ensure((nwords + 1) * sizeof(unsigned)));
-    unsigned *active = w.cand.as<unsigned>();
-    CK(cudaMemsetAsync(active + nwords, 0, sizeof(unsigned), s));
-    dim3 grid(WX, (g.n[1] + TY - 1) / TY, (g.n[2] + TZ - 1) / TZ);
-    { k_count<<<grid, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), active, active + nwords); N2M_COUNT(); }
+    CKS(w.signs.ensure(nwords * sizeof(unsigned)));
+    {
+        const unsigned blocks = (unsigned)std::min<size_t>((nwords + 7) / 8, 152u * 64u);
+        k_signs<<<blocks, 256, 0, s>>>(v, WX, (unsigned)nwords, w.signs.as<unsigned>());
+        N2M_COUNT();
+    }
+    {
+        const unsigned blocks = (unsigned)std::min<size_t>((nwords + 255) / 256, 152u * 16u);
+        k_words<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, (unsigned)nwords, w.signs.as<unsigned>(),
+                                       w.words.as<uint4>(), w.counts.as<uint4>());
+        N2M_COUNT();
+    }
     CKL();
-    return scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s);
+    CKS(scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s));
+    const unsigned blocks = (unsigned)std::min<size_t>((nwords + 255) / 256, 152u * 16u);
+    { k_active<<<blocks, 256, 0, s>>>(w.counts.as<uint4>(), d_total, (unsigned)nwords, w.cand.as<unsigned>()); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
 }
 
 n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,

@@ -182,6 +182,31 @@ static __device__ Tiling select_tiling(const float *c, int lut, bool classic) {
     return T;
 }
 
+// The tiling of configurations that need no face or interior test (every
+// classic configuration; Lewiner cases 1, 2, 5, 8, 9, 11, 14), without the
+// corner values.  Returns false for the ambiguous cases.
+__device__ __forceinline__ bool quick_tiling(int lut, bool classic, Tiling &T) {
+    if (classic) {
+        T.off = O2(CASESCLASSIC, lut);
+        int n = 0;
+        while (n < 5 && d_lut[T.off + 3 * n] != -1) n++;
+        T.n = n;
+        T.cv = false;
+        return true;
+    }
+    const int cf = L2(CASES, lut, 1);
+    switch (L2(CASES, lut, 0)) {
+    case 1: T = {O2(TILING1, cf), 1, false}; return true;
+    case 2: T = {O2(TILING2, cf), 2, false}; return true;
+    case 5: T = {O2(TILING5, cf), 3, false}; return true;
+    case 8: T = {O2(TILING8, cf), 2, false}; return true;
+    case 9: T = {O2(TILING9, cf), 4, false}; return true;
+    case 11: T = {O2(TILING11, cf), 4, false}; return true;
+    case 14: T = {O2(TILING14, cf), 4, false}; return true;
+    default: return false;
+    }
+}
+
 __device__ __forceinline__ int cube_lut(const float *c) {
     int lut = 0;
     for (int p = 0; p < 8; p++) lut |= (c[p] > 0.f) << p;
