@@ -98,25 +98,41 @@ __device__ __noinline__ unsigned ambiguous_count(const GV &g, int x, int y, int 
 }
 
 // Count pass, part 1: the sign (grid value > 0) of every grid point as one
-// bit, word-aligned like the counts (bit x&31 of signs[(z*NY + y)*WX + x/32]);
-// one warp per word.  Rows strictly inside the volume (no darkening, wrap or
-// padding) read the volume directly, the others go through gval.
-__global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nwords, unsigned *signs) {
+// bit, word-aligned like the counts (bit x&31 of signs[(z*NY + y)*WX + x/32]).
+// A warp takes whole rows, SW words at a time with all their loads in flight.
+// Words strictly inside the volume (no darkening, wrap or padding) read the
+// volume directly, the others go through gval.
+constexpr int SW = 8;
+
+__global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nrows, unsigned *signs) {
     const int lane = threadIdx.x & 31;
-    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += (gridDim.x * blockDim.x) >> 5) {
-        const unsigned xw = w % WX, row = w / WX;
+    for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += (gridDim.x * blockDim.x) >> 5) {
         const int y = (int)(row % (unsigned)g.NY), z = (int)(row / (unsigned)g.NY);
-        const int x0 = (int)xw * 32, x = x0 + lane;
         const int vy = g.lo1 + y, vz = g.lo2 + z;
-        bool s;
-        if (g.lo0 + x0 >= 1 && g.lo0 + x0 + 31 <= g.dx - 2 && vy >= 1 && vy <= g.dy - 2 && vz >= 1 && vz <= g.dz - 2) {
-            const float raw = __ldg(g.vol + ((long long)(g.lo0 + x) + (long long)vy * g.dx + (long long)vz * g.dxy));
-            s = x < g.NX && __fsub_rn(raw, g.iso) > -N2M_FLT_EPS;   // the FLT_EPSILON clamp maps (-eps, eps) to +eps
-        } else {
-            s = x < g.NX && gval(g, x, y, z) > 0.f;
+        const bool rsimple = vy >= 1 && vy <= g.dy - 2 && vz >= 1 && vz <= g.dz - 2;
+        const float *rp = g.vol + ((long long)g.lo0 + (long long)vy * g.dx + (long long)vz * g.dxy);
+        for (unsigned xw0 = 0; xw0 < WX; xw0 += SW) {
+            float raw[SW];
+#pragma unroll
+            for (int k = 0; k < SW; k++) {
+                const int x0 = (int)(xw0 + k) * 32;
+                const bool simple = rsimple && xw0 + k < WX && g.lo0 + x0 >= 1 && g.lo0 + x0 + 31 <= g.dx - 2;
+                raw[k] = simple ? __ldg(rp + x0 + lane) : 0.f;
+            }
+            unsigned mine = 0;
+#pragma unroll
+            for (int k = 0; k < SW; k++) {
+                if (xw0 + k >= WX) break;   // whole warp
+                const int x0 = (int)(xw0 + k) * 32, x = x0 + lane;
+                const bool simple = rsimple && g.lo0 + x0 >= 1 && g.lo0 + x0 + 31 <= g.dx - 2;
+                bool sg;
+                if (simple) sg = x < g.NX && __fsub_rn(raw[k], g.iso) > -N2M_FLT_EPS;   // clamp maps (-eps, eps) to +eps
+                else sg = x < g.NX && gval(g, x, y, z) > 0.f;
+                const unsigned m = __ballot_sync(0xffffffffu, sg);
+                if (lane == k) mine = m;
+            }
+            if (lane < SW && xw0 + lane < WX) signs[row * WX + xw0 + lane] = mine;
         }
-        const unsigned m = __ballot_sync(0xffffffffu, s);
-        if (lane == 0) signs[w] = m;
     }
 }
 
@@ -232,140 +248,186 @@ __device__ __forceinline__ void add_cand(int *cand, unsigned *n, int cap, int id
     if (k < (unsigned)cap) cand[k] = id;
 }
 
-// one warp per active word
+// c-vertex of a cube: mean of its crossing edge vertices (src/MarchingCubes.c:1029-1082)
+__device__ __noinline__ void emit_cvertex(const float *c, int x, int y, int z, float flo0, float flo1, float flo2,
+                                          int v12, vec3d *pts, int *ccand, unsigned *nccand, int cap) {
+    float n = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int e = 0; e < 12; e++) {
+        const int own = k_edge[e][0], ax = k_edge[e][1], ca = k_edge[e][2], cbn = k_edge[e][3];
+        if ((c[ca] > 0.f) == (c[cbn] > 0.f)) continue;
+        const float u = edge_u(c[ca], c[cbn]);
+        float px = (float)(x + ((own ^ (own >> 1)) & 1)), py = (float)(y + ((own >> 1) & 1)), pz = (float)(z + ((own >> 2) & 1));
+        if (ax == 0) px = __fadd_rn(px, u);
+        else if (ax == 1) py = __fadd_rn(py, u);
+        else pz = __fadd_rn(pz, u);
+        n = __fadd_rn(n, 1.f);
+        sx = __fadd_rn(sx, px); sy = __fadd_rn(sy, py); sz = __fadd_rn(sz, pz);
+    }
+    if (n > 0.f) { sx = __fdiv_rn(sx, n); sy = __fdiv_rn(sy, n); sz = __fdiv_rn(sz, n); }
+    const float X = __fadd_rn(sx, flo0), Y = __fadd_rn(sy, flo1), Z = __fadd_rn(sz, flo2);
+    pts[v12] = {f2d(X), f2d(Y), f2d(Z)};
+    if (fminf(frac_dist(X), fminf(frac_dist(Y), frac_dist(Z))) < 1.5e-5f) add_cand(ccand, nccand, cap, v12);
+}
+
+// corner values of cube (x, y, z), by gval's rules (simple: strictly inside
+// the volume)
+__device__ __noinline__ void cube_values(const GV &g, bool simple, int x, int y, int z, float *c) {
+    if (simple) {
+        const float *p = g.vol + ((long long)(g.lo0 + x) + (long long)(y + g.lo1) * g.dx + (long long)(z + g.lo2) * g.dxy);
+        const long long sy = g.dx, sz = g.dxy;
+        c[0] = ival(g, p); c[1] = ival(g, p + 1); c[2] = ival(g, p + 1 + sy); c[3] = ival(g, p + sy);
+        c[4] = ival(g, p + sz); c[5] = ival(g, p + 1 + sz); c[6] = ival(g, p + 1 + sy + sz); c[7] = ival(g, p + sy + sz);
+    } else {
+        c[0] = gval(g, x, y, z); c[1] = gval(g, x + 1, y, z); c[2] = gval(g, x + 1, y + 1, z); c[3] = gval(g, x, y + 1, z);
+        c[4] = gval(g, x, y, z + 1); c[5] = gval(g, x + 1, y, z + 1); c[6] = gval(g, x + 1, y + 1, z + 1);
+        c[7] = gval(g, x, y + 1, z + 1);
+    }
+}
+
+// One warp per active word.  Its items are spread densely over the lanes:
+// first the word's edge vertices (in id order), then its triangles (in
+// output order), so no lane idles on the many points of a word that cross
+// nothing.  Cube configurations come from the sign-bit volume of the count
+// pass; only ambiguous cubes read corner values for the face/interior tests.
+// Vertex ids of neighbouring words come from the masks and offsets of the 8
+// words a cube can touch, staged in shared memory.
 __global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, const uint4 *__restrict__ words,
-                                              const uint4 *__restrict__ offs, const unsigned *__restrict__ active,
-                                              unsigned nactive, unsigned nwords, uint4 totals, vec3d *pts,
-                                              vec3i *tris, int *cand, unsigned *ncand, int *ccand, unsigned *nccand,
-                                              int cap) {
-    const unsigned lane = threadIdx.x & 31u;
+                                              const uint4 *__restrict__ offs, const unsigned *__restrict__ signs,
+                                              const unsigned *__restrict__ active, unsigned nactive, uint4 totals,
+                                              vec3d *pts, vec3i *tris, int *cand, unsigned *ncand, int *ccand,
+                                              unsigned *nccand, int cap) {
+    __shared__ unsigned short vlist[8][96];   // per warp: lane << 2 | axis of the word's edge vertices
+    __shared__ unsigned short tlist[8][384];  // per warp: lane << 4 | j of the word's triangles
+    __shared__ int toff[8][32], v12s[8][32];
+    __shared__ uint4 nbm[8][8];               // masks of the words (dx, dy, dz) = (k&1, k>>1&1, k>>2)
+    __shared__ unsigned nbo[8][8];            // and their first vertex ids
+    const unsigned lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     const float flo0 = (float)g.lo0, flo1 = (float)g.lo1, flo2 = (float)g.lo2;
+    const unsigned slice = WX * (unsigned)g.NY;
     for (unsigned aw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; aw < nactive; aw += (gridDim.x * blockDim.x) >> 5) {
         const unsigned w = active[aw];
         const unsigned row = w / WX, xw = w - row * WX;
         const int z = (int)(row / (unsigned)g.NY), y = (int)(row - (unsigned)z * (unsigned)g.NY);
-        const int x = (int)(xw * 32u + lane);
+        const int x0 = (int)(xw * 32u);
         const uint4 o = offs[w];
         const uint4 m = words[w];
-        const bool in = x < g.NX;
-        const bool hx = in && x < g.NX - 1, hy = in && y < g.NY - 1, hz = in && z < g.NZ - 1;
-        const bool cube = hx && hy && hz;
-        const bool ex = (m.x >> lane) & 1u, ey = (m.y >> lane) & 1u, ez = (m.z >> lane) & 1u;
-        float c[8];
+        const bool nxw = xw + 1 < WX, hy = y < g.NY - 1, hz = z < g.NZ - 1;
+        if (lane < 8) {
+            const unsigned ddx = lane & 1u, ddy = (lane >> 1) & 1u, ddz = lane >> 2;
+            const bool ok = (!ddx || nxw) && (!ddy || hy) && (!ddz || hz);
+            const unsigned wn = w + ddx + ddy * WX + ddz * slice;
+            nbm[wid][lane] = ok ? words[wn] : make_uint4(0u, 0u, 0u, 0u);
+            nbo[wid][lane] = ok ? offs[wn].x : 0u;
+        }
         // the word's cubes strictly inside the volume: no darkening, wrap or padding
-        const int x0 = (int)(xw * 32u);
         const bool simple = g.lo0 + x0 >= 1 && g.lo0 + x0 + 32 <= g.dx - 2 && g.lo1 + y >= 1 && g.lo1 + y + 1 <= g.dy - 2 &&
                             g.lo2 + z >= 1 && g.lo2 + z + 1 <= g.dz - 2;
-        if (simple) {
-            if (in) {
-                const float *p = g.vol + ((unsigned)(g.lo0 + x) + (unsigned)(y + g.lo1) * (unsigned)g.dx +
-                                          (unsigned)(z + g.lo2) * (unsigned)g.dxy);
-                const unsigned sy = (unsigned)g.dx, sz = (unsigned)g.dxy;
-                c[0] = ival(g, p);
-                c[1] = hx ? ival(g, p + 1) : c[0];
-                c[3] = hy ? ival(g, p + sy) : c[0];
-                c[4] = hz ? ival(g, p + sz) : c[0];
-                if (cube) {
-                    c[2] = ival(g, p + 1 + sy);
-                    c[5] = ival(g, p + 1 + sz);
-                    c[6] = ival(g, p + 1 + sy + sz);
-                    c[7] = ival(g, p + sy + sz);
-                }
-            }
-        } else if (in) {
-            c[0] = gval(g, x, y, z);
-            c[1] = hx ? gval(g, x + 1, y, z) : c[0];
-            c[3] = hy ? gval(g, x, y + 1, z) : c[0];
-            c[4] = hz ? gval(g, x, y, z + 1) : c[0];
-            if (cube) {
-                c[2] = gval(g, x + 1, y + 1, z);
-                c[5] = gval(g, x + 1, y, z + 1);
-                c[6] = gval(g, x + 1, y + 1, z + 1);
-                c[7] = gval(g, x, y + 1, z + 1);
-            }
+        // ---- edge vertices
+        const unsigned ex = (m.x >> lane) & 1u, ey = (m.y >> lane) & 1u, ez = (m.z >> lane) & 1u;
+        {
+            unsigned k = __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt);
+            if (ex) vlist[wid][k++] = (unsigned short)(lane << 2);
+            if (ey) vlist[wid][k++] = (unsigned short)(lane << 2 | 1u);
+            if (ez) vlist[wid][k] = (unsigned short)(lane << 2 | 2u);
         }
-        // edge vertices owned by this point (src/MarchingCubes.c:935-1026)
-        if (ex | ey | ez) {
-            const unsigned lt = (1u << lane) - 1u;
-            int id = (int)(o.x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt));
-            const float fx = (float)x, fy = (float)y, fz = (float)z;
-            const double gx = f2d(__fadd_rn(fx, flo0)), gy = f2d(__fadd_rn(fy, flo1)), gz = f2d(__fadd_rn(fz, flo2));
-            if (ex) {
-                const float X = __fadd_rn(__fadd_rn(fx, edge_u(c[0], c[1])), flo0);
-                pts[id] = {f2d(X), gy, gz};
-                if (frac_dist(X) < 1.5e-5f) add_cand(cand, ncand, cap, id);
-                id++;
+        const unsigned nv = __popc(m.x) + __popc(m.y) + __popc(m.z);
+        __syncwarp();
+        for (unsigned k = lane; k < nv; k += 32) {
+            const unsigned e = vlist[wid][k], l = e >> 2, ax = e & 3u;
+            const int px = x0 + (int)l;
+            const int qx = px + (ax == 0), qy = y + (ax == 1), qz = z + (ax == 2);
+            float c0, c1;
+            if (simple) {
+                const float *p = g.vol + ((long long)(g.lo0 + px) + (long long)(y + g.lo1) * g.dx + (long long)(z + g.lo2) * g.dxy);
+                c0 = ival(g, p);
+                c1 = ival(g, p + (ax == 0 ? 1ll : (ax == 1 ? (long long)g.dx : g.dxy)));
+            } else {
+                c0 = gval(g, px, y, z);
+                c1 = gval(g, qx, qy, qz);
             }
-            if (ey) {
-                const float Y = __fadd_rn(__fadd_rn(fy, edge_u(c[0], c[3])), flo1);
-                pts[id] = {gx, f2d(Y), gz};
-                if (frac_dist(Y) < 1.5e-5f) add_cand(cand, ncand, cap, id);
-                id++;
-            }
-            if (ez) {
-                const float Z = __fadd_rn(__fadd_rn(fz, edge_u(c[0], c[4])), flo2);
-                pts[id] = {gx, gy, f2d(Z)};
-                if (frac_dist(Z) < 1.5e-5f) add_cand(cand, ncand, cap, id);
-            }
+            const float u = edge_u(c0, c1);
+            float X = __fadd_rn((float)px, flo0), Y = __fadd_rn((float)y, flo1), Z = __fadd_rn((float)z, flo2);
+            float axv;
+            if (ax == 0) axv = X = __fadd_rn(__fadd_rn((float)px, u), flo0);
+            else if (ax == 1) axv = Y = __fadd_rn(__fadd_rn((float)y, u), flo1);
+            else axv = Z = __fadd_rn(__fadd_rn((float)z, u), flo2);
+            const int id = (int)(o.x + k);
+            pts[id] = {f2d(X), f2d(Y), f2d(Z)};
+            if (frac_dist(axv) < 1.5e-5f) add_cand(cand, ncand, cap, id);
         }
+        // ---- cubes: configuration from the sign bits
+        const int x = x0 + (int)lane;
         Tiling T = {0, 0, false};
-        float cl[8];   // corner array for the face/interior tests and the c-vertex only
-        if (cube) {
-            const int lut = cube_lut(c);
-            if (lut != 0 && lut != 255 && !quick_tiling(lut, classic, T)) {
-#pragma unroll
-                for (int k = 0; k < 8; k++) cl[k] = c[k];
-                T = select_tiling(cl, lut, classic);
+        float cl[8];   // corner values, ambiguous cubes only
+        if (hy && hz) {
+            const unsigned a0 = __ldg(signs + w), b0 = __ldg(signs + w + WX), c0 = __ldg(signs + w + slice),
+                           d0 = __ldg(signs + w + slice + WX);
+            unsigned an = 0, bn = 0, cn = 0, dn = 0;
+            if (nxw) {
+                an = __ldg(signs + w + 1); bn = __ldg(signs + w + WX + 1);
+                cn = __ldg(signs + w + slice + 1); dn = __ldg(signs + w + slice + WX + 1);
+            }
+            const unsigned a1 = __funnelshift_r(a0, an, 1), b1 = __funnelshift_r(b0, bn, 1), c1 = __funnelshift_r(c0, cn, 1),
+                           d1 = __funnelshift_r(d0, dn, 1);
+            if (x < g.NX - 1) {
+                const int lut = (int)((a0 >> lane) & 1u) | (int)((a1 >> lane) & 1u) << 1 | (int)((b1 >> lane) & 1u) << 2 |
+                                (int)((b0 >> lane) & 1u) << 3 | (int)((c0 >> lane) & 1u) << 4 | (int)((c1 >> lane) & 1u) << 5 |
+                                (int)((d1 >> lane) & 1u) << 6 | (int)((d0 >> lane) & 1u) << 7;
+                if (lut != 0 && lut != 255 && !quick_tiling(lut, classic, T)) {
+                    cube_values(g, simple, x, y, z, cl);
+                    T = select_tiling(cl, lut, classic);
+                }
             }
         }
         const int cnt = T.n | ((int)T.cv << 16);
-        int sc = cnt;   // warp exclusive scan of (triangles, c-vertices)
+        int sc = cnt;   // warp inclusive scan of (triangles, c-vertices)
         for (int d = 1; d < 32; d <<= 1) {
             const int a = __shfl_up_sync(0xffffffffu, sc, d);
             if ((int)lane >= d) sc += a;
         }
+        const int ntri = __shfl_sync(0xffffffffu, sc, 31) & 0xffff;
         sc -= cnt;
         const int tb = sc & 0xffff, cb = sc >> 16;
-        if (T.n == 0) continue;
         int v12 = -1;
-        if (T.cv) {   // c-vertex: mean of the cube's edge vertices (src/MarchingCubes.c:1029-1082)
+        if (T.cv) {
             v12 = (int)(totals.x + o.z + cb);
-            float n = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
-            for (int e = 0; e < 12; e++) {
-                const int own = k_edge[e][0], ax = k_edge[e][1], ca = k_edge[e][2], cbn = k_edge[e][3];
-                if ((cl[ca] > 0.f) == (cl[cbn] > 0.f)) continue;
-                const float u = edge_u(cl[ca], cl[cbn]);
-                float px = (float)(x + ((own ^ (own >> 1)) & 1)), py = (float)(y + ((own >> 1) & 1)),
-                      pz = (float)(z + ((own >> 2) & 1));
-                if (ax == 0) px = __fadd_rn(px, u);
-                else if (ax == 1) py = __fadd_rn(py, u);
-                else pz = __fadd_rn(pz, u);
-                n = __fadd_rn(n, 1.f);
-                sx = __fadd_rn(sx, px); sy = __fadd_rn(sy, py); sz = __fadd_rn(sz, pz);
-            }
-            if (n > 0.f) { sx = __fdiv_rn(sx, n); sy = __fdiv_rn(sy, n); sz = __fdiv_rn(sz, n); }
-            const float X = __fadd_rn(sx, flo0), Y = __fadd_rn(sy, flo1), Z = __fadd_rn(sz, flo2);
-            pts[v12] = {f2d(X), f2d(Y), f2d(Z)};
-            if (fminf(frac_dist(X), fminf(frac_dist(Y), frac_dist(Z))) < 1.5e-5f) add_cand(ccand, nccand, cap, v12);
+            emit_cvertex(cl, x, y, z, flo0, flo1, flo2, v12, pts, ccand, nccand, cap);
         }
-        // triangles, stored reversed (v3,v2,v1) as marchingCubes() returns them
-        const unsigned NY = (unsigned)g.NY;
-        int tv[3];
-        for (int t = 0; t < 3 * T.n; t++) {
-            const int code = d_lut[T.off + t];
-            int v = v12;
-            if (code >= 0 && code < 12) {
-                const unsigned e = edge_code(code);
-                v = vid(words, offs, NY, WX, x + (int)(e & 1u), y + (int)((e >> 1) & 1u), z + (int)((e >> 2) & 1u),
-                        (int)(e >> 3));
-            } else if (code != 12) {
-                v = -1;
-            }
-            tv[t % 3] = v;
-            if (t % 3 == 2) tris[o.y + tb + t / 3] = {tv[2], tv[1], tv[0]};
+        if (T.n) {
+            toff[wid][lane] = T.off;
+            v12s[wid][lane] = v12;
+            for (int j = 0; j < T.n; j++) tlist[wid][tb + j] = (unsigned short)(lane << 4 | (unsigned)j);
         }
+        __syncwarp();
+        // ---- triangles, stored reversed (v3,v2,v1) as marchingCubes() returns them
+        for (int k = (int)lane; k < ntri; k += 32) {
+            const unsigned e = tlist[wid][k], l = e >> 4, j = e & 15u;
+            const int off = toff[wid][l] + 3 * (int)j;
+            int tv[3];
+#pragma unroll
+            for (int t = 0; t < 3; t++) {
+                const int code = d_lut[off + t];
+                int v = -1;
+                if (code >= 0 && code < 12) {
+                    const unsigned ec = edge_code(code);
+                    const unsigned tl = l + (ec & 1u);                  // target point: x0 + tl (tl <= 32)
+                    const unsigned nbk = (tl >> 5) | (ec & 6u);          // neighbour word (dx | dy << 1 | dz << 2)
+                    const unsigned tlane = tl & 31u, tlt = (1u << tlane) - 1u, ax = ec >> 3;
+                    const uint4 nm = nbm[wid][nbk];
+                    unsigned id = nbo[wid][nbk] + __popc(nm.x & tlt) + __popc(nm.y & tlt) + __popc(nm.z & tlt);
+                    if (ax >= 1) id += (nm.x >> tlane) & 1u;
+                    if (ax == 2) id += (nm.y >> tlane) & 1u;
+                    v = (int)id;
+                } else if (code == 12) {
+                    v = v12s[wid][l];
+                }
+                tv[t] = v;
+            }
+            tris[o.y + k] = {tv[2], tv[1], tv[0]};
+        }
+        __syncwarp();   // the lists are reused by the next word
     }
-    (void)nwords;
 }
 
 // ---- adjoint of the vertex positions w.r.t. the processed volume -----------------
@@ -525,8 +587,9 @@ n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4
     CKS(w.cand.ensure((nwords + 1) * sizeof(unsigned)));
     CKS(w.signs.ensure(nwords * sizeof(unsigned)));
     {
-        const unsigned blocks = (unsigned)std::min<size_t>((nwords + 7) / 8, 152u * 64u);
-        k_signs<<<blocks, 256, 0, s>>>(v, WX, (unsigned)nwords, w.signs.as<unsigned>());
+        const unsigned nrows = (unsigned)g.n[1] * (unsigned)g.n[2];
+        const unsigned blocks = std::min<unsigned>((nrows + 7) / 8, 152u * 16u);
+        k_signs<<<blocks, 256, 0, s>>>(v, WX, nrows, w.signs.as<unsigned>());
         N2M_COUNT();
     }
     {
@@ -551,7 +614,7 @@ n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, v
     const unsigned nact = c.nactive;
     if (nact == 0) return N2M_OK;
     const unsigned blocks = std::min<unsigned>((nact + 7) / 8, 152u * 16u);
-    { k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.cand.as<unsigned>(), nact, (unsigned)nwords, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand, d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
+    { k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.signs.as<unsigned>(), w.cand.as<unsigned>(), nact, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand, d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

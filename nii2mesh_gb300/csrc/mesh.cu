@@ -76,9 +76,32 @@ __device__ bool degenerate_ref(vec3d A, vec3d B, vec3d C) {
 // path: the area from an FP32 cross product of (double) edge vectors, minus a
 // bound on its rounding error, exceeding 4e-7 (> 3x FLT_EPSILON) proves the
 // triangle is kept.
+// float value of d if d is exactly a float (zero or normal), by bit assembly:
+// the F2F conversion issues on the FP64 pipe, a small fraction of the integer
+// rate on this part
+__device__ __forceinline__ bool d2f_exact(double d, float &f) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    const unsigned long long m = b & 0xfffffffffffffull;
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    if (e == 0 && m == 0) { f = __uint_as_float(sign); return true; }
+    if ((m & 0x1fffffffull) || e < 897u || e > 1150u) return false;   // low bits set or outside the normal float range
+    f = __uint_as_float(sign | ((e - 896u) << 23) | (unsigned)(m >> 29));
+    return true;
+}
+
 __device__ __forceinline__ bool degenerate(vec3d A, vec3d B, vec3d C) {
-    const float ux = (float)(B.x - A.x), uy = (float)(B.y - A.y), uz = (float)(B.z - A.z);
-    const float vx = (float)(C.x - A.x), vy = (float)(C.y - A.y), vz = (float)(C.z - A.z);
+    float ax, ay, az, bx, by, bz, qx, qy, qz;
+    float ux, uy, uz, vx, vy, vz;
+    if (d2f_exact(A.x, ax) & d2f_exact(A.y, ay) & d2f_exact(A.z, az) & d2f_exact(B.x, bx) & d2f_exact(B.y, by) &
+        d2f_exact(B.z, bz) & d2f_exact(C.x, qx) & d2f_exact(C.y, qy) & d2f_exact(C.z, qz)) {
+        // float coordinates: the FP32 difference is the double difference rounded to float
+        ux = bx - ax; uy = by - ay; uz = bz - az;
+        vx = qx - ax; vy = qy - ay; vz = qz - az;
+    } else {
+        ux = (float)(B.x - A.x); uy = (float)(B.y - A.y); uz = (float)(B.z - A.z);
+        vx = (float)(C.x - A.x); vy = (float)(C.y - A.y); vz = (float)(C.z - A.z);
+    }
     const float cx = uy * vz - uz * vy, cy = uz * vx - ux * vz, cz = ux * vy - uy * vx;
     const float cr = sqrtf(cx * cx + cy * cy + cz * cz);
     const float nu = sqrtf(ux * ux + uy * uy + uz * uz), nv = sqrtf(vx * vx + vy * vy + vz * vz);
