@@ -121,3 +121,4 @@ N2M_HD bool tap5_fast(float a, float b, float c, float d, float e, float *out) {
     }
     return false;
 }
+

@@ -13,10 +13,11 @@
 //   and the triangle and c-vertex counts of its 32 cubes with bit operations
 //   and the MC33 decision of the few cubes that cross the surface.
 // scan: exclusive scan over words -> vertex/triangle/c-vertex offsets.
-// emit pass: only words that own output recompute their cubes; an edge
+// emit pass: a warp takes 32 active words (words that own output) at a time
+//   and works through their edge vertices and triangles densely; an edge
 //   vertex id anywhere in the grid is offset(word) + popcounts of the word's
-//   masks below the lane, so every edge is emitted exactly once (this replaces
-//   the reference's vertex weld for shared edges).
+//   masks below the point, so every edge is emitted exactly once (this
+//   replaces the reference's vertex weld for shared edges).
 // Vertices whose final coordinates sit within 1.5e-5 of a grid point (edge
 // vertices) or of a grid plane (c-vertices) are recorded as weld candidates:
 // only such vertices can lie within the weld tolerance (1e-5) of another.
@@ -213,15 +214,32 @@ __device__ __forceinline__ float ival(const GV &g, const float *p) {
     return fabsf(v) < N2M_FLT_EPS ? N2M_FLT_EPS : v;
 }
 
-// exact float -> double by assembling the bits (the F2F conversion issues on
-// the FP64 pipe, a small fraction of the integer rate on this part)
+// exact float -> double by assembling the bits in integer registers (a
+// conversion instruction would issue on the pipe this part shares with FP64;
+// a predicated one still issues)
 __device__ __forceinline__ double f2d(float f) {
     const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
-    if (e == 0xffu || (e == 0u && m)) return (double)f;   // non-finite, subnormal
     const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
-    if (e == 0u) return __longlong_as_double((long long)sign);
-    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29)));
+    unsigned long long de, dm;
+    if (e == 0xffu) {               // Inf, NaN
+        de = 0x7ffull;
+        dm = (unsigned long long)m << 29;
+    } else if (e != 0u) {           // normal
+        de = e + 896u;
+        dm = (unsigned long long)m << 29;
+    } else if (m != 0u) {           // subnormal: m * 2^-149, leading bit p
+        const int p = 31 - __clz((int)m);
+        de = (unsigned long long)(p - 149 + 1023);
+        dm = ((unsigned long long)m << (52 - p)) & 0xfffffffffffffull;
+    } else {                        // signed zero
+        de = 0;
+        dm = 0;
+    }
+    return __longlong_as_double((long long)(sign | (de << 52) | dm));
 }
+
+// exact float of 0 <= v < 2^23 by bit assembly (no I2F conversion)
+__device__ __forceinline__ float i2f_small(int v) { return __int_as_float(0x4B000000 | v) - 8388608.f; }
 
 // tiling edge code 0..11 -> owner offset (bit 0: +x, 1: +y, 2: +z) and axis (bits 3-4)
 __device__ __forceinline__ unsigned edge_code(int code) {
@@ -284,83 +302,107 @@ __device__ __noinline__ void cube_values(const GV &g, bool simple, int x, int y,
     }
 }
 
-// One warp per active word.  Its items are spread densely over the lanes:
-// first the word's edge vertices (in id order), then its triangles (in
-// output order), so no lane idles on the many points of a word that cross
-// nothing.  Cube configurations come from the sign-bit volume of the count
-// pass; only ambiguous cubes read corner values for the face/interior tests.
-// Vertex ids of neighbouring words come from the masks and offsets of the 8
-// words a cube can touch, staged in shared memory.
-__global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, const uint4 *__restrict__ words,
-                                              const uint4 *__restrict__ offs, const unsigned *__restrict__ signs,
-                                              const unsigned *__restrict__ active, unsigned nactive, uint4 totals,
-                                              vec3d *pts, vec3i *tris, int *cand, unsigned *ncand, int *ccand,
-                                              unsigned *nccand, int cap) {
-    __shared__ unsigned short vlist[8][96];   // per warp: lane << 2 | axis of the word's edge vertices
-    __shared__ unsigned short tlist[8][384];  // per warp: lane << 4 | j of the word's triangles
-    __shared__ int toff[8][32], v12s[8][32];
-    __shared__ uint4 nbm[8][8];               // masks of the words (dx, dy, dz) = (k&1, k>>1&1, k>>2)
-    __shared__ unsigned nbo[8][8];            // and their first vertex ids
+// Group emit: a warp takes 32 consecutive active words, one per lane.  Each
+// lane lists its word's edge vertices and the triangles of its unambiguous
+// cubes into warp-private shared-memory lists (positions from the scanned
+// offsets, so the lists come out in output order); then all 32 lanes work
+// through the lists densely.  Ambiguous cubes (face/interior tests, maybe a
+// c-vertex) and list overflow are handled by the owning lane directly.
+constexpr int EG_WARPS = 4, EG_VCAP = 1024, EG_TCAP = 1024;
+constexpr unsigned EG_HOLE = 0xffffffffu;
+
+__device__ __forceinline__ void emit_vertex(const GV &g, bool simple, int x0, int y, int z, int p, int ax, int id,
+                                            float flo0, float flo1, float flo2, vec3d *pts, int *cand, unsigned *ncand,
+                                            int cap) {
+    const int px = x0 + p;
+    float c0, c1;
+    if (simple) {
+        const float *q = g.vol + ((long long)(g.lo0 + px) + (long long)(y + g.lo1) * g.dx + (long long)(z + g.lo2) * g.dxy);
+        c0 = ival(g, q);
+        c1 = ival(g, q + (ax == 0 ? 1ll : (ax == 1 ? (long long)g.dx : g.dxy)));
+    } else {
+        c0 = gval(g, px, y, z);
+        c1 = gval(g, px + (ax == 0), y + (ax == 1), z + (ax == 2));
+    }
+    const float u = edge_u(c0, c1);
+    const float fx = i2f_small(px), fy = i2f_small(y), fz = i2f_small(z);
+    float X = __fadd_rn(fx, flo0), Y = __fadd_rn(fy, flo1), Z = __fadd_rn(fz, flo2), axv;
+    if (ax == 0) axv = X = __fadd_rn(__fadd_rn(fx, u), flo0);
+    else if (ax == 1) axv = Y = __fadd_rn(__fadd_rn(fy, u), flo1);
+    else axv = Z = __fadd_rn(__fadd_rn(fz, u), flo2);
+    pts[id] = {f2d(X), f2d(Y), f2d(Z)};
+    if (frac_dist(axv) < 1.5e-5f) add_cand(cand, ncand, cap, id);
+}
+
+__device__ __forceinline__ void emit_triangle(const uint4 *__restrict__ words, const uint4 *__restrict__ offs,
+                                              unsigned NY, unsigned WX, int x, int y, int z, int off, int v12,
+                                              vec3i *dst) {
+    int tv[3];
+#pragma unroll
+    for (int t = 0; t < 3; t++) {
+        const int code = d_lut[off + t];
+        int v = -1;
+        if (code >= 0 && code < 12) {
+            const unsigned ec = edge_code(code);
+            v = vid(words, offs, NY, WX, x + (int)(ec & 1u), y + (int)((ec >> 1) & 1u), z + (int)((ec >> 2) & 1u),
+                    (int)(ec >> 3));
+        } else if (code == 12) {
+            v = v12;
+        }
+        tv[t] = v;
+    }
+    *dst = {tv[2], tv[1], tv[0]};
+}
+
+__global__ void __launch_bounds__(EG_WARPS * 32) k_emit(GV g, bool classic, unsigned WX, const uint4 *__restrict__ words,
+                                                          const uint4 *__restrict__ offs, const unsigned *__restrict__ signs,
+                                                          const unsigned *__restrict__ active, unsigned nactive,
+                                                          uint4 totals, vec3d *pts, vec3i *tris, int *cand,
+                                                          unsigned *ncand, int *ccand, unsigned *nccand, int cap) {
+    __shared__ unsigned short vitem[EG_WARPS][EG_VCAP];   // lane << 7 | point << 2 | axis
+    __shared__ unsigned titem[EG_WARPS][EG_TCAP];          // lane << 27 | point << 22 | tiling offset, or a hole
+    __shared__ unsigned qtile[256];                        // unambiguous tilings: offset << 8 | triangles; 0xff: tests
+    for (int i = threadIdx.x; i < 256; i += EG_WARPS * 32) {
+        Tiling T = {0, 0, false};
+        qtile[i] = quick_tiling(i, classic, T) ? (unsigned)T.off << 8 | (unsigned)T.n : 0xffu;
+    }
+    __syncthreads();
     const unsigned lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
     const float flo0 = (float)g.lo0, flo1 = (float)g.lo1, flo2 = (float)g.lo2;
-    const unsigned slice = WX * (unsigned)g.NY;
-    for (unsigned aw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; aw < nactive; aw += (gridDim.x * blockDim.x) >> 5) {
-        const unsigned w = active[aw];
+    const unsigned slice = WX * (unsigned)g.NY, NY = (unsigned)g.NY;
+    const unsigned ngroups = (nactive + 31) / 32;
+    for (unsigned grp = blockIdx.x * EG_WARPS + wid; grp < ngroups; grp += gridDim.x * EG_WARPS) {
+        const unsigned aw = grp * 32 + lane;
+        const bool live = aw < nactive;
+        const unsigned w = live ? active[aw] : active[nactive - 1];
         const unsigned row = w / WX, xw = w - row * WX;
-        const int z = (int)(row / (unsigned)g.NY), y = (int)(row - (unsigned)z * (unsigned)g.NY);
+        const int z = (int)(row / NY), y = (int)(row - (unsigned)z * NY);
         const int x0 = (int)(xw * 32u);
         const uint4 o = offs[w];
-        const uint4 m = words[w];
-        const bool nxw = xw + 1 < WX, hy = y < g.NY - 1, hz = z < g.NZ - 1;
-        if (lane < 8) {
-            const unsigned ddx = lane & 1u, ddy = (lane >> 1) & 1u, ddz = lane >> 2;
-            const bool ok = (!ddx || nxw) && (!ddy || hy) && (!ddz || hz);
-            const unsigned wn = w + ddx + ddy * WX + ddz * slice;
-            nbm[wid][lane] = ok ? words[wn] : make_uint4(0u, 0u, 0u, 0u);
-            nbo[wid][lane] = ok ? offs[wn].x : 0u;
-        }
-        // the word's cubes strictly inside the volume: no darkening, wrap or padding
+        const uint4 m = live ? words[w] : make_uint4(0u, 0u, 0u, 0u);
         const bool simple = g.lo0 + x0 >= 1 && g.lo0 + x0 + 32 <= g.dx - 2 && g.lo1 + y >= 1 && g.lo1 + y + 1 <= g.dy - 2 &&
                             g.lo2 + z >= 1 && g.lo2 + z + 1 <= g.dz - 2;
-        // ---- edge vertices
-        const unsigned ex = (m.x >> lane) & 1u, ey = (m.y >> lane) & 1u, ez = (m.z >> lane) & 1u;
+        const unsigned vbase = __shfl_sync(0xffffffffu, o.x, 0), tbase = __shfl_sync(0xffffffffu, o.y, 0);
+        // ---- list the word's edge vertices (ids consecutive from o.x)
         {
-            unsigned k = __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt);
-            if (ex) vlist[wid][k++] = (unsigned short)(lane << 2);
-            if (ey) vlist[wid][k++] = (unsigned short)(lane << 2 | 1u);
-            if (ez) vlist[wid][k] = (unsigned short)(lane << 2 | 2u);
-        }
-        const unsigned nv = __popc(m.x) + __popc(m.y) + __popc(m.z);
-        __syncwarp();
-        for (unsigned k = lane; k < nv; k += 32) {
-            const unsigned e = vlist[wid][k], l = e >> 2, ax = e & 3u;
-            const int px = x0 + (int)l;
-            const int qx = px + (ax == 0), qy = y + (ax == 1), qz = z + (ax == 2);
-            float c0, c1;
-            if (simple) {
-                const float *p = g.vol + ((long long)(g.lo0 + px) + (long long)(y + g.lo1) * g.dx + (long long)(z + g.lo2) * g.dxy);
-                c0 = ival(g, p);
-                c1 = ival(g, p + (ax == 0 ? 1ll : (ax == 1 ? (long long)g.dx : g.dxy)));
-            } else {
-                c0 = gval(g, px, y, z);
-                c1 = gval(g, qx, qy, qz);
+            unsigned k = o.x - vbase;
+            unsigned pm = m.x | m.y | m.z;
+            while (pm) {
+                const int p = __ffs(pm) - 1;
+                pm &= pm - 1;
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) {
+                    const unsigned mk = ax == 0 ? m.x : (ax == 1 ? m.y : m.z);
+                    if (!((mk >> p) & 1u)) continue;
+                    if (k < (unsigned)EG_VCAP) vitem[wid][k] = (unsigned short)(lane << 7 | (unsigned)p << 2 | (unsigned)ax);
+                    else emit_vertex(g, simple, x0, y, z, p, ax, (int)(vbase + k), flo0, flo1, flo2, pts, cand, ncand, cap);
+                    k++;
+                }
             }
-            const float u = edge_u(c0, c1);
-            float X = __fadd_rn((float)px, flo0), Y = __fadd_rn((float)y, flo1), Z = __fadd_rn((float)z, flo2);
-            float axv;
-            if (ax == 0) axv = X = __fadd_rn(__fadd_rn((float)px, u), flo0);
-            else if (ax == 1) axv = Y = __fadd_rn(__fadd_rn((float)y, u), flo1);
-            else axv = Z = __fadd_rn(__fadd_rn((float)z, u), flo2);
-            const int id = (int)(o.x + k);
-            pts[id] = {f2d(X), f2d(Y), f2d(Z)};
-            if (frac_dist(axv) < 1.5e-5f) add_cand(cand, ncand, cap, id);
         }
-        // ---- cubes: configuration from the sign bits
-        const int x = x0 + (int)lane;
-        Tiling T = {0, 0, false};
-        float cl[8];   // corner values, ambiguous cubes only
-        if (hy && hz) {
+        // ---- list the triangles of the word's cubes (positions from o.y)
+        const bool hy = y < g.NY - 1, hz = z < g.NZ - 1, nxw = xw + 1 < WX;
+        if (live && hy && hz) {
             const unsigned a0 = __ldg(signs + w), b0 = __ldg(signs + w + WX), c0 = __ldg(signs + w + slice),
                            d0 = __ldg(signs + w + slice + WX);
             unsigned an = 0, bn = 0, cn = 0, dn = 0;
@@ -370,63 +412,77 @@ __global__ void __launch_bounds__(256) k_emit(GV g, bool classic, unsigned WX, c
             }
             const unsigned a1 = __funnelshift_r(a0, an, 1), b1 = __funnelshift_r(b0, bn, 1), c1 = __funnelshift_r(c0, cn, 1),
                            d1 = __funnelshift_r(d0, dn, 1);
-            if (x < g.NX - 1) {
-                const int lut = (int)((a0 >> lane) & 1u) | (int)((a1 >> lane) & 1u) << 1 | (int)((b1 >> lane) & 1u) << 2 |
-                                (int)((b0 >> lane) & 1u) << 3 | (int)((c0 >> lane) & 1u) << 4 | (int)((c1 >> lane) & 1u) << 5 |
-                                (int)((d1 >> lane) & 1u) << 6 | (int)((d0 >> lane) & 1u) << 7;
-                if (lut != 0 && lut != 255 && !quick_tiling(lut, classic, T)) {
-                    cube_values(g, simple, x, y, z, cl);
-                    T = select_tiling(cl, lut, classic);
+            const unsigned hxm = x0 + 33 <= g.NX ? 0xffffffffu : (g.NX - 1 - x0 > 0 ? (1u << (g.NX - 1 - x0)) - 1u : 0u);
+            unsigned mix = (a0 | a1 | b0 | b1 | c0 | c1 | d0 | d1) & ~(a0 & a1 & b0 & b1 & c0 & c1 & d0 & d1) & hxm;
+            unsigned k = o.y - tbase;
+            int cv = (int)(totals.x + o.z);
+            while (mix) {
+                const int p = __ffs(mix) - 1;
+                mix &= mix - 1;
+                const int lut = (int)((a0 >> p) & 1u) | (int)((a1 >> p) & 1u) << 1 | (int)((b1 >> p) & 1u) << 2 |
+                                (int)((b0 >> p) & 1u) << 3 | (int)((c0 >> p) & 1u) << 4 | (int)((c1 >> p) & 1u) << 5 |
+                                (int)((d1 >> p) & 1u) << 6 | (int)((d0 >> p) & 1u) << 7;
+                const unsigned q = qtile[lut];
+                if (q != 0xffu) {
+                    const int off = (int)(q >> 8), n = (int)(q & 0xffu);
+                    for (int j = 0; j < n; j++, k++) {
+                        if (k < (unsigned)EG_TCAP) titem[wid][k] = lane << 27 | (unsigned)p << 22 | (unsigned)(off + 3 * j);
+                        else emit_triangle(words, offs, NY, WX, x0 + p, y, z, off + 3 * j, -1, tris + tbase + k);
+                    }
+                } else {   // face/interior tests and the c-vertex: this lane
+                    float cl[8];
+                    cube_values(g, simple, x0 + p, y, z, cl);
+                    const Tiling T = select_tiling(cl, lut, classic);
+                    int v12 = -1;
+                    if (T.cv) {
+                        v12 = cv++;
+                        emit_cvertex(cl, x0 + p, y, z, flo0, flo1, flo2, v12, pts, ccand, nccand, cap);
+                    }
+                    for (int j = 0; j < T.n; j++, k++) {
+                        emit_triangle(words, offs, NY, WX, x0 + p, y, z, T.off + 3 * j, v12, tris + tbase + k);
+                        if (k < (unsigned)EG_TCAP) titem[wid][k] = EG_HOLE;
+                    }
                 }
             }
         }
-        const int cnt = T.n | ((int)T.cv << 16);
-        int sc = cnt;   // warp inclusive scan of (triangles, c-vertices)
-        for (int d = 1; d < 32; d <<= 1) {
-            const int a = __shfl_up_sync(0xffffffffu, sc, d);
-            if ((int)lane >= d) sc += a;
+        // ---- group totals: the last live lane's end positions
+        const unsigned nl = min(32u, nactive - grp * 32);
+        const uint4 ol = offs[__shfl_sync(0xffffffffu, w, nl - 1)];   // every lane reads the same word
+        const unsigned lastw = __shfl_sync(0xffffffffu, w, nl - 1);
+        const uint4 ml = words[lastw];
+        unsigned ntl = 0;   // triangles of the last word: next word's offset minus its own
+        {
+            const unsigned nw = (unsigned)WX * (unsigned)g.NY * (unsigned)g.NZ;
+            const unsigned next_y = lastw + 1 < nw ? offs[lastw + 1].y : totals.y;
+            ntl = next_y - ol.y;
         }
-        const int ntri = __shfl_sync(0xffffffffu, sc, 31) & 0xffff;
-        sc -= cnt;
-        const int tb = sc & 0xffff, cb = sc >> 16;
-        int v12 = -1;
-        if (T.cv) {
-            v12 = (int)(totals.x + o.z + cb);
-            emit_cvertex(cl, x, y, z, flo0, flo1, flo2, v12, pts, ccand, nccand, cap);
-        }
-        if (T.n) {
-            toff[wid][lane] = T.off;
-            v12s[wid][lane] = v12;
-            for (int j = 0; j < T.n; j++) tlist[wid][tb + j] = (unsigned short)(lane << 4 | (unsigned)j);
-        }
+        const unsigned nvg = min((unsigned)EG_VCAP, ol.x + __popc(ml.x) + __popc(ml.y) + __popc(ml.z) - vbase);
+        const unsigned ntg = min((unsigned)EG_TCAP, ol.y + ntl - tbase);
         __syncwarp();
-        // ---- triangles, stored reversed (v3,v2,v1) as marchingCubes() returns them
-        for (int k = (int)lane; k < ntri; k += 32) {
-            const unsigned e = tlist[wid][k], l = e >> 4, j = e & 15u;
-            const int off = toff[wid][l] + 3 * (int)j;
-            int tv[3];
-#pragma unroll
-            for (int t = 0; t < 3; t++) {
-                const int code = d_lut[off + t];
-                int v = -1;
-                if (code >= 0 && code < 12) {
-                    const unsigned ec = edge_code(code);
-                    const unsigned tl = l + (ec & 1u);                  // target point: x0 + tl (tl <= 32)
-                    const unsigned nbk = (tl >> 5) | (ec & 6u);          // neighbour word (dx | dy << 1 | dz << 2)
-                    const unsigned tlane = tl & 31u, tlt = (1u << tlane) - 1u, ax = ec >> 3;
-                    const uint4 nm = nbm[wid][nbk];
-                    unsigned id = nbo[wid][nbk] + __popc(nm.x & tlt) + __popc(nm.y & tlt) + __popc(nm.z & tlt);
-                    if (ax >= 1) id += (nm.x >> tlane) & 1u;
-                    if (ax == 2) id += (nm.y >> tlane) & 1u;
-                    v = (int)id;
-                } else if (code == 12) {
-                    v = v12s[wid][l];
-                }
-                tv[t] = v;
-            }
-            tris[o.y + k] = {tv[2], tv[1], tv[0]};
+        // ---- dense vertices
+        for (unsigned b = 0; b < nvg; b += 32) {
+            const unsigned k = b + lane;
+            const unsigned e = k < nvg ? vitem[wid][k] : 0u;
+            const int l = (int)(e >> 7);
+            const int sx0 = __shfl_sync(0xffffffffu, x0, l), sy = __shfl_sync(0xffffffffu, y, l),
+                      sz = __shfl_sync(0xffffffffu, z, l);
+            const bool ssimple = __shfl_sync(0xffffffffu, simple, l);
+            if (k < nvg)
+                emit_vertex(g, ssimple, sx0, sy, sz, (int)((e >> 2) & 31u), (int)(e & 3u), (int)(vbase + k), flo0, flo1, flo2,
+                            pts, cand, ncand, cap);
         }
-        __syncwarp();   // the lists are reused by the next word
+        // ---- dense triangles
+        for (unsigned b = 0; b < ntg; b += 32) {
+            const unsigned k = b + lane;
+            const unsigned e = k < ntg ? titem[wid][k] : EG_HOLE;
+            const int l = (int)((e >> 27) & 31u);
+            const int sx0 = __shfl_sync(0xffffffffu, x0, l), sy = __shfl_sync(0xffffffffu, y, l),
+                      sz = __shfl_sync(0xffffffffu, z, l);
+            if (e != EG_HOLE)
+                emit_triangle(words, offs, NY, WX, sx0 + (int)((e >> 22) & 31u), sy, sz, (int)(e & 0x3fffffu), -1,
+                              tris + tbase + k);
+        }
+        __syncwarp();   // the lists are reused by the next group
     }
 }
 
@@ -610,11 +666,18 @@ n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, v
                    int *d_cand, unsigned *d_ncand, int cand_cap, cudaStream_t s) {
     const GV v = make_gv(g);
     const unsigned WX = (unsigned)((g.n[0] + 31) / 32);
-    const size_t nwords = (size_t)WX * g.n[1] * g.n[2];
     const unsigned nact = c.nactive;
     if (nact == 0) return N2M_OK;
-    const unsigned blocks = std::min<unsigned>((nact + 7) / 8, 152u * 16u);
-    { k_emit<<<blocks, 256, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.signs.as<unsigned>(), w.cand.as<unsigned>(), nact, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand, d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
+    static int resident = 0;   // CTAs of k_emit that fit the GPU at once
+    if (!resident) {
+        int dev = 0, sms = 0, per_sm = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit, EG_WARPS * 32, 0));
+        resident = sms * std::max(per_sm, 1);
+    }
+    const unsigned gblocks = std::min<unsigned>(((nact + 31) / 32 + EG_WARPS - 1) / EG_WARPS, (unsigned)resident);
+    { k_emit<<<gblocks, EG_WARPS * 32, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.signs.as<unsigned>(), w.cand.as<unsigned>(), nact, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand, d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

@@ -213,7 +213,13 @@ __device__ __forceinline__ int cube_lut(const float *c) {
     return lut;
 }
 
-__device__ __forceinline__ float frac_dist(float f) { return fabsf(f - rintf(f)); }
+// distance of a grid coordinate 0 <= f < 2^22 to the nearest integer; adding
+// 1.5 * 2^23 rounds to an integer in the FP32 adder (rintf would issue on
+// the conversion pipe, which this part shares with FP64)
+__device__ __forceinline__ float frac_dist(float f) {
+    const float r = __fsub_rn(__fadd_rn(f, 12582912.f), 12582912.f);
+    return fabsf(__fsub_rn(f, r));
+}
 
 // cube edge e of the tiling tables: owner corner, axis, the two corners it
 // interpolates (owner first)
