@@ -13,6 +13,7 @@ Volumes are numpy float32 arrays shaped (nz, ny, nx) — x fastest, exactly the
 reference's memory layout.  Meshes are (tris int32 (nt,3), pts float64 (np,3)).
 """
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -37,12 +38,20 @@ def _vol(img):
     return a
 
 
+def _owned(L, ptr, n, ctype, dtype):
+    """numpy (n, 3) view of library-malloc'd memory, freed with libc free()
+    once the last array referring to it is gone (no copy of the mesh)."""
+    addr = ptr.value if isinstance(ptr, C.c_void_p) else ptr
+    if not n:
+        L.libc_free(addr)
+        return np.zeros((0, 3), dtype)
+    buf = (ctype * (3 * n)).from_address(addr)
+    weakref.finalize(buf, L.libc_free, addr)
+    return np.frombuffer(buf, dtype).reshape(n, 3)
+
+
 def _take(L, tp, pp, nt, np_):
-    t = np.ctypeslib.as_array(C.cast(tp, C.POINTER(C.c_int)), shape=(nt, 3)).copy() if nt else np.zeros((0, 3), np.int32)
-    p = np.ctypeslib.as_array(C.cast(pp, C.POINTER(C.c_double)), shape=(np_, 3)).copy() if np_ else np.zeros((0, 3))
-    L.libc_free(tp)
-    L.libc_free(pp)
-    return t, p
+    return _owned(L, tp, nt, C.c_int, np.int32), _owned(L, pp, np_, C.c_double, np.float64)
 
 
 class Context:

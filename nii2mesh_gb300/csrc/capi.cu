@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <thread>
 #include <vector>
 
 #include "n2m_internal.cuh"
@@ -64,6 +65,55 @@ void DevBuf::release() {
 }
 
 // ---- context ------------------------------------------------------------------------
+// Output buffers of a host-memory meshify call.  They are malloc'd (the
+// caller frees them with free(), as the reference's callers do) as soon as the
+// raw mesh size is known, and their pages are faulted in by host threads while
+// the GPU finishes: first-touch page faults of a fresh 100+ MB buffer cost more
+// than the device-to-host copy itself.
+struct HostOut {
+    char *pts = nullptr, *tris = nullptr;
+    size_t pb = 0, tb = 0;
+    std::vector<std::thread> th;
+    void start(size_t pbytes, size_t tbytes) {
+        discard();
+        pts = (char *)malloc(pbytes);
+        tris = (char *)malloc(tbytes);
+        if (!pts || !tris) {
+            free(pts);
+            free(tris);
+            pts = tris = nullptr;
+            return;
+        }
+        pb = pbytes;
+        tb = tbytes;
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int n = (int)std::min(16u, std::max(1u, hw));
+        const size_t total = pb + tb;
+        try {
+            for (int i = 0; i < n; i++)
+                th.emplace_back([this, i, n, total] {
+                    const size_t page = 4096, lo = total * i / n, hi = total * (i + 1) / n;
+                    for (size_t o = (lo + page - 1) / page * page; o < hi; o += page) {
+                        if (o < pb) pts[o] = 0;
+                        else tris[o - pb] = 0;
+                    }
+                });
+        } catch (...) {   // no threads: the copy faults the pages in itself
+        }
+    }
+    void join() {
+        for (auto &t : th) t.join();
+        th.clear();
+    }
+    void discard() {
+        join();
+        free(pts);
+        free(tris);
+        pts = tris = nullptr;
+        pb = tb = 0;
+    }
+};
+
 struct n2m_context {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -93,6 +143,11 @@ struct n2m_context {
     vec3d *res_pts = nullptr;
     vec3i *res_tris = nullptr;
     int res_np = 0, res_nt = 0;
+    // host-memory calls: staged input upload and pre-faulted outputs
+    cudaStream_t copy = nullptr;
+    StagedInput stage;
+    bool want_host = false;
+    HostOut hout;
 };
 
 extern "C" int n2m_device_count(void) {
@@ -124,6 +179,16 @@ extern "C" n2m_status n2m_context_create(n2m_context **out, int device) {
             n2m_set_error("event creation failed");
             return N2M_ERR_CUDA;
         }
+    if (cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking) != cudaSuccess) {
+        n2m_set_error("stream creation failed");
+        return N2M_ERR_CUDA;
+    }
+    c->stage.copy = c->copy;
+    for (int i = 0; i <= N2M_STAGE_SLABS; i++)
+        if (cudaEventCreateWithFlags(&c->stage.ev[i], cudaEventDisableTiming) != cudaSuccess) {
+            n2m_set_error("event creation failed");
+            return N2M_ERR_CUDA;
+        }
     *out = c;
     return N2M_OK;
 }
@@ -148,6 +213,13 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
         if (c->evs[i]) cudaEventDestroy(c->evs[i]);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    c->hout.discard();
+    if (c->copy) {
+        cudaStreamSynchronize(c->copy);
+        cudaStreamDestroy(c->copy);
+    }
+    for (int i = 0; i <= N2M_STAGE_SLABS; i++)
+        if (c->stage.ev[i]) cudaEventDestroy(c->stage.ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -330,7 +402,8 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     CK(cudaEventRecord(c->evs[0], c->stream));
     if (smooth) {
         CKS(c->stmp.ensure(n * sizeof(float)));
-        CKS(launch_smooth(d_src, vol, c->stmp.as<float>(), nx, ny, nz, iso, dst, c->stream));
+        CKS(launch_smooth(d_src, vol, c->stmp.as<float>(), nx, ny, nz, iso, dst, c->stream,
+                          c->stage.host ? &c->stage : nullptr));
     }
     else CKS(launch_stats(label ? vol : d_src, nx, ny, nz, iso, true, dst, c->stream));
     CK(cudaEventRecord(c->evs[1], c->stream));
@@ -491,6 +564,7 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     CKS(prepare(c, d_src, dim, o, o.verbose, P, rep));
     int nv, nt, ncand;
     CKS(march(c, P, dim, o.cubes, &nv, &nt, &ncand));
+    if (c->want_host) c->hout.start((size_t)std::max(nv, 1) * sizeof(vec3d), (size_t)std::max(nt, 1) * sizeof(vec3i));
     vec3d *pts = c->pts_raw.as<vec3d>();
     int np = nv;
     int welded = 0;
@@ -580,17 +654,35 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
 }
 
 n2m_status to_host_mesh(n2m_context *c, vec3i **t, vec3d **p, int *nt, int *np) {
-    vec3d *hp = (vec3d *)malloc((size_t)c->res_np * sizeof(vec3d));
-    vec3i *ht = (vec3i *)malloc((size_t)std::max(c->res_nt, 1) * sizeof(vec3i));
-    if (!hp || !ht) {
+    const size_t pbytes = (size_t)c->res_np * sizeof(vec3d), tbytes = (size_t)std::max(c->res_nt, 1) * sizeof(vec3i);
+    c->hout.join();
+    vec3d *hp;
+    vec3i *ht;
+    if (c->hout.pts && c->hout.pb >= pbytes && c->hout.tb >= tbytes) {   // pre-faulted (sized for the raw mesh)
+        hp = (vec3d *)c->hout.pts;
+        ht = (vec3i *)c->hout.tris;
+        c->hout.pts = c->hout.tris = nullptr;
+        c->hout.pb = c->hout.tb = 0;
+    } else {
+        c->hout.discard();
+        hp = (vec3d *)malloc(std::max<size_t>(pbytes, 1));
+        ht = (vec3i *)malloc(tbytes);
+        if (!hp || !ht) {
+            free(hp);
+            free(ht);
+            n2m_set_error("host allocation failed");
+            return N2M_ERR_OOM;
+        }
+    }
+    cudaError_t e = cudaMemcpyAsync(hp, c->res_pts, pbytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ht, c->res_tris, (size_t)c->res_nt * sizeof(vec3i), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
         free(hp);
         free(ht);
-        n2m_set_error("host allocation failed");
-        return N2M_ERR_OOM;
+        n2m_set_error("mesh readback: %s", cudaGetErrorString(e));
+        return N2M_ERR_CUDA;
     }
-    CK(cudaMemcpyAsync(hp, c->res_pts, (size_t)c->res_np * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(ht, c->res_tris, (size_t)c->res_nt * sizeof(vec3i), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
     *t = ht;
     *p = hp;
     *nt = c->res_nt;
@@ -637,13 +729,28 @@ extern "C" n2m_status n2m_meshify(n2m_context *c, const float *img, const int di
     if (!c || !opt || !dim || !img || !t || !p || !nt || !np) return N2M_ERR_BAD_ARGS;
     CK(cudaSetDevice(c->device));
     const size_t n = (size_t)dim[0] * dim[1] * dim[2];
-    CKS(upload(c, img, n));
-    CKS(pipeline(c, c->in.as<float>(), dim, *opt, rep));
+    // with pre-smoothing the upload is staged: the x pass of each slab starts as soon as it has arrived
+    const bool staged = opt->pre_smooth && dim[0] >= 5 && dim[1] >= 5 && dim[2] >= 5 && smooth_can_stage(dim[0], dim[1], dim[2]);
+    if (staged) {
+        CKS(c->in.ensure(n * sizeof(float)));
+        c->stage.host = img;
+    } else {
+        CKS(upload(c, img, n));
+    }
+    c->want_host = true;
+    n2m_status s = pipeline(c, c->in.as<float>(), dim, *opt, rep);
+    c->stage.host = nullptr;
+    c->want_host = false;
     c->fwd.post_smooth = opt->post_smooth > 0 ? opt->post_smooth : 0;
-    if (opt->post_smooth > 0)
-        CKS(mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc,
-                           c->scan, c->stream));
-    return to_host_mesh(c, t, p, nt, np);
+    if (s == N2M_OK && opt->post_smooth > 0)
+        s = mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc, c->scan,
+                           c->stream);
+    if (s == N2M_OK) s = to_host_mesh(c, t, p, nt, np);
+    if (s != N2M_OK) {
+        cudaStreamSynchronize(c->copy);   // no staged copy may still read the caller's volume
+        c->hout.discard();
+    }
+    return s;
 }
 
 // Adjoint of the last n2m_meshify_device / n2m_meshify call on ctx with fixed

@@ -67,9 +67,19 @@ struct VolStats {
 
 // ---- kernels' host launchers (stream-ordered, no syncs) ----------------------
 // smooth.cu
-// tmp: one volume of scratch
+// A host volume copied to `in` slab by slab on the `copy` stream while the
+// x pass of the slabs already copied runs (the three-pass path only).
+constexpr int N2M_STAGE_SLABS = 16;
+struct StagedInput {
+    const float *host = nullptr;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev[N2M_STAGE_SLABS + 1] = {};
+};
+// tmp: one volume of scratch; stage: see StagedInput (may be null)
 n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny, int nz, float iso, VolStats *st,
-                         cudaStream_t s);
+                         cudaStream_t s, const StagedInput *stage = nullptr);
+// whether launch_smooth can take a StagedInput for this volume
+bool smooth_can_stage(int nx, int ny, int nz);
 // transposed pre-smooth: g_img = Sx^T Sy^T Sz^T g (tmp: one volume of scratch)
 n2m_status launch_smooth_adjoint(const float *g, float *tmp, float *out, int nx, int ny, int nz, cudaStream_t s);
 n2m_status launch_stats(const float *vol, int nx, int ny, int nz, float iso, bool minmax, VolStats *st,

@@ -138,15 +138,15 @@ struct FixStage {
     }
 };
 
-// x pass: each warp takes whole rows.
-__global__ void __launch_bounds__(256) k_pass_x(Pass P, unsigned nrows) {
+// x pass: each warp takes whole rows (rows row0 .. row1-1 of the volume).
+__global__ void __launch_bounds__(256) k_pass_x(Pass P, unsigned row0, unsigned row1) {
     __shared__ unsigned stage_buf[8][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     FixStage<false> F{stage_buf[w], 0};   // < 32 entries between steps, + 32
     Acc acc;   // unused by the x pass
     const int nx = P.nx;
     const unsigned nwarps = gridDim.x * (blockDim.x / 32);
-    for (unsigned row = blockIdx.x * (blockDim.x / 32) + w; row < nrows; row += nwarps) {
+    for (unsigned row = row0 + blockIdx.x * (blockDim.x / 32) + w; row < row1; row += nwarps) {
         const unsigned r0 = row * (unsigned)nx;
         for (int x0 = 0; x0 < nx; x0 += 32) {
             const int x = x0 + lane;
@@ -254,9 +254,11 @@ int resident_blocks(const void *fn, int threads) {
 constexpr int KRUN = 8, KSEG = 8;
 }  // namespace
 
+bool smooth_can_stage(int nx, int ny, int nz) { return (size_t)nx * ny * nz < ((size_t)1 << 32); }
+
 // nx*ny*nz < 2^32: three passes; larger volumes: the fused CTA-column kernel.
 n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny, int nz, float iso, VolStats *st,
-                         cudaStream_t s) {
+                         cudaStream_t s, const StagedInput *stage) {
     const size_t n = (size_t)nx * ny * nz;
     if (n < ((size_t)1 << 32)) {
         static int gx = 0, ga = 0, gz = 0;
@@ -268,7 +270,24 @@ n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny
         const unsigned nxy = (unsigned)nx * ny;
         const Pass px{in, out, 1u, nx, ny, nxy, iso, st}, py{out, tmp, (unsigned)nx, nx, ny, nxy, iso, st},
             pz{tmp, out, nxy, nx, ny, nxy, iso, st};
-        { k_pass_x<<<gx, 256, 0, s>>>(px, (unsigned)ny * nz); N2M_COUNT(); }
+        if (stage && stage->host) {
+            // the copy stream may only overwrite `in` once earlier work on s is done with it
+            CK(cudaEventRecord(stage->ev[N2M_STAGE_SLABS], s));
+            CK(cudaStreamWaitEvent(stage->copy, stage->ev[N2M_STAGE_SLABS], 0));
+            for (int k = 0; k < N2M_STAGE_SLABS; k++) {
+                const int z0 = (int)((long long)nz * k / N2M_STAGE_SLABS), z1 = (int)((long long)nz * (k + 1) / N2M_STAGE_SLABS);
+                if (z1 <= z0) continue;
+                const size_t off = (size_t)z0 * nxy, bytes = (size_t)(z1 - z0) * nxy * sizeof(float);
+                CK(cudaMemcpyAsync((float *)in + off, stage->host + off, bytes, cudaMemcpyHostToDevice, stage->copy));
+                CK(cudaEventRecord(stage->ev[k], stage->copy));
+                CK(cudaStreamWaitEvent(s, stage->ev[k], 0));
+                const unsigned r0 = (unsigned)z0 * ny, r1 = (unsigned)z1 * ny;
+                const unsigned g = std::min<unsigned>((unsigned)gx, std::max<unsigned>(1u, (r1 - r0 + 7) / 8));
+                { k_pass_x<<<g, 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
+            }
+        } else {
+            { k_pass_x<<<gx, 256, 0, s>>>(px, 0u, (unsigned)ny * nz); N2M_COUNT(); }
+        }
         { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, (unsigned)nz); N2M_COUNT(); }
         { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 1u); N2M_COUNT(); }
         CKL();
