@@ -100,39 +100,47 @@ __device__ __noinline__ unsigned ambiguous_count(const GV &g, int x, int y, int 
 
 // Count pass, part 1: the sign (grid value > 0) of every grid point as one
 // bit, word-aligned like the counts (bit x&31 of signs[(z*NY + y)*WX + x/32]).
-// A warp takes whole rows, SW words at a time with all their loads in flight.
-// Words strictly inside the volume (no darkening, wrap or padding) read the
-// volume directly, the others go through gval.
-constexpr int SW = 8;
+// A warp takes whole rows, SW words at a time with all their loads in
+// flight.  Runs of SW words strictly inside the volume and the grid read the
+// volume directly; border words go through gval, out of line.
+constexpr int SW = 16;
+
+__device__ __noinline__ unsigned word_signs_slow(const GV &g, int x0, int y, int z) {
+    const int x = x0 + (int)(threadIdx.x & 31);
+    return __ballot_sync(0xffffffffu, x < g.NX && gval(g, x, y, z) > 0.f);
+}
 
 __global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nrows, unsigned *signs) {
     const int lane = threadIdx.x & 31;
+    // words xw whose 32 points lie strictly inside the volume in x and inside the grid
+    const int xs0 = max(0, (1 - g.lo0 + 31) / 32);
+    const int xs1 = min((g.dx - 2 - g.lo0 - 31) >= 0 ? (g.dx - 2 - g.lo0 - 31) / 32 : -1, g.NX / 32 - 1);
     for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += (gridDim.x * blockDim.x) >> 5) {
         const int y = (int)(row % (unsigned)g.NY), z = (int)(row / (unsigned)g.NY);
         const int vy = g.lo1 + y, vz = g.lo2 + z;
         const bool rsimple = vy >= 1 && vy <= g.dy - 2 && vz >= 1 && vz <= g.dz - 2;
-        const float *rp = g.vol + ((long long)g.lo0 + (long long)vy * g.dx + (long long)vz * g.dxy);
-        for (unsigned xw0 = 0; xw0 < WX; xw0 += SW) {
+        const float *rp = g.vol + ((long long)g.lo0 + (long long)vy * g.dx + (long long)vz * g.dxy) + lane;
+        unsigned *out = signs + (size_t)row * WX;
+        const int f0 = rsimple ? xs0 : (int)WX, f1 = rsimple ? xs1 + 1 : (int)WX;   // direct words [f0, f1)
+        for (int xw = 0; xw < min(f0, (int)WX); xw++) {
+            const unsigned m = word_signs_slow(g, xw * 32, y, z);
+            if (lane == 0) out[xw] = m;
+        }
+        for (int xw0 = f0; xw0 < f1; xw0 += SW) {
             float raw[SW];
 #pragma unroll
-            for (int k = 0; k < SW; k++) {
-                const int x0 = (int)(xw0 + k) * 32;
-                const bool simple = rsimple && xw0 + k < WX && g.lo0 + x0 >= 1 && g.lo0 + x0 + 31 <= g.dx - 2;
-                raw[k] = simple ? __ldg(rp + x0 + lane) : 0.f;
-            }
+            for (int k = 0; k < SW; k++) raw[k] = xw0 + k < f1 ? __ldg(rp + (xw0 + k) * 32) : 0.f;
             unsigned mine = 0;
 #pragma unroll
             for (int k = 0; k < SW; k++) {
-                if (xw0 + k >= WX) break;   // whole warp
-                const int x0 = (int)(xw0 + k) * 32, x = x0 + lane;
-                const bool simple = rsimple && g.lo0 + x0 >= 1 && g.lo0 + x0 + 31 <= g.dx - 2;
-                bool sg;
-                if (simple) sg = x < g.NX && __fsub_rn(raw[k], g.iso) > -N2M_FLT_EPS;   // clamp maps (-eps, eps) to +eps
-                else sg = x < g.NX && gval(g, x, y, z) > 0.f;
-                const unsigned m = __ballot_sync(0xffffffffu, sg);
+                const unsigned m = __ballot_sync(0xffffffffu, __fsub_rn(raw[k], g.iso) > -N2M_FLT_EPS);   // clamp maps (-eps, eps) to +eps
                 if (lane == k) mine = m;
             }
-            if (lane < SW && xw0 + lane < WX) signs[row * WX + xw0 + lane] = mine;
+            if (lane < SW && xw0 + lane < f1) out[xw0 + lane] = mine;
+        }
+        for (int xw = max(f1, f0); xw < (int)WX; xw++) {
+            const unsigned m = word_signs_slow(g, xw * 32, y, z);
+            if (lane == 0) out[xw] = m;
         }
     }
 }
