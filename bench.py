@@ -36,10 +36,15 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Gvox/s smooth+MC+weld at 512³; atlas meshes/s batched vs loop; fwd+bwd ms @128³"
 WORKLOAD = "ct512: 512^3 f32 CT-like, iso 300, -p 1 -l 0 -b 0 -o 0 -r 1 -s 0 (Lewiner MC33)"
 ISO = 300.0
-# DRAM bytes per launch of the dominant kernel from the committed ncu capture
-# (profiles/ summary of the same workload); None until captured.
-NCU_TRAFFIC = {}
-# algorithmic bytes per stage (per unit): see DESIGN.md "Roofline"
+# DRAM bytes (read + write) per step of each stage on this workload, from one ncu capture of
+# `bench.py --profile 512` (profiles/meshify_ct512_kernels.md): smoothing = its three pass
+# kernels, count = k_signs + k_words + k_active + scans, emit = k_emit.
+NCU_TRAFFIC = {"smooth": 3509e6, "count": 967e6, "emit": 415e6, "degenerate": 346e6}
+# what bounds each stage (measured in the same profiles)
+STAGE_BOUND = {"smooth": "FP32 instruction issue: exact double-rounding proof per tap (~72-80 % issue active); "
+                         "three streaming passes at ~8.1 B/voxel each"}
+# algorithmic bytes per stage (per unit): smooth 8 B/voxel, count 4 B/grid point,
+# emit 24 B/vertex + 12 B/triangle, degenerate 24 B/triangle
 STAGE_NAMES = ("smooth", "cluster", "count", "emit", "weld", "degenerate", "hc")
 
 
@@ -230,6 +235,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--profile", type=int, default=0, metavar="N",
+                    help="profiling driver: two meshify calls on the CT-like workload at N^3 (same generator, "
+                         "structure count scaled by volume), stage times printed; no bench line")
     a = ap.parse_args()
     warmup = max(a.warmup, 3)
     import numpy as np
@@ -254,6 +262,17 @@ def main():
 
     import torch
     import nii2mesh_gb300 as n2m
+    if a.profile:
+        n = a.profile
+        pv = synth.ct512(n=n, count=max(1, int(round(300 * (n / 512) ** 3))))
+        d = torch.from_numpy(pv).cuda()
+        ctx = n2m.Context(0)
+        for _ in range(2):
+            _, _, nt, nv, rep = ctx.meshify_device(d.data_ptr(), (n, n, n), ISO, n2m.MC33, True, False, False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": n, "triangles": nt, "vertices": nv,
+                          "stage_ms": dict(zip(STAGE_NAMES, [round(x, 4) for x in rep["ms_stage"][:7]]))}))
+        return
     rank, world, dist = dist_setup(a.gpus)
     dev = torch.cuda.current_device()
     vol = synth.ct512()
@@ -307,7 +326,9 @@ def main():
         ach = algo[name] / (stage_ms[top] * 1e-3) / 1e9
         roof = {"bound": "hbm", "kernel_stage": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                "algorithmic_bytes": algo[name], "traffic": NCU_TRAFFIC.get(name)}
+                "algorithmic_bytes": algo[name], "traffic": NCU_TRAFFIC.get(name),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels, one step",
+                "limited_by": STAGE_BOUND.get(name)}
 
     # e2e through the C ABI with host buffers (pinned input, mesh copied back)
     pinned = torch.from_numpy(vol).pin_memory().numpy()
