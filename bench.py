@@ -229,6 +229,48 @@ def atlas_metric(n2m, torch, reps=3):
     return out
 
 
+def threshold_metric(n2m, torch, reps=5):
+    """setThreshold (Otsu on the robust range) of the brain-sized u8 volume
+    (182x218x182, nii2mesh's default isolevel; medium = mode 2, dark = mode 1
+    with the three-level search): device-resident, host volume through the C
+    ABI, and the CPU path (one core)."""
+    from nii2mesh_gb300 import synth
+    vol = np.ascontiguousarray(synth.brain().astype(np.float32))
+    d = torch.from_numpy(vol).cuda()
+    ctx = n2m.Context(torch.cuda.current_device())
+    out = {"workload": "brain182: 182x218x182 u8-valued f32 (7.2 M voxels)"}
+    for mode in (2, 1):
+        ctx.set_threshold_device(d.data_ptr(), vol.size, mode)
+        ts, th = [], []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            iso = ctx.set_threshold_device(d.data_ptr(), vol.size, mode)
+            ts.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            ctx.set_threshold(vol, mode)
+            th.append(time.perf_counter() - t0)
+        out[f"mode{mode}_device_ms"] = round(1e3 * statistics.median(ts), 3)
+        out[f"mode{mode}_e2e_ms"] = round(1e3 * statistics.median(th), 3)
+        out[f"mode{mode}_iso"] = iso
+        try:
+            from oracle.oracle import Reference, reference_available
+            cpu = Reference(False) if reference_available() else None
+            kind = "reference"
+        except Exception:
+            cpu = None
+        if cpu is None:
+            from oracle.oracle import Oracle
+            cpu, kind = Oracle(), "port"
+        t0 = time.perf_counter()
+        ci = cpu.set_threshold(vol, mode)
+        out[f"mode{mode}_cpu_ms"] = round(1e3 * (time.perf_counter() - t0), 3)
+        out[f"mode{mode}_matches_cpu"] = bool(ci == iso)
+        out["cpu_kind"] = kind
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -357,6 +399,7 @@ def main():
                "sample": f"one full 512^3 meshify ({times[0]:.1f} s)"}
     adj = adjoint_metric(n2m, torch) if world == 1 else None
     atl = atlas_metric(n2m, torch) if world == 1 else None
+    thr = threshold_metric(n2m, torch) if world == 1 else None
     line = {"metric": METRIC, "value": round(value, 4), "unit": "Gvox/s", "n_gpus": world, "steps": a.steps,
             "warmup": warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
@@ -364,7 +407,7 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU", "triangles": nt, "vertices": nv},
             "stage_ms": {n: round(v, 4) for n, v in zip(STAGE_NAMES, stage_ms)},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck,
-            "adjoint": adj, "atlas": atl}
+            "adjoint": adj, "atlas": atl, "threshold": thr}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

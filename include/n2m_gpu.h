@@ -107,6 +107,10 @@ int marchingCubes(float *img, short dim[3], int lo[3], int hi[3], int originalMC
 int bwlabel(float *img, int conn, size_t dim[3], bool onlyLargest, bool fillBubbles);
 /* replaces apply_sform() (src/meshify.h:10). */
 void apply_sform(vec3i *t, vec3d *p, int nt, int np, float srow_x[4], float srow_y[4], float srow_z[4]);
+/* replaces setThreshold() (src/isolevel.h:7, body src/isolevel.c:245-277):
+ * Otsu isolevel on the robust (2nd-98th percentile) range; mode 1 dark,
+ * 2 medium, 3 bright.  img is a host array of nvox floats. */
+float setThreshold(float *img, int nvox, int darkMediumBright123);
 /* Mirrors the USE_CLASSIC_CUBES build flag for the drop-in marchingCubes()
  * and meshify(): nonzero selects Bourke's oldcubes. Returns the old value. */
 int n2m_set_oldcubes(int enable);
@@ -159,6 +163,12 @@ n2m_status n2m_atlas_device(n2m_context *ctx, const int16_t *d_labels, const int
 /* Host volume in; everything malloc'd (free() each array). */
 n2m_status n2m_atlas(n2m_context *ctx, const int16_t *labels, const int dim[3], const n2m_options *opt, int mode,
                      int *nmesh, n2m_atlas_mesh **meshes, vec3d **pts, vec3i **tris, int64_t *npts, int64_t *ntris);
+
+/* Otsu isolevel of setThreshold() (src/isolevel.c:245-277) with an explicit
+ * status: img is a host array (n2m_set_threshold) or a device array
+ * (n2m_set_threshold_device) of nvox floats; the value goes to *iso. */
+n2m_status n2m_set_threshold(n2m_context *ctx, const float *img, int64_t nvox, int mode, float *iso);
+n2m_status n2m_set_threshold_device(n2m_context *ctx, const float *d_img, int64_t nvox, int mode, float *iso);
 
 /* HC smoothing of device-resident meshes (d_verts updated in place). */
 n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,

@@ -23,7 +23,8 @@ from ._lib import AtlasMesh, N2MError, Options, Report, vec3d, vec3i
 MC33, CLASSIC_TABLE, OLDCUBES = 0, 1, 2
 ATLAS_BATCHED, ATLAS_LOOP = 0, 1
 
-__all__ = ["Context", "meshify", "laplacian_smoothHC", "marching_cubes", "bwlabel", "apply_sform", "N2MError",
+__all__ = ["Context", "meshify", "laplacian_smoothHC", "marching_cubes", "bwlabel", "apply_sform", "set_threshold",
+           "N2MError",
            "MC33", "CLASSIC_TABLE", "OLDCUBES", "lib"]
 
 
@@ -110,6 +111,20 @@ class Context:
                                               C.byref(nt), C.byref(np_), C.byref(rep)), "n2m_meshify_device")
         return tp.value, pp.value, nt.value, np_.value, rep.as_dict()
 
+
+    def set_threshold(self, img, mode=2):
+        """Otsu isolevel of a host volume (n2m_set_threshold); mode 1 dark, 2 medium, 3 bright."""
+        a = np.ascontiguousarray(img, dtype=np.float32)
+        out = C.c_float()
+        _lib.check(self._L.n2m_set_threshold(self.h, a.ctypes.data, a.size, int(mode), C.byref(out)), "n2m_set_threshold")
+        return out.value
+
+    def set_threshold_device(self, d_img_ptr, nvox, mode=2):
+        """Otsu isolevel of a device volume (n2m_set_threshold_device)."""
+        out = C.c_float()
+        _lib.check(self._L.n2m_set_threshold_device(self.h, C.c_void_p(d_img_ptr), int(nvox), int(mode), C.byref(out)),
+                   "n2m_set_threshold_device")
+        return out.value
 
     def atlas(self, labels, cubes=MC33, pre_smooth=True, only_largest=True, fill_bubbles=True, post_smooth=5,
               mode=ATLAS_BATCHED):
@@ -218,3 +233,11 @@ def apply_sform(pts, tris, srow_x, srow_y, srow_z):
     f = lambda r: (C.c_float * 4)(*r)
     L.apply_sform(t.ctypes.data, p.ctypes.data, len(t), len(p), f(srow_x), f(srow_y), f(srow_z))
     return t, p
+
+
+def set_threshold(img, mode=2):
+    """setThreshold() (src/isolevel.h:7): Otsu isolevel on the robust range;
+    mode 1 dark, 2 medium, 3 bright."""
+    L = _lib.load()
+    a = np.ascontiguousarray(img, dtype=np.float32).ravel()
+    return float(L.setThreshold(a.ctypes.data, a.size, int(mode)))

@@ -125,6 +125,7 @@ struct n2m_context {
     LabelWork lab;
     DegWork deg;
     HcWork hc;
+    ThresholdWork th;
     void *pinned = nullptr;   // small readbacks
     DevBuf gA, gB, gs, gtmp;   // adjoint scratch
     AtlasWork aw;
@@ -205,7 +206,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->mc.signs, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
-                      &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb};
+                      &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->th.buf, &c->th.table};
     for (DevBuf *b : bufs) b->release();
     if (c->aw.exec) cudaGraphExecDestroy((cudaGraphExec_t)c->aw.exec);
     if (c->pinned) cudaFreeHost(c->pinned);
@@ -995,6 +996,28 @@ extern "C" void laplacian_smoothHC(vec3d *verts, vec3i *tris, int nvert, int ntr
         }
     }
     if (s != N2M_OK) report_failure("laplacian_smoothHC", s);
+}
+
+extern "C" n2m_status n2m_set_threshold_device(n2m_context *c, const float *d_img, int64_t nvox, int mode, float *iso) {
+    if (!c || !iso || (nvox > 0 && !d_img)) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    return isolevel_otsu(d_img, nvox, mode, c->th, c->stream, iso);
+}
+
+extern "C" n2m_status n2m_set_threshold(n2m_context *c, const float *img, int64_t nvox, int mode, float *iso) {
+    if (!c || !iso || (nvox > 0 && !img)) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    if (nvox > 0) CKS(upload(c, img, (size_t)nvox));
+    return isolevel_otsu(c->in.as<float>(), nvox, mode, c->th, c->stream, iso);
+}
+
+extern "C" float setThreshold(float *img, int nvox, int darkMediumBright123) {
+    n2m_context *c;
+    float iso = 1.0f;
+    n2m_status s = default_ctx(&c);
+    if (s == N2M_OK) s = n2m_set_threshold(c, img, nvox, darkMediumBright123, &iso);
+    if (s != N2M_OK) report_failure("setThreshold", s);
+    return iso;
 }
 
 extern "C" void apply_sform(vec3i *t, vec3d *p, int nt, int np, float srow_x[4], float srow_y[4], float srow_z[4]) {

@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <string>
+#include <vector>
 
 #include "../../include/n2m_gpu.h"
 
@@ -44,6 +45,11 @@ struct DevBuf {
 // ---- ordered-int encoding of floats for atomicMin/atomicMax ------------------
 __device__ __forceinline__ int f2ord(float f) {
     int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+inline int f2ord_host(float f) {
+    int i;
+    memcpy(&i, &f, 4);
     return i >= 0 ? i : i ^ 0x7fffffff;
 }
 __host__ __device__ __forceinline__ float ord2f(int i) {
@@ -102,6 +108,14 @@ n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn
 // bwlabel() semantics on a float volume (nonzero = foreground); *d_nl gets the label count
 n2m_status run_bwlabel(float *vol, int nx, int ny, int nz, int conn, bool only_largest, bool fill_bubbles,
                        LabelWork &w, ScanWork &sw, int *d_nl, cudaStream_t s);
+
+// isolevel.cu: setThreshold (Otsu on the robust range) of a device volume
+struct ThresholdWork {
+    DevBuf buf, table;
+    std::vector<double> P;
+};
+n2m_status isolevel_otsu(const float *d_img, long long nvox, int mode123, ThresholdWork &w, cudaStream_t s,
+                         float *result);
 
 // mc.cu
 struct McGrid {

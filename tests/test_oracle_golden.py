@@ -65,6 +65,19 @@ def test_thresholds(oracle):
         assert oracle.set_threshold(INPUTS[name], int(mode)) == pytest.approx(val, abs=0, rel=0)
 
 
+TH = json.loads((GOLD / "threshold.json").read_text())
+TH_INPUTS = dict(np.load(GOLD / "threshold_inputs.npz"))
+
+
+@pytest.mark.parametrize("case", sorted(TH))
+def test_threshold_edge_cases(oracle, case):
+    """setThreshold edge cases (constant, all-NaN, < 100 voxels, NaNs, zero
+    background, ties, outliers, heavy tails) — reference values from
+    tests/golden/make_threshold_golden.py, modes 1-3, bit for bit."""
+    for mode, val in TH[case].items():
+        assert oracle.set_threshold(TH_INPUTS[case], int(mode)) == val
+
+
 def test_bwlabel(oracle):
     for e in G["bwlabel"]:
         lab, n = oracle.bwlabel(INPUTS["blobs40"], e["conn"], e["only_largest"], e["fill_bubbles"])
