@@ -229,6 +229,40 @@ def atlas_metric(n2m, torch, reps=3):
     return out
 
 
+def brain_metric(n2m, torch, reps=5):
+    """The brain-sized uint8 workload (182x218x182, Otsu medium isolevel,
+    -p 1 -l 1 -b 1 -s 20, Lewiner) end to end from host memory: raw uint8
+    voxels through n2m_meshify_typed (cast on the device) vs the float32
+    volume through n2m_meshify, and the CPU path on one core."""
+    from nii2mesh_gb300 import synth
+    raw = np.ascontiguousarray(synth.brain())
+    vol = raw.astype(np.float32)
+    ctx = n2m.Context(torch.cuda.current_device())
+    iso = ctx.set_threshold(vol, 2)
+    out = {"workload": "brain182: 182x218x182 uint8, Otsu medium iso, -p 1 -l 1 -b 1 -s 20, Lewiner", "iso": iso}
+    for name, fn in (("u8", lambda: ctx.meshify_typed(raw, 1.0, 0.0, iso, n2m.MC33, True, True, True, 20)),
+                     ("f32", lambda: ctx.meshify(vol, iso, n2m.MC33, True, True, True, 20))):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            t, p, rep = fn()
+            ts.append(time.perf_counter() - t0)
+            del t, p
+        out[f"e2e_{name}_ms"] = round(1e3 * statistics.median(ts), 3)
+        out[f"h2d_{name}_bytes"] = int(raw.size * (1 if name == "u8" else 4))
+        out["triangles"] = rep["ntri"]
+    ctx.close()
+    from oracle.oracle import Oracle
+    o = Oracle()
+    t0 = time.perf_counter()
+    m = o.meshify(vol, iso, 0, True, True, True)
+    o.laplacian_smoothHC(m[1], m[0], 0.1, 0.5, 20, True)
+    out["cpu_ms"] = round(1e3 * (time.perf_counter() - t0), 1)
+    out["cpu_kind"] = "port"
+    return out
+
+
 def threshold_metric(n2m, torch, reps=5):
     """setThreshold (Otsu on the robust range) of the brain-sized u8 volume
     (182x218x182, nii2mesh's default isolevel; medium = mode 2, dark = mode 1
@@ -400,6 +434,7 @@ def main():
     adj = adjoint_metric(n2m, torch) if world == 1 else None
     atl = atlas_metric(n2m, torch) if world == 1 else None
     thr = threshold_metric(n2m, torch) if world == 1 else None
+    brn = brain_metric(n2m, torch) if world == 1 else None
     line = {"metric": METRIC, "value": round(value, 4), "unit": "Gvox/s", "n_gpus": world, "steps": a.steps,
             "warmup": warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
@@ -407,7 +442,7 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU", "triangles": nt, "vertices": nv},
             "stage_ms": {n: round(v, 4) for n, v in zip(STAGE_NAMES, stage_ms)},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck,
-            "adjoint": adj, "atlas": atl, "threshold": thr}
+            "adjoint": adj, "atlas": atl, "threshold": thr, "brain": brn}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -164,6 +164,18 @@ n2m_status n2m_atlas_device(n2m_context *ctx, const int16_t *d_labels, const int
 n2m_status n2m_atlas(n2m_context *ctx, const int16_t *labels, const int dim[3], const n2m_options *opt, int mode,
                      int *nmesh, n2m_atlas_mesh **meshes, vec3d **pts, vec3i **tris, int64_t *npts, int64_t *ntris);
 
+/* NIfTI voxel types that load_nii() casts to float (src/nii2mesh.c:114-175). */
+enum { N2M_DT_UINT8 = 2, N2M_DT_INT16 = 4, N2M_DT_FLOAT32 = 16, N2M_DT_UINT16 = 512 };
+/* Device cast of raw NIfTI voxels, out[i] = raw[i] * scl_slope + scl_inter
+ * (scl_slope 0 means 1), as load_nii() does on the host (src/nii2mesh.c:160-175). */
+n2m_status n2m_cast_voxels_device(n2m_context *ctx, const void *d_raw, int datatype, float scl_slope, float scl_inter,
+                                  int64_t nvox, float *d_out);
+/* n2m_meshify on raw NIfTI voxels in host memory: the voxels are sent as
+ * they are (1, 2 or 4 bytes each) and cast on the device. */
+n2m_status n2m_meshify_typed(n2m_context *ctx, const void *img, int datatype, float scl_slope, float scl_inter,
+                             const int dim[3], const n2m_options *opt, vec3i **t, vec3d **p, int *nt, int *np,
+                             n2m_report *rep);
+
 /* Otsu isolevel of setThreshold() (src/isolevel.c:245-277) with an explicit
  * status: img is a host array (n2m_set_threshold) or a device array
  * (n2m_set_threshold_device) of nvox floats; the value goes to *iso. */

@@ -21,6 +21,8 @@ from . import _lib
 from ._lib import AtlasMesh, N2MError, Options, Report, vec3d, vec3i
 
 MC33, CLASSIC_TABLE, OLDCUBES = 0, 1, 2
+# NIfTI datatype codes of the voxel types load_nii reads (src/nii2mesh.c:114-117)
+_NIFTI_DT = {np.dtype(np.uint8): 2, np.dtype(np.int16): 4, np.dtype(np.float32): 16, np.dtype(np.uint16): 512}
 ATLAS_BATCHED, ATLAS_LOOP = 0, 1
 
 __all__ = ["Context", "meshify", "laplacian_smoothHC", "marching_cubes", "bwlabel", "apply_sform", "set_threshold",
@@ -111,6 +113,30 @@ class Context:
                                               C.byref(nt), C.byref(np_), C.byref(rep)), "n2m_meshify_device")
         return tp.value, pp.value, nt.value, np_.value, rep.as_dict()
 
+
+    def meshify_typed(self, raw, scl_slope, scl_inter, iso, cubes=MC33, pre_smooth=True, only_largest=True,
+                      fill_bubbles=False, post_smooth=0, verbose=False):
+        """n2m_meshify_typed: raw NIfTI voxels (uint8, int16, uint16 or float32
+        numpy array shaped (nz, ny, nx)) sent as they are and cast on the device
+        as load_nii does (src/nii2mesh.c:160-175)."""
+        a = np.ascontiguousarray(raw)
+        if a.ndim != 3 or a.dtype not in _NIFTI_DT:
+            raise ValueError("raw must be a 3-D uint8/int16/uint16/float32 array")
+        nz, ny, nx = a.shape
+        o = self._opts(iso, cubes, pre_smooth, only_largest, fill_bubbles, post_smooth, verbose)
+        tp, pp, nt, np_ = C.c_void_p(), C.c_void_p(), C.c_int(), C.c_int()
+        rep = Report()
+        _lib.check(self._L.n2m_meshify_typed(self.h, a.ctypes.data, _NIFTI_DT[a.dtype], float(scl_slope), float(scl_inter),
+                                             (C.c_int * 3)(nx, ny, nz), C.byref(o), C.byref(tp), C.byref(pp),
+                                             C.byref(nt), C.byref(np_), C.byref(rep)), "n2m_meshify_typed")
+        t, p = _take(self._L, tp, pp, nt.value, np_.value)
+        return t, p, rep.as_dict()
+
+    def cast_voxels_device(self, d_raw_ptr, dtype, scl_slope, scl_inter, nvox, d_out_ptr):
+        """n2m_cast_voxels_device: device raw voxels -> device float32."""
+        _lib.check(self._L.n2m_cast_voxels_device(self.h, C.c_void_p(d_raw_ptr), _NIFTI_DT[np.dtype(dtype)],
+                                                  float(scl_slope), float(scl_inter), int(nvox), C.c_void_p(d_out_ptr)),
+                   "n2m_cast_voxels_device")
 
     def set_threshold(self, img, mode=2):
         """Otsu isolevel of a host volume (n2m_set_threshold); mode 1 dark, 2 medium, 3 bright."""

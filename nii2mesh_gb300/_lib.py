@@ -19,7 +19,8 @@ SYMBOLS = ["n2m_context_create", "n2m_context_destroy", "n2m_context_stream", "n
            "n2m_status_string", "n2m_device_count", "meshify", "laplacian_smoothHC", "marchingCubes", "bwlabel",
            "apply_sform", "n2m_set_oldcubes", "n2m_meshify", "n2m_meshify_device", "n2m_smooth_hc_device",
            "n2m_kernel_launches", "n2m_meshify_backward", "n2m_smooth_hc_noalloc", "n2m_atlas", "n2m_atlas_device",
-           "setThreshold", "n2m_set_threshold", "n2m_set_threshold_device"]
+           "setThreshold", "n2m_set_threshold", "n2m_set_threshold_device", "n2m_cast_voxels_device",
+           "n2m_meshify_typed"]
 
 
 class vec3d(C.Structure):
@@ -87,6 +88,9 @@ def load(path=None):
     L.setThreshold.restype = C.c_float
     L.n2m_set_threshold.argtypes = [vp, vp, C.c_int64, C.c_int, C.POINTER(C.c_float)]
     L.n2m_set_threshold_device.argtypes = [vp, vp, C.c_int64, C.c_int, C.POINTER(C.c_float)]
+    L.n2m_cast_voxels_device.argtypes = [vp, vp, C.c_int, C.c_float, C.c_float, C.c_int64, vp]
+    L.n2m_meshify_typed.argtypes = [vp, vp, C.c_int, C.c_float, C.c_float, ip, C.POINTER(Options), C.POINTER(vp),
+                                    C.POINTER(vp), ip, ip, C.POINTER(Report)]
     L.n2m_set_oldcubes.argtypes = [C.c_int]
     L.n2m_meshify.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip, C.POINTER(Report)]
     L.n2m_meshify_device.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip,

@@ -119,7 +119,7 @@ struct n2m_context {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evs[8] = {};   // stage boundaries of the last pipeline run
-    DevBuf in, vol, stmp, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath, hmesh;
+    DevBuf in, raw, vol, stmp, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath, hmesh;
     McWork mc;
     ScanWork scan;
     LabelWork lab;
@@ -201,7 +201,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
     DevBuf *bufs[] = {&c->aw.cnt, &c->aw.bb, &c->aw.boxes, &c->aw.queue, &c->aw.arena, &c->aw.mask, &c->aw.keep,
                       &c->aw.lab, &c->aw.edge, &c->aw.ucnt, &c->aw.words, &c->aw.counts, &c->aw.active, &c->aw.tot,
                       &c->aw.pts, &c->aw.pts2, &c->aw.tris, &c->aw.tris2, &c->aw.cand, &c->aw.gath, &c->aw.weld,
-                      &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->vol, &c->stmp, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
+                      &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->raw, &c->vol, &c->stmp, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
                       &c->tris_raw, &c->pts, &c->tris, &c->ntf, &c->weld, &c->gath, &c->hmesh,
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->mc.signs, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
@@ -725,6 +725,29 @@ extern "C" n2m_status n2m_meshify_device(n2m_context *c, const float *d_img, con
     return N2M_OK;
 }
 
+namespace {
+// pipeline on c->in (filled or being filled by a staged upload), HC, and the
+// mesh into pre-faulted malloc memory; on failure no copy may still read the
+// caller's volume and no output buffer is kept
+n2m_status meshify_host_tail(n2m_context *c, const int dim[3], const n2m_options *opt, vec3i **t, vec3d **p, int *nt,
+                             int *np, n2m_report *rep) {
+    c->want_host = true;
+    n2m_status s = pipeline(c, c->in.as<float>(), dim, *opt, rep);
+    c->stage.host = nullptr;
+    c->want_host = false;
+    c->fwd.post_smooth = opt->post_smooth > 0 ? opt->post_smooth : 0;
+    if (s == N2M_OK && opt->post_smooth > 0)
+        s = mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc, c->scan,
+                           c->stream);
+    if (s == N2M_OK) s = to_host_mesh(c, t, p, nt, np);
+    if (s != N2M_OK) {
+        cudaStreamSynchronize(c->copy);
+        c->hout.discard();
+    }
+    return s;
+}
+}  // namespace
+
 extern "C" n2m_status n2m_meshify(n2m_context *c, const float *img, const int dim[3], const n2m_options *opt,
                                   vec3i **t, vec3d **p, int *nt, int *np, n2m_report *rep) {
     if (!c || !opt || !dim || !img || !t || !p || !nt || !np) return N2M_ERR_BAD_ARGS;
@@ -738,26 +761,59 @@ extern "C" n2m_status n2m_meshify(n2m_context *c, const float *img, const int di
     } else {
         CKS(upload(c, img, n));
     }
-    c->want_host = true;
-    n2m_status s = pipeline(c, c->in.as<float>(), dim, *opt, rep);
-    c->stage.host = nullptr;
-    c->want_host = false;
-    c->fwd.post_smooth = opt->post_smooth > 0 ? opt->post_smooth : 0;
-    if (s == N2M_OK && opt->post_smooth > 0)
-        s = mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc, c->scan,
-                           c->stream);
-    if (s == N2M_OK) s = to_host_mesh(c, t, p, nt, np);
-    if (s != N2M_OK) {
-        cudaStreamSynchronize(c->copy);   // no staged copy may still read the caller's volume
-        c->hout.discard();
-    }
-    return s;
+    return meshify_host_tail(c, dim, opt, t, p, nt, np, rep);
 }
 
-// Adjoint of the last n2m_meshify_device / n2m_meshify call on ctx with fixed
-// topology: dL/d(final vertex) -> dL/d(input voxel), through the HC
-// iterations, the weld, the marching-cubes edge interpolation and c-vertex
-// means, and the transposed pre-smooth stencil.
+extern "C" n2m_status n2m_cast_voxels_device(n2m_context *c, const void *d_raw, int datatype, float scl_slope,
+                                             float scl_inter, int64_t nvox, float *d_out) {
+    if (!c || (nvox > 0 && (!d_raw || !d_out))) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    CKS(launch_cast(d_raw, datatype, scl_slope, scl_inter, nvox, d_out, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return N2M_OK;
+}
+
+extern "C" n2m_status n2m_meshify_typed(n2m_context *c, const void *img, int datatype, float scl_slope, float scl_inter,
+                                        const int dim[3], const n2m_options *opt, vec3i **t, vec3d **p, int *nt,
+                                        int *np, n2m_report *rep) {
+    if (!c || !opt || !dim || !img || !t || !p || !nt || !np) return N2M_ERR_BAD_ARGS;
+    const int bpp = nifti_bytes_per_voxel(datatype);
+    if (!bpp) {
+        n2m_set_error("unsupported NIfTI datatype %d (uint8 2, int16 4, float32 16, uint16 512)", datatype);
+        return N2M_ERR_BAD_ARGS;
+    }
+    if (dim[0] <= 0 || dim[1] <= 0 || dim[2] <= 0) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    c->hout.discard();
+    const size_t nxy = (size_t)dim[0] * dim[1], n = nxy * dim[2];
+    CKS(c->raw.ensure(n * bpp));
+    CKS(c->in.ensure(n * sizeof(float)));
+    // raw slabs on the copy stream; each is cast on the main stream as soon as it has arrived
+    CK(cudaEventRecord(c->stage.ev[N2M_STAGE_SLABS], c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->stage.ev[N2M_STAGE_SLABS], 0));
+    n2m_status s = N2M_OK;
+    for (int k = 0; k < N2M_STAGE_SLABS && s == N2M_OK; k++) {
+        const size_t z0 = (size_t)dim[2] * k / N2M_STAGE_SLABS, z1 = (size_t)dim[2] * (k + 1) / N2M_STAGE_SLABS;
+        if (z1 <= z0) continue;
+        const size_t off = z0 * nxy, cnt = (z1 - z0) * nxy;
+        if (cudaMemcpyAsync((char *)c->raw.p + off * bpp, (const char *)img + off * bpp, cnt * bpp, cudaMemcpyHostToDevice,
+                            c->copy) != cudaSuccess ||
+            cudaEventRecord(c->stage.ev[k], c->copy) != cudaSuccess ||
+            cudaStreamWaitEvent(c->stream, c->stage.ev[k], 0) != cudaSuccess) {
+            n2m_set_error("staged upload: %s", cudaGetErrorString(cudaGetLastError()));
+            s = N2M_ERR_CUDA;
+            break;
+        }
+        s = launch_cast((const char *)c->raw.p + off * bpp, datatype, scl_slope, scl_inter, (long long)cnt,
+                        c->in.as<float>() + off, c->stream);
+    }
+    if (s != N2M_OK) {
+        cudaStreamSynchronize(c->copy);
+        return s;
+    }
+    return meshify_host_tail(c, dim, opt, t, p, nt, np, rep);
+}
+
 extern "C" n2m_status n2m_meshify_backward(n2m_context *c, const float *d_grad_pts, float *d_grad_img) {
     if (!c || !d_grad_pts || !d_grad_img) return N2M_ERR_BAD_ARGS;
     if (!c->fwd.valid) {

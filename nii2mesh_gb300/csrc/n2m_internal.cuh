@@ -109,6 +109,11 @@ n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn
 n2m_status run_bwlabel(float *vol, int nx, int ny, int nz, int conn, bool only_largest, bool fill_bubbles,
                        LabelWork &w, ScanWork &sw, int *d_nl, cudaStream_t s);
 
+// decode.cu: NIfTI voxel cast (bytes per voxel 0 = unsupported datatype)
+int nifti_bytes_per_voxel(int datatype);
+n2m_status launch_cast(const void *d_raw, int datatype, float slope, float inter, long long n, float *d_out,
+                       cudaStream_t s);
+
 // isolevel.cu: setThreshold (Otsu on the robust range) of a device volume
 struct ThresholdWork {
     DevBuf buf, table;

@@ -5,6 +5,8 @@
 #   libn2m_ref_lewiner.so : meshify + Lewiner MarchingCubes.c   (`make lewiner`)
 #   libn2m_ref_classic.so : meshify + oldcubes.c                (`make` default)
 #   mctest                : MarchingCubes.c -DMC_SELF_TEST       (self-test)
+#   libn2m_ref_cli.so     : the nii2mesh program with its main() renamed, for
+#                           load_nii (NIfTI voxel cast fixtures)
 # -ffp-contract=off and -fsigned-char make an aarch64 build produce the same
 # bits as the x86-64 one.  Usage: oracle/build_ref.sh [reference-src-dir]
 set -e
@@ -22,4 +24,6 @@ fi
 cc $CF -shared -o "$OUT/libn2m_ref_lewiner.so" $COMMON "$SRC/MarchingCubes.c" $ZL -lm
 cc $CF -shared -DUSE_CLASSIC_CUBES -o "$OUT/libn2m_ref_classic.so" $COMMON "$SRC/oldcubes.c" $ZL -lm
 cc -O2 -ffp-contract=off -fsigned-char -w -DMC_SELF_TEST -o "$OUT/mctest" "$SRC/MarchingCubes.c" -lm
+cc $CF -shared -DHAVE_FORMATS -Dmain=n2m_ref_cli_main -o "$OUT/libn2m_ref_cli.so" $COMMON "$SRC/MarchingCubes.c" \
+   "$SRC/nii2mesh.c" "$SRC/base64.c" $ZL -lm
 echo "built $OUT"

@@ -258,6 +258,18 @@ class Reference:
         return float(self.lib.setThreshold(a, a.size, mode))
 
 
+# NIfTI datatypes load_nii reads (src/nii2mesh.c:114-117)
+NIFTI_DT = {np.dtype(np.uint8): 2, np.dtype(np.int16): 4, np.dtype(np.float32): 16, np.dtype(np.uint16): 512}
+
+
+def cast_voxels(raw, scl_slope, scl_inter):
+    """load_nii's voxel cast (src/nii2mesh.c:122, :160-175) in float32 numpy
+    arithmetic: (voxel * scl_slope) + scl_inter, multiply and add each rounded;
+    a zero slope means 1."""
+    slope = np.float32(scl_slope) if scl_slope != 0 else np.float32(1.0)
+    return (np.asarray(raw).astype(np.float32) * slope) + np.float32(scl_inter)
+
+
 def reference_available(classic=False):
     return (REF_DIR / ("libn2m_ref_classic.so" if classic else "libn2m_ref_lewiner.so")).exists()
 

@@ -78,6 +78,16 @@ def test_threshold_edge_cases(oracle, case):
         assert oracle.set_threshold(TH_INPUTS[case], int(mode)) == val
 
 
+def test_nifti_cast():
+    """the oracle's voxel cast equals the reference's load_nii output
+    (tests/golden/make_nifti_golden.py) bit for bit on all four datatypes"""
+    from oracle.oracle import cast_voxels
+    g = np.load(GOLD / "nifti.npz")
+    for k in range(sum(1 for n in g.files if n.startswith("raw"))):
+        meta = g[f"meta{k}"]
+        assert np.array_equal(cast_voxels(g[f"raw{k}"], meta[1], meta[2]).view(np.uint32), g[f"out{k}"].view(np.uint32))
+
+
 def test_bwlabel(oracle):
     for e in G["bwlabel"]:
         lab, n = oracle.bwlabel(INPUTS["blobs40"], e["conn"], e["only_largest"], e["fill_bubbles"])
