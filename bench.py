@@ -314,6 +314,8 @@ def main():
     ap.add_argument("--profile", type=int, default=0, metavar="N",
                     help="profiling driver: two meshify calls on the CT-like workload at N^3 (same generator, "
                          "structure count scaled by volume), stage times printed; no bench line")
+    ap.add_argument("--profile-atlas", action="store_true",
+                    help="profiling driver: two batched atlas calls on the 256^3 label workload; no bench line")
     a = ap.parse_args()
     warmup = max(a.warmup, 3)
     import numpy as np
@@ -338,6 +340,16 @@ def main():
 
     import torch
     import nii2mesh_gb300 as n2m
+    if a.profile_atlas:
+        lab = synth.atlas256()
+        d = torch.from_numpy(lab).cuda()
+        ctx = n2m.Context(0)
+        for _ in range(2):
+            nm, ok, nv, nt, rep = ctx.atlas_device(d.data_ptr(), (256, 256, 256), mode=n2m.ATLAS_BATCHED)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_atlas": 256, "meshes": ok, "vertices": nv, "triangles": nt,
+                          "stage_ms": [round(x, 4) for x in rep["ms_stage"][:5]]}))
+        return
     if a.profile:
         n = a.profile
         pv = synth.ct512(n=n, count=max(1, int(round(300 * (n / 512) ** 3))))

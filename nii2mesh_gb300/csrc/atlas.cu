@@ -236,20 +236,44 @@ __global__ void k_a_mask(const ABox *boxes, int nb, unsigned nch, unsigned *q, u
     for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) { m[c.i] = arena[c.i] >= B.iso; });
 }
 
+// Union-find start: every voxel of the wanted class points at the start of its
+// run along x (found with a ballot within the warp; a run that enters the
+// warp from the left points at the voxel before the warp), so the x links
+// never need a union.  Other voxels get -1.  Parents are smaller indices of
+// the same component, as the hooking rule requires.
 __global__ void k_a_uf_init(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const unsigned char *m,
                             unsigned char want, int *L) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) { L[c.i] = m[c.i] == want ? (int)c.i : -1; });
+    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
+        const int lane = threadIdx.x & 31;
+        // the lanes of this step: consecutive voxels, a prefix of the warp
+        const long long left_in_box = (long long)B.n[0] * B.n[1] * B.n[2] - (c.i - B.arena - lane);
+        const unsigned act = left_in_box >= 32 ? 0xffffffffu : (1u << left_in_box) - 1u;
+        const bool fg = m[c.i] == want;
+        const bool left_fg = __shfl_up_sync(act, fg, 1);
+        const bool cont = fg && c.x > 0 && (lane > 0 ? left_fg : m[c.i - 1] == want);
+        const unsigned starts = __ballot_sync(act, fg && !cont);
+        int parent = -1;
+        if (fg) {
+            const unsigned le = starts & (lane == 31 ? 0xffffffffu : (2u << lane) - 1u);
+            parent = le ? (int)(c.i - (lane - (31 - __clz(le)))) : (int)(c.i - lane - 1);
+        }
+        L[c.i] = parent;
+    });
 }
 
 __global__ void k_a_uf_merge(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, int *L, int nnb) {
     for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
         if (L[c.i] < 0 || skip_box(B)) return;
-        for (int k = 0; k < nnb; k++) {
+        // the -x neighbour (k = 0) is linked by the run start; a contact whose two
+        // left voxels also touch is implied by theirs (both pairs lie in the same runs)
+        const bool left = c.x > 0 && L[c.i - 1] >= 0;
+        for (int k = 1; k < nnb; k++) {
             const int xx = c.x + k_half[k][0], yy = c.y + k_half[k][1], zz = c.z + k_half[k][2];
             if (xx < 0 || yy < 0 || zz < 0 || xx >= B.n[0] || yy >= B.n[1]) continue;
             const long long j = B.arena + ((long long)zz * B.n[1] + yy) * B.n[0] + xx;
             const int lj = L[j];
-            if (lj >= 0 && lj != L[c.i]) uf::unite(L, (int)c.i, (int)j);
+            if (lj < 0 || (left && xx > 0 && L[j - 1] >= 0)) continue;
+            if (lj != L[c.i]) uf::unite(L, (int)c.i, (int)j);
         }
     });
 }

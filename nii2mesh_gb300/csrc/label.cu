@@ -29,9 +29,28 @@ __global__ void k_nonzero(const float *__restrict__ vol, long long n, unsigned c
 }
 
 // L[i] = i where m[i] == want, else -1
-__global__ void k_uf_init(const unsigned char *__restrict__ m, long long n, unsigned char want, int *L) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        L[i] = m[i] == want ? (int)i : -1;
+// Union-find start: every voxel of the wanted class points at the start of its
+// run along x (ballot within the warp; a run entering the warp from the left
+// points at the voxel before the warp), so x links need no union; others -1.
+__global__ void k_uf_init(const unsigned char *__restrict__ m, Dims d, unsigned char want, int *L) {
+    const long long n = d.n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int lane = threadIdx.x & 31;
+        // the lanes of this step: consecutive voxels, a prefix of the warp
+        const long long left = n - (i - lane);
+        const unsigned act = left >= 32 ? 0xffffffffu : (1u << left) - 1u;
+        const bool fg = m[i] == want;
+        const bool left_fg = __shfl_up_sync(act, fg, 1);
+        const bool xpos = (i % d.nx) != 0;
+        const bool cont = fg && xpos && (lane > 0 ? left_fg : m[i - 1] == want);
+        const unsigned starts = __ballot_sync(act, fg && !cont);
+        int parent = -1;
+        if (fg) {
+            const unsigned le = starts & (lane == 31 ? 0xffffffffu : (2u << lane) - 1u);
+            parent = le ? (int)(i - (lane - (31 - __clz(le)))) : (int)(i - lane - 1);
+        }
+        L[i] = parent;
+    }
 }
 
 __constant__ signed char k_half[13][3] = {{-1, 0, 0},  {0, -1, 0}, {0, 0, -1},  {-1, -1, 0}, {1, -1, 0},
@@ -44,12 +63,16 @@ __global__ void k_uf_merge(int *L, Dims d, int nnb) {
         const int z = (int)(i / d.nxy);
         const long long r = i - z * d.nxy;
         const int y = (int)(r / d.nx), x = (int)(r - (long long)y * d.nx);
-        for (int k = 0; k < nnb; k++) {
+        // the -x neighbour (k = 0) is linked by the run start; a contact whose two
+        // left voxels also touch is implied by theirs (both pairs lie in the same runs)
+        const bool left = x > 0 && L[i - 1] >= 0;
+        for (int k = 1; k < nnb; k++) {
             const int xx = x + k_half[k][0], yy = y + k_half[k][1], zz = z + k_half[k][2];
             if (xx < 0 || yy < 0 || zz < 0 || xx >= d.nx || yy >= d.ny) continue;
             const long long j = zz * d.nxy + (long long)yy * d.nx + xx;
             const int lj = L[j];
-            if (lj >= 0 && lj != L[i]) unite(L, (int)i, (int)j);
+            if (lj < 0 || (left && xx > 0 && L[j - 1] >= 0)) continue;
+            if (lj != L[i]) unite(L, (int)i, (int)j);
         }
     }
 }
@@ -177,7 +200,7 @@ inline unsigned gsz(long long n) {
 
 n2m_status components(LabelWork &w, Dims d, unsigned char want, int conn, unsigned *d_nroots, cudaStream_t s) {
     int *L = w.lab.as<int>();
-    { k_uf_init<<<gsz(d.n), 256, 0, s>>>(w.mask.as<unsigned char>(), d.n, want, L); N2M_COUNT(); }
+    { k_uf_init<<<gsz(d.n), 256, 0, s>>>(w.mask.as<unsigned char>(), d, want, L); N2M_COUNT(); }
     { k_uf_merge<<<gsz(d.n), 256, 0, s>>>(L, d, conn == 6 ? 3 : conn == 18 ? 9 : 13); N2M_COUNT(); }
     if (d_nroots) CK(cudaMemsetAsync(d_nroots, 0, sizeof(unsigned), s));
     { k_uf_flatten<<<gsz(d.n), 256, 0, s>>>(L, d.n, d_nroots); N2M_COUNT(); }
