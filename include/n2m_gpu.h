@@ -73,7 +73,9 @@ typedef struct {
     /* device time per stage (CUDA events on the context stream):
      * [0] pre-smooth kernel (or the range pass), [1] clustering + range/bbox,
      * [2] marching-cubes count pass + scan, [3] emit pass, [4] weld,
-     * [5] degenerate removal, [6] HC post-smoothing, [7] unused */
+     * [5] degenerate removal, [6] HC post-smoothing, [7] host-memory calls
+     * only: the mesh's way into the caller's memory after the device work
+     * (waiting for the output pages, device-to-host copy; host clock) */
     float ms_stage[8];
     int64_t kernel_launches; /* kernels this call launched */
 } n2m_report;

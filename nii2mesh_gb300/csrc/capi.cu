@@ -15,7 +15,10 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -66,14 +69,45 @@ void DevBuf::release() {
 
 // ---- context ------------------------------------------------------------------------
 // Output buffers of a host-memory meshify call.  They are malloc'd (the
-// caller frees them with free(), as the reference's callers do) as soon as the
-// raw mesh size is known, and their pages are faulted in by host threads while
-// the GPU finishes: first-touch page faults of a fresh 100+ MB buffer cost more
-// than the device-to-host copy itself.
+// caller frees them with free(), as the reference's callers do) before the
+// GPU work starts (sized like the last call's mesh) or as soon as the raw
+// mesh size is known, and their pages are faulted in by a pool of host
+// threads while the GPU works: first-touch page faults of a fresh 100+ MB
+// buffer cost more than the device-to-host copy itself.
 struct HostOut {
     char *pts = nullptr, *tris = nullptr;
     size_t pb = 0, tb = 0;
-    std::vector<std::thread> th;
+    // worker pool, created on first use and kept for the context's lifetime
+    std::vector<std::thread> pool;
+    std::mutex mu;
+    std::condition_variable cv_job, cv_done;
+    unsigned long long job = 0;   // generation of the current job
+    int pending = 0;              // workers still busy with it
+    bool quit = false;
+    void work(int i, int n) {
+        unsigned long long seen = 0;
+        for (;;) {
+            char *p, *t;
+            size_t a, b;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv_job.wait(lk, [&] { return quit || job != seen; });
+                if (quit) return;
+                seen = job;
+                p = pts;
+                t = tris;
+                a = pb;
+                b = tb;
+            }
+            const size_t page = 4096, total = a + b, lo = total * i / n, hi = total * (i + 1) / n;
+            for (size_t o = (lo + page - 1) / page * page; o < hi; o += page) {
+                if (o < a) p[o] = 0;
+                else t[o - a] = 0;
+            }
+            std::lock_guard<std::mutex> lk(mu);
+            if (--pending == 0) cv_done.notify_all();
+        }
+    }
     void start(size_t pbytes, size_t tbytes) {
         discard();
         pts = (char *)malloc(pbytes);
@@ -86,24 +120,23 @@ struct HostOut {
         }
         pb = pbytes;
         tb = tbytes;
-        const unsigned hw = std::thread::hardware_concurrency();
-        const int n = (int)std::min(16u, std::max(1u, hw));
-        const size_t total = pb + tb;
-        try {
-            for (int i = 0; i < n; i++)
-                th.emplace_back([this, i, n, total] {
-                    const size_t page = 4096, lo = total * i / n, hi = total * (i + 1) / n;
-                    for (size_t o = (lo + page - 1) / page * page; o < hi; o += page) {
-                        if (o < pb) pts[o] = 0;
-                        else tris[o - pb] = 0;
-                    }
-                });
-        } catch (...) {   // no threads: the copy faults the pages in itself
+        if (pool.empty()) {
+            const unsigned hw = std::thread::hardware_concurrency();   // leave two cores to the calling thread
+            const int n = (int)std::min(16u, std::max(1u, hw > 2 ? hw - 2 : 1u));
+            try {
+                for (int i = 0; i < n; i++) pool.emplace_back([this, i, n] { work(i, n); });
+            } catch (...) {   // fewer workers (or none: the copy then faults the pages in itself)
+            }
         }
+        if (pool.empty()) return;
+        std::lock_guard<std::mutex> lk(mu);
+        pending = (int)pool.size();
+        job++;
+        cv_job.notify_all();
     }
     void join() {
-        for (auto &t : th) t.join();
-        th.clear();
+        std::unique_lock<std::mutex> lk(mu);
+        cv_done.wait(lk, [&] { return pending == 0; });
     }
     void discard() {
         join();
@@ -111,6 +144,15 @@ struct HostOut {
         free(tris);
         pts = tris = nullptr;
         pb = tb = 0;
+    }
+    ~HostOut() {
+        discard();
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            quit = true;
+        }
+        cv_job.notify_all();
+        for (auto &t : pool) t.join();
     }
 };
 
@@ -149,6 +191,8 @@ struct n2m_context {
     StagedInput stage;
     bool want_host = false;
     HostOut hout;
+    size_t hint_pb = 0, hint_tb = 0;   // raw mesh bytes of the last host-memory call (early pre-faulting)
+    bool pts_early = false;            // the final vertices are already on their way to hout.pts
 };
 
 extern "C" int n2m_device_count(void) {
@@ -565,7 +609,12 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     CKS(prepare(c, d_src, dim, o, o.verbose, P, rep));
     int nv, nt, ncand;
     CKS(march(c, P, dim, o.cubes, &nv, &nt, &ncand));
-    if (c->want_host) c->hout.start((size_t)std::max(nv, 1) * sizeof(vec3d), (size_t)std::max(nt, 1) * sizeof(vec3i));
+    if (c->want_host) {   // keep buffers started early if they are large enough, else start them now
+        const size_t pb = (size_t)std::max(nv, 1) * sizeof(vec3d), tb = (size_t)std::max(nt, 1) * sizeof(vec3i);
+        if (!c->hout.pts || c->hout.pb < pb || c->hout.tb < tb) c->hout.start(pb, tb);
+        c->hint_pb = pb;
+        c->hint_tb = tb;
+    }
     vec3d *pts = c->pts_raw.as<vec3d>();
     int np = nv;
     int welded = 0;
@@ -614,8 +663,19 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     }
     CKS(c->tris.ensure((size_t)nt * sizeof(vec3i)));
     CKS(c->ntf.ensure(sizeof(unsigned)));
+    c->pts_early = false;
+    const bool early = c->want_host && o.post_smooth <= 0;   // vertices are final after the weld
+    if (early) CK(cudaEventRecord(c->stage.ev[0], c->stream));
     CKS(mesh_remove_degenerate(pts, c->tris_raw.as<vec3i>(), nt, c->tris.as<vec3i>(), c->ntf.as<unsigned>(), c->deg,
                                c->scan, c->stream));
+    if (early) {   // copy them out on the second stream while the degenerate filter runs
+        c->hout.join();
+        if (c->hout.pts && c->hout.pb >= (size_t)np * sizeof(vec3d)) {
+            CK(cudaStreamWaitEvent(c->copy, c->stage.ev[0], 0));
+            CK(cudaMemcpyAsync(c->hout.pts, pts, (size_t)np * sizeof(vec3d), cudaMemcpyDeviceToHost, c->copy));
+            c->pts_early = true;
+        }
+    }
     CK(cudaEventRecord(c->evs[6], c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
     unsigned ntf;
@@ -654,9 +714,13 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     return N2M_OK;
 }
 
-n2m_status to_host_mesh(n2m_context *c, vec3i **t, vec3d **p, int *nt, int *np) {
+n2m_status to_host_mesh(n2m_context *c, vec3i **t, vec3d **p, int *nt, int *np, n2m_report *rep = nullptr) {
+    const auto t0 = std::chrono::steady_clock::now();
     const size_t pbytes = (size_t)c->res_np * sizeof(vec3d), tbytes = (size_t)std::max(c->res_nt, 1) * sizeof(vec3i);
     c->hout.join();
+    bool early = c->pts_early;   // final vertices already copied into hout.pts on the second stream
+    c->pts_early = false;
+    if (early) CK(cudaStreamSynchronize(c->copy));
     vec3d *hp;
     vec3i *ht;
     if (c->hout.pts && c->hout.pb >= pbytes && c->hout.tb >= tbytes) {   // pre-faulted (sized for the raw mesh)
@@ -665,6 +729,7 @@ n2m_status to_host_mesh(n2m_context *c, vec3i **t, vec3d **p, int *nt, int *np) 
         c->hout.pts = c->hout.tris = nullptr;
         c->hout.pb = c->hout.tb = 0;
     } else {
+        early = false;
         c->hout.discard();
         hp = (vec3d *)malloc(std::max<size_t>(pbytes, 1));
         ht = (vec3i *)malloc(tbytes);
@@ -675,7 +740,7 @@ n2m_status to_host_mesh(n2m_context *c, vec3i **t, vec3d **p, int *nt, int *np) 
             return N2M_ERR_OOM;
         }
     }
-    cudaError_t e = cudaMemcpyAsync(hp, c->res_pts, pbytes, cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = early ? cudaSuccess : cudaMemcpyAsync(hp, c->res_pts, pbytes, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ht, c->res_tris, (size_t)c->res_nt * sizeof(vec3i), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
@@ -688,6 +753,7 @@ n2m_status to_host_mesh(n2m_context *c, vec3i **t, vec3d **p, int *nt, int *np) 
     *p = hp;
     *nt = c->res_nt;
     *np = c->res_np;
+    if (rep) rep->ms_stage[7] = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return N2M_OK;
 }
 
@@ -732,6 +798,8 @@ namespace {
 n2m_status meshify_host_tail(n2m_context *c, const int dim[3], const n2m_options *opt, vec3i **t, vec3d **p, int *nt,
                              int *np, n2m_report *rep) {
     c->want_host = true;
+    // fault in output pages sized like the last call's mesh while the GPU works (re-sized after the count if short)
+    if (c->hint_pb) c->hout.start(c->hint_pb + c->hint_pb / 8, c->hint_tb + c->hint_tb / 8);
     n2m_status s = pipeline(c, c->in.as<float>(), dim, *opt, rep);
     c->stage.host = nullptr;
     c->want_host = false;
@@ -739,9 +807,10 @@ n2m_status meshify_host_tail(n2m_context *c, const int dim[3], const n2m_options
     if (s == N2M_OK && opt->post_smooth > 0)
         s = mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc, c->scan,
                            c->stream);
-    if (s == N2M_OK) s = to_host_mesh(c, t, p, nt, np);
+    if (s == N2M_OK) s = to_host_mesh(c, t, p, nt, np, rep);
     if (s != N2M_OK) {
         cudaStreamSynchronize(c->copy);
+        c->pts_early = false;
         c->hout.discard();
     }
     return s;
