@@ -174,24 +174,27 @@ __global__ void __launch_bounds__(256) k_pass_x(Pass P, unsigned row0, unsigned 
 // 32 inner positions and a run of K positions along the axis; each lane
 // slides a register window along the axis.  STATS: the z pass, which also
 // reduces range and bbox.
+// Outputs positions [p_lo, p_hi) along the axis of outer slices
+// [outer0, outer0 + nouter) (the staged upload runs the passes slab by slab).
 template <int K, int SEGS, bool STATS>
-__global__ void __launch_bounds__(256, 4) k_pass_axis(Pass P, int len, unsigned nouter) {
+__global__ void __launch_bounds__(256, 4) k_pass_axis(Pass P, int len, unsigned outer0, unsigned nouter, int p_lo,
+                                                      int p_hi) {
     __shared__ unsigned stage_buf[8][32 * (K + 1)];   // < 32 entries between runs, + 32 per step
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     FixStage<STATS> F{stage_buf[wid], 0};
     const unsigned inner = P.stride;
     const unsigned nseg = (inner + 31) / 32, nchunk = (nseg + SEGS - 1) / SEGS;
-    const unsigned nrun = (unsigned)(len + K - 1) / K;
+    const unsigned nrun = (unsigned)(p_hi - p_lo + K - 1) / K;
     const unsigned ntask = nchunk * nrun * nouter;
     const unsigned nwarps = gridDim.x * (blockDim.x / 32);
     Acc acc;
     acc.init();
     for (unsigned t = blockIdx.x * (blockDim.x / 32) + wid; t < ntask; t += nwarps) {
         const unsigned chunk = t % nchunk, rest = t / nchunk;
-        const int p0 = (int)(rest % nrun) * K;
-        const unsigned o = rest / nrun;
+        const int p0 = p_lo + (int)(rest % nrun) * K;
+        const unsigned o = outer0 + rest / nrun;
         const unsigned sbeg = chunk * SEGS, send = min(sbeg + SEGS, nseg);
-        const bool interior = p0 >= 2 && p0 + K <= len - 2;   // no face rows, whole run inside
+        const bool interior = p0 >= 2 && p0 + K <= len - 2 && p0 + K <= p_hi;   // no face rows, whole run inside
         for (unsigned seg = sbeg; seg < send; seg++) {
             const unsigned i = seg * 32 + lane;
             const bool act = i < inner;
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_axis(Pass P, int len, unsigned 
                     const int pos = p0 + k;
                     bool fail = false;
                     const unsigned v = base + (unsigned)pos * inner;
-                    if (act && pos < len) {
+                    if (act && pos < p_hi) {
                         float r = w[k + 2];
                         if (pos >= 2 && pos <= len - 3) fail = !tap5_fast(w[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], &r);
                         if (!fail) {
@@ -274,6 +277,9 @@ n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny
             // the copy stream may only overwrite `in` once earlier work on s is done with it
             CK(cudaEventRecord(stage->ev[N2M_STAGE_SLABS], s));
             CK(cudaStreamWaitEvent(stage->copy, stage->ev[N2M_STAGE_SLABS], 0));
+            // per slab: x and y passes as soon as it has arrived, then the z pass of
+            // every slice whose five y-pass inputs are done
+            int zdone = 0;
             for (int k = 0; k < N2M_STAGE_SLABS; k++) {
                 const int z0 = (int)((long long)nz * k / N2M_STAGE_SLABS), z1 = (int)((long long)nz * (k + 1) / N2M_STAGE_SLABS);
                 if (z1 <= z0) continue;
@@ -284,12 +290,18 @@ n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny
                 const unsigned r0 = (unsigned)z0 * ny, r1 = (unsigned)z1 * ny;
                 const unsigned g = std::min<unsigned>((unsigned)gx, std::max<unsigned>(1u, (r1 - r0 + 7) / 8));
                 { k_pass_x<<<g, 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
+                { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, (unsigned)z0, (unsigned)(z1 - z0), 0, ny); N2M_COUNT(); }
+                const int zready = z1 == nz ? nz : z1 - 2;
+                if (zready > zdone) {
+                    { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 0u, 1u, zdone, zready); N2M_COUNT(); }
+                    zdone = zready;
+                }
             }
         } else {
             { k_pass_x<<<gx, 256, 0, s>>>(px, 0u, (unsigned)ny * nz); N2M_COUNT(); }
+            { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, 0u, (unsigned)nz, 0, ny); N2M_COUNT(); }
+            { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 0u, 1u, 0, nz); N2M_COUNT(); }
         }
-        { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, (unsigned)nz); N2M_COUNT(); }
-        { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 1u); N2M_COUNT(); }
         CKL();
         return N2M_OK;
     }
