@@ -99,6 +99,23 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def slowest_rank_ms(ms, dist, device=None):
+    """The job's time: the maximum over ranks of each rank's timed-region
+    milliseconds (replicas: every rank meshes its own copy of the workload).
+    Works on NCCL (CUDA tensor) and gloo (CPU tensor) process groups."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank, world, ms):
+    """Whole-job throughput: units of all ranks over the slowest rank's time, in G units/s."""
+    return world * units_per_rank / (ms * 1e-3) / 1e9
+
+
 def dist_setup(n):
     import torch
     if n <= 1:
@@ -390,12 +407,8 @@ def main():
     ck = clocks.stop()
     if dist:
         dist.barrier()
-    ms = ev0.elapsed_time(ev1) / a.steps
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * nvox / (ms * 1e-3) / 1e9
+    ms = slowest_rank_ms(ev0.elapsed_time(ev1) / a.steps, dist, f"cuda:{dev}")
+    value = job_value(nvox, world, ms)
     nt, nv = reps[-1]["ntri"], reps[-1]["nvert"]
     launches = sum(r["kernel_launches"] for r in reps)
     stage_ms = [statistics.mean(r["ms_stage"][i] for r in reps) for i in range(7)]
@@ -427,11 +440,7 @@ def main():
         t0 = time.perf_counter()
         tris, pts, _ = ctx.meshify(pinned, ISO, n2m.MC33, True, False, False)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_ms = statistics.median(e2e_t) * 1e3
-    if dist:
-        t = torch.tensor([e2e_ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = slowest_rank_ms(statistics.median(e2e_t) * 1e3, dist, f"cuda:{dev}")
     e2e = {"value": round(world * nvox / (e2e_ms * 1e-3) / 1e9, 4), "unit": "Gvox/s",
            "h2d_bytes_per_step": 4 * nvox, "d2h_bytes_per_step": 24 * len(pts) + 12 * len(tris),
            "ms_per_step": round(e2e_ms, 3)}
