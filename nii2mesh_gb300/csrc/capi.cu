@@ -258,7 +258,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->aw.pts, &c->aw.pts2, &c->aw.tris, &c->aw.tris2, &c->aw.cand, &c->aw.gath, &c->aw.weld,
                       &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->raw, &c->vol, &c->stmp, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
                       &c->tris_raw, &c->pts, &c->tris, &c->ntf, &c->weld, &c->gath, &c->hmesh,
-                      &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->mc.signs, &c->scan.part,
+                      &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->mc.signs, &c->mc.ctr, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
                       &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->th.buf, &c->th.table};

@@ -366,7 +366,8 @@ __global__ void __launch_bounds__(EG_WARPS * 32) k_emit(GV g, bool classic, unsi
                                                           const uint4 *__restrict__ offs, const unsigned *__restrict__ signs,
                                                           const unsigned *__restrict__ active, unsigned nactive,
                                                           uint4 totals, vec3d *pts, vec3i *tris, int *cand,
-                                                          unsigned *ncand, int *ccand, unsigned *nccand, int cap) {
+                                                          unsigned *ncand, int *ccand, unsigned *nccand, int cap,
+                                                          unsigned *next_group) {
     __shared__ unsigned short vitem[EG_WARPS][EG_VCAP];   // lane << 7 | point << 2 | axis
     __shared__ unsigned titem[EG_WARPS][EG_TCAP];          // lane << 27 | point << 22 | tiling offset, or a hole
     __shared__ unsigned qtile[256];                        // unambiguous tilings: offset << 8 | triangles; 0xff: tests
@@ -379,7 +380,11 @@ __global__ void __launch_bounds__(EG_WARPS * 32) k_emit(GV g, bool classic, unsi
     const float flo0 = (float)g.lo0, flo1 = (float)g.lo1, flo2 = (float)g.lo2;
     const unsigned slice = WX * (unsigned)g.NY, NY = (unsigned)g.NY;
     const unsigned ngroups = (nactive + 31) / 32;
-    for (unsigned grp = blockIdx.x * EG_WARPS + wid; grp < ngroups; grp += gridDim.x * EG_WARPS) {
+    for (;;) {   // groups are handed out one at a time: their work varies a lot
+        unsigned grp = 0;
+        if (lane == 0) grp = atomicAdd(next_group, 1u);
+        grp = __shfl_sync(0xffffffffu, grp, 0);
+        if (grp >= ngroups) break;
         const unsigned aw = grp * 32 + lane;
         const bool live = aw < nactive;
         const unsigned w = live ? active[aw] : active[nactive - 1];
@@ -685,7 +690,9 @@ n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, v
         resident = sms * std::max(per_sm, 1);
     }
     const unsigned gblocks = std::min<unsigned>(((nact + 31) / 32 + EG_WARPS - 1) / EG_WARPS, (unsigned)resident);
-    { k_emit<<<gblocks, EG_WARPS * 32, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.signs.as<unsigned>(), w.cand.as<unsigned>(), nact, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand, d_cand + cand_cap, d_ncand + 1, cand_cap); N2M_COUNT(); }
+    CKS(w.ctr.ensure(sizeof(unsigned)));
+    CK(cudaMemsetAsync(w.ctr.p, 0, sizeof(unsigned), s));
+    { k_emit<<<gblocks, EG_WARPS * 32, 0, s>>>(v, variant == N2M_CUBES_CLASSIC_TABLE, WX, w.words.as<uint4>(), w.counts.as<uint4>(), w.signs.as<unsigned>(), w.cand.as<unsigned>(), nact, make_uint4(c.nv_edge, c.nt, c.nc, 0), d_pts, d_tris, d_cand, d_ncand, d_cand + cand_cap, d_ncand + 1, cand_cap, w.ctr.as<unsigned>()); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

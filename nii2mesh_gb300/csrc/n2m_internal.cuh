@@ -131,7 +131,7 @@ struct McGrid {
     float iso, edge_max, pad_val;   // pad_val = float(min' - iso)
 };
 struct McWork {
-    DevBuf words, counts, cand, verts_tmp, tris_tmp, signs;
+    DevBuf words, counts, cand, verts_tmp, tris_tmp, signs, ctr;
 };
 struct McCounts {
     unsigned nv_edge, nt, nc, nactive;
