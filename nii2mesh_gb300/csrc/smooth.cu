@@ -169,6 +169,46 @@ __global__ void __launch_bounds__(256) k_pass_x(Pass P, unsigned row0, unsigned 
     F.finish(P, acc, lane);
 }
 
+// x pass for rows whose length is a multiple of 4 (16-byte aligned rows):
+// each thread takes 4 consecutive voxels with three float4 loads (its own and
+// the neighbours' halves, mostly L1 hits) and one float4 store; voxels whose
+// fast path fails are stored as placeholders and fixed by the same warp.
+__global__ void __launch_bounds__(256) k_pass_x4(Pass P, unsigned row0, unsigned row1) {
+    __shared__ unsigned stage_buf[8][32 * 5];   // < 32 between drains, + 4 per lane per step
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    FixStage<false> F{stage_buf[w], 0};
+    Acc acc;   // unused by the x pass
+    const int nx = P.nx, nq = nx / 4;
+    const unsigned nwarps = gridDim.x * (blockDim.x / 32);
+    for (unsigned row = row0 + blockIdx.x * (blockDim.x / 32) + w; row < row1; row += nwarps) {
+        const float4 *r4 = reinterpret_cast<const float4 *>(P.in + (size_t)row * nx);
+        float4 *o4 = reinterpret_cast<float4 *>(P.out + (size_t)row * nx);
+        for (int q0 = 0; q0 < nq; q0 += 32) {
+            const int q = q0 + lane, x0 = 4 * q;
+            const bool act = q < nq;
+            const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 A = act && q > 0 ? __ldg(r4 + q - 1) : zero;
+            const float4 B = act ? __ldg(r4 + q) : zero;
+            const float4 C = act && q + 1 < nq ? __ldg(r4 + q + 1) : zero;
+            const float v[12] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w, C.x, C.y, C.z, C.w};   // x0-4 .. x0+7
+            float o[4];
+            bool fail[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int x = x0 + j;
+                o[j] = v[4 + j];
+                fail[j] = act && x >= 2 && x <= nx - 3 && !tap5_fast(v[2 + j], v[3 + j], v[4 + j], v[5 + j], v[6 + j], &o[j]);
+            }
+            if (act) o4[q] = make_float4(o[0], o[1], o[2], o[3]);
+            const unsigned base = row * (unsigned)nx + (unsigned)x0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) F.push(fail[j], base + j, lane);
+            F.drain(P, acc, lane);
+        }
+    }
+    F.finish(P, acc, lane);
+}
+
 // y and z passes: the volume is viewed as (outer, len, inner) with the pass
 // axis of length len and stride inner.  A task is SEGS consecutive groups of
 // 32 inner positions and a run of K positions along the axis; each lane
@@ -264,15 +304,24 @@ n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny
                          cudaStream_t s, const StagedInput *stage) {
     const size_t n = (size_t)nx * ny * nz;
     if (n < ((size_t)1 << 32)) {
-        static int gx = 0, ga = 0, gz = 0;
+        static int gx = 0, gx4 = 0, ga = 0, gz = 0;
         if (!gx) {
             gx = resident_blocks((const void *)k_pass_x, 256);
+            gx4 = resident_blocks((const void *)k_pass_x4, 256);
             ga = resident_blocks((const void *)k_pass_axis<KRUN, KSEG, false>, 256);
             gz = resident_blocks((const void *)k_pass_axis<KRUN, KSEG, true>, 256);
         }
         const unsigned nxy = (unsigned)nx * ny;
         const Pass px{in, out, 1u, nx, ny, nxy, iso, st}, py{out, tmp, (unsigned)nx, nx, ny, nxy, iso, st},
             pz{tmp, out, nxy, nx, ny, nxy, iso, st};
+        // 16-byte rows: the float4 x pass
+        const bool x4 = nx % 4 == 0 && ((uintptr_t)in & 15) == 0 && ((uintptr_t)out & 15) == 0;
+        auto pass_x = [&](unsigned r0, unsigned r1, unsigned g) -> n2m_status {
+            if (x4) { k_pass_x4<<<std::min<unsigned>(g, (unsigned)gx4), 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
+            else { k_pass_x<<<std::min<unsigned>(g, (unsigned)gx), 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
+            CKL();
+            return N2M_OK;
+        };
         if (stage && stage->host) {
             // the copy stream may only overwrite `in` once earlier work on s is done with it
             CK(cudaEventRecord(stage->ev[N2M_STAGE_SLABS], s));
@@ -288,8 +337,7 @@ n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny
                 CK(cudaEventRecord(stage->ev[k], stage->copy));
                 CK(cudaStreamWaitEvent(s, stage->ev[k], 0));
                 const unsigned r0 = (unsigned)z0 * ny, r1 = (unsigned)z1 * ny;
-                const unsigned g = std::min<unsigned>((unsigned)gx, std::max<unsigned>(1u, (r1 - r0 + 7) / 8));
-                { k_pass_x<<<g, 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
+                CKS(pass_x(r0, r1, std::max<unsigned>(1u, (r1 - r0 + 7) / 8)));
                 { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, (unsigned)z0, (unsigned)(z1 - z0), 0, ny); N2M_COUNT(); }
                 const int zready = z1 == nz ? nz : z1 - 2;
                 if (zready > zdone) {
@@ -298,7 +346,7 @@ n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny
                 }
             }
         } else {
-            { k_pass_x<<<gx, 256, 0, s>>>(px, 0u, (unsigned)ny * nz); N2M_COUNT(); }
+            CKS(pass_x(0u, (unsigned)ny * nz, 0xffffffffu));
             { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, 0u, (unsigned)nz, 0, ny); N2M_COUNT(); }
             { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 0u, 1u, 0, nz); N2M_COUNT(); }
         }
