@@ -113,6 +113,13 @@ void apply_sform(vec3i *t, vec3d *p, int nt, int np, float srow_x[4], float srow
  * Otsu isolevel on the robust (2nd-98th percentile) range; mode 1 dark,
  * 2 medium, 3 bright.  img is a host array of nvox floats. */
 float setThreshold(float *img, int nvox, int darkMediumBright123);
+/* replaces save_mesh() (src/meshify.h:8, body src/meshify.c:984-1019): the
+ * format follows the file name's extension as in the reference (.mz3, .gii,
+ * .inflated/.pial FreeSurfer, .json, .off, .obj, .ply, .stl, .vtk; any other
+ * name gets ".mz3" appended); isGz writes mz3 as gzip and GIfTI arrays
+ * zlib-compressed.  The file is encoded on the GPU.  Returns EXIT_SUCCESS or
+ * EXIT_FAILURE (file not writable, no device). */
+int save_mesh(const char *fnm, vec3i *tris, vec3d *pts, int ntri, int npt, bool isGz);
 /* Mirrors the USE_CLASSIC_CUBES build flag for the drop-in marchingCubes()
  * and meshify(): nonzero selects Bourke's oldcubes. Returns the old value. */
 int n2m_set_oldcubes(int enable);
@@ -183,6 +190,41 @@ n2m_status n2m_meshify_typed(n2m_context *ctx, const void *img, int datatype, fl
  * (n2m_set_threshold_device) of nvox floats; the value goes to *iso. */
 n2m_status n2m_set_threshold(n2m_context *ctx, const float *img, int64_t nvox, int mode, float *iso);
 n2m_status n2m_set_threshold_device(n2m_context *ctx, const float *d_img, int64_t nvox, int mode, float *iso);
+
+/* ---- mesh writers (save_mesh, src/meshify.c:602-1019) -------------------------- */
+typedef enum {
+    N2M_FMT_MZ3 = 0,        /* .mz3 (gzip when is_gz) */
+    N2M_FMT_GII = 1,        /* .gii: base64 arrays (zlib + base64 when is_gz) */
+    N2M_FMT_FREESURFER = 2, /* .inflated / .pial */
+    N2M_FMT_JSON = 3,
+    N2M_FMT_OFF = 4,
+    N2M_FMT_OBJ = 5,
+    N2M_FMT_PLY = 6,
+    N2M_FMT_STL = 7,
+    N2M_FMT_VTK = 8
+} n2m_mesh_format;
+/* The format save_mesh() picks for a file name; -1 when it appends ".mz3". */
+int n2m_mesh_format_of(const char *fnm);
+/* The bytes save_mesh() writes for `format`, in malloc'd memory (*out, *out_len;
+ * release with free()).  Host mesh (n2m_encode_mesh) or device mesh
+ * (n2m_encode_mesh_device, e.g. the result of n2m_meshify_device).  The
+ * FreeSurfer format embeds the current local time like the reference. */
+n2m_status n2m_encode_mesh(n2m_context *ctx, int format, const vec3i *tris, const vec3d *pts, int ntri, int npt,
+                           int is_gz, unsigned char **out, size_t *out_len);
+n2m_status n2m_encode_mesh_device(n2m_context *ctx, int format, const vec3i *d_tris, const vec3d *d_pts, int ntri,
+                                  int npt, int is_gz, unsigned char **out, size_t *out_len);
+/* save_mesh() with a status: host mesh, or a mesh already in device memory. */
+n2m_status n2m_save_mesh(n2m_context *ctx, const char *fnm, const vec3i *tris, const vec3d *pts, int ntri, int npt,
+                         int is_gz);
+n2m_status n2m_save_mesh_device(n2m_context *ctx, const char *fnm, const vec3i *d_tris, const vec3d *d_pts, int ntri,
+                                int npt, int is_gz);
+/* Deflate nbytes of device memory (< 2^31) as a raw deflate stream, a zlib
+ * stream or a gzip file body into malloc'd memory (*out, *out_len). */
+#define N2M_DEFLATE_RAW 0
+#define N2M_DEFLATE_ZLIB 1
+#define N2M_DEFLATE_GZIP 2
+n2m_status n2m_deflate_device(n2m_context *ctx, const void *d_src, size_t nbytes, int container, unsigned char **out,
+                              size_t *out_len);
 
 /* HC smoothing of device-resident meshes (d_verts updated in place). */
 n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,

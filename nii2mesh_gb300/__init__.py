@@ -13,6 +13,8 @@ Volumes are numpy float32 arrays shaped (nz, ny, nx) — x fastest, exactly the
 reference's memory layout.  Meshes are (tris int32 (nt,3), pts float64 (np,3)).
 """
 import ctypes as C
+import queue
+import threading
 import weakref
 
 import numpy as np
@@ -24,9 +26,12 @@ MC33, CLASSIC_TABLE, OLDCUBES = 0, 1, 2
 # NIfTI datatype codes of the voxel types load_nii reads (src/nii2mesh.c:114-117)
 _NIFTI_DT = {np.dtype(np.uint8): 2, np.dtype(np.int16): 4, np.dtype(np.float32): 16, np.dtype(np.uint16): 512}
 ATLAS_BATCHED, ATLAS_LOOP = 0, 1
+# mesh file formats (n2m_mesh_format) and deflate containers
+FMT_MZ3, FMT_GII, FMT_FREESURFER, FMT_JSON, FMT_OFF, FMT_OBJ, FMT_PLY, FMT_STL, FMT_VTK = range(9)
+DEFLATE_RAW, DEFLATE_ZLIB, DEFLATE_GZIP = 0, 1, 2
 
 __all__ = ["Context", "meshify", "laplacian_smoothHC", "marching_cubes", "bwlabel", "apply_sform", "set_threshold",
-           "N2MError",
+           "save_mesh", "mesh_format_of", "N2MError",
            "MC33", "CLASSIC_TABLE", "OLDCUBES", "lib"]
 
 
@@ -41,6 +46,37 @@ def _vol(img):
     return a
 
 
+class _Reaper:
+    """Frees large result buffers on a background thread.  Releasing a
+    pre-faulted mesh of a few hundred MB unmaps every page (~1.4 ms for the
+    170 MB of a 512^3 CT mesh); done here it overlaps the caller's next call
+    instead of blocking the thread that dropped the arrays."""
+
+    BIG = 8 << 20
+
+    def __init__(self):
+        self.q = None
+        self.lock = threading.Lock()
+
+    def free(self, L, addr, nbytes):
+        if nbytes < self.BIG:
+            L.libc_free(addr)
+            return
+        with self.lock:
+            if self.q is None:
+                self.q = queue.SimpleQueue()
+                threading.Thread(target=self._run, args=(L, self.q), name="n2m-free", daemon=True).start()
+        self.q.put(addr)
+
+    @staticmethod
+    def _run(L, q):
+        while True:
+            L.libc_free(q.get())   # ctypes releases the GIL for the call
+
+
+_reaper = _Reaper()
+
+
 def _owned(L, ptr, n, ctype, dtype):
     """numpy (n, 3) view of library-malloc'd memory, freed with libc free()
     once the last array referring to it is gone (no copy of the mesh)."""
@@ -49,7 +85,7 @@ def _owned(L, ptr, n, ctype, dtype):
         L.libc_free(addr)
         return np.zeros((0, 3), dtype)
     buf = (ctype * (3 * n)).from_address(addr)
-    weakref.finalize(buf, L.libc_free, addr)
+    weakref.finalize(buf, _reaper.free, L, addr, 3 * n * C.sizeof(ctype))
     return np.frombuffer(buf, dtype).reshape(n, 3)
 
 
@@ -151,6 +187,54 @@ class Context:
         _lib.check(self._L.n2m_set_threshold_device(self.h, C.c_void_p(d_img_ptr), int(nvox), int(mode), C.byref(out)),
                    "n2m_set_threshold_device")
         return out.value
+
+    def _bytes(self, ptr, n):
+        """bytes of library-malloc'd memory, released afterwards"""
+        try:
+            return C.string_at(ptr, n) if n else b""
+        finally:
+            self._L.libc_free(ptr)
+
+    def encode_mesh(self, fmt, tris, pts, gz=False):
+        """The file save_mesh() writes in format `fmt` (FMT_* or a file name),
+        encoded on the GPU, as bytes (n2m_encode_mesh)."""
+        if isinstance(fmt, str):
+            fmt = mesh_format_of(fmt)
+        t = np.ascontiguousarray(tris, dtype=np.int32)
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        out, n = C.c_void_p(), C.c_size_t()
+        _lib.check(self._L.n2m_encode_mesh(self.h, int(fmt), t.ctypes.data, p.ctypes.data, len(t), len(p), int(gz),
+                                           C.byref(out), C.byref(n)), "n2m_encode_mesh")
+        return self._bytes(out, n.value)
+
+    def encode_mesh_device(self, fmt, d_tris_ptr, d_pts_ptr, ntri, npt, gz=False):
+        """encode_mesh of a mesh in device memory (n2m_encode_mesh_device)."""
+        if isinstance(fmt, str):
+            fmt = mesh_format_of(fmt)
+        out, n = C.c_void_p(), C.c_size_t()
+        _lib.check(self._L.n2m_encode_mesh_device(self.h, int(fmt), C.c_void_p(d_tris_ptr), C.c_void_p(d_pts_ptr),
+                                                  int(ntri), int(npt), int(gz), C.byref(out), C.byref(n)),
+                   "n2m_encode_mesh_device")
+        return self._bytes(out, n.value)
+
+    def save_mesh(self, fnm, tris, pts, gz=False):
+        """save_mesh() with a status (n2m_save_mesh)."""
+        t = np.ascontiguousarray(tris, dtype=np.int32)
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        _lib.check(self._L.n2m_save_mesh(self.h, str(fnm).encode(), t.ctypes.data, p.ctypes.data, len(t), len(p),
+                                         int(gz)), "n2m_save_mesh")
+
+    def save_mesh_device(self, fnm, d_tris_ptr, d_pts_ptr, ntri, npt, gz=False):
+        """save_mesh() of a mesh in device memory (n2m_save_mesh_device)."""
+        _lib.check(self._L.n2m_save_mesh_device(self.h, str(fnm).encode(), C.c_void_p(d_tris_ptr), C.c_void_p(d_pts_ptr),
+                                                int(ntri), int(npt), int(gz)), "n2m_save_mesh_device")
+
+    def deflate_device(self, d_ptr, nbytes, container=DEFLATE_GZIP):
+        """Deflate nbytes of device memory (n2m_deflate_device) -> bytes."""
+        out, n = C.c_void_p(), C.c_size_t()
+        _lib.check(self._L.n2m_deflate_device(self.h, C.c_void_p(d_ptr), int(nbytes), int(container), C.byref(out),
+                                              C.byref(n)), "n2m_deflate_device")
+        return self._bytes(out, n.value)
 
     def atlas(self, labels, cubes=MC33, pre_smooth=True, only_largest=True, fill_bubbles=True, post_smooth=5,
               mode=ATLAS_BATCHED):
@@ -267,3 +351,18 @@ def set_threshold(img, mode=2):
     L = _lib.load()
     a = np.ascontiguousarray(img, dtype=np.float32).ravel()
     return float(L.setThreshold(a.ctypes.data, a.size, int(mode)))
+
+
+def mesh_format_of(fnm):
+    """The format save_mesh() picks for a file name (FMT_*); -1 when it appends ".mz3"."""
+    return int(_lib.load().n2m_mesh_format_of(str(fnm).encode()))
+
+
+def save_mesh(fnm, tris, pts, is_gz=False):
+    """save_mesh() (src/meshify.h:8): writes the mesh in the format of the file
+    name's extension.  Returns 0 (EXIT_SUCCESS) or 1 (EXIT_FAILURE)."""
+    L = _lib.load()
+    t = np.ascontiguousarray(tris, dtype=np.int32)
+    p = np.ascontiguousarray(pts, dtype=np.float64)
+    return int(L.save_mesh(str(fnm).encode(), t.ctypes.data, p.ctypes.data, len(t), len(p), bool(is_gz)))
+

@@ -204,6 +204,7 @@ struct n2m_context {
     HostOut hout;
     size_t hint_pb = 0, hint_tb = 0;   // raw mesh bytes of the last host-memory call (early pre-faulting)
     bool pts_early = false;            // the final vertices are already on their way to hout.pts
+    WriterWork wr;                     // mesh writers
 };
 
 extern "C" int n2m_device_count(void) {
@@ -261,10 +262,14 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->mc.signs, &c->mc.ctr, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
-                      &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->th.buf, &c->th.table};
+                      &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->th.buf, &c->th.table,
+                      &c->wr.mt, &c->wr.mp, &c->wr.pack, &c->wr.pack2, &c->wr.lens, &c->wr.flag, &c->wr.out, &c->wr.df.tok,
+                      &c->wr.df.info, &c->wr.df.hist, &c->wr.df.codes, &c->wr.df.hdr, &c->wr.df.sizes, &c->wr.df.seg,
+                      &c->wr.df.misc, &c->wr.df.out};
     for (DevBuf *b : bufs) b->release();
     if (c->aw.exec) cudaGraphExecDestroy((cudaGraphExec_t)c->aw.exec);
     if (c->pinned) cudaFreeHost(c->pinned);
+    if (c->wr.host) cudaFreeHost(c->wr.host);
     for (int i = 0; i < 8; i++)
         if (c->evs[i]) cudaEventDestroy(c->evs[i]);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1247,3 +1252,171 @@ extern "C" int marchingCubes(float *img, short dim[3], int lo[3], int hi[3], int
     }
     return EXIT_SUCCESS;
 }
+
+// ---- mesh writers ------------------------------------------------------------------------------
+extern "C" int n2m_mesh_format_of(const char *fnm) { return fnm ? mesh_format_of(fnm) : -1; }
+
+namespace {
+// host mesh -> context buffers (vertices after the triangles, 8-byte aligned)
+n2m_status upload_mesh(n2m_context *c, const vec3i *tris, const vec3d *pts, int nt, int np, const vec3i **dt,
+                       const vec3d **dp) {
+    if (nt < 0 || np < 0 || (nt && !tris) || (np && !pts)) return N2M_ERR_BAD_ARGS;
+    CKS(c->wr.mt.ensure((size_t)nt * sizeof(vec3i) + 16));
+    CKS(c->wr.mp.ensure((size_t)np * sizeof(vec3d) + 16));
+    if (nt) CK(cudaMemcpyAsync(c->wr.mt.p, tris, (size_t)nt * sizeof(vec3i), cudaMemcpyHostToDevice, c->stream));
+    if (np) CK(cudaMemcpyAsync(c->wr.mp.p, pts, (size_t)np * sizeof(vec3d), cudaMemcpyHostToDevice, c->stream));
+    *dt = c->wr.mt.as<vec3i>();
+    *dp = c->wr.mp.as<vec3d>();
+    return N2M_OK;
+}
+
+n2m_status to_malloc(n2m_context *c, const unsigned char *d, size_t len, unsigned char **out, size_t *out_len) {
+    unsigned char *h = (unsigned char *)malloc(std::max<size_t>(len, 1));
+    if (!h) {
+        n2m_set_error("host allocation failed");
+        return N2M_ERR_OOM;
+    }
+    if (len && (cudaMemcpyAsync(h, d, len, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                cudaStreamSynchronize(c->stream) != cudaSuccess)) {
+        free(h);
+        n2m_set_error("encoded mesh readback: %s", cudaGetErrorString(cudaGetLastError()));
+        return N2M_ERR_CUDA;
+    }
+    *out = h;
+    *out_len = len;
+    return N2M_OK;
+}
+
+// encoded bytes -> file, through the context's pinned staging buffer in pieces (copy of piece k+1 overlaps the
+// write of piece k)
+n2m_status write_file(n2m_context *c, const char *fnm, const unsigned char *d, size_t len) {
+    constexpr size_t PIECE = 32u << 20;
+    const size_t cap = std::min(len, 2 * PIECE);
+    if (c->wr.host_cap < cap) {
+        if (c->wr.host) cudaFreeHost(c->wr.host);
+        c->wr.host = nullptr;
+        c->wr.host_cap = 0;
+        CK(cudaHostAlloc(&c->wr.host, std::max<size_t>(cap, 1), cudaHostAllocDefault));
+        c->wr.host_cap = cap;
+    }
+    FILE *f = fopen(fnm, "wb");
+    if (!f) {
+        n2m_set_error("cannot open %s for writing", fnm);
+        return N2M_ERR_BAD_ARGS;
+    }
+    unsigned char *h = (unsigned char *)c->wr.host;
+    n2m_status st = N2M_OK;
+    size_t done = 0;
+    int k = 0;
+    // piece k goes to half (k & 1) of the staging buffer
+    if (len && cudaMemcpyAsync(h, d, std::min(len, PIECE), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) st = N2M_ERR_CUDA;
+    while (st == N2M_OK && done < len) {
+        const size_t n = std::min(len - done, PIECE);
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+            st = N2M_ERR_CUDA;
+            break;
+        }
+        const size_t next = done + n;
+        if (next < len &&
+            cudaMemcpyAsync(h + ((k + 1) & 1) * PIECE, d + next, std::min(len - next, PIECE), cudaMemcpyDeviceToHost,
+                            c->stream) != cudaSuccess) {
+            st = N2M_ERR_CUDA;
+            break;
+        }
+        if (fwrite(h + (k & 1) * PIECE, 1, n, f) != n) {
+            n2m_set_error("write to %s failed", fnm);
+            st = N2M_ERR_BAD_ARGS;
+            break;
+        }
+        done = next;
+        k++;
+    }
+    cudaStreamSynchronize(c->stream);
+    if (fclose(f) != 0 && st == N2M_OK) {
+        n2m_set_error("write to %s failed", fnm);
+        st = N2M_ERR_BAD_ARGS;
+    }
+    if (st == N2M_ERR_CUDA) n2m_set_error("mesh file readback: %s", cudaGetErrorString(cudaGetLastError()));
+    return st;
+}
+
+n2m_status save_device(n2m_context *c, const char *fnm, const vec3i *dt, const vec3d *dp, int nt, int np, int gz) {
+    if (!fnm) return N2M_ERR_BAD_ARGS;
+    int fmt = mesh_format_of(fnm);
+    std::string name(fnm);
+    if (fmt < 0) {   // save_mesh appends ".mz3" to names it does not recognise
+        name += ".mz3";
+        fmt = N2M_FMT_MZ3;
+    }
+    const unsigned char *d;
+    size_t len;
+    CKS(encode_mesh_device(fmt, dt, dp, nt, np, gz != 0, c->wr, c->scan, c->stream, &d, &len));
+    return write_file(c, name.c_str(), d, len);
+}
+}  // namespace
+
+extern "C" n2m_status n2m_encode_mesh_device(n2m_context *c, int format, const vec3i *d_tris, const vec3d *d_pts,
+                                             int ntri, int npt, int is_gz, unsigned char **out, size_t *out_len) {
+    if (!c || !out || !out_len) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    const unsigned char *d;
+    size_t len;
+    CKS(encode_mesh_device(format, d_tris, d_pts, ntri, npt, is_gz != 0, c->wr, c->scan, c->stream, &d, &len));
+    return to_malloc(c, d, len, out, out_len);
+}
+
+extern "C" n2m_status n2m_encode_mesh(n2m_context *c, int format, const vec3i *tris, const vec3d *pts, int ntri,
+                                      int npt, int is_gz, unsigned char **out, size_t *out_len) {
+    if (!c || !out || !out_len) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    const vec3i *dt;
+    const vec3d *dp;
+    CKS(upload_mesh(c, tris, pts, ntri, npt, &dt, &dp));
+    const unsigned char *d;
+    size_t len;
+    CKS(encode_mesh_device(format, dt, dp, ntri, npt, is_gz != 0, c->wr, c->scan, c->stream, &d, &len));
+    return to_malloc(c, d, len, out, out_len);
+}
+
+extern "C" n2m_status n2m_save_mesh_device(n2m_context *c, const char *fnm, const vec3i *d_tris, const vec3d *d_pts,
+                                           int ntri, int npt, int is_gz) {
+    if (!c) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    return save_device(c, fnm, d_tris, d_pts, ntri, npt, is_gz);
+}
+
+extern "C" n2m_status n2m_save_mesh(n2m_context *c, const char *fnm, const vec3i *tris, const vec3d *pts, int ntri,
+                                    int npt, int is_gz) {
+    if (!c) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    const vec3i *dt;
+    const vec3d *dp;
+    CKS(upload_mesh(c, tris, pts, ntri, npt, &dt, &dp));
+    return save_device(c, fnm, dt, dp, ntri, npt, is_gz);
+}
+
+extern "C" int save_mesh(const char *fnm, vec3i *tris, vec3d *pts, int ntri, int npt, bool isGz) {
+    n2m_context *c;
+    n2m_status s = default_ctx(&c);
+    if (s == N2M_OK) s = n2m_save_mesh(c, fnm, tris, pts, ntri, npt, isGz ? 1 : 0);
+    if (s != N2M_OK) {
+        report_failure("save_mesh", s);
+        return EXIT_FAILURE;
+    }
+    return EXIT_SUCCESS;
+}
+
+extern "C" n2m_status n2m_deflate_device(n2m_context *c, const void *d_src, size_t nbytes, int container,
+                                         unsigned char **out, size_t *out_len) {
+    if (!c || !out || !out_len || (nbytes && !d_src)) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    // the deflate kernels read whole aligned words up to 8 bytes past the end: work on a padded copy
+    CKS(c->wr.pack.ensure(nbytes + 16));
+    if (nbytes) CK(cudaMemcpyAsync(c->wr.pack.p, d_src, nbytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemsetAsync(c->wr.pack.as<unsigned char>() + nbytes, 0, 16, c->stream));
+    size_t len;
+    CKS(deflate_device(c->wr.pack.p, nbytes, container, c->wr.df, c->scan, c->stream, &len));
+    CKS(deflate_check(c->wr.df, c->stream));
+    return to_malloc(c, c->wr.df.out.as<unsigned char>(), len, out, out_len);
+}
+

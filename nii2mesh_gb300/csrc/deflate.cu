@@ -1,0 +1,773 @@
+// deflate.cu — gzip (RFC 1952), zlib (RFC 1950) and raw deflate (RFC 1951)
+// streams of a device buffer, for the mesh writers: save_mz3 writes its file
+// through gzopen/gzwrite (src/meshify.c:602-679) and save_gii zlib-compresses
+// each data array before base64 (src/meshify.c:863-873, 904-914).  zlib at its
+// default level does ~15 MB/s on one core; here the input is cut into 32 KB
+// chunks, each coded by one warp as one dynamic-Huffman block:
+//
+//   k_lz        match finding and parsing.  A 4-byte hash table per warp in
+//               shared memory holds the most recent position of each hash from
+//               earlier 32-byte tiles; inside a tile the most recent earlier lane
+//               with the same hash comes from __match_any_sync (one candidate
+//               per position; on mesh bytes this lands within ~4 % of zlib's
+//               level-6 size).  The parse is greedy with one-step lazy
+//               evaluation, walked over the tile's match-start ballot (one step
+//               per match, not per byte).  Emits 32-bit tokens and the block's
+//               symbol histogram.
+//   k_huff      per chunk: canonical Huffman codes (lengths <= 15; code-length
+//               code <= 7) from the histogram, the block header bits and the
+//               coded size; a stored block instead when that is smaller.
+//   scan        chunk byte offsets (every chunk ends on a byte boundary: a
+//               non-final dynamic block is followed by an empty stored block, the
+//               "sync flush" of RFC 1951 3.2.4).
+//   k_emit      one warp per chunk writes its bits through a shared-memory ring
+//               of 32-bit words (shared atomics; no global atomics), flushed as
+//               bytes in order.
+//   k_seg/k_fold CRC-32 (gzip) or Adler-32 (zlib) of 1 KB segments, folded with
+//               the polynomial / modular concatenation rules.
+//
+// The compressed bytes differ from zlib's (different match search); the
+// decompressed bytes are identical, which is the parity the tests check.
+#include "n2m_internal.cuh"
+
+namespace {
+constexpr int DF_CHUNK = 32768;                  // input bytes per block
+constexpr int DF_HBITS = 13, DF_HSIZE = 1 << DF_HBITS;
+constexpr int DF_WARPS = 4;                      // chunks per CTA
+constexpr int DF_MAXLEN = 258;
+constexpr int DF_NLIT = 286, DF_NDIST = 30, DF_NSYM = 320;   // histogram stride: 286 + 30, padded
+constexpr int DF_HDR_WORDS = 160;                // block header bits per chunk (<= 4498 used)
+constexpr int DF_SEG = 1024;                     // checksum segment
+constexpr unsigned CRC_POLY = 0xEDB88320u;       // CRC-32, reflected
+constexpr unsigned ADLER_MOD = 65521u;
+
+struct DfInfo {
+    unsigned hdr_bits;   // block header bits (BFINAL, BTYPE, code description)
+    unsigned stored;     // 1: the chunk is written as a stored block
+    unsigned ntok;
+    unsigned len;        // input bytes of the chunk
+};
+
+__device__ __forceinline__ unsigned load4(const unsigned *__restrict__ w, long long p) {
+    const long long i = p >> 2;
+    const unsigned sh = (unsigned)(p & 3) * 8u;
+    const unsigned lo = __ldg(w + i);
+    if (!sh) return lo;
+    return __funnelshift_r(lo, __ldg(w + i + 1), sh);
+}
+
+// length of the match of p against c (first 4 bytes known equal), at most maxl
+__device__ __forceinline__ int match_len(const unsigned *__restrict__ src, long long p, long long c, int maxl) {
+    int l = 4;
+    while (l < maxl) {
+        const unsigned x = load4(src, p + l) ^ load4(src, c + l);
+        if (x) return min(l + ((__ffs(x) - 1) >> 3), maxl);
+        l += 4;
+    }
+    return maxl;
+}
+
+// RFC 1951 3.2.5: length 3..258 -> symbol 257..285 + extra bits
+__host__ __device__ __forceinline__ void len_code(unsigned L, unsigned &sym, unsigned &nx, unsigned &xv) {
+    if (L == 258) {
+        sym = 285;
+        nx = xv = 0;
+        return;
+    }
+    const unsigned v = L - 3;
+    if (v < 8) {
+        sym = 257 + v;
+        nx = xv = 0;
+        return;
+    }
+#ifdef __CUDA_ARCH__
+    const unsigned nb = 31 - __clz(v);
+#else
+    const unsigned nb = 31 - __builtin_clz(v);
+#endif
+    sym = 257 + 4 * (nb - 1) + ((v >> (nb - 2)) & 3u);
+    nx = nb - 2;
+    xv = v & ((1u << nx) - 1);
+}
+// distance 1..32768 -> symbol 0..29 + extra bits
+__host__ __device__ __forceinline__ void dist_code(unsigned d, unsigned &sym, unsigned &nx, unsigned &xv) {
+    const unsigned v = d - 1;
+    if (v < 4) {
+        sym = v;
+        nx = xv = 0;
+        return;
+    }
+#ifdef __CUDA_ARCH__
+    const unsigned nb = 31 - __clz(v);
+#else
+    const unsigned nb = 31 - __builtin_clz(v);
+#endif
+    sym = 2 * nb + ((v >> (nb - 1)) & 1u);
+    nx = nb - 1;
+    xv = v & ((1u << nx) - 1);
+}
+__device__ __forceinline__ unsigned len_extra_bits(unsigned sym) { return (sym < 265 || sym == 285) ? 0u : (sym - 261) / 4; }
+__device__ __forceinline__ unsigned dist_extra_bits(unsigned d) { return d < 4 ? 0u : d / 2 - 1; }
+
+// ---- match finding and parsing --------------------------------------------------------------
+// src must have n + 8 readable bytes (4-byte aligned); tokens: DF_CHUNK per chunk
+__global__ void __launch_bounds__(32 * DF_WARPS) k_lz(const unsigned *__restrict__ src, long long n, int nchunks,
+                                                      unsigned *__restrict__ tokens, DfInfo *__restrict__ info,
+                                                      unsigned *__restrict__ ghist) {
+    extern __shared__ unsigned short sm_ht[];   // DF_WARPS hash tables of DF_HSIZE chunk offsets
+    __shared__ unsigned hist_s[DF_WARPS][DF_NSYM];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chunk = blockIdx.x * DF_WARPS + warp;
+    if (chunk >= nchunks) return;   // whole warp; no block barrier below
+    unsigned short *ht = sm_ht + warp * DF_HSIZE;
+    unsigned *hist = hist_s[warp];
+    for (int i = lane; i < DF_HSIZE; i += 32) ht[i] = 0xFFFFu;
+    for (int i = lane; i < DF_NSYM; i += 32) hist[i] = 0;
+    __syncwarp();
+    const long long c0 = (long long)chunk * DF_CHUNK;
+    const int len_c = (int)min((long long)DF_CHUNK, n - c0);
+    unsigned *tok = tokens + (size_t)chunk * DF_CHUNK;
+    const unsigned lt = (1u << lane) - 1;
+    int next = 0, ntk = 0;
+    for (int t0 = 0; t0 < len_c; t0 += 32) {
+        const int o = t0 + lane;
+        const bool in = o < len_c, valid = o + 4 <= len_c;
+        const unsigned w4 = in ? load4(src, c0 + o) : 0u;
+        const unsigned h = valid ? (w4 * 2654435761u) >> (32 - DF_HBITS) : (0x10000u | (unsigned)lane);
+        const unsigned same = __match_any_sync(0xffffffffu, h);
+        int cand = -1;
+        if (valid) {
+            const unsigned lower = same & lt;
+            if (lower) cand = t0 + 31 - __clz(lower);
+            else if (ht[h] != 0xFFFFu) cand = ht[h];
+        }
+        __syncwarp();
+        if (valid && (same >> lane) == 1u) ht[h] = (unsigned short)o;   // the last lane of each hash
+        int mlen = 0, mdist = 0;
+        if (valid) {
+            const int maxl = min(DF_MAXLEN, len_c - o);
+            if (cand >= 0 && load4(src, c0 + cand) == w4) {
+                mlen = match_len(src, c0 + o, c0 + cand, maxl);
+                mdist = o - cand;
+            }
+        }
+        // greedy parse with one-step lazy evaluation over the match starts of this tile
+        const unsigned mm = __ballot_sync(0xffffffffu, mlen >= 4);
+        const unsigned tmask = (len_c - t0 >= 32) ? 0xffffffffu : ((1u << (len_c - t0)) - 1);
+        unsigned lit = 0, mat = 0;
+        int pos = next - t0;
+        while (pos < 32) {
+            const unsigned rest = mm & (0xffffffffu << pos);
+            if (!rest) {
+                lit |= 0xffffffffu << pos;
+                pos = 32;
+                break;
+            }
+            const int q = __ffs(rest) - 1;
+            lit |= ((1u << q) - 1) & (0xffffffffu << pos);
+            const int lq = __shfl_sync(0xffffffffu, mlen, q);
+            const int lq1 = __shfl_sync(0xffffffffu, mlen, (q + 1) & 31);
+            if (q < 31 && lq1 > lq) {
+                lit |= 1u << q;
+                pos = q + 1;
+                continue;
+            }
+            mat |= 1u << q;
+            pos = q + lq;
+        }
+        next = t0 + pos;
+        lit &= tmask;
+        const unsigned all = lit | mat;
+        if ((all >> lane) & 1u) {
+            unsigned t;
+            if ((mat >> lane) & 1u) {
+                t = 0x80000000u | ((unsigned)(mlen - 3) << 15) | (unsigned)(mdist - 1);
+                unsigned sym, nx, xv;
+                len_code((unsigned)mlen, sym, nx, xv);
+                atomicAdd(&hist[sym], 1u);
+                dist_code((unsigned)mdist, sym, nx, xv);
+                atomicAdd(&hist[DF_NLIT + sym], 1u);
+            } else {
+                t = w4 & 0xFFu;
+                atomicAdd(&hist[t], 1u);
+            }
+            tok[ntk + __popc(all & lt)] = t;
+        }
+        ntk += __popc(all);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        hist[256] += 1;   // end of block
+        info[chunk].ntok = (unsigned)ntk;
+        info[chunk].len = (unsigned)max(len_c, 0);
+    }
+    __syncwarp();
+    for (int i = lane; i < DF_NSYM; i += 32) ghist[(size_t)chunk * DF_NSYM + i] = hist[i];
+}
+
+// ---- per-chunk Huffman codes ----------------------------------------------------------------
+struct HuffScratch {
+    unsigned keys[512];                 // sort keys: frequency << 9 | symbol
+    unsigned w[2 * DF_NLIT];            // internal node weights (nodes m .. 2m-2)
+    unsigned short par[2 * DF_NLIT];    // parent of every node
+    unsigned char dep[2 * DF_NLIT];
+    unsigned freq[DF_NSYM];             // histogram (phantom symbols added for the code construction)
+    unsigned char len[DF_NSYM];         // code lengths: literal/length 0..285, distance 286..315
+    unsigned code[DF_NSYM];             // bit-reversed code | length << 16
+    unsigned short rle[DF_NSYM];        // code-length symbols: symbol | extra value << 5
+    unsigned clf[19], clc[19];
+    unsigned char cll[19];
+    unsigned hdr[DF_HDR_WORDS];
+};
+
+// warp-wide bitonic sort of keys[0, n), n a power of two
+__device__ void warp_sort(unsigned *keys, int n, int lane) {
+    for (int k = 2; k <= n; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < n; i += 32) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned a = keys[i], b = keys[l];
+                    if ((a > b) == ((i & k) == 0)) {
+                        keys[i] = b;
+                        keys[l] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+}
+
+// Huffman code lengths (<= limit) of f[0, nsym) into L[0, nsym); at least two
+// symbols of f must be nonzero.  Frequencies are halved until the tree fits.
+__device__ void build_lengths(HuffScratch &S, const unsigned *f, int nsym, int limit, unsigned char *L, int lane) {
+    const int padn = nsym <= 32 ? 32 : 512;
+    for (int shift = 0;; shift++) {
+        for (int i = lane; i < padn; i += 32) {
+            unsigned k = 0xFFFFFFFFu;
+            if (i < nsym && f[i]) k = ((shift ? ((f[i] >> shift) | 1u) : f[i]) << 9) | (unsigned)i;
+            S.keys[i] = k;
+        }
+        __syncwarp();
+        warp_sort(S.keys, padn, lane);
+        int ok = 1;
+        if (lane == 0) {
+            int m = 0;
+            while (m < padn && S.keys[m] != 0xFFFFFFFFu) m++;
+            // two queues: sorted leaves 0..m-1 and internal nodes m.. in creation order
+            int li = 0, ii = m, ni = m;
+            for (int k = 0; k < m - 1; k++) {
+                int ab[2];
+                unsigned wab[2];
+                for (int t = 0; t < 2; t++) {
+                    if (li < m && (ii >= ni || (S.keys[li] >> 9) <= S.w[ii])) {
+                        ab[t] = li;
+                        wab[t] = S.keys[li] >> 9;
+                        li++;
+                    } else {
+                        ab[t] = ii;
+                        wab[t] = S.w[ii];
+                        ii++;
+                    }
+                }
+                S.w[ni] = wab[0] + wab[1];
+                S.par[ab[0]] = (unsigned short)ni;
+                S.par[ab[1]] = (unsigned short)ni;
+                ni++;
+            }
+            const int root = 2 * m - 2;
+            S.dep[root] = 0;
+            int maxd = 0;
+            for (int j = root - 1; j >= 0; j--) {
+                S.dep[j] = S.dep[S.par[j]] + 1;
+                if (j < m && S.dep[j] > maxd) maxd = S.dep[j];
+            }
+            ok = maxd <= limit;
+            if (ok) {
+                for (int i = 0; i < nsym; i++) L[i] = 0;
+                for (int i = 0; i < m; i++) L[S.keys[i] & 511u] = S.dep[i];
+            }
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        __syncwarp();
+        if (ok) return;
+    }
+}
+
+// canonical codes (RFC 1951 3.2.2), stored bit-reversed for LSB-first output
+__device__ void assign_codes(const unsigned char *L, unsigned *code, int nsym) {
+    unsigned blc[16] = {0}, nc[16];
+    for (int s = 0; s < nsym; s++) blc[L[s]]++;
+    blc[0] = 0;
+    unsigned c = 0;
+    for (int b = 1; b < 16; b++) {
+        c = (c + blc[b - 1]) << 1;
+        nc[b] = c;
+    }
+    for (int s = 0; s < nsym; s++) {
+        const unsigned l = L[s];
+        code[s] = l ? ((__brev(nc[l]++) >> (32 - l)) | (l << 16)) : 0u;
+    }
+}
+
+struct BitSink {
+    unsigned *buf;
+    unsigned pos;
+    __device__ void put(unsigned v, unsigned nb) {   // nb <= 25
+        if (!nb) return;
+        const unsigned wi = pos >> 5, sh = pos & 31;
+        buf[wi] |= v << sh;
+        if (sh + nb > 32) buf[wi + 1] |= v >> (32 - sh);
+        pos += nb;
+    }
+};
+
+__constant__ unsigned char c_clorder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+
+__global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restrict__ ghist, int nchunks,
+                                                        DfInfo *__restrict__ info, unsigned *__restrict__ gcodes,
+                                                        unsigned *__restrict__ ghdr, unsigned *__restrict__ sizes) {
+    __shared__ HuffScratch sc[DF_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chunk = blockIdx.x * DF_WARPS + warp;
+    if (chunk >= nchunks) return;
+    HuffScratch &S = sc[warp];
+    const bool last = chunk == nchunks - 1;
+    for (int i = lane; i < DF_NSYM; i += 32) S.freq[i] = i < DF_NLIT + DF_NDIST ? ghist[(size_t)chunk * DF_NSYM + i] : 0u;
+    for (int i = lane; i < DF_HDR_WORDS; i += 32) S.hdr[i] = 0;
+    __syncwarp();
+    if (lane == 0) {
+        // every code needs two symbols: phantoms 0/1 where the block uses fewer
+        int used = 0;
+        for (int i = 0; i < DF_NLIT; i++) used += S.freq[i] != 0;
+        for (int i = 0; used < 2; i++)
+            if (!S.freq[i]) S.freq[i] = 1, used++;
+        used = 0;
+        for (int i = 0; i < DF_NDIST; i++) used += S.freq[DF_NLIT + i] != 0;
+        for (int i = 0; used < 2; i++)
+            if (!S.freq[DF_NLIT + i]) S.freq[DF_NLIT + i] = 1, used++;
+    }
+    __syncwarp();
+    build_lengths(S, S.freq, DF_NLIT, 15, S.len, lane);
+    build_lengths(S, S.freq + DF_NLIT, DF_NDIST, 15, S.len + DF_NLIT, lane);
+    int ncl = 0;
+    if (lane == 0) {
+        assign_codes(S.len, S.code, DF_NLIT);
+        assign_codes(S.len + DF_NLIT, S.code + DF_NLIT, DF_NDIST);
+        int hlit = DF_NLIT, hdist = DF_NDIST;
+        while (hlit > 257 && !S.len[hlit - 1]) hlit--;
+        while (hdist > 1 && !S.len[DF_NLIT + hdist - 1]) hdist--;
+        // run-length code of the code lengths (runs may cross from literal/length to distance)
+        const int total = hlit + hdist;
+        int nr = 0;
+        for (int i = 0; i < total;) {
+            const unsigned v = i < hlit ? S.len[i] : S.len[DF_NLIT + i - hlit];
+            int run = 1;
+            while (i + run < total && (i + run < hlit ? S.len[i + run] : S.len[DF_NLIT + i + run - hlit]) == v) run++;
+            int r = run;
+            if (v == 0) {
+                while (r >= 11) {
+                    const int c = min(r, 138);
+                    S.rle[nr++] = (unsigned short)(18 | (c - 11) << 5);
+                    r -= c;
+                }
+                if (r >= 3) {
+                    S.rle[nr++] = (unsigned short)(17 | (r - 3) << 5);
+                    r = 0;
+                }
+                while (r-- > 0) S.rle[nr++] = 0;
+            } else {
+                S.rle[nr++] = (unsigned short)v;
+                r--;
+                while (r >= 3) {
+                    const int c = min(r, 6);
+                    S.rle[nr++] = (unsigned short)(16 | (c - 3) << 5);
+                    r -= c;
+                }
+                while (r-- > 0) S.rle[nr++] = (unsigned short)v;
+            }
+            i += run;
+        }
+        for (int i = 0; i < 19; i++) S.clf[i] = 0;
+        for (int i = 0; i < nr; i++) S.clf[S.rle[i] & 31]++;
+        int used = 0;
+        for (int i = 0; i < 19; i++) used += S.clf[i] != 0;
+        for (int i = 0; used < 2; i++)
+            if (!S.clf[i]) S.clf[i] = 1, used++;
+        S.keys[0] = (unsigned)hlit;   // handed to the other lanes' code below through shared memory
+        S.keys[1] = (unsigned)hdist;
+        S.keys[2] = (unsigned)nr;
+        ncl = 0;
+    }
+    __syncwarp();
+    const int hlit = (int)S.keys[0], hdist = (int)S.keys[1], nr = (int)S.keys[2];
+    __syncwarp();
+    build_lengths(S, S.clf, 19, 7, S.cll, lane);
+    if (lane == 0) {
+        assign_codes(S.cll, S.clc, 19);
+        ncl = 19;
+        while (ncl > 4 && !S.cll[c_clorder[ncl - 1]]) ncl--;
+        BitSink b{S.hdr, 0};
+        b.put(last ? 1u : 0u, 1);
+        b.put(2u, 2);   // BTYPE 10: dynamic Huffman codes
+        b.put((unsigned)(hlit - 257), 5);
+        b.put((unsigned)(hdist - 1), 5);
+        b.put((unsigned)(ncl - 4), 4);
+        for (int k = 0; k < ncl; k++) b.put(S.cll[c_clorder[k]], 3);
+        for (int i = 0; i < nr; i++) {
+            const unsigned sym = S.rle[i] & 31u, x = S.rle[i] >> 5;
+            b.put(S.clc[sym] & 0xFFFFu, S.clc[sym] >> 16);
+            if (sym == 16) b.put(x, 2);
+            else if (sym == 17) b.put(x, 3);
+            else if (sym == 18) b.put(x, 7);
+        }
+        // coded size with the real (not phantom) frequencies
+        unsigned long long bits = b.pos;
+        const unsigned *f = ghist + (size_t)chunk * DF_NSYM;
+        for (int s = 0; s < DF_NLIT; s++)
+            if (f[s]) bits += (unsigned long long)f[s] * (S.len[s] + (s > 256 ? len_extra_bits((unsigned)s) : 0u));
+        for (int d = 0; d < DF_NDIST; d++)
+            if (f[DF_NLIT + d]) bits += (unsigned long long)f[DF_NLIT + d] * (S.len[DF_NLIT + d] + dist_extra_bits((unsigned)d));
+        const unsigned long long dyn = last ? (bits + 7) / 8 : (bits + 3 + 7) / 8 + 4;
+        const unsigned len = info[chunk].len;
+        const unsigned long long st = 5ull + len;
+        const bool stored = st <= dyn;
+        info[chunk].hdr_bits = b.pos;
+        info[chunk].stored = stored;
+        sizes[chunk] = (unsigned)(stored ? st : dyn);
+    }
+    __syncwarp();
+    for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) gcodes[(size_t)chunk * DF_NSYM + i] = S.code[i];
+    for (int i = lane; i < DF_HDR_WORDS; i += 32) ghdr[(size_t)chunk * DF_HDR_WORDS + i] = S.hdr[i];
+}
+
+// ---- bit output -------------------------------------------------------------------------------
+constexpr int RING = 128;   // words; one put advances at most 32 * 57 bits
+
+// warp-wide: lane i appends v (nb <= 57 bits) after lanes < i; complete words go to dst as bytes
+// (never past lim, the planned size of the chunk)
+__device__ __forceinline__ void ring_put(unsigned *ring, unsigned &bp, unsigned &fw, unsigned long long v, unsigned nb,
+                                         unsigned char *__restrict__ dst, unsigned lim, int lane) {
+    unsigned x = nb;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, x, 31);
+    if (nb) {
+        const unsigned p = bp + x - nb, wi = p >> 5, sh = p & 31;
+        const unsigned long long vs = v << sh;
+        atomicOr(&ring[wi & (RING - 1)], (unsigned)vs);
+        if (sh + nb > 32) atomicOr(&ring[(wi + 1) & (RING - 1)], (unsigned)(vs >> 32));
+        if (sh + nb > 64) atomicOr(&ring[(wi + 2) & (RING - 1)], (unsigned)(v >> (64 - sh)));
+    }
+    bp += total;
+    __syncwarp();
+    const unsigned full = bp >> 5;
+    for (unsigned w = fw + lane; w < full; w += 32) {
+        const unsigned val = ring[w & (RING - 1)];
+        ring[w & (RING - 1)] = 0;
+        for (unsigned b = 0; b < 4; b++)
+            if (4 * w + b < lim) dst[4 * w + b] = (unsigned char)(val >> (8 * b));
+    }
+    fw = full;
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * DF_WARPS) k_emit(const unsigned char *__restrict__ src, const unsigned *__restrict__ tokens,
+                                                        const DfInfo *__restrict__ info, const unsigned *__restrict__ gcodes,
+                                                        const unsigned *__restrict__ ghdr, const unsigned *__restrict__ offs,
+                                                        int nchunks, unsigned char *__restrict__ out,
+                                                        unsigned *__restrict__ err) {
+    __shared__ unsigned ring_s[DF_WARPS][RING];
+    __shared__ unsigned code_s[DF_WARPS][DF_NLIT + DF_NDIST];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chunk = blockIdx.x * DF_WARPS + warp;
+    if (chunk >= nchunks) return;
+    const DfInfo I = info[chunk];
+    const bool last = chunk == nchunks - 1;
+    unsigned char *dst = out + offs[chunk];
+    const unsigned lim = offs[chunk + 1] - offs[chunk];   // planned size: no byte is written beyond it
+    const size_t c0 = (size_t)chunk * DF_CHUNK;
+    if (I.stored) {
+        if (lim != 5 + I.len) {
+            if (lane == 0) atomicOr(err, 1u);
+            return;
+        }
+        if (lane == 0) {
+            dst[0] = last ? 1 : 0;   // BFINAL, BTYPE 00, then padding to the byte
+            dst[1] = (unsigned char)I.len;
+            dst[2] = (unsigned char)(I.len >> 8);
+            dst[3] = (unsigned char)~I.len;
+            dst[4] = (unsigned char)(~I.len >> 8);
+        }
+        for (unsigned i = lane; i < I.len; i += 32) dst[5 + i] = src[c0 + i];
+        return;
+    }
+    unsigned *ring = ring_s[warp];
+    unsigned *code = code_s[warp];
+    for (int i = lane; i < RING; i += 32) ring[i] = 0;
+    for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) code[i] = gcodes[(size_t)chunk * DF_NSYM + i];
+    __syncwarp();
+    unsigned bp = 0, fw = 0;
+    const unsigned *hdr = ghdr + (size_t)chunk * DF_HDR_WORDS;
+    for (unsigned w0 = 0; w0 * 32 < I.hdr_bits; w0 += 32) {
+        const unsigned wi = w0 + lane;
+        unsigned nb = 0;
+        unsigned long long v = 0;
+        if (wi * 32 < I.hdr_bits) {
+            nb = min(32u, I.hdr_bits - wi * 32);
+            v = hdr[wi] & (nb == 32 ? 0xffffffffu : ((1u << nb) - 1));
+        }
+        ring_put(ring, bp, fw, v, nb, dst, lim, lane);
+    }
+    const unsigned *tok = tokens + c0;
+    for (unsigned t0 = 0; t0 < I.ntok; t0 += 32) {
+        unsigned nb = 0;
+        unsigned long long v = 0;
+        if (t0 + lane < I.ntok) {
+            const unsigned t = tok[t0 + lane];
+            if (t & 0x80000000u) {
+                unsigned ls, lx, lv, ds, dx, dv;
+                len_code(((t >> 15) & 0xFFu) + 3, ls, lx, lv);
+                dist_code((t & 0x7FFFu) + 1, ds, dx, dv);
+                const unsigned lc = code[ls], dc = code[DF_NLIT + ds];
+                const unsigned ll = lc >> 16, dl = dc >> 16;
+                v = (unsigned long long)(lc & 0xFFFFu) | ((unsigned long long)lv << ll) |
+                    ((unsigned long long)(dc & 0xFFFFu) << (ll + lx)) | ((unsigned long long)dv << (ll + lx + dl));
+                nb = ll + lx + dl + dx;
+            } else {
+                const unsigned c = code[t];
+                v = c & 0xFFFFu;
+                nb = c >> 16;
+            }
+        }
+        ring_put(ring, bp, fw, v, nb, dst, lim, lane);
+    }
+    {   // end of block; then the empty stored block that byte-aligns a non-final chunk
+        const unsigned c = code[256];
+        ring_put(ring, bp, fw, lane == 0 ? (c & 0xFFFFu) : 0ull, lane == 0 ? (c >> 16) : 0u, dst, lim, lane);
+        if (!last) {
+            ring_put(ring, bp, fw, 0ull, lane == 0 ? 3u : 0u, dst, lim, lane);
+            bp = (bp + 7) & ~7u;
+            ring_put(ring, bp, fw, lane == 0 ? 0xFFFF0000ull : 0ull, lane == 0 ? 32u : 0u, dst, lim, lane);
+        }
+    }
+    const unsigned nbytes = (bp + 7) >> 3;
+    for (unsigned w = fw + lane; w * 4 < nbytes; w += 32) {
+        const unsigned val = ring[w & (RING - 1)];
+        for (unsigned b = 0; b < 4 && 4 * w + b < nbytes && 4 * w + b < lim; b++)
+            dst[4 * w + b] = (unsigned char)(val >> (8 * b));
+    }
+    if (lane == 0 && nbytes != lim) atomicOr(err, 1u);
+}
+
+// ---- checksums ----------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned gf2_mul(unsigned a, unsigned b) {   // a*b mod the CRC-32 polynomial (reflected)
+    unsigned p = 0;
+#pragma unroll 4
+    for (int i = 0; i < 32; i++) {   // bit 31-i of a is the coefficient of x^i
+        if (a & (0x80000000u >> i)) p ^= b;
+        b = (b & 1u) ? (b >> 1) ^ CRC_POLY : b >> 1;
+    }
+    return p;
+}
+__device__ __forceinline__ unsigned gf2_xpow8(const unsigned *xp, unsigned long long n) {   // x^(8n) mod P
+    unsigned r = 0x80000000u;
+    for (int k = 0; n; k++, n >>= 1)
+        if (n & 1) r = gf2_mul(r, xp[k]);
+    return r;
+}
+
+// per 1 KB segment: CRC-32 (finalised) or the Adler sums (sum of bytes, sum of (len - i) * byte)
+__global__ void __launch_bounds__(256) k_seg(const unsigned *__restrict__ src, long long n, int adler,
+                                             unsigned *__restrict__ segv) {
+    __shared__ unsigned tab[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        unsigned c = (unsigned)i;
+        for (int k = 0; k < 8; k++) c = (c & 1u) ? (c >> 1) ^ CRC_POLY : c >> 1;
+        tab[i] = c;
+    }
+    __syncthreads();
+    const long long nseg = (n + DF_SEG - 1) / DF_SEG;
+    const long long seg = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (seg >= nseg) return;
+    const long long s0 = seg * DF_SEG;
+    const unsigned L = (unsigned)min((long long)DF_SEG, n - s0);
+    const unsigned *p = src + s0 / 4;
+    if (!adler) {
+        unsigned crc = 0xFFFFFFFFu;
+        for (unsigned i = 0; i < L; i += 4) {
+            const unsigned w = __ldg(p + i / 4);
+            for (unsigned b = 0; b < 4 && i + b < L; b++) crc = tab[(crc ^ (w >> (8 * b))) & 0xFFu] ^ (crc >> 8);
+        }
+        segv[seg] = ~crc;
+    } else {
+        unsigned s = 0, ws = 0;
+        for (unsigned i = 0; i < L; i += 4) {
+            const unsigned w = __ldg(p + i / 4);
+            for (unsigned b = 0; b < 4 && i + b < L; b++) {
+                const unsigned v = (w >> (8 * b)) & 0xFFu;
+                s += v;
+                ws += (L - i - b) * v;
+            }
+        }
+        segv[2 * seg] = s % ADLER_MOD;
+        segv[2 * seg + 1] = ws % ADLER_MOD;
+    }
+}
+
+// fold the segments: one block of 1024 threads; result -> *out
+__global__ void __launch_bounds__(1024) k_fold(const unsigned *__restrict__ segv, long long n, int adler,
+                                               unsigned *__restrict__ out) {
+    __shared__ unsigned xp[64];
+    __shared__ unsigned a_s[1024], b_s[1024];
+    __shared__ unsigned long long l_s[1024];
+    const int t = threadIdx.x;
+    if (t == 0) {
+        xp[0] = 0x00800000u;   // x^8
+        for (int k = 1; k < 64; k++) xp[k] = gf2_mul(xp[k - 1], xp[k - 1]);
+    }
+    __syncthreads();
+    const long long nseg = (n + DF_SEG - 1) / DF_SEG;
+    const long long per = (nseg + 1023) / 1024;
+    const long long s0 = min(nseg, t * per), s1 = min(nseg, s0 + per);
+    unsigned a = 0, b = 0;
+    unsigned long long len = 0;
+    const unsigned xseg = adler ? 0u : gf2_xpow8(xp, DF_SEG);
+    for (long long i = s0; i < s1; i++) {
+        const unsigned L = (unsigned)min((long long)DF_SEG, n - i * DF_SEG);
+        if (!adler) {
+            a = gf2_mul(a, L == DF_SEG ? xseg : gf2_xpow8(xp, L)) ^ segv[i];
+        } else {
+            const unsigned sy = segv[2 * i], wy = segv[2 * i + 1];
+            b = (unsigned)((b + (unsigned long long)(L % ADLER_MOD) * a + wy) % ADLER_MOD);
+            a = (a + sy) % ADLER_MOD;
+        }
+        len += L;
+    }
+    a_s[t] = a;
+    b_s[t] = b;
+    l_s[t] = len;
+    for (int st = 1; st < 1024; st <<= 1) {
+        __syncthreads();
+        if ((t % (2 * st)) == 0 && t + st < 1024) {
+            const unsigned ay = a_s[t + st], by = b_s[t + st];
+            const unsigned long long ly = l_s[t + st];
+            if (!adler) {
+                a_s[t] = gf2_mul(a_s[t], gf2_xpow8(xp, ly)) ^ ay;
+            } else {
+                b_s[t] = (unsigned)((b_s[t] + (ly % ADLER_MOD) * a_s[t] + by) % ADLER_MOD);
+                a_s[t] = (a_s[t] + ay) % ADLER_MOD;
+            }
+            l_s[t] += ly;
+        }
+    }
+    __syncthreads();
+    if (t == 0) {
+        if (!adler) *out = a_s[0];
+        else *out = (((unsigned)(((unsigned long long)n % ADLER_MOD + b_s[0]) % ADLER_MOD)) << 16) | ((1u + a_s[0]) % ADLER_MOD);
+    }
+}
+
+// container header and trailer around the stream of `body` bytes
+__global__ void k_wrap(unsigned char *out, int container, unsigned long long body, long long n,
+                       const unsigned *__restrict__ chk) {
+    if (threadIdx.x || blockIdx.x) return;
+    if (container == N2M_DEFLATE_GZIP) {
+        const unsigned char h[10] = {0x1f, 0x8b, 8, 0, 0, 0, 0, 0, 0, 3};   // no name, mtime 0, OS Unix (as gzopen writes)
+        for (int i = 0; i < 10; i++) out[i] = h[i];
+        unsigned char *t = out + 10 + body;
+        const unsigned c = *chk, sz = (unsigned)n;
+        for (int i = 0; i < 4; i++) t[i] = (unsigned char)(c >> (8 * i));
+        for (int i = 0; i < 4; i++) t[4 + i] = (unsigned char)(sz >> (8 * i));
+    } else if (container == N2M_DEFLATE_ZLIB) {
+        out[0] = 0x78;   // deflate, 32 KB window
+        out[1] = 0x9c;   // default level; (0x78 * 256 + 0x9c) % 31 == 0
+        unsigned char *t = out + 2 + body;
+        const unsigned c = *chk;
+        for (int i = 0; i < 4; i++) t[i] = (unsigned char)(c >> (24 - 8 * i));   // big-endian
+    }
+}
+}  // namespace
+
+size_t deflate_bound(size_t n) {
+    const size_t nchunks = n ? (n + DF_CHUNK - 1) / DF_CHUNK : 1;
+    return n + 5 * nchunks + 18;
+}
+
+n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWork &w, ScanWork &sw, cudaStream_t s,
+                          size_t *out_len) {
+    if (((uintptr_t)d_src & 3) || container < N2M_DEFLATE_RAW || container > N2M_DEFLATE_GZIP || n > 0x7fffffffull) {
+        n2m_set_error("deflate: bad arguments (source not 4-byte aligned, unknown container or more than 2^31-1 bytes)");
+        return N2M_ERR_BAD_ARGS;
+    }
+    const int nchunks = n ? (int)((n + DF_CHUNK - 1) / DF_CHUNK) : 1;
+    const long long nseg = (long long)((n + DF_SEG - 1) / DF_SEG);
+    CKS(w.tok.ensure((size_t)nchunks * DF_CHUNK * sizeof(unsigned)));
+    CKS(w.info.ensure((size_t)nchunks * sizeof(DfInfo)));
+    CKS(w.hist.ensure((size_t)nchunks * DF_NSYM * sizeof(unsigned)));
+    CKS(w.codes.ensure((size_t)nchunks * DF_NSYM * sizeof(unsigned)));
+    CKS(w.hdr.ensure((size_t)nchunks * DF_HDR_WORDS * sizeof(unsigned)));
+    CKS(w.sizes.ensure((size_t)(nchunks + 1) * sizeof(unsigned)));
+    CKS(w.seg.ensure((size_t)std::max<long long>(2 * nseg, 1) * sizeof(unsigned)));
+    CKS(w.misc.ensure(4 * sizeof(unsigned)));
+    unsigned *misc = w.misc.as<unsigned>();   // [0] checksum, [1] error flag
+    CK(cudaMemsetAsync(misc, 0, 4 * sizeof(unsigned), s));
+    const unsigned blocks = (unsigned)((nchunks + DF_WARPS - 1) / DF_WARPS);
+    const int smem = DF_WARPS * DF_HSIZE * (int)sizeof(unsigned short);
+    CK(cudaFuncSetAttribute(k_lz, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    k_lz<<<blocks, 32 * DF_WARPS, smem, s>>>((const unsigned *)d_src, (long long)n, nchunks, w.tok.as<unsigned>(),
+                                             w.info.as<DfInfo>(), w.hist.as<unsigned>());
+    N2M_COUNT();
+    CKL();
+    k_huff<<<blocks, 32 * DF_WARPS, 0, s>>>(w.hist.as<unsigned>(), nchunks, w.info.as<DfInfo>(), w.codes.as<unsigned>(),
+                                           w.hdr.as<unsigned>(), w.sizes.as<unsigned>());
+    N2M_COUNT();
+    CKL();
+    CKS(scan_u32(w.sizes.as<unsigned>(), (size_t)nchunks, w.sizes.as<unsigned>() + nchunks, sw, s));
+    const int adler = container == N2M_DEFLATE_ZLIB;
+    if (container != N2M_DEFLATE_RAW) {
+        if (nseg > 0) {
+            k_seg<<<(unsigned)((nseg + 255) / 256), 256, 0, s>>>((const unsigned *)d_src, (long long)n, adler,
+                                                                 w.seg.as<unsigned>());
+            N2M_COUNT();
+            CKL();
+        }
+        k_fold<<<1, 1024, 0, s>>>(w.seg.as<unsigned>(), (long long)n, adler, misc);
+        N2M_COUNT();
+        CKL();
+    }
+    unsigned body = 0;
+    CK(cudaMemcpyAsync(&body, w.sizes.as<unsigned>() + nchunks, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const size_t head = container == N2M_DEFLATE_GZIP ? 10 : container == N2M_DEFLATE_ZLIB ? 2 : 0;
+    const size_t tail = container == N2M_DEFLATE_GZIP ? 8 : container == N2M_DEFLATE_ZLIB ? 4 : 0;
+    const size_t total = head + body + tail;
+    CKS(w.out.ensure(total + 16));
+    unsigned char *out = w.out.as<unsigned char>();
+    k_emit<<<blocks, 32 * DF_WARPS, 0, s>>>((const unsigned char *)d_src, w.tok.as<unsigned>(), w.info.as<DfInfo>(),
+                                           w.codes.as<unsigned>(), w.hdr.as<unsigned>(), w.sizes.as<unsigned>(), nchunks,
+                                           out + head, misc + 1);
+    N2M_COUNT();
+    CKL();
+    if (container != N2M_DEFLATE_RAW) {
+        k_wrap<<<1, 1, 0, s>>>(out, container, body, (long long)n, misc);
+        N2M_COUNT();
+        CKL();
+    }
+    *out_len = total;
+    return N2M_OK;
+}
+
+n2m_status deflate_check(DeflateWork &w, cudaStream_t s) {
+    unsigned err = 0;
+    CK(cudaMemcpyAsync(&err, w.misc.as<unsigned>() + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (err) {
+        n2m_set_error("deflate: coded size differs from the planned size");
+        return N2M_ERR_INTERNAL;
+    }
+    return N2M_OK;
+}

@@ -114,6 +114,28 @@ int nifti_bytes_per_voxel(int datatype);
 n2m_status launch_cast(const void *d_raw, int datatype, float slope, float inter, long long n, float *d_out,
                        cudaStream_t s);
 
+// deflate.cu: gzip / zlib / raw deflate of n bytes at d_src (4-byte aligned, n + 8
+// readable bytes); the stream goes to w.out, its length to *out_len (synchronizes
+// once to size the output).  deflate_check reads back the emitter's self-check.
+struct DeflateWork {
+    DevBuf tok, info, hist, codes, hdr, sizes, seg, misc, out;
+};
+size_t deflate_bound(size_t n);
+n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWork &w, ScanWork &sw, cudaStream_t s,
+                          size_t *out_len);
+n2m_status deflate_check(DeflateWork &w, cudaStream_t s);
+
+// writers.cu: the bytes save_mesh() writes, assembled in device memory
+struct WriterWork {
+    DevBuf mt, mp, pack, pack2, lens, flag, out;
+    DeflateWork df;
+    void *host = nullptr;   // pinned staging for file writes
+    size_t host_cap = 0;
+};
+int mesh_format_of(const char *fnm);   // N2M_FMT_*, or -1 (save_mesh appends ".mz3")
+n2m_status encode_mesh_device(int format, const vec3i *d_t, const vec3d *d_p, int nt, int np, bool gz, WriterWork &w,
+                              ScanWork &sw, cudaStream_t s, const unsigned char **d_out, size_t *len);
+
 // isolevel.cu: setThreshold (Otsu on the robust range) of a device volume
 struct ThresholdWork {
     DevBuf buf, table;

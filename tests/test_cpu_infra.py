@@ -28,6 +28,23 @@ def test_exact_tap_sum_matches_double(tmp_path):
     assert float(frac) > 0.95
 
 
+def test_text_formatter_matches_printf(tmp_path):
+    """The device %g / %d formatter of the text mesh writers
+    (nii2mesh_gb300/csrc/fmt.cuh, compiled for the host) prints exactly what the
+    C library's printf prints (src/meshify.c:683-723 call fprintf "%g"): any bit
+    pattern, mesh coordinates, float grids, exact ties at the seventh digit,
+    powers of ten and their neighbours; its wide path on every value too."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    exe = tmp_path / "fmt_check"
+    subprocess.run([cxx, "-O2", "-ffp-contract=off", "-o", str(exe), str(ROOT / "tests/cpu_harness/fmt_check.cpp")],
+                   check=True)
+    out = subprocess.run([str(exe), "600000", "5"], capture_output=True, text=True)
+    cases, bad = out.stdout.split()[-2:]
+    assert out.returncode == 0 and int(bad) == 0 and int(cases) > 1000000, out.stdout
+
+
 def test_abi_exports_every_declared_symbol():
     """libn2m_gpu.so loads without a GPU and exports every entry point that
     include/n2m_gpu.h declares (no compute call is made)."""

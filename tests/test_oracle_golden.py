@@ -124,3 +124,25 @@ def test_oracle_vs_reference_random(oracle, seed):
             a, b = oracle.meshify(vol, 50.0, variant, *flags), ref.meshify(vol, 50.0, variant, *flags)
             ok, d, msg = mesh_equal(a, b, 0.0)
             assert ok, msg
+
+
+WRITER_EXTS = ["mz3", "gii", "inflated", "pial", "json", "off", "obj", "ply", "stl", "vtk", "xyz"]
+
+
+@pytest.mark.parametrize("case", ["sphere", "special", "empty"])
+def test_writers_match_reference(case):
+    """oracle/writers.py writes the reference's files (tests/golden/writers.npz,
+    made by the reference's own save_mesh): every format, with and without
+    isGz; compressed sections and the FreeSurfer time stamp compared after
+    normalisation; an unknown extension gets .mz3 appended."""
+    from oracle import writers as W
+    g = np.load(GOLD / "writers.npz")
+    t, p = g[f"tris_{case}"], g[f"pts_{case}"]
+    for ext in WRITER_EXTS:
+        for gz in (False, True):
+            want = g[f"{case}_{ext}{'_gz' if gz else ''}"].tobytes()
+            fmt = W.format_of(f"{case}.{ext}")
+            assert (fmt < 0) == (ext == "xyz")
+            got = W.encode(W.FMT_MZ3 if fmt < 0 else fmt, t, p, gz)
+            assert W.normalize(got) == W.normalize(want), (case, ext, gz)
+
