@@ -322,6 +322,70 @@ def threshold_metric(n2m, torch, reps=5):
     return out
 
 
+def writer_metric(n2m, torch, vol, reps=3):
+    """save_mesh of the 512^3 CT mesh as nii2mesh writes it by default (.mz3
+    gzip: quality 1 sets isGz, src/nii2mesh.c:350) and as OBJ text: the GPU
+    encode of the device-resident mesh (bytes left in device memory), the whole
+    n2m_save_mesh_device call (encode, readback, file write), and the CPU path
+    (zlib level 6 as gzopen uses / the %g restatement, one core) on a bounded
+    sample, scaled."""
+    import gzip
+    import tempfile
+    import zlib
+    from oracle import writers as W
+    dev = torch.cuda.current_device()
+    ctx = n2m.Context(dev)
+    d = torch.from_numpy(vol).cuda()
+    nz, ny, nx = vol.shape
+    dt, dp, nt, nv, _ = ctx.meshify_device(d.data_ptr(), (nx, ny, nz), ISO, n2m.MC33, True, False, False)
+    out = {"workload": "ct512 mesh (%d triangles, %d vertices) from the 512^3 meshify" % (nt, nv)}
+    tmp = tempfile.mkdtemp(prefix="n2m_bench_")
+    host = {}
+    for name, fmt, gz, ext in (("mz3_gz", n2m.FMT_MZ3, True, "mz3"), ("obj", n2m.FMT_OBJ, False, "obj")):
+        ctx.encode_mesh_to_device(fmt, dt, dp, nt, nv, gz)
+        te, ts = [], []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, nbytes = ctx.encode_mesh_to_device(fmt, dt, dp, nt, nv, gz)
+            torch.cuda.synchronize()
+            te.append(time.perf_counter() - t0)
+            path = os.path.join(tmp, "mesh." + ext)
+            t0 = time.perf_counter()
+            ctx.save_mesh_device(path, dt, dp, nt, nv, gz)
+            ts.append(time.perf_counter() - t0)
+        host[name] = open(path, "rb").read()
+        os.remove(path)
+        out[name] = {"encode_device_ms": round(1e3 * statistics.median(te), 3),
+                     "save_ms": round(1e3 * statistics.median(ts), 3), "bytes": int(nbytes)}
+    raw = ctx.encode_mesh_device(n2m.FMT_MZ3, dt, dp, nt, nv, False)
+    assert gzip.decompress(host["mz3_gz"]) == raw, "gzip mz3 does not decompress to the plain mz3"
+    out["mz3_gz"]["ratio"] = round(len(host["mz3_gz"]) / len(raw), 4)
+    # CPU: zlib level 6 on 24 MB of the body (scaled to the whole), and the ratio both get on that sample
+    sample = raw[: 24 << 20]
+    t0 = time.perf_counter()
+    zs = zlib.compress(sample, 6)
+    zt = time.perf_counter() - t0
+    keep = torch.frombuffer(bytearray(sample), dtype=torch.uint8).cuda()
+    ours = ctx.deflate_device(keep.data_ptr(), len(sample), n2m.DEFLATE_GZIP)
+    out["mz3_gz"]["cpu"] = {"ms_scaled": round(1e3 * zt * len(raw) / len(sample), 1), "cores": 1,
+                            "kind": "zlib level 6 (the reference's gzopen level)",
+                            "sample": "%d MB of the mz3 body (%.2f s)" % (len(sample) >> 20, zt),
+                            "zlib6_ratio_sample": round(len(zs) / len(sample), 4),
+                            "gpu_ratio_sample": round(len(ours) / len(sample), 4)}
+    # OBJ: the %g / %d restatement on 100k vertices + 200k triangles, scaled by lines
+    tris = np.frombuffer(raw, np.int32, 3 * nt, 16).reshape(nt, 3)
+    pts = np.frombuffer(raw, np.float32, 3 * nv, 16 + 12 * nt).reshape(nv, 3).astype(np.float64)
+    t0 = time.perf_counter()
+    W.obj(tris[:200000], pts[:100000])
+    ot = time.perf_counter() - t0
+    out["obj"]["cpu"] = {"ms_scaled": round(1e3 * ot * (nt + nv) / 300000, 1), "cores": 1, "kind": "port",
+                         "sample": "100k vertex + 200k triangle lines (%.2f s)" % ot}
+    ctx.close()
+    os.rmdir(tmp)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -331,6 +395,8 @@ def main():
     ap.add_argument("--profile", type=int, default=0, metavar="N",
                     help="profiling driver: two meshify calls on the CT-like workload at N^3 (same generator, "
                          "structure count scaled by volume), stage times printed; no bench line")
+    ap.add_argument("--profile-writer", type=int, default=0, metavar="N",
+                    help="profiling driver: mesh the N^3 CT-like volume, then encode it twice as .mz3 gzip and once as .obj")
     ap.add_argument("--profile-atlas", action="store_true",
                     help="profiling driver: two batched atlas calls on the 256^3 label workload; no bench line")
     a = ap.parse_args()
@@ -366,6 +432,20 @@ def main():
         torch.cuda.synchronize()
         print(json.dumps({"profile_atlas": 256, "meshes": ok, "vertices": nv, "triangles": nt,
                           "stage_ms": [round(x, 4) for x in rep["ms_stage"][:5]]}))
+        return
+    if a.profile_writer:
+        n = a.profile_writer
+        pv = synth.ct512(n=n, count=max(1, int(round(300 * (n / 512) ** 3))))
+        d = torch.from_numpy(pv).cuda()
+        ctx = n2m.Context(0)
+        dt, dp, nt, nv, _ = ctx.meshify_device(d.data_ptr(), (n, n, n), ISO, n2m.MC33, True, False, False)
+        res = {}
+        for fmt, gz in ((n2m.FMT_MZ3, True), (n2m.FMT_MZ3, True), (n2m.FMT_OBJ, False)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, nb = ctx.encode_mesh_to_device(fmt, dt, dp, nt, nv, gz)
+            res["mz3_gz" if gz else "obj"] = [nb, round(1e3 * (time.perf_counter() - t0), 3)]
+        print(json.dumps({"profile_writer": n, "triangles": nt, "vertices": nv, "bytes_ms": res}))
         return
     if a.profile:
         n = a.profile
@@ -456,6 +536,7 @@ def main():
     atl = atlas_metric(n2m, torch) if world == 1 else None
     thr = threshold_metric(n2m, torch) if world == 1 else None
     brn = brain_metric(n2m, torch) if world == 1 else None
+    wrt = writer_metric(n2m, torch, vol) if world == 1 else None
     line = {"metric": METRIC, "value": round(value, 4), "unit": "Gvox/s", "n_gpus": world, "steps": a.steps,
             "warmup": warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
@@ -463,7 +544,7 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU", "triangles": nt, "vertices": nv},
             "stage_ms": {n: round(v, 4) for n, v in zip(STAGE_NAMES, stage_ms)},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck,
-            "adjoint": adj, "atlas": atl, "threshold": thr, "brain": brn}
+            "adjoint": adj, "atlas": atl, "threshold": thr, "brain": brn, "writer": wrt}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

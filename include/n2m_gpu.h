@@ -213,6 +213,10 @@ n2m_status n2m_encode_mesh(n2m_context *ctx, int format, const vec3i *tris, cons
                            int is_gz, unsigned char **out, size_t *out_len);
 n2m_status n2m_encode_mesh_device(n2m_context *ctx, int format, const vec3i *d_tris, const vec3d *d_pts, int ntri,
                                   int npt, int is_gz, unsigned char **out, size_t *out_len);
+/* The same bytes left in context-owned device memory (*d_out, valid until the
+ * next call on ctx), for callers that send them on from the GPU. */
+n2m_status n2m_encode_mesh_to_device(n2m_context *ctx, int format, const vec3i *d_tris, const vec3d *d_pts, int ntri,
+                                     int npt, int is_gz, const unsigned char **d_out, size_t *out_len);
 /* save_mesh() with a status: host mesh, or a mesh already in device memory. */
 n2m_status n2m_save_mesh(n2m_context *ctx, const char *fnm, const vec3i *tris, const vec3d *pts, int ntri, int npt,
                          int is_gz);

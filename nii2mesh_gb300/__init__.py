@@ -217,6 +217,17 @@ class Context:
                    "n2m_encode_mesh_device")
         return self._bytes(out, n.value)
 
+    def encode_mesh_to_device(self, fmt, d_tris_ptr, d_pts_ptr, ntri, npt, gz=False):
+        """encode_mesh leaving the bytes in device memory (n2m_encode_mesh_to_device):
+        returns (device pointer, length), valid until the next call on this context."""
+        if isinstance(fmt, str):
+            fmt = mesh_format_of(fmt)
+        out, n = C.c_void_p(), C.c_size_t()
+        _lib.check(self._L.n2m_encode_mesh_to_device(self.h, int(fmt), C.c_void_p(d_tris_ptr), C.c_void_p(d_pts_ptr),
+                                                     int(ntri), int(npt), int(gz), C.byref(out), C.byref(n)),
+                   "n2m_encode_mesh_to_device")
+        return out.value, n.value
+
     def save_mesh(self, fnm, tris, pts, gz=False):
         """save_mesh() with a status (n2m_save_mesh)."""
         t = np.ascontiguousarray(tris, dtype=np.int32)

@@ -21,7 +21,7 @@ SYMBOLS = ["n2m_context_create", "n2m_context_destroy", "n2m_context_stream", "n
            "n2m_kernel_launches", "n2m_meshify_backward", "n2m_smooth_hc_noalloc", "n2m_atlas", "n2m_atlas_device",
            "setThreshold", "n2m_set_threshold", "n2m_set_threshold_device", "n2m_cast_voxels_device",
            "n2m_meshify_typed", "save_mesh", "n2m_mesh_format_of", "n2m_encode_mesh", "n2m_encode_mesh_device",
-           "n2m_save_mesh", "n2m_save_mesh_device", "n2m_deflate_device"]
+           "n2m_encode_mesh_to_device",           "n2m_save_mesh", "n2m_save_mesh_device", "n2m_deflate_device"]
 
 
 class vec3d(C.Structure):
@@ -109,6 +109,7 @@ def load(path=None):
     L.n2m_mesh_format_of.argtypes = [C.c_char_p]
     L.n2m_encode_mesh.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp), szp]
     L.n2m_encode_mesh_device.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp), szp]
+    L.n2m_encode_mesh_to_device.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp), szp]
     L.n2m_save_mesh.argtypes = [vp, C.c_char_p, vp, vp, C.c_int, C.c_int, C.c_int]
     L.n2m_save_mesh_device.argtypes = [vp, C.c_char_p, vp, vp, C.c_int, C.c_int, C.c_int]
     L.n2m_deflate_device.argtypes = [vp, vp, C.c_size_t, C.c_int, C.POINTER(vp), szp]

@@ -263,10 +263,9 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
                       &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->th.buf, &c->th.table,
-                      &c->wr.mt, &c->wr.mp, &c->wr.pack, &c->wr.pack2, &c->wr.lens, &c->wr.flag, &c->wr.out, &c->wr.df.tok,
-                      &c->wr.df.info, &c->wr.df.hist, &c->wr.df.codes, &c->wr.df.hdr, &c->wr.df.sizes, &c->wr.df.seg,
-                      &c->wr.df.misc, &c->wr.df.out};
+                      &c->wr.mt, &c->wr.mp, &c->wr.pack, &c->wr.pack2, &c->wr.lens, &c->wr.flag, &c->wr.out};
     for (DevBuf *b : bufs) b->release();
+    deflate_release(c->wr.df);
     if (c->aw.exec) cudaGraphExecDestroy((cudaGraphExec_t)c->aw.exec);
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->wr.host) cudaFreeHost(c->wr.host);
@@ -1363,6 +1362,16 @@ extern "C" n2m_status n2m_encode_mesh_device(n2m_context *c, int format, const v
     size_t len;
     CKS(encode_mesh_device(format, d_tris, d_pts, ntri, npt, is_gz != 0, c->wr, c->scan, c->stream, &d, &len));
     return to_malloc(c, d, len, out, out_len);
+}
+
+extern "C" n2m_status n2m_encode_mesh_to_device(n2m_context *c, int format, const vec3i *d_tris, const vec3d *d_pts,
+                                                int ntri, int npt, int is_gz, const unsigned char **d_out,
+                                                size_t *out_len) {
+    if (!c || !d_out || !out_len) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    CKS(encode_mesh_device(format, d_tris, d_pts, ntri, npt, is_gz != 0, c->wr, c->scan, c->stream, d_out, out_len));
+    CK(cudaStreamSynchronize(c->stream));
+    return N2M_OK;
 }
 
 extern "C" n2m_status n2m_encode_mesh(n2m_context *c, int format, const vec3i *tris, const vec3d *pts, int ntri,

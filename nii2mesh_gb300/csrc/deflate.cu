@@ -2,15 +2,16 @@
 // streams of a device buffer, for the mesh writers: save_mz3 writes its file
 // through gzopen/gzwrite (src/meshify.c:602-679) and save_gii zlib-compresses
 // each data array before base64 (src/meshify.c:863-873, 904-914).  zlib at its
-// default level does ~15 MB/s on one core; here the input is cut into 32 KB
-// chunks, each coded by one warp as one dynamic-Huffman block:
+// default level does ~15 MB/s on one core; here the input is cut into 16-32 KB
+// chunks (sized so that k_lz runs in one wave), each coded by one warp as one
+// dynamic-Huffman block:
 //
 //   k_lz        match finding and parsing.  A 4-byte hash table per warp in
-//               shared memory holds the most recent position of each hash from
-//               earlier 32-byte tiles; inside a tile the most recent earlier lane
-//               with the same hash comes from __match_any_sync (one candidate
-//               per position; on mesh bytes this lands within ~4 % of zlib's
-//               level-6 size).  The parse is greedy with one-step lazy
+//               shared memory holds the two most recent positions of each hash
+//               from earlier 32-byte tiles; inside a tile the most recent earlier
+//               lanes with the same hash come from __match_any_sync (two
+//               candidates per position; on mesh bytes this lands within ~5 %
+//               of zlib's level-6 size).  The parse is greedy with one-step lazy
 //               evaluation, walked over the tile's match-start ballot (one step
 //               per match, not per byte).  Emits 32-bit tokens and the block's
 //               symbol histogram.
@@ -20,20 +21,23 @@
 //   scan        chunk byte offsets (every chunk ends on a byte boundary: a
 //               non-final dynamic block is followed by an empty stored block, the
 //               "sync flush" of RFC 1951 3.2.4).
-//   k_emit      one warp per chunk writes its bits through a shared-memory ring
+//   k_bits      one warp per chunk writes its bits through a shared-memory ring
 //               of 32-bit words (shared atomics; no global atomics), flushed as
 //               bytes in order.
-//   k_seg/k_fold CRC-32 (gzip) or Adler-32 (zlib) of 1 KB segments, folded with
-//               the polynomial / modular concatenation rules.
+//   k_cksum     CRC-32 (gzip) or Adler-32 (zlib): every 1 KB segment's share of
+//               the checksum is independent (CRC-32 is linear over XOR), so
+//               threads reduce them with warp shuffles and one atomic per block.
 //
 // The compressed bytes differ from zlib's (different match search); the
 // decompressed bytes are identical, which is the parity the tests check.
 #include "n2m_internal.cuh"
 
 namespace {
-constexpr int DF_CHUNK = 32768;                  // input bytes per block
-constexpr int DF_HBITS = 13, DF_HSIZE = 1 << DF_HBITS;
-constexpr int DF_WARPS = 4;                      // chunks per CTA
+constexpr int DF_CHUNK_MIN = 16384, DF_CHUNK_MAX = 32768;   // input bytes per block (chosen per call)
+constexpr int DF_HBITS = 10, DF_HSIZE = 1 << DF_HBITS;   // hash buckets per chunk, two positions each
+constexpr int LZ_WARPS = 16;                     // chunks per CTA of k_lz (4.6 KB of shared memory each: 48 warps / SM)
+constexpr int DF_WARPS = 4;                      // chunks per CTA of k_huff
+constexpr int BITS_WARPS = 8;                    // chunks per CTA of k_bits
 constexpr int DF_MAXLEN = 258;
 constexpr int DF_NLIT = 286, DF_NDIST = 30, DF_NSYM = 320;   // histogram stride: 286 + 30, padded
 constexpr int DF_HDR_WORDS = 160;                // block header bits per chunk (<= 4498 used)
@@ -110,45 +114,68 @@ __device__ __forceinline__ unsigned len_extra_bits(unsigned sym) { return (sym <
 __device__ __forceinline__ unsigned dist_extra_bits(unsigned d) { return d < 4 ? 0u : d / 2 - 1; }
 
 // ---- match finding and parsing --------------------------------------------------------------
-// src must have n + 8 readable bytes (4-byte aligned); tokens: DF_CHUNK per chunk
-__global__ void __launch_bounds__(32 * DF_WARPS) k_lz(const unsigned *__restrict__ src, long long n, int nchunks,
-                                                      unsigned *__restrict__ tokens, DfInfo *__restrict__ info,
-                                                      unsigned *__restrict__ ghist) {
-    extern __shared__ unsigned short sm_ht[];   // DF_WARPS hash tables of DF_HSIZE chunk offsets
-    __shared__ unsigned hist_s[DF_WARPS][DF_NSYM];
+// src must have n + 8 readable bytes (4-byte aligned); chunks of ch bytes; tokens: ch per chunk.
+// Hash bucket: the chunk offsets of the two most recent positions with that hash
+// (newest in the low half, 0xFFFF = none).  Histogram: 16-bit counts in pairs.
+__global__ void __launch_bounds__(32 * LZ_WARPS, 3) k_lz(const unsigned *__restrict__ src, long long n, int nchunks,
+                                                         int ch, unsigned *__restrict__ tokens,
+                                                         DfInfo *__restrict__ info, unsigned *__restrict__ ghist) {
+    extern __shared__ unsigned sm_ht[];   // LZ_WARPS tables of DF_HSIZE buckets
+    __shared__ unsigned hist_s[LZ_WARPS][DF_NSYM / 2];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int chunk = blockIdx.x * DF_WARPS + warp;
+    const int chunk = blockIdx.x * LZ_WARPS + warp;
     if (chunk >= nchunks) return;   // whole warp; no block barrier below
-    unsigned short *ht = sm_ht + warp * DF_HSIZE;
+    unsigned *ht = sm_ht + warp * DF_HSIZE;
     unsigned *hist = hist_s[warp];
-    for (int i = lane; i < DF_HSIZE; i += 32) ht[i] = 0xFFFFu;
-    for (int i = lane; i < DF_NSYM; i += 32) hist[i] = 0;
+    for (int i = lane; i < DF_HSIZE; i += 32) ht[i] = 0xFFFFFFFFu;
+    for (int i = lane; i < DF_NSYM / 2; i += 32) hist[i] = 0;
     __syncwarp();
-    const long long c0 = (long long)chunk * DF_CHUNK;
-    const int len_c = (int)min((long long)DF_CHUNK, n - c0);
-    unsigned *tok = tokens + (size_t)chunk * DF_CHUNK;
+    const long long c0 = (long long)chunk * ch;
+    const int len_c = (int)min((long long)ch, n - c0);
+    unsigned *tok = tokens + (size_t)chunk * ch;
     const unsigned lt = (1u << lane) - 1;
     int next = 0, ntk = 0;
     for (int t0 = 0; t0 < len_c; t0 += 32) {
         const int o = t0 + lane;
         const bool in = o < len_c, valid = o + 4 <= len_c;
         const unsigned w4 = in ? load4(src, c0 + o) : 0u;
-        const unsigned h = valid ? (w4 * 2654435761u) >> (32 - DF_HBITS) : (0x10000u | (unsigned)lane);
+        const unsigned h = valid ? (w4 * 2654435761u) >> (32 - DF_HBITS) : (0x10000u | (unsigned)lane);   // lanes
+        // without 4 bytes get keys no hash can take
         const unsigned same = __match_any_sync(0xffffffffu, h);
-        int cand = -1;
+        // candidates, most recent first: earlier lanes of this tile with the same hash, then the bucket
+        const unsigned lower = same & lt;
+        int c1 = -1, c2 = -1;
+        unsigned bk = 0xFFFFFFFFu;
         if (valid) {
-            const unsigned lower = same & lt;
-            if (lower) cand = t0 + 31 - __clz(lower);
-            else if (ht[h] != 0xFFFFu) cand = ht[h];
+            bk = ht[h];
+            const int b0 = (bk & 0xFFFFu) != 0xFFFFu ? (int)(bk & 0xFFFFu) : -1;
+            const int b1 = (bk >> 16) != 0xFFFFu ? (int)(bk >> 16) : -1;
+            if (lower) {
+                const int q1 = 31 - __clz(lower);
+                c1 = t0 + q1;
+                const unsigned l2 = lower & ~(1u << q1);
+                c2 = l2 ? t0 + 31 - __clz(l2) : b0;
+            } else {
+                c1 = b0;
+                c2 = b1;
+            }
         }
         __syncwarp();
-        if (valid && (same >> lane) == 1u) ht[h] = (unsigned short)o;   // the last lane of each hash
+        if (valid && (same >> lane) == 1u)   // the last lane of each hash keeps itself and the one before
+            ht[h] = ((lower ? (unsigned)(t0 + 31 - __clz(lower)) : (bk & 0xFFFFu)) << 16) | (unsigned)o;
         int mlen = 0, mdist = 0;
         if (valid) {
             const int maxl = min(DF_MAXLEN, len_c - o);
-            if (cand >= 0 && load4(src, c0 + cand) == w4) {
-                mlen = match_len(src, c0 + o, c0 + cand, maxl);
-                mdist = o - cand;
+            if (c1 >= 0 && load4(src, c0 + c1) == w4) {
+                mlen = match_len(src, c0 + o, c0 + c1, maxl);
+                mdist = o - c1;
+            }
+            if (c2 >= 0 && mlen < maxl && load4(src, c0 + c2) == w4) {
+                const int l = match_len(src, c0 + o, c0 + c2, maxl);
+                if (l > mlen) {
+                    mlen = l;
+                    mdist = o - c2;
+                }
             }
         }
         // greedy parse with one-step lazy evaluation over the match starts of this tile
@@ -184,12 +211,13 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_lz(const unsigned *__restrict
                 t = 0x80000000u | ((unsigned)(mlen - 3) << 15) | (unsigned)(mdist - 1);
                 unsigned sym, nx, xv;
                 len_code((unsigned)mlen, sym, nx, xv);
-                atomicAdd(&hist[sym], 1u);
+                atomicAdd(&hist[sym >> 1], 1u << (16 * (sym & 1u)));
                 dist_code((unsigned)mdist, sym, nx, xv);
-                atomicAdd(&hist[DF_NLIT + sym], 1u);
+                sym += DF_NLIT;
+                atomicAdd(&hist[sym >> 1], 1u << (16 * (sym & 1u)));
             } else {
                 t = w4 & 0xFFu;
-                atomicAdd(&hist[t], 1u);
+                atomicAdd(&hist[t >> 1], 1u << (16 * (t & 1u)));
             }
             tok[ntk + __popc(all & lt)] = t;
         }
@@ -197,12 +225,11 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_lz(const unsigned *__restrict
     }
     __syncwarp();
     if (lane == 0) {
-        hist[256] += 1;   // end of block
         info[chunk].ntok = (unsigned)ntk;
         info[chunk].len = (unsigned)max(len_c, 0);
     }
-    __syncwarp();
-    for (int i = lane; i < DF_NSYM; i += 32) ghist[(size_t)chunk * DF_NSYM + i] = hist[i];
+    for (int i = lane; i < DF_NSYM; i += 32)   // unpacked; symbol 256 (end of block) once
+        ghist[(size_t)chunk * DF_NSYM + i] = ((hist[i >> 1] >> (16 * (i & 1))) & 0xFFFFu) + (i == 256 ? 1u : 0u);
 }
 
 // ---- per-chunk Huffman codes ----------------------------------------------------------------
@@ -217,6 +244,7 @@ struct HuffScratch {
     unsigned short rle[DF_NSYM];        // code-length symbols: symbol | extra value << 5
     unsigned clf[19], clc[19];
     unsigned char cll[19];
+    unsigned cnt[16];                   // codes per length, then the next code of each length
     unsigned hdr[DF_HDR_WORDS];
 };
 
@@ -250,9 +278,8 @@ __device__ void build_lengths(HuffScratch &S, const unsigned *f, int nsym, int l
         }
         __syncwarp();
         warp_sort(S.keys, padn, lane);
-        int ok = 1;
+        int ok = 1, m = 0;
         if (lane == 0) {
-            int m = 0;
             while (m < padn && S.keys[m] != 0xFFFFFFFFu) m++;
             // two queues: sorted leaves 0..m-1 and internal nodes m.. in creation order
             int li = 0, ii = m, ni = m;
@@ -283,30 +310,47 @@ __device__ void build_lengths(HuffScratch &S, const unsigned *f, int nsym, int l
                 if (j < m && S.dep[j] > maxd) maxd = S.dep[j];
             }
             ok = maxd <= limit;
-            if (ok) {
-                for (int i = 0; i < nsym; i++) L[i] = 0;
-                for (int i = 0; i < m; i++) L[S.keys[i] & 511u] = S.dep[i];
-            }
         }
         ok = __shfl_sync(0xffffffffu, ok, 0);
+        m = __shfl_sync(0xffffffffu, m, 0);
         __syncwarp();
-        if (ok) return;
+        if (ok) {
+            for (int i = lane; i < nsym; i += 32) L[i] = 0;
+            __syncwarp();
+            for (int i = lane; i < m; i += 32) L[S.keys[i] & 511u] = S.dep[i];
+            __syncwarp();
+            return;
+        }
     }
 }
 
-// canonical codes (RFC 1951 3.2.2), stored bit-reversed for LSB-first output
-__device__ void assign_codes(const unsigned char *L, unsigned *code, int nsym) {
-    unsigned blc[16] = {0}, nc[16];
-    for (int s = 0; s < nsym; s++) blc[L[s]]++;
-    blc[0] = 0;
-    unsigned c = 0;
-    for (int b = 1; b < 16; b++) {
-        c = (c + blc[b - 1]) << 1;
-        nc[b] = c;
+// canonical codes (RFC 1951 3.2.2), stored bit-reversed for LSB-first output; warp-wide:
+// a symbol's code is the first code of its length plus the number of smaller
+// symbols of that length (ranked 32 symbols at a time with __match_any_sync)
+__device__ void assign_codes(const unsigned char *L, unsigned *code, int nsym, unsigned *cnt, int lane) {
+    if (lane < 16) cnt[lane] = 0;
+    __syncwarp();
+    for (int s = lane; s < nsym; s += 32)
+        if (L[s]) atomicAdd(&cnt[L[s]], 1u);
+    __syncwarp();
+    if (lane == 0) {
+        unsigned c = 0, prev = 0;
+        for (int b = 1; b < 16; b++) {
+            c = (c + prev) << 1;
+            prev = cnt[b];
+            cnt[b] = c;
+        }
     }
-    for (int s = 0; s < nsym; s++) {
-        const unsigned l = L[s];
-        code[s] = l ? ((__brev(nc[l]++) >> (32 - l)) | (l << 16)) : 0u;
+    __syncwarp();
+    for (int base = 0; base < nsym; base += 32) {
+        const int sym = base + lane;
+        const unsigned l = sym < nsym ? L[sym] : 0u;
+        const unsigned peers = __match_any_sync(0xffffffffu, l);
+        const unsigned c = cnt[l] + __popc(peers & ((1u << lane) - 1));
+        if (sym < nsym) code[sym] = l ? ((__brev(c) >> (32 - l)) | (l << 16)) : 0u;
+        __syncwarp();
+        if (l && (peers >> lane) == 1u) cnt[l] += __popc(peers);   // the last lane of each length
+        __syncwarp();
     }
 }
 
@@ -351,9 +395,9 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restri
     build_lengths(S, S.freq, DF_NLIT, 15, S.len, lane);
     build_lengths(S, S.freq + DF_NLIT, DF_NDIST, 15, S.len + DF_NLIT, lane);
     int ncl = 0;
+    assign_codes(S.len, S.code, DF_NLIT, S.cnt, lane);
+    assign_codes(S.len + DF_NLIT, S.code + DF_NLIT, DF_NDIST, S.cnt, lane);
     if (lane == 0) {
-        assign_codes(S.len, S.code, DF_NLIT);
-        assign_codes(S.len + DF_NLIT, S.code + DF_NLIT, DF_NDIST);
         int hlit = DF_NLIT, hdist = DF_NDIST;
         while (hlit > 257 && !S.len[hlit - 1]) hlit--;
         while (hdist > 1 && !S.len[DF_NLIT + hdist - 1]) hdist--;
@@ -403,8 +447,8 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restri
     const int hlit = (int)S.keys[0], hdist = (int)S.keys[1], nr = (int)S.keys[2];
     __syncwarp();
     build_lengths(S, S.clf, 19, 7, S.cll, lane);
+    assign_codes(S.cll, S.clc, 19, S.cnt, lane);
     if (lane == 0) {
-        assign_codes(S.cll, S.clc, 19);
         ncl = 19;
         while (ncl > 4 && !S.cll[c_clorder[ncl - 1]]) ncl--;
         BitSink b{S.hdr, 0};
@@ -421,20 +465,30 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restri
             else if (sym == 17) b.put(x, 3);
             else if (sym == 18) b.put(x, 7);
         }
-        // coded size with the real (not phantom) frequencies
-        unsigned long long bits = b.pos;
+        S.keys[3] = b.pos;
+    }
+    __syncwarp();
+    {   // coded size with the real (not phantom) frequencies, summed over the lanes
         const unsigned *f = ghist + (size_t)chunk * DF_NSYM;
-        for (int s = 0; s < DF_NLIT; s++)
-            if (f[s]) bits += (unsigned long long)f[s] * (S.len[s] + (s > 256 ? len_extra_bits((unsigned)s) : 0u));
-        for (int d = 0; d < DF_NDIST; d++)
-            if (f[DF_NLIT + d]) bits += (unsigned long long)f[DF_NLIT + d] * (S.len[DF_NLIT + d] + dist_extra_bits((unsigned)d));
-        const unsigned long long dyn = last ? (bits + 7) / 8 : (bits + 3 + 7) / 8 + 4;
-        const unsigned len = info[chunk].len;
-        const unsigned long long st = 5ull + len;
-        const bool stored = st <= dyn;
-        info[chunk].hdr_bits = b.pos;
-        info[chunk].stored = stored;
-        sizes[chunk] = (unsigned)(stored ? st : dyn);
+        unsigned long long bits = 0;
+        for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) {
+            const unsigned fi = f[i];
+            if (fi)
+                bits += (unsigned long long)fi * (S.len[i] + (i < DF_NLIT ? (i > 256 ? len_extra_bits((unsigned)i) : 0u)
+                                                                          : dist_extra_bits((unsigned)(i - DF_NLIT))));
+        }
+        for (int d = 16; d > 0; d >>= 1) bits += __shfl_xor_sync(0xffffffffu, bits, d);
+        if (lane == 0) {
+            const unsigned hb = S.keys[3];
+            bits += hb;
+            const unsigned long long dyn = last ? (bits + 7) / 8 : (bits + 3 + 7) / 8 + 4;
+            const unsigned len = info[chunk].len;
+            const unsigned long long st = 5ull + len;
+            const bool stored = st <= dyn;
+            info[chunk].hdr_bits = hb;
+            info[chunk].stored = stored;
+            sizes[chunk] = (unsigned)(stored ? st : dyn);
+        }
     }
     __syncwarp();
     for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) gcodes[(size_t)chunk * DF_NSYM + i] = S.code[i];
@@ -475,21 +529,21 @@ __device__ __forceinline__ void ring_put(unsigned *ring, unsigned &bp, unsigned 
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(32 * DF_WARPS) k_emit(const unsigned char *__restrict__ src, const unsigned *__restrict__ tokens,
+__global__ void __launch_bounds__(32 * BITS_WARPS) k_bits(const unsigned char *__restrict__ src, const unsigned *__restrict__ tokens,
                                                         const DfInfo *__restrict__ info, const unsigned *__restrict__ gcodes,
                                                         const unsigned *__restrict__ ghdr, const unsigned *__restrict__ offs,
-                                                        int nchunks, unsigned char *__restrict__ out,
+                                                        int nchunks, int ch, unsigned char *__restrict__ out,
                                                         unsigned *__restrict__ err) {
-    __shared__ unsigned ring_s[DF_WARPS][RING];
-    __shared__ unsigned code_s[DF_WARPS][DF_NLIT + DF_NDIST];
+    __shared__ unsigned ring_s[BITS_WARPS][RING];
+    __shared__ unsigned code_s[BITS_WARPS][DF_NLIT + DF_NDIST];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int chunk = blockIdx.x * DF_WARPS + warp;
+    const int chunk = blockIdx.x * BITS_WARPS + warp;
     if (chunk >= nchunks) return;
     const DfInfo I = info[chunk];
     const bool last = chunk == nchunks - 1;
     unsigned char *dst = out + offs[chunk];
     const unsigned lim = offs[chunk + 1] - offs[chunk];   // planned size: no byte is written beyond it
-    const size_t c0 = (size_t)chunk * DF_CHUNK;
+    const size_t c0 = (size_t)chunk * ch;
     if (I.stored) {
         if (lim != 5 + I.len) {
             if (lane == 0) atomicOr(err, 1u);
@@ -523,11 +577,13 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_emit(const unsigned char *__r
         ring_put(ring, bp, fw, v, nb, dst, lim, lane);
     }
     const unsigned *tok = tokens + c0;
+    unsigned tnext = lane < I.ntok ? tok[lane] : 0u;   // the next group's tokens are loaded one group ahead
     for (unsigned t0 = 0; t0 < I.ntok; t0 += 32) {
         unsigned nb = 0;
         unsigned long long v = 0;
+        const unsigned t = tnext;
+        if (t0 + 32 + lane < I.ntok) tnext = tok[t0 + 32 + lane];
         if (t0 + lane < I.ntok) {
-            const unsigned t = tok[t0 + lane];
             if (t & 0x80000000u) {
                 unsigned ls, lx, lv, ds, dx, dv;
                 len_code(((t >> 15) & 0xFFu) + 3, ls, lx, lv);
@@ -573,128 +629,156 @@ __device__ __forceinline__ unsigned gf2_mul(unsigned a, unsigned b) {   // a*b m
     }
     return p;
 }
-__device__ __forceinline__ unsigned gf2_xpow8(const unsigned *xp, unsigned long long n) {   // x^(8n) mod P
-    unsigned r = 0x80000000u;
-    for (int k = 0; n; k++, n >>= 1)
-        if (n & 1) r = gf2_mul(r, xp[k]);
-    return r;
-}
 
-// per 1 KB segment: CRC-32 (finalised) or the Adler sums (sum of bytes, sum of (len - i) * byte)
-__global__ void __launch_bounds__(256) k_seg(const unsigned *__restrict__ src, long long n, int adler,
-                                             unsigned *__restrict__ segv) {
-    __shared__ unsigned tab[256];
+// Checksum of the whole input from independent 1 KB segments, one per thread:
+// CRC-32 is linear over XOR, crc(A1 .. Ak) = XOR_i crc(A_i) * x^(8 * bytes after A_i)
+// mod P; Adler-32's sums add up with the same weights (B gains, for every byte,
+// the number of bytes from it to the end).  Warp and block reductions, one
+// atomic per block into acc (CRC: acc[0] XOR; Adler: acc[0] += sum of bytes,
+// acc[1] += weighted sum).
+struct XPow {
+    unsigned p[40];   // x^(8 * 2^k) mod P
+};
+__global__ void __launch_bounds__(256) k_cksum(const unsigned *__restrict__ src, long long n, int adler, XPow xp,
+                                             unsigned long long *__restrict__ acc) {
+    // slicing-by-4 tables: tab[0] the byte table, tab[k][i] = tab[k-1][i] advanced by one zero byte
+    __shared__ unsigned tab[4][256];
+    __shared__ unsigned long long red[2][8];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
         unsigned c = (unsigned)i;
         for (int k = 0; k < 8; k++) c = (c & 1u) ? (c >> 1) ^ CRC_POLY : c >> 1;
-        tab[i] = c;
+        tab[0][i] = c;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        unsigned c = tab[0][i];
+        for (int k = 1; k < 4; k++) {
+            c = (c >> 8) ^ tab[0][c & 0xFFu];
+            tab[k][i] = c;
+        }
     }
     __syncthreads();
     const long long nseg = (n + DF_SEG - 1) / DF_SEG;
     const long long seg = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (seg >= nseg) return;
-    const long long s0 = seg * DF_SEG;
-    const unsigned L = (unsigned)min((long long)DF_SEG, n - s0);
-    const unsigned *p = src + s0 / 4;
-    if (!adler) {
-        unsigned crc = 0xFFFFFFFFu;
-        for (unsigned i = 0; i < L; i += 4) {
-            const unsigned w = __ldg(p + i / 4);
-            for (unsigned b = 0; b < 4 && i + b < L; b++) crc = tab[(crc ^ (w >> (8 * b))) & 0xFFu] ^ (crc >> 8);
+    unsigned long long a = 0, b = 0;
+    if (seg < nseg) {
+        const long long s0 = seg * DF_SEG;
+        const unsigned L = (unsigned)min((long long)DF_SEG, n - s0);
+        const unsigned long long after = (unsigned long long)(n - s0 - L);
+        const unsigned *p = src + s0 / 4;
+        if (!adler) {
+            unsigned crc = 0xFFFFFFFFu;
+            unsigned i = 0;
+            for (; i + 4 <= L; i += 4) {   // four bytes per step
+                const unsigned c = crc ^ __ldg(p + i / 4);
+                crc = tab[3][c & 0xFFu] ^ tab[2][(c >> 8) & 0xFFu] ^ tab[1][(c >> 16) & 0xFFu] ^ tab[0][c >> 24];
+            }
+            if (i < L) {   // the last 1-3 bytes of the input
+                const unsigned w = __ldg(p + i / 4);
+                for (unsigned k = 0; i + k < L; k++) crc = tab[0][(crc ^ (w >> (8 * k))) & 0xFFu] ^ (crc >> 8);
+            }
+            unsigned x = 0x80000000u;   // x^(8 after)
+            unsigned long long e = after;
+            for (int k = 0; e; k++, e >>= 1)
+                if (e & 1) x = gf2_mul(x, xp.p[k]);
+            a = gf2_mul(~crc, x);
+        } else {
+            unsigned sm = 0, ws = 0;
+            for (unsigned i = 0; i < L; i += 4) {
+                const unsigned w = __ldg(p + i / 4);
+                for (unsigned k = 0; k < 4 && i + k < L; k++) {
+                    const unsigned v = (w >> (8 * k)) & 0xFFu;
+                    sm += v;
+                    ws += (L - i - k) * v;
+                }
+            }
+            a = sm;
+            b = ws + (after % ADLER_MOD) * (unsigned long long)sm;
         }
-        segv[seg] = ~crc;
-    } else {
-        unsigned s = 0, ws = 0;
-        for (unsigned i = 0; i < L; i += 4) {
-            const unsigned w = __ldg(p + i / 4);
-            for (unsigned b = 0; b < 4 && i + b < L; b++) {
-                const unsigned v = (w >> (8 * b)) & 0xFFu;
-                s += v;
-                ws += (L - i - b) * v;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long oa = __shfl_xor_sync(0xffffffffu, a, d), ob = __shfl_xor_sync(0xffffffffu, b, d);
+        if (adler) {
+            a += oa;
+            b += ob;
+        } else {
+            a ^= oa;
+        }
+    }
+    if (lane == 0) {
+        red[0][warp] = a;
+        red[1][warp] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            if (adler) {
+                a += red[0][w];
+                b += red[1][w];
+            } else {
+                a ^= red[0][w];
             }
         }
-        segv[2 * seg] = s % ADLER_MOD;
-        segv[2 * seg + 1] = ws % ADLER_MOD;
+        if (adler) {
+            atomicAdd(acc, a);
+            atomicAdd(acc + 1, b);
+        } else {
+            atomicXor(acc, a);
+        }
     }
 }
 
-// fold the segments: one block of 1024 threads; result -> *out
-__global__ void __launch_bounds__(1024) k_fold(const unsigned *__restrict__ segv, long long n, int adler,
-                                               unsigned *__restrict__ out) {
-    __shared__ unsigned xp[64];
-    __shared__ unsigned a_s[1024], b_s[1024];
-    __shared__ unsigned long long l_s[1024];
-    const int t = threadIdx.x;
-    if (t == 0) {
-        xp[0] = 0x00800000u;   // x^8
-        for (int k = 1; k < 64; k++) xp[k] = gf2_mul(xp[k - 1], xp[k - 1]);
-    }
-    __syncthreads();
-    const long long nseg = (n + DF_SEG - 1) / DF_SEG;
-    const long long per = (nseg + 1023) / 1024;
-    const long long s0 = min(nseg, t * per), s1 = min(nseg, s0 + per);
-    unsigned a = 0, b = 0;
-    unsigned long long len = 0;
-    const unsigned xseg = adler ? 0u : gf2_xpow8(xp, DF_SEG);
-    for (long long i = s0; i < s1; i++) {
-        const unsigned L = (unsigned)min((long long)DF_SEG, n - i * DF_SEG);
-        if (!adler) {
-            a = gf2_mul(a, L == DF_SEG ? xseg : gf2_xpow8(xp, L)) ^ segv[i];
-        } else {
-            const unsigned sy = segv[2 * i], wy = segv[2 * i + 1];
-            b = (unsigned)((b + (unsigned long long)(L % ADLER_MOD) * a + wy) % ADLER_MOD);
-            a = (a + sy) % ADLER_MOD;
+XPow xpow_table() {   // host: x^(8 * 2^k) mod P by repeated squaring
+    auto mul = [](unsigned a, unsigned b) {
+        unsigned p = 0;
+        for (int i = 0; i < 32; i++) {
+            if (a & (0x80000000u >> i)) p ^= b;
+            b = (b & 1u) ? (b >> 1) ^ CRC_POLY : b >> 1;
         }
-        len += L;
-    }
-    a_s[t] = a;
-    b_s[t] = b;
-    l_s[t] = len;
-    for (int st = 1; st < 1024; st <<= 1) {
-        __syncthreads();
-        if ((t % (2 * st)) == 0 && t + st < 1024) {
-            const unsigned ay = a_s[t + st], by = b_s[t + st];
-            const unsigned long long ly = l_s[t + st];
-            if (!adler) {
-                a_s[t] = gf2_mul(a_s[t], gf2_xpow8(xp, ly)) ^ ay;
-            } else {
-                b_s[t] = (unsigned)((b_s[t] + (ly % ADLER_MOD) * a_s[t] + by) % ADLER_MOD);
-                a_s[t] = (a_s[t] + ay) % ADLER_MOD;
-            }
-            l_s[t] += ly;
-        }
-    }
-    __syncthreads();
-    if (t == 0) {
-        if (!adler) *out = a_s[0];
-        else *out = (((unsigned)(((unsigned long long)n % ADLER_MOD + b_s[0]) % ADLER_MOD)) << 16) | ((1u + a_s[0]) % ADLER_MOD);
-    }
+        return p;
+    };
+    XPow t;
+    t.p[0] = 0x00800000u;   // x^8
+    for (int k = 1; k < 40; k++) t.p[k] = mul(t.p[k - 1], t.p[k - 1]);
+    return t;
 }
 
 // container header and trailer around the stream of `body` bytes
 __global__ void k_wrap(unsigned char *out, int container, unsigned long long body, long long n,
-                       const unsigned *__restrict__ chk) {
+                       const unsigned long long *__restrict__ acc) {
     if (threadIdx.x || blockIdx.x) return;
     if (container == N2M_DEFLATE_GZIP) {
         const unsigned char h[10] = {0x1f, 0x8b, 8, 0, 0, 0, 0, 0, 0, 3};   // no name, mtime 0, OS Unix (as gzopen writes)
         for (int i = 0; i < 10; i++) out[i] = h[i];
         unsigned char *t = out + 10 + body;
-        const unsigned c = *chk, sz = (unsigned)n;
+        const unsigned c = (unsigned)acc[0], sz = (unsigned)n;
         for (int i = 0; i < 4; i++) t[i] = (unsigned char)(c >> (8 * i));
         for (int i = 0; i < 4; i++) t[4 + i] = (unsigned char)(sz >> (8 * i));
     } else if (container == N2M_DEFLATE_ZLIB) {
         out[0] = 0x78;   // deflate, 32 KB window
         out[1] = 0x9c;   // default level; (0x78 * 256 + 0x9c) % 31 == 0
         unsigned char *t = out + 2 + body;
-        const unsigned c = *chk;
+        const unsigned A = (unsigned)((1ull + acc[0]) % ADLER_MOD);
+        const unsigned B = (unsigned)(((unsigned long long)n % ADLER_MOD + acc[1] % ADLER_MOD) % ADLER_MOD);
+        const unsigned c = (B << 16) | A;
         for (int i = 0; i < 4; i++) t[i] = (unsigned char)(c >> (24 - 8 * i));   // big-endian
     }
 }
 }  // namespace
 
 size_t deflate_bound(size_t n) {
-    const size_t nchunks = n ? (n + DF_CHUNK - 1) / DF_CHUNK : 1;
+    const size_t nchunks = n ? (n + DF_CHUNK_MIN - 1) / DF_CHUNK_MIN : 1;
     return n + 5 * nchunks + 18;
+}
+
+void deflate_release(DeflateWork &w) {
+    DevBuf *bufs[] = {&w.tok, &w.info, &w.hist, &w.codes, &w.hdr, &w.sizes, &w.misc, &w.out};
+    for (DevBuf *b : bufs) b->release();
+    if (w.side) cudaStreamDestroy((cudaStream_t)w.side);
+    if (w.ev_in) cudaEventDestroy((cudaEvent_t)w.ev_in);
+    if (w.ev_ck) cudaEventDestroy((cudaEvent_t)w.ev_ck);
+    w.side = w.ev_in = w.ev_ck = nullptr;
 }
 
 n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWork &w, ScanWork &sw, cudaStream_t s,
@@ -703,23 +787,51 @@ n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWor
         n2m_set_error("deflate: bad arguments (source not 4-byte aligned, unknown container or more than 2^31-1 bytes)");
         return N2M_ERR_BAD_ARGS;
     }
-    const int nchunks = n ? (int)((n + DF_CHUNK - 1) / DF_CHUNK) : 1;
+    const int smem = LZ_WARPS * DF_HSIZE * (int)sizeof(unsigned);
+    if (!w.lz_slots) {   // chunks k_lz keeps in flight on the whole GPU
+        int dev = 0, sms = 0, per_sm = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CK(cudaFuncSetAttribute(k_lz, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lz, 32 * LZ_WARPS, smem));
+        w.lz_slots = std::max(1, sms * per_sm * LZ_WARPS);
+        CK(cudaStreamCreateWithFlags((cudaStream_t *)&w.side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags((cudaEvent_t *)&w.ev_in, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags((cudaEvent_t *)&w.ev_ck, cudaEventDisableTiming));
+    }
+    // chunk size: the input in one wave of k_lz when 16-32 KB chunks allow it (every warp's
+    // time is set by its chunk's serial tile loop, so a second, partial wave costs nearly a full one)
+    size_t ch = (n + w.lz_slots - 1) / w.lz_slots;
+    ch = std::min<size_t>(DF_CHUNK_MAX, std::max<size_t>(DF_CHUNK_MIN, (ch + 4095) / 4096 * 4096));
+    const int nchunks = n ? (int)((n + ch - 1) / ch) : 1;
     const long long nseg = (long long)((n + DF_SEG - 1) / DF_SEG);
-    CKS(w.tok.ensure((size_t)nchunks * DF_CHUNK * sizeof(unsigned)));
+    CKS(w.tok.ensure((size_t)nchunks * ch * sizeof(unsigned)));
     CKS(w.info.ensure((size_t)nchunks * sizeof(DfInfo)));
     CKS(w.hist.ensure((size_t)nchunks * DF_NSYM * sizeof(unsigned)));
     CKS(w.codes.ensure((size_t)nchunks * DF_NSYM * sizeof(unsigned)));
     CKS(w.hdr.ensure((size_t)nchunks * DF_HDR_WORDS * sizeof(unsigned)));
     CKS(w.sizes.ensure((size_t)(nchunks + 1) * sizeof(unsigned)));
-    CKS(w.seg.ensure((size_t)std::max<long long>(2 * nseg, 1) * sizeof(unsigned)));
-    CKS(w.misc.ensure(4 * sizeof(unsigned)));
-    unsigned *misc = w.misc.as<unsigned>();   // [0] checksum, [1] error flag
-    CK(cudaMemsetAsync(misc, 0, 4 * sizeof(unsigned), s));
+    CKS(w.misc.ensure(4 * sizeof(unsigned long long)));
+    unsigned long long *acc = w.misc.as<unsigned long long>();   // [0], [1] checksum sums, [2] error flag
+    CK(cudaMemsetAsync(acc, 0, 4 * sizeof(unsigned long long), s));
+    // the checksum runs on the side stream next to k_lz (latency-bound, leaves bandwidth over)
+    const int adler = container == N2M_DEFLATE_ZLIB;
+    const bool cksum = container != N2M_DEFLATE_RAW && nseg > 0;
+    if (cksum) {
+        static const XPow xp = xpow_table();
+        CK(cudaEventRecord((cudaEvent_t)w.ev_in, s));
+        CK(cudaStreamWaitEvent((cudaStream_t)w.side, (cudaEvent_t)w.ev_in, 0));
+        k_cksum<<<(unsigned)((nseg + 255) / 256), 256, 0, (cudaStream_t)w.side>>>((const unsigned *)d_src, (long long)n,
+                                                                                adler, xp, acc);
+        N2M_COUNT();
+        CKL();
+        CK(cudaEventRecord((cudaEvent_t)w.ev_ck, (cudaStream_t)w.side));
+    }
     const unsigned blocks = (unsigned)((nchunks + DF_WARPS - 1) / DF_WARPS);
-    const int smem = DF_WARPS * DF_HSIZE * (int)sizeof(unsigned short);
     CK(cudaFuncSetAttribute(k_lz, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    k_lz<<<blocks, 32 * DF_WARPS, smem, s>>>((const unsigned *)d_src, (long long)n, nchunks, w.tok.as<unsigned>(),
-                                             w.info.as<DfInfo>(), w.hist.as<unsigned>());
+    k_lz<<<(unsigned)((nchunks + LZ_WARPS - 1) / LZ_WARPS), 32 * LZ_WARPS, smem, s>>>(
+        (const unsigned *)d_src, (long long)n, nchunks, (int)ch, w.tok.as<unsigned>(), w.info.as<DfInfo>(),
+        w.hist.as<unsigned>());
     N2M_COUNT();
     CKL();
     k_huff<<<blocks, 32 * DF_WARPS, 0, s>>>(w.hist.as<unsigned>(), nchunks, w.info.as<DfInfo>(), w.codes.as<unsigned>(),
@@ -727,18 +839,6 @@ n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWor
     N2M_COUNT();
     CKL();
     CKS(scan_u32(w.sizes.as<unsigned>(), (size_t)nchunks, w.sizes.as<unsigned>() + nchunks, sw, s));
-    const int adler = container == N2M_DEFLATE_ZLIB;
-    if (container != N2M_DEFLATE_RAW) {
-        if (nseg > 0) {
-            k_seg<<<(unsigned)((nseg + 255) / 256), 256, 0, s>>>((const unsigned *)d_src, (long long)n, adler,
-                                                                 w.seg.as<unsigned>());
-            N2M_COUNT();
-            CKL();
-        }
-        k_fold<<<1, 1024, 0, s>>>(w.seg.as<unsigned>(), (long long)n, adler, misc);
-        N2M_COUNT();
-        CKL();
-    }
     unsigned body = 0;
     CK(cudaMemcpyAsync(&body, w.sizes.as<unsigned>() + nchunks, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -747,13 +847,14 @@ n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWor
     const size_t total = head + body + tail;
     CKS(w.out.ensure(total + 16));
     unsigned char *out = w.out.as<unsigned char>();
-    k_emit<<<blocks, 32 * DF_WARPS, 0, s>>>((const unsigned char *)d_src, w.tok.as<unsigned>(), w.info.as<DfInfo>(),
-                                           w.codes.as<unsigned>(), w.hdr.as<unsigned>(), w.sizes.as<unsigned>(), nchunks,
-                                           out + head, misc + 1);
+    k_bits<<<(unsigned)((nchunks + BITS_WARPS - 1) / BITS_WARPS), 32 * BITS_WARPS, 0, s>>>(
+        (const unsigned char *)d_src, w.tok.as<unsigned>(), w.info.as<DfInfo>(), w.codes.as<unsigned>(),
+        w.hdr.as<unsigned>(), w.sizes.as<unsigned>(), nchunks, (int)ch, out + head, (unsigned *)(acc + 2));
     N2M_COUNT();
     CKL();
+    if (cksum) CK(cudaStreamWaitEvent(s, (cudaEvent_t)w.ev_ck, 0));
     if (container != N2M_DEFLATE_RAW) {
-        k_wrap<<<1, 1, 0, s>>>(out, container, body, (long long)n, misc);
+        k_wrap<<<1, 1, 0, s>>>(out, container, body, (long long)n, acc);
         N2M_COUNT();
         CKL();
     }
@@ -763,7 +864,7 @@ n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWor
 
 n2m_status deflate_check(DeflateWork &w, cudaStream_t s) {
     unsigned err = 0;
-    CK(cudaMemcpyAsync(&err, w.misc.as<unsigned>() + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&err, w.misc.as<unsigned long long>() + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (err) {
         n2m_set_error("deflate: coded size differs from the planned size");

@@ -118,9 +118,12 @@ n2m_status launch_cast(const void *d_raw, int datatype, float slope, float inter
 // readable bytes); the stream goes to w.out, its length to *out_len (synchronizes
 // once to size the output).  deflate_check reads back the emitter's self-check.
 struct DeflateWork {
-    DevBuf tok, info, hist, codes, hdr, sizes, seg, misc, out;
+    DevBuf tok, info, hist, codes, hdr, sizes, misc, out;
+    int lz_slots = 0;                                       // chunks the match finder keeps in flight
+    void *side = nullptr, *ev_in = nullptr, *ev_ck = nullptr;   // checksum stream and its events
 };
 size_t deflate_bound(size_t n);
+void deflate_release(DeflateWork &w);
 n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWork &w, ScanWork &sw, cudaStream_t s,
                           size_t *out_len);
 n2m_status deflate_check(DeflateWork &w, cudaStream_t s);
