@@ -47,55 +47,76 @@ N2M_HD inline int bitlen128(u128 x) {
     return lo ? 64 - clz64(lo) : 0;
 }
 
-// write the 6 significant digits D (10^5 <= D < 10^6) with decimal exponent X in %g style
-N2M_HD inline int emit_g6(unsigned D, int X, bool neg, char *out) {
-    char dg[6];
-    for (int i = 5; i >= 0; i--) {
-        dg[i] = (char)('0' + D % 10u);
+// character sinks: a char buffer, or 32-bit words of a 4-byte-aligned buffer
+// (no per-thread array, so the device formatter stays in registers)
+struct CharSink {
+    char *p;
+    int n = 0;
+    N2M_HD void put(char c) { p[n++] = c; }
+};
+struct WordSink {
+    unsigned *dst;
+    unsigned cur = 0;
+    int n = 0;
+    N2M_HD void put(char c) {
+        cur |= (unsigned)(unsigned char)c << (8 * (n & 3));
+        if ((n & 3) == 3) {
+            dst[n >> 2] = cur;
+            cur = 0;
+        }
+        ++n;
+    }
+    N2M_HD void done() {
+        if (n & 3) dst[n >> 2] = cur;
+    }
+};
+
+// the 6 significant digits D (10^5 <= D < 10^6) with decimal exponent X in %g style
+template <class S>
+N2M_HD inline void emit_g6(unsigned D, int X, bool neg, S &out) {
+    unsigned dg = 0;   // digit i (0 = most significant) in bits 4(5-i)..
+    for (int i = 0; i < 6; i++) {
+        dg |= (D % 10u) << (4 * i);
         D /= 10u;
     }
+    auto digit = [&](int i) { return (char)('0' + ((dg >> (4 * (5 - i))) & 15u)); };
     int nd = 6;   // significant digits after removing trailing zeros
-    while (nd > 1 && dg[nd - 1] == '0') nd--;
-    int n = 0;
-    if (neg) out[n++] = '-';
+    while (nd > 1 && ((dg >> (4 * (6 - nd))) & 15u) == 0) nd--;
+    if (neg) out.put('-');
     if (X >= -4 && X < 6) {
         if (X >= 0) {
-            for (int i = 0; i <= X; i++) out[n++] = dg[i];
+            for (int i = 0; i <= X; i++) out.put(digit(i));
             if (nd > X + 1) {
-                out[n++] = '.';
-                for (int i = X + 1; i < nd; i++) out[n++] = dg[i];
+                out.put('.');
+                for (int i = X + 1; i < nd; i++) out.put(digit(i));
             }
         } else {
-            out[n++] = '0';
-            out[n++] = '.';
-            for (int i = 0; i < -X - 1; i++) out[n++] = '0';
-            for (int i = 0; i < nd; i++) out[n++] = dg[i];
+            out.put('0');
+            out.put('.');
+            for (int i = 0; i < -X - 1; i++) out.put('0');
+            for (int i = 0; i < nd; i++) out.put(digit(i));
         }
     } else {
-        out[n++] = dg[0];
+        out.put(digit(0));
         if (nd > 1) {
-            out[n++] = '.';
-            for (int i = 1; i < nd; i++) out[n++] = dg[i];
+            out.put('.');
+            for (int i = 1; i < nd; i++) out.put(digit(i));
         }
-        out[n++] = 'e';
+        out.put('e');
         int ax = X;
         if (ax < 0) {
-            out[n++] = '-';
+            out.put('-');
             ax = -ax;
         } else {
-            out[n++] = '+';
+            out.put('+');
         }
         if (ax >= 100) {
-            out[n++] = (char)('0' + ax / 100);
+            out.put((char)('0' + ax / 100));
             ax %= 100;
-            out[n++] = (char)('0' + ax / 10);
-            out[n++] = (char)('0' + ax % 10);
-        } else {
-            out[n++] = (char)('0' + ax / 10);
-            out[n++] = (char)('0' + ax % 10);
         }
+        out.put((char)('0' + ax / 10));
+        out.put((char)('0' + ax % 10));
     }
-    return n;
 }
 
 // 6 significant digits of m * 2^e (m > 0) by exact expansion in base 10^9 (any double)
@@ -158,11 +179,22 @@ N2M_HD N2M_NOINLINE inline int fmt_g6_wide(unsigned long long m, int e, bool neg
             X++;
         }
     }
-    return emit_g6(D, X, neg, out);
+    CharSink cs{out};
+    emit_g6(D, X, neg, cs);
+    return cs.n;
 }
 
-// printf("%g", v); returns the length (at most 13)
-N2M_HD inline int fmt_g6(double v, char *out) {
+// the wide path through a sink (kept out of line: its limb array is only touched for rare values)
+template <class S>
+N2M_HD N2M_NOINLINE void fmt_g6_wide_to(unsigned long long m, int e, bool neg, S &out) {
+    char b[16];
+    const int n = fmt_g6_wide(m, e, neg, b);
+    for (int i = 0; i < n; i++) out.put(b[i]);
+}
+
+// printf("%g", v) into a sink (at most 13 characters)
+template <class S>
+N2M_HD inline void fmt_g6(double v, S &out) {
     unsigned long long bits;
 #ifdef __CUDA_ARCH__
     bits = (unsigned long long)__double_as_longlong(v);
@@ -172,51 +204,72 @@ N2M_HD inline int fmt_g6(double v, char *out) {
     const bool neg = bits >> 63;
     const int ex = (int)((bits >> 52) & 0x7FF);
     const unsigned long long fr = bits & ((1ull << 52) - 1);
-    int n = 0;
     if (ex == 0x7FF) {
-        if (neg) out[n++] = '-';
-        const char *s = fr ? "nan" : "inf";
-        for (int i = 0; i < 3; i++) out[n++] = s[i];
-        return n;
+        if (neg) out.put('-');
+        out.put(fr ? 'n' : 'i');
+        out.put(fr ? 'a' : 'n');
+        out.put(fr ? 'n' : 'f');
+        return;
     }
     if (ex == 0 && fr == 0) {
-        if (neg) out[n++] = '-';
-        out[n++] = '0';
-        return n;
+        if (neg) out.put('-');
+        out.put('0');
+        return;
     }
     const unsigned long long m = ex ? (fr | (1ull << 52)) : fr;
     const int e = (ex ? ex : 1) - 1075;
     const int E2 = e + (64 - clz64(m)) - 1;        // 2^E2 <= |v| < 2^(E2+1)
-    if (E2 < -56 || E2 > 119) return fmt_g6_wide(m, e, neg, out);
+    if (E2 < -56 || E2 > 119) {
+        fmt_g6_wide_to(m, e, neg, out);
+        return;
+    }
     int X = (E2 * 78913) >> 18;                     // floor(E2 * log10(2)): X or X-1 of the true exponent
     for (int iter = 0; iter < 3; iter++) {
         const int k = 5 - X;                        // scale by 10^k
         u128 T, R, half;                            // T = floor(|v| 10^k); fraction R / (2 half)
         bool exact_half_known = true;
         if (k >= 0) {
-            if (k > 22) return fmt_g6_wide(m, e, neg, out);
+            if (k > 22) {
+                fmt_g6_wide_to(m, e, neg, out);
+                return;
+            }
             const u128 N = (u128)m * pow10_128(k);
             if (e >= 0) {
-                if (bitlen128(N) + e > 127) return fmt_g6_wide(m, e, neg, out);
+                if (bitlen128(N) + e > 127) {
+                    fmt_g6_wide_to(m, e, neg, out);
+                    return;
+                }
                 T = N << e;
                 R = 0;
                 half = 1;
             } else {
                 const int s = -e;
-                if (s > 126) return fmt_g6_wide(m, e, neg, out);
+                if (s > 126) {
+                    fmt_g6_wide_to(m, e, neg, out);
+                    return;
+                }
                 T = N >> s;
                 R = N & ((((u128)1) << s) - 1);
                 half = ((u128)1) << (s - 1);
             }
         } else {
             const int j = -k;
-            if (j > 37) return fmt_g6_wide(m, e, neg, out);
+            if (j > 37) {
+                fmt_g6_wide_to(m, e, neg, out);
+                return;
+            }
             u128 M = m, Dv = pow10_128(j);
             if (e >= 0) {
-                if (64 - clz64(m) + e > 127) return fmt_g6_wide(m, e, neg, out);
+                if (64 - clz64(m) + e > 127) {
+                    fmt_g6_wide_to(m, e, neg, out);
+                    return;
+                }
                 M = M << e;
             } else {
-                if (bitlen128(Dv) + (-e) > 126) return fmt_g6_wide(m, e, neg, out);
+                if (bitlen128(Dv) + (-e) > 126) {
+                    fmt_g6_wide_to(m, e, neg, out);
+                    return;
+                }
                 Dv = Dv << (-e);
             }
             T = M / Dv;
@@ -242,23 +295,36 @@ N2M_HD inline int fmt_g6(double v, char *out) {
             D = 100000u;
             X++;
         }
-        return emit_g6(D, X, neg, out);
+        emit_g6(D, X, neg, out);
+        return;
     }
-    return fmt_g6_wide(m, e, neg, out);
+    fmt_g6_wide_to(m, e, neg, out);
 }
 
-// printf("%d", v)
-N2M_HD inline int fmt_d(int v, char *out) {
-    char t[11];
-    int n = 0, k = 0;
+// printf("%d", v) into a sink
+template <class S>
+N2M_HD inline void fmt_d(int v, S &out) {
     unsigned u = v < 0 ? 0u - (unsigned)v : (unsigned)v;
-    if (v < 0) out[n++] = '-';
+    if (v < 0) out.put('-');
+    unsigned long long dg = 0;   // decimal digits, 4 bits each, least significant first
+    int k = 0;
     do {
-        t[k++] = (char)('0' + u % 10u);
+        dg |= (unsigned long long)(u % 10u) << (4 * k++);
         u /= 10u;
     } while (u);
-    while (k) out[n++] = t[--k];
-    return n;
+    while (k) out.put((char)('0' + ((dg >> (4 * --k)) & 15u)));
+}
+
+// char-buffer forms (return the length)
+N2M_HD inline int fmt_g6(double v, char *out) {
+    CharSink cs{out};
+    fmt_g6(v, cs);
+    return cs.n;
+}
+N2M_HD inline int fmt_d(int v, char *out) {
+    CharSink cs{out};
+    fmt_d(v, cs);
+    return cs.n;
 }
 
 }  // namespace n2mfmt

@@ -8,7 +8,7 @@
 // Binary sections are packed by one thread per vertex / triangle straight
 // from the ABI mesh (vec3d -> float32 rounded to nearest, byte-swapped where
 // the reference swaps); text lines (%g / %d) are formatted one thread per
-// line into 48-byte slots, scanned and compacted.
+// line, in registers, into 48-byte slots, then scanned and compacted by warps.
 #include <string.h>
 #include <time.h>
 
@@ -103,56 +103,78 @@ __global__ void k_base64(const unsigned char *__restrict__ in, long long n, unsi
     o[3] = i + 2 < n ? (unsigned char)c_b64[b2 & 63u] : (unsigned char)'=';
 }
 
-// one text line per vertex (%g) or triangle (%d of index + 1): pre num sep num sep num post
+// one text line per vertex (%g) or triangle (%d of index + 1): pre num sep num sep num post,
+// at most 48 characters, formatted in registers into the line's 48-byte slot
 constexpr int SLOT = 48;
-struct LineFmt {
-    char pre[4], sep[4], post[4];
+struct LineFmt {      // up to 4 characters each, first character in the low byte
+    unsigned pre, sep, post;
     int npre, nsep, npost;
 };
+template <class S>
+__device__ __forceinline__ void put_word(S &out, unsigned w, int n) {
+    for (int j = 0; j < n; j++) out.put((char)(w >> (8 * j)));
+}
 template <bool TRI>
-__global__ void k_txt_fmt(const void *__restrict__ src, int n, LineFmt f, unsigned char *__restrict__ slots,
+__global__ void k_txt_fmt(const void *__restrict__ src, int n, LineFmt f, unsigned *__restrict__ slots,
                           unsigned *__restrict__ lens) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    char buf[SLOT];
-    int k = 0;
-    for (int j = 0; j < f.npre; j++) buf[k++] = f.pre[j];
+    n2mfmt::WordSink out{slots + (size_t)(SLOT / 4) * i};
+    put_word(out, f.pre, f.npre);
     for (int c = 0; c < 3; c++) {
-        if (c) for (int j = 0; j < f.nsep; j++) buf[k++] = f.sep[j];
-        if (TRI) {
-            const int *t = (const int *)src + 3 * (size_t)i;
-            k += n2mfmt::fmt_d(t[c] + 1, buf + k);
-        } else {
-            const double *p = (const double *)src + 3 * (size_t)i;
-            k += n2mfmt::fmt_g6(p[c], buf + k);
-        }
+        if (c) put_word(out, f.sep, f.nsep);
+        if (TRI) n2mfmt::fmt_d(((const int *)src)[3 * (size_t)i + c] + 1, out);
+        else n2mfmt::fmt_g6(((const double *)src)[3 * (size_t)i + c], out);
     }
-    for (int j = 0; j < f.npost; j++) buf[k++] = f.post[j];
-    unsigned char *s = slots + (size_t)SLOT * i;
-    for (int j = 0; j < k; j++) s[j] = (unsigned char)buf[j];
-    lens[i] = (unsigned)k;
+    put_word(out, f.post, f.npost);
+    out.done();
+    lens[i] = (unsigned)out.n;
 }
 
+// slots -> the text: one warp per 32 lines; the 32 slots are staged in shared
+// memory and the warp writes its contiguous output bytes lane by lane.
 // offs: exclusive offsets (n + 1 entries)
-__global__ void k_txt_copy(const unsigned char *__restrict__ slots, const unsigned *__restrict__ offs, int n,
-                           unsigned char *__restrict__ dst) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const unsigned o = offs[i], len = offs[i + 1] - o;
-    const unsigned char *s = slots + (size_t)SLOT * i;
-    for (unsigned j = 0; j < len; j++) dst[o + j] = s[j];
+constexpr int COPY_WARPS = 8;
+__global__ void __launch_bounds__(32 * COPY_WARPS) k_txt_copy(const unsigned *__restrict__ slots,
+                                                              const unsigned *__restrict__ offs, int n,
+                                                              unsigned char *__restrict__ dst) {
+    __shared__ unsigned sw[COPY_WARPS][32 * SLOT / 4];
+    __shared__ unsigned so[COPY_WARPS][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long i0 = ((long long)blockIdx.x * COPY_WARPS + warp) * 32;
+    if (i0 >= n) return;
+    const int cnt = (int)min(32ll, n - i0);
+    const unsigned *src = slots + (size_t)i0 * (SLOT / 4);
+    for (int k = lane; k < cnt * (SLOT / 4); k += 32) sw[warp][k] = src[k];
+    if (lane <= cnt) so[warp][lane] = offs[i0 + lane];
+    if (lane == 0 && cnt == 32) so[warp][32] = offs[i0 + 32];
+    __syncwarp();
+    const unsigned end = so[warp][cnt];
+    for (unsigned b = so[warp][0] + lane; b < end; b += 32) {
+        int lo = 0, hi = cnt;   // so[lo] <= b < so[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (so[warp][mid] <= b) lo = mid;
+            else hi = mid;
+        }
+        const unsigned off = b - so[warp][lo];
+        dst[b] = (unsigned char)(sw[warp][lo * (SLOT / 4) + (off >> 2)] >> (8 * (off & 3)));
+    }
 }
 
 unsigned grid(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 LineFmt line_fmt(const char *pre, const char *sep, const char *post) {
+    auto pack = [](const char *t, int &n) {
+        n = (int)strlen(t);
+        unsigned w = 0;
+        for (int j = 0; j < n; j++) w |= (unsigned)(unsigned char)t[j] << (8 * j);
+        return w;
+    };
     LineFmt f{};
-    f.npre = (int)strlen(pre);
-    f.nsep = (int)strlen(sep);
-    f.npost = (int)strlen(post);
-    memcpy(f.pre, pre, f.npre);
-    memcpy(f.sep, sep, f.nsep);
-    memcpy(f.post, post, f.npost);
+    f.pre = pack(pre, f.npre);
+    f.sep = pack(sep, f.nsep);
+    f.post = pack(post, f.npost);
     return f;
 }
 
@@ -199,7 +221,7 @@ n2m_status encode_text(int format, const vec3i *d_t, const vec3d *d_p, int nt, i
     }
     CKS(w.pack.ensure((size_t)std::max<long long>(nl, 1) * SLOT));
     CKS(w.lens.ensure((size_t)(nl + 2) * sizeof(unsigned)));
-    unsigned char *slots = w.pack.as<unsigned char>();
+    unsigned *slots = w.pack.as<unsigned>();
     unsigned *lens = w.lens.as<unsigned>();
     if (np) {
         k_txt_fmt<false><<<grid(np, 128), 128, 0, s>>>(d_p, np, fv, slots, lens);
@@ -207,7 +229,7 @@ n2m_status encode_text(int format, const vec3i *d_t, const vec3d *d_p, int nt, i
         CKL();
     }
     if (nt) {
-        k_txt_fmt<true><<<grid(nt, 128), 128, 0, s>>>(d_t, nt, ft, slots + (size_t)SLOT * np, lens + np);
+        k_txt_fmt<true><<<grid(nt, 128), 128, 0, s>>>(d_t, nt, ft, slots + (size_t)(SLOT / 4) * np, lens + np);
         N2M_COUNT();
         CKL();
     }
@@ -223,7 +245,7 @@ n2m_status encode_text(int format, const vec3i *d_t, const vec3d *d_p, int nt, i
     CKS(a.text(head));
     unsigned char *o = w.out.as<unsigned char>();
     if (np) {
-        k_txt_copy<<<grid(np, 128), 128, 0, s>>>(slots, lens, np, o + a.pos);
+        k_txt_copy<<<grid(np, 32 * COPY_WARPS), 32 * COPY_WARPS, 0, s>>>(slots, lens, np, o + a.pos);
         N2M_COUNT();
         CKL();
     }
@@ -231,7 +253,8 @@ n2m_status encode_text(int format, const vec3i *d_t, const vec3d *d_p, int nt, i
     CKS(a.text(mid));
     if (nt) {
         // offsets of the triangle lines are relative to the start of the body
-        k_txt_copy<<<grid(nt, 128), 128, 0, s>>>(slots + (size_t)SLOT * np, lens + np, nt, o + a.pos - vbytes);
+        k_txt_copy<<<grid(nt, 32 * COPY_WARPS), 32 * COPY_WARPS, 0, s>>>(slots + (size_t)(SLOT / 4) * np, lens + np, nt,
+                                                                         o + a.pos - vbytes);
         N2M_COUNT();
         CKL();
     }
