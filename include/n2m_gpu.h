@@ -129,6 +129,14 @@ int n2m_set_oldcubes(int enable);
 n2m_status n2m_meshify(n2m_context *ctx, const float *img, const int dim[3], const n2m_options *opt, vec3i **t,
                        vec3d **p, int *nt, int *np, n2m_report *rep);
 
+/* n2m_meshify into caller-owned host buffers (t: t_cap triangles, p: p_cap
+ * vertices; pinned memory copies fastest): no allocation and no page faulting
+ * per call, for callers that mesh many volumes.  *nt and *np get the mesh's
+ * counts; when it does not fit the call fails with N2M_ERR_TOO_LARGE and *nt,
+ * *np say how much room it needs. */
+n2m_status n2m_meshify_into(n2m_context *ctx, const float *img, const int dim[3], const n2m_options *opt, vec3i *t,
+                            int64_t t_cap, vec3d *p, int64_t p_cap, int *nt, int *np, n2m_report *rep);
+
 /* Device-resident variant: d_img is a device pointer (float32, x fastest).
  * The mesh stays in context-owned device memory (valid until the next call on
  * ctx): *d_t (vec3i[*nt]) and *d_p (vec3d[*np]). */

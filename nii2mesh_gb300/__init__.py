@@ -137,6 +137,32 @@ class Context:
         t, p = _take(self._L, tp, pp, nt.value, np_.value)
         return t, p, rep.as_dict()
 
+    def meshify_into(self, img, tris_out, pts_out, iso, cubes=MC33, pre_smooth=True, only_largest=True,
+                     fill_bubbles=False, post_smooth=0, verbose=False):
+        """n2m_meshify_into: the mesh goes into caller-owned arrays (int32 (T, 3)
+        and float64 (V, 3), C-contiguous; pinned memory copies fastest) that can
+        be reused from call to call.  Returns (nt, np, report); the mesh is
+        tris_out[:nt], pts_out[:np].  Raises N2MError (N2M_ERR_TOO_LARGE, with
+        .needed = (nt, np)) when it does not fit."""
+        a = _vol(img)
+        nz, ny, nx = a.shape
+        for arr, dt in ((tris_out, np.int32), (pts_out, np.float64)):
+            if arr.dtype != dt or arr.ndim != 2 or arr.shape[1] != 3 or not arr.flags.c_contiguous:
+                raise ValueError("outputs must be C-contiguous int32 (T, 3) and float64 (V, 3) arrays")
+        o = self._opts(iso, cubes, pre_smooth, only_largest, fill_bubbles, post_smooth, verbose)
+        nt, np_ = C.c_int(), C.c_int()
+        rep = Report()
+        st = self._L.n2m_meshify_into(self.h, a.ctypes.data, (C.c_int * 3)(nx, ny, nz), C.byref(o),
+                                      tris_out.ctypes.data, len(tris_out), pts_out.ctypes.data, len(pts_out),
+                                      C.byref(nt), C.byref(np_), C.byref(rep))
+        if st != 0:
+            try:
+                _lib.check(st, "n2m_meshify_into")
+            except N2MError as e:
+                e.needed = (nt.value, np_.value)
+                raise
+        return nt.value, np_.value, rep.as_dict()
+
     def meshify_device(self, d_img_ptr, dims_xyz, iso, cubes=MC33, pre_smooth=True, only_largest=True,
                        fill_bubbles=False, post_smooth=0):
         """Device volume (pointer) in; mesh stays on the device.  Returns

@@ -203,7 +203,11 @@ struct n2m_context {
     bool want_host = false;
     HostOut hout;
     size_t hint_pb = 0, hint_tb = 0;   // raw mesh bytes of the last host-memory call (early pre-faulting)
-    bool pts_early = false;            // the final vertices are already on their way to hout.pts
+    bool pts_early = false;            // the final vertices are already on their way to the host
+    // n2m_meshify_into: caller-owned host output buffers (no allocation, no page faulting)
+    vec3i *user_t = nullptr;
+    vec3d *user_p = nullptr;
+    size_t user_tcap = 0, user_pcap = 0;
     WriterWork wr;                     // mesh writers
 };
 
@@ -624,7 +628,7 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     CKS(prepare(c, d_src, dim, o, o.verbose, P, rep));
     int nv, nt, ncand;
     CKS(march(c, P, dim, o.cubes, &nv, &nt, &ncand));
-    if (c->want_host) {   // keep buffers started early if they are large enough, else start them now
+    if (c->want_host && !c->user_p) {   // keep buffers started early if they are large enough, else start them now
         const size_t pb = (size_t)std::max(nv, 1) * sizeof(vec3d), tb = (size_t)std::max(nt, 1) * sizeof(vec3i);
         if (!c->hout.pts || c->hout.pb < pb || c->hout.tb < tb) c->hout.start(pb, tb);
         c->hint_pb = pb;
@@ -684,10 +688,16 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     CKS(mesh_remove_degenerate(pts, c->tris_raw.as<vec3i>(), nt, c->tris.as<vec3i>(), c->ntf.as<unsigned>(), c->deg,
                                c->scan, c->stream));
     if (early) {   // copy them out on the second stream while the degenerate filter runs
-        c->hout.join();
-        if (c->hout.pts && c->hout.pb >= (size_t)np * sizeof(vec3d)) {
+        void *dst = nullptr;
+        if (c->user_p) {
+            if ((size_t)np <= c->user_pcap) dst = c->user_p;
+        } else {
+            c->hout.join();
+            if (c->hout.pts && c->hout.pb >= (size_t)np * sizeof(vec3d)) dst = c->hout.pts;
+        }
+        if (dst) {
             CK(cudaStreamWaitEvent(c->copy, c->stage.ev[0], 0));
-            CK(cudaMemcpyAsync(c->hout.pts, pts, (size_t)np * sizeof(vec3d), cudaMemcpyDeviceToHost, c->copy));
+            CK(cudaMemcpyAsync(dst, pts, (size_t)np * sizeof(vec3d), cudaMemcpyDeviceToHost, c->copy));
             c->pts_early = true;
         }
     }
@@ -772,6 +782,28 @@ n2m_status to_host_mesh(n2m_context *c, vec3i **t, vec3d **p, int *nt, int *np, 
     return N2M_OK;
 }
 
+// the mesh into the caller's buffers (n2m_meshify_into)
+n2m_status to_user_mesh(n2m_context *c, int *nt, int *np, n2m_report *rep) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool early = c->pts_early;
+    c->pts_early = false;
+    if (early) CK(cudaStreamSynchronize(c->copy));
+    *nt = c->res_nt;
+    *np = c->res_np;
+    if ((size_t)c->res_nt > c->user_tcap || (size_t)c->res_np > c->user_pcap) {
+        n2m_set_error("mesh of %d triangles and %d vertices does not fit the output buffers (%zu, %zu)", c->res_nt,
+                      c->res_np, c->user_tcap, c->user_pcap);
+        return N2M_ERR_TOO_LARGE;
+    }
+    if (!early && c->res_np)
+        CK(cudaMemcpyAsync(c->user_p, c->res_pts, (size_t)c->res_np * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream));
+    if (c->res_nt)
+        CK(cudaMemcpyAsync(c->user_t, c->res_tris, (size_t)c->res_nt * sizeof(vec3i), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (rep) rep->ms_stage[7] = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return N2M_OK;
+}
+
 n2m_status upload(n2m_context *c, const float *img, size_t n) {
     CKS(c->in.ensure(n * sizeof(float)));
     CK(cudaMemcpyAsync(c->in.p, img, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
@@ -814,7 +846,7 @@ n2m_status meshify_host_tail(n2m_context *c, const int dim[3], const n2m_options
                              int *np, n2m_report *rep) {
     c->want_host = true;
     // fault in output pages sized like the last call's mesh while the GPU works (re-sized after the count if short)
-    if (c->hint_pb) c->hout.start(c->hint_pb + c->hint_pb / 8, c->hint_tb + c->hint_tb / 8);
+    if (c->hint_pb && !c->user_p) c->hout.start(c->hint_pb + c->hint_pb / 8, c->hint_tb + c->hint_tb / 8);
     n2m_status s = pipeline(c, c->in.as<float>(), dim, *opt, rep);
     c->stage.host = nullptr;
     c->want_host = false;
@@ -822,7 +854,7 @@ n2m_status meshify_host_tail(n2m_context *c, const int dim[3], const n2m_options
     if (s == N2M_OK && opt->post_smooth > 0)
         s = mesh_smooth_hc(c->res_pts, c->res_tris, c->res_np, c->res_nt, 0.1, 0.5, opt->post_smooth, true, c->hc, c->scan,
                            c->stream);
-    if (s == N2M_OK) s = to_host_mesh(c, t, p, nt, np, rep);
+    if (s == N2M_OK) s = c->user_p ? to_user_mesh(c, nt, np, rep) : to_host_mesh(c, t, p, nt, np, rep);
     if (s != N2M_OK) {
         cudaStreamSynchronize(c->copy);
         c->pts_early = false;
@@ -830,12 +862,10 @@ n2m_status meshify_host_tail(n2m_context *c, const int dim[3], const n2m_options
     }
     return s;
 }
-}  // namespace
 
-extern "C" n2m_status n2m_meshify(n2m_context *c, const float *img, const int dim[3], const n2m_options *opt,
-                                  vec3i **t, vec3d **p, int *nt, int *np, n2m_report *rep) {
-    if (!c || !opt || !dim || !img || !t || !p || !nt || !np) return N2M_ERR_BAD_ARGS;
-    CK(cudaSetDevice(c->device));
+// host volume in (staged upload when pre-smoothing), mesh out through meshify_host_tail
+n2m_status meshify_host(n2m_context *c, const float *img, const int dim[3], const n2m_options *opt, vec3i **t,
+                        vec3d **p, int *nt, int *np, n2m_report *rep) {
     const size_t n = (size_t)dim[0] * dim[1] * dim[2];
     // with pre-smoothing the upload is staged: the x pass of each slab starts as soon as it has arrived
     const bool staged = opt->pre_smooth && dim[0] >= 5 && dim[1] >= 5 && dim[2] >= 5 && smooth_can_stage(dim[0], dim[1], dim[2]);
@@ -846,6 +876,32 @@ extern "C" n2m_status n2m_meshify(n2m_context *c, const float *img, const int di
         CKS(upload(c, img, n));
     }
     return meshify_host_tail(c, dim, opt, t, p, nt, np, rep);
+}
+}  // namespace
+
+extern "C" n2m_status n2m_meshify(n2m_context *c, const float *img, const int dim[3], const n2m_options *opt,
+                                  vec3i **t, vec3d **p, int *nt, int *np, n2m_report *rep) {
+    if (!c || !opt || !dim || !img || !t || !p || !nt || !np) return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    return meshify_host(c, img, dim, opt, t, p, nt, np, rep);
+}
+
+extern "C" n2m_status n2m_meshify_into(n2m_context *c, const float *img, const int dim[3], const n2m_options *opt,
+                                       vec3i *t, int64_t t_cap, vec3d *p, int64_t p_cap, int *nt, int *np,
+                                       n2m_report *rep) {
+    if (!c || !opt || !dim || !img || !nt || !np || t_cap < 0 || p_cap < 0 || (t_cap && !t) || (p_cap && !p))
+        return N2M_ERR_BAD_ARGS;
+    CK(cudaSetDevice(c->device));
+    static vec3d no_pts;   // a non-null marker when the caller passes no vertex space
+    c->user_t = t;
+    c->user_p = p ? p : &no_pts;
+    c->user_tcap = (size_t)t_cap;
+    c->user_pcap = p ? (size_t)p_cap : 0;
+    const n2m_status s = meshify_host(c, img, dim, opt, nullptr, nullptr, nt, np, rep);
+    c->user_t = nullptr;
+    c->user_p = nullptr;
+    c->user_tcap = c->user_pcap = 0;
+    return s;
 }
 
 extern "C" n2m_status n2m_cast_voxels_device(n2m_context *c, const void *d_raw, int datatype, float scl_slope,

@@ -122,3 +122,29 @@ def test_bbox_touches_volume_faces(gpu, oracle):
         got, want = run_both(gpu, oracle, vol, 4.0, variant, True, False, False)
         ok, d, msg = mesh_equal(got, want, POS_TOL)
         assert ok, msg
+
+
+def test_meshify_into_caller_buffers(gpu):
+    """n2m_meshify_into writes the same mesh as n2m_meshify into reused caller
+    arrays (pageable and pinned), staged and unstaged uploads, with and without
+    HC post-smoothing; a mesh that does not fit fails with N2M_ERR_TOO_LARGE
+    and reports the room it needs"""
+    import torch
+    ctx = gpu.Context(0)
+    vol = synth.ct512(seed=6, n=80, count=10)
+    for smooth, post in ((True, 0), (False, 0), (True, 3)):
+        t, p, _ = ctx.meshify(vol, 300.0, gpu.MC33, smooth, False, False, post)
+        for pinned in (False, True):
+            if pinned:
+                tb = torch.empty((len(t) + 100, 3), dtype=torch.int32, pin_memory=True).numpy()
+                pb = torch.empty((len(p) + 100, 3), dtype=torch.float64, pin_memory=True).numpy()
+            else:
+                tb, pb = np.empty((len(t) + 100, 3), np.int32), np.empty((len(p) + 100, 3), np.float64)
+            for _ in range(2):
+                nt, nv, rep = ctx.meshify_into(vol, tb, pb, 300.0, gpu.MC33, smooth, False, False, post)
+                assert (nt, nv) == (len(t), len(p))
+                assert np.array_equal(tb[:nt], t) and np.array_equal(pb[:nv], p)
+    small_t, small_p = np.empty((10, 3), np.int32), np.empty((len(p), 3), np.float64)
+    with pytest.raises(gpu.N2MError) as e:
+        ctx.meshify_into(vol, small_t, small_p, 300.0, gpu.MC33, True, False, False, 3)
+    assert e.value.status == 8 and e.value.needed == (len(t), len(p))
