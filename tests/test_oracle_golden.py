@@ -146,3 +146,77 @@ def test_writers_match_reference(case):
             got = W.encode(W.FMT_MZ3 if fmt < 0 else fmt, t, p, gz)
             assert W.normalize(got) == W.normalize(want), (case, ext, gz)
 
+
+
+REF_DATA = Path("/root/reference/data")
+
+
+def _load_reference_volume(name):
+    """a volume of the reference's data/ folder read by its own load_nii
+    (oracle/_ref/libn2m_ref_cli.so): float32 (nz, ny, nx) and the header"""
+    import ctypes as C
+    from oracle.oracle import REF_DIR
+    lib = C.CDLL(str(REF_DIR / "libn2m_ref_cli.so"))
+    lib.load_nii.restype = C.c_void_p
+    lib.load_nii.argtypes = [C.c_char_p, C.c_void_p]
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    hdr = C.create_string_buffer(348)
+    p = lib.load_nii(str(REF_DATA / name).encode(), hdr)
+    assert p, name
+    dims = np.frombuffer(hdr.raw, np.int16, 8, 40)
+    nx, ny, nz = (int(d) for d in dims[1:4])
+    vol = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_float)), shape=(nx * ny * nz,)).copy()
+    libc.free(p)
+    srow = np.frombuffer(hdr.raw, np.float32, 12, 280).reshape(3, 4)
+    return vol.reshape(nz, ny, nx), srow
+
+
+@pytest.mark.skipif(not ((REF_DATA / "bet.nii.gz").exists() and reference_available() and reference_available(True)),
+                    reason="needs the reference tree (its data/ images and oracle/_ref)")
+@pytest.mark.parametrize("name", ["bet.nii.gz", "pve_1.nii.gz", "pve_2.nii.gz"])
+def test_real_images_oracle_vs_reference(oracle, name):
+    """The reference's own images (data/, read by its load_nii): the default
+    isolevel (Otsu medium, src/nii2mesh.c:586) bit for bit, then meshify with
+    the CLI defaults (-p 1 -l 1 -b 0), Lewiner and classic tables and the
+    oldcubes build, oracle against the reference mesh for mesh; with -b 1 and
+    HC post-smoothing plus the header's sform on the Lewiner mesh."""
+    vol, srow = _load_reference_volume(name)
+    ref, refc = Reference(False), Reference(True)
+    iso = ref.set_threshold(vol, 2)
+    assert oracle.set_threshold(vol, 2) == iso
+    for variant, r in ((MC33, ref), (MC_CLASSIC_TABLE, ref), (OLDCUBES, refc)):
+        want = r.meshify(vol, iso, variant, True, True, False)
+        got = oracle.meshify(vol, iso, variant, True, True, False)
+        ok, d, msg = mesh_equal(got, want, 0.0)
+        assert ok, (name, variant, msg)
+    want = ref.meshify(vol, iso, MC33, True, True, True)
+    got = oracle.meshify(vol, iso, MC33, True, True, True)
+    ok, d, msg = mesh_equal(got, want, 0.0)
+    assert ok, (name, "fill bubbles", msg)
+    t, p = want
+    ps_r, ps_o = ref.laplacian_smoothHC(p, t, iters=5), oracle.laplacian_smoothHC(p, t, iters=5)
+    assert np.array_equal(ps_r, ps_o)
+    tr, pr = ref.apply_sform(ps_r, t, *srow)
+    to, po = oracle.apply_sform(ps_o, t, *srow)
+    assert np.array_equal(tr, to) and np.array_equal(pr, po)
+
+
+@pytest.mark.skipif(not ((REF_DATA / "D99_atlas_v2.0_right.nii.gz").exists() and reference_available()),
+                    reason="needs the reference tree (its data/ images and oracle/_ref)")
+def test_real_atlas_labels_oracle_vs_reference(oracle):
+    """D99 atlas labels (data/, read by load_nii) binarised as the atlas loop
+    does (src/nii2mesh.c:555-563) and meshed at iso 0.5 with -l 1 -b 1: a large
+    and a small label, oracle against the reference"""
+    vol, _ = _load_reference_volume("D99_atlas_v2.0_right.nii.gz")
+    labels, counts = np.unique(vol[vol > 0].astype(np.int32), return_counts=True)
+    ref = Reference(False)
+    for lab in (labels[np.argmax(counts)], labels[np.argmin(counts)]):
+        m, _ = oracle.binarize_label(vol, int(lab))
+        want = ref.meshify(m, 0.5, MC33, True, True, True)
+        got = oracle.meshify(m, 0.5, MC33, True, True, True)
+        if want is None:
+            assert got is None
+            continue
+        ok, d, msg = mesh_equal(got, want, 0.0)
+        assert ok, (int(lab), msg)
