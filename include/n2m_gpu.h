@@ -261,6 +261,13 @@ n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d
 n2m_status n2m_smooth_hc_noalloc(vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri, double alpha,
                                  double beta, int iter, bool lock_edges, void *stream);
 
+/* ---- test hook -------------------------------------------------------------------
+ * Host-side fault injection: the after-th device buffer allocation from now on
+ * (0 = the next one) fails with N2M_ERR_OOM, once; a negative value disarms.
+ * Returns the previous setting.  Every entry point must then fail cleanly and
+ * the context stay usable. */
+int n2m_debug_fail_allocations(int after);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,7 +21,7 @@ SYMBOLS = ["n2m_context_create", "n2m_context_destroy", "n2m_context_stream", "n
            "n2m_kernel_launches", "n2m_meshify_backward", "n2m_smooth_hc_noalloc", "n2m_atlas", "n2m_atlas_device",
            "setThreshold", "n2m_set_threshold", "n2m_set_threshold_device", "n2m_cast_voxels_device",
            "n2m_meshify_typed", "save_mesh", "n2m_mesh_format_of", "n2m_encode_mesh", "n2m_encode_mesh_device",
-           "n2m_encode_mesh_to_device", "n2m_meshify_into",           "n2m_save_mesh", "n2m_save_mesh_device", "n2m_deflate_device"]
+           "n2m_encode_mesh_to_device", "n2m_meshify_into", "n2m_debug_fail_allocations",           "n2m_save_mesh", "n2m_save_mesh_device", "n2m_deflate_device"]
 
 
 class vec3d(C.Structure):
@@ -94,6 +94,7 @@ def load(path=None):
                                     C.POINTER(vp), ip, ip, C.POINTER(Report)]
     L.n2m_set_oldcubes.argtypes = [C.c_int]
     L.n2m_meshify.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip, C.POINTER(Report)]
+    L.n2m_debug_fail_allocations.argtypes = [C.c_int]
     L.n2m_meshify_into.argtypes = [vp, vp, ip, C.POINTER(Options), vp, C.c_int64, vp, C.c_int64, ip, ip,
                                    C.POINTER(Report)]
     L.n2m_meshify_device.argtypes = [vp, vp, ip, C.POINTER(Options), C.POINTER(vp), C.POINTER(vp), ip, ip,

@@ -48,8 +48,20 @@ extern "C" const char *n2m_status_string(int s) {
     return (s >= 0 && s <= 10) ? names[s] : "unknown";
 }
 
+// host-side fault injection (tests): the k-th device allocation from now fails, once
+static std::atomic<int> g_fail_alloc{-1};
+extern "C" int n2m_debug_fail_allocations(int after) { return g_fail_alloc.exchange(after < 0 ? -1 : after); }
+
 n2m_status DevBuf::ensure(size_t bytes) {
     if (bytes <= cap) return N2M_OK;
+    int k = g_fail_alloc.load();
+    while (k >= 0 && !g_fail_alloc.compare_exchange_weak(k, k - 1)) {
+    }
+    if (k == 0) {
+        release();
+        n2m_set_error("allocation of %zu bytes failed (injected)", bytes);
+        return N2M_ERR_OOM;
+    }
     release();
     size_t want = bytes + bytes / 8 + 256;
     cudaError_t e = cudaMalloc(&p, want);
@@ -614,6 +626,11 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
 
 // the whole meshify on device input; result in c->res_*
 n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const n2m_options &o, n2m_report *rep) {
+    // no adjoint of an earlier call once this one has started: it may re-allocate what that one used
+    c->fwd.valid = false;
+    c->res_pts = nullptr;
+    c->res_tris = nullptr;
+    c->res_np = c->res_nt = 0;
     if (!d_src || dim[0] <= 0 || dim[1] <= 0 || dim[2] <= 0) {
         n2m_set_error("bad volume arguments");
         return N2M_ERR_BAD_ARGS;
