@@ -147,6 +147,71 @@ def cpu_reference(vol, steps, warmup):
     return nvox / statistics.median(times) / 1e9, kind, times, len(m[0])
 
 
+def _reference_worker(path, rounds, start, done, out):
+    """one host core: meshify the volume at `path` once per round, in step with the others"""
+    from oracle.oracle import Oracle, Reference, reference_available
+    impl = Reference(False) if reference_available() else Oracle()
+    vol = np.load(path)
+    for _ in range(rounds):
+        start.wait()
+        m = impl.meshify(vol, ISO, 0, True, False, False)
+        out.put(0 if m is None else len(m[0]))
+        done.wait()
+
+
+def cpu_reference_parallel(vol, steps, warmup, procs):
+    """The reference algorithm on `procs` host cores at once: meshify is
+    single-threaded, so each core meshes its own copy of the volume and a step
+    is the wall time until all of them are done (procs volumes per step)."""
+    import multiprocessing as mp
+    from oracle.oracle import reference_available
+    kind = "reference" if reference_available() else "port"
+    tmp = tempfile.mkdtemp(prefix="n2m_ref_", dir="/dev/shm" if os.path.isdir("/dev/shm") else None)
+    path = os.path.join(tmp, "vol.npy")
+    np.save(path, vol)
+    ctx = mp.get_context("spawn")
+    start, done, out = ctx.Barrier(procs + 1), ctx.Barrier(procs + 1), ctx.Queue()
+    rounds = warmup + steps
+    ws = [ctx.Process(target=_reference_worker, args=(path, rounds, start, done, out), daemon=True)
+          for _ in range(procs)]
+    for w in ws:
+        w.start()
+    times, ntri = [], 0
+    try:
+        for i in range(rounds):
+            start.wait(timeout=600)
+            t0 = time.perf_counter()
+            res = [out.get(timeout=600) for _ in range(procs)]
+            t1 = time.perf_counter()
+            done.wait(timeout=600)
+            assert all(r > 0 for r in res)
+            ntri = res[0]
+            if i >= warmup:
+                times.append(t1 - t0)
+    finally:
+        for w in ws:
+            w.join(timeout=60)
+        os.remove(path)
+        os.rmdir(tmp)
+    return procs * vol.size / statistics.median(times) / 1e9, kind, times, ntri
+
+
+def host_procs(bytes_per_proc=4.5e9):
+    """host cores for concurrent reference runs, bounded by the memory each run needs"""
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    avail = None
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    if avail is None:
+        return 1
+    return max(1, min(cores, int(0.6 * avail / bytes_per_proc)))
+
+
 def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
     """fwd and fwd+bwd ms on the 128^3 differentiation workload (pre-smooth,
     Lewiner MC, 10 HC iterations; loss = sum(|v - c| - 40)^2), and the time of
@@ -410,13 +475,15 @@ def main():
             return
         vol = synth.ct512()
         steps = max(1, min(a.steps, 3))
-        gv, kind, times, nt = cpu_reference(vol, steps, 1)
+        procs = host_procs()
+        gv, kind, times, nt = cpu_reference_parallel(vol, steps, 1, procs)
         line = {"metric": METRIC, "value": round(gv, 6), "unit": "Gvox/s", "n_gpus": a.gpus, "steps": steps,
                 "warmup": 1, "ms_per_step": round(1e3 * statistics.median(times), 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
                 "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"}, "impl": "reference",
-                "cpu_baseline": {"value": round(gv, 6), "unit": "Gvox/s", "cores": 1, "kind": kind,
-                                 "sample": "full 512^3 volume per step (meshify is single-threaded)"},
+                "cpu_baseline": {"value": round(gv, 6), "unit": "Gvox/s", "cores": procs, "kind": kind,
+                                 "sample": f"{procs} full 512^3 meshify calls per step, one per host core "
+                                           f"(meshify itself is single-threaded)"},
                 "e2e": {"value": round(gv, 6), "unit": "Gvox/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
