@@ -148,3 +148,25 @@ def test_meshify_into_caller_buffers(gpu):
     with pytest.raises(gpu.N2MError) as e:
         ctx.meshify_into(vol, small_t, small_p, 300.0, gpu.MC33, True, False, False, 3)
     assert e.value.status == 8 and e.value.needed == (len(t), len(p))
+
+
+@pytest.mark.parametrize("shape", [(23, 29, 37), (40, 48, 64), (17, 61, 33)])
+@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE])
+def test_ragged_shapes_no_clustering(gpu, oracle, shape, variant):
+    """pre-smoothing without clustering on shapes whose rows and slices are not
+    multiples of 32 voxels (MC words straddle rows of the volume), host (staged
+    upload) and device paths against the oracle, with an isolevel in range and
+    one that falls back to mid-range"""
+    import torch
+    rng = np.random.default_rng(sum(shape))
+    vol = (rng.normal(0, 30, shape) + 100 * (rng.random(shape) < 0.3)).astype(np.float32)
+    for iso in (40.0, 1e6):   # 1e6: out of range, the isolevel falls back
+        got, want = run_both(gpu, oracle, vol, iso, variant, True, False, False)
+        ok, d, msg = mesh_equal(got, want, POS_TOL)
+        assert ok, (iso, msg)
+        ctx = gpu.Context(0)
+        dv = torch.from_numpy(vol).cuda()
+        nz, ny, nx = shape
+        cubes = gpu.CLASSIC_TABLE if variant == MC_CLASSIC_TABLE else gpu.MC33
+        dt, dp, nt, nv, _ = ctx.meshify_device(dv.data_ptr(), (nx, ny, nz), iso, cubes, True, False, False)
+        assert (nt, nv) == (len(want[0]), len(want[1]))
