@@ -430,12 +430,15 @@ __device__ __forceinline__ float agval(const AtlasVol &v, const ABox &B, const f
     const long long j = (long long)(B.glo[0] + x) + (long long)(y + B.glo[1]) * v.nx + (long long)(z + B.glo[2]) * v.nxy;
     float val;
     if (j < v.nvox) {
+        // the box grid ends at the volume's dims: a coordinate past them by one wraps into the next row / slice
         int vx = B.glo[0] + x, vy = y + B.glo[1], vz = z + B.glo[2];
-        if (vx >= v.nx || vy >= v.ny) {
-            vz = (int)(j / v.nxy);
-            const long long r = j - (long long)vz * v.nxy;
-            vy = (int)(r / v.nx);
-            vx = (int)(r - (long long)vy * v.nx);
+        if (vx >= v.nx) {
+            vx -= v.nx;
+            vy++;
+        }
+        if (vy >= v.ny) {
+            vy -= v.ny;
+            vz++;
         }
         const int lx = vx - B.o[0], ly = vy - B.o[1], lz = vz - B.o[2];
         val = (lx >= 0 && ly >= 0 && lz >= 0 && lx < B.n[0] && ly < B.n[1] && lz < B.n[2])

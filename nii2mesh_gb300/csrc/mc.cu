@@ -47,12 +47,16 @@ __device__ __forceinline__ float gval(const GV &g, int x, int y, int z) {
     float v;
     if (j < g.nvox) {
         v = __ldg(g.vol + j);
+        // the voxel j really is: the grid ends at dim, so a coordinate is past the volume by at most
+        // one (the padding column / row), which wraps into the next row / slice
         int vx = g.lo0 + x, vy = y + g.lo1, vz = z + g.lo2;
-        if (vx >= g.dx || vy >= g.dy) {
-            vz = (int)(j / g.dxy);
-            const long long r = j - (long long)vz * g.dxy;
-            vy = (int)(r / g.dx);
-            vx = (int)(r - (long long)vy * g.dx);
+        if (vx >= g.dx) {
+            vx -= g.dx;
+            vy++;
+        }
+        if (vy >= g.dy) {
+            vy -= g.dy;
+            vz++;
         }
         if (vx == 0 || vy == 0 || vz == 0 || vx == g.dx - 1 || vy == g.dy - 1 || vz == g.dz - 1)
             v = fminf(g.edge_max, v);
@@ -510,12 +514,14 @@ __device__ __forceinline__ float gval_src(const GV &g, int x, int y, int z, long
     if (j < g.nvox) {
         v = __ldg(g.vol + j);
         src = j;
-        int vx = g.lo0 + x, vy = y + g.lo1, vz = z + g.lo2;
-        if (vx >= g.dx || vy >= g.dy) {
-            vz = (int)(j / g.dxy);
-            const long long r = j - (long long)vz * g.dxy;
-            vy = (int)(r / g.dx);
-            vx = (int)(r - (long long)vy * g.dx);
+        int vx = g.lo0 + x, vy = y + g.lo1, vz = z + g.lo2;   // wrapped as in gval
+        if (vx >= g.dx) {
+            vx -= g.dx;
+            vy++;
+        }
+        if (vy >= g.dy) {
+            vy -= g.dy;
+            vz++;
         }
         if ((vx == 0 || vy == 0 || vz == 0 || vx == g.dx - 1 || vy == g.dy - 1 || vz == g.dz - 1) && !(v <= g.edge_max)) {
             v = g.edge_max;
