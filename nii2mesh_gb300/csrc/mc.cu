@@ -106,12 +106,23 @@ __device__ __noinline__ unsigned ambiguous_count(const GV &g, int x, int y, int 
 // bit, word-aligned like the counts (bit x&31 of signs[(z*NY + y)*WX + x/32]).
 // A warp takes whole rows, SW words at a time with all their loads in
 // flight.  Runs of SW words strictly inside the volume and the grid read the
-// volume directly; border words go through gval, out of line.
+// volume directly.  Border words (the first and last of a row, every word of a
+// row on a face) apply gval's cases lane by lane on the linear voxel index
+// j = row start + x: the padding column (x one past the volume) is the next
+// row's first voxel, which is on a face; a row on a face of the volume (or the
+// padding row, which wraps to y = 0 of the next slice) has every point
+// darkened; j past the volume is the padding value.
 constexpr int SW = 16;
 
-__device__ __noinline__ unsigned word_signs_slow(const GV &g, int x0, int y, int z) {
-    const int x = x0 + (int)(threadIdx.x & 31);
-    return __ballot_sync(0xffffffffu, x < g.NX && gval(g, x, y, z) > 0.f);
+__device__ __forceinline__ unsigned border_word(const GV &g, long long rb, bool rface, int xw, int lane) {
+    const int x = xw * 32 + lane, vx = g.lo0 + x;
+    float d = g.pad;
+    if (x < g.NX && rb + x < g.nvox) {
+        const float v = __ldg(g.vol + rb + x);
+        d = __fsub_rn((rface || vx == 0 || vx >= g.dx - 1) ? fminf(g.edge_max, v) : v, g.iso);
+    }
+    // the FLT_EPSILON clamp maps (-eps, eps) to +eps: positive <=> d > -eps
+    return __ballot_sync(0xffffffffu, x < g.NX && d > -N2M_FLT_EPS);
 }
 
 __global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nrows, unsigned *signs) {
@@ -122,12 +133,13 @@ __global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nrows
     for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += (gridDim.x * blockDim.x) >> 5) {
         const int y = (int)(row % (unsigned)g.NY), z = (int)(row / (unsigned)g.NY);
         const int vy = g.lo1 + y, vz = g.lo2 + z;
-        const bool rsimple = vy >= 1 && vy <= g.dy - 2 && vz >= 1 && vz <= g.dz - 2;
-        const float *rp = g.vol + ((long long)g.lo0 + (long long)vy * g.dx + (long long)vz * g.dxy) + lane;
+        const bool rface = !(vy >= 1 && vy <= g.dy - 2 && vz >= 1 && vz <= g.dz - 2);
+        const long long rb = (long long)g.lo0 + (long long)vy * g.dx + (long long)vz * g.dxy;   // j of grid x = 0
+        const float *rp = g.vol + rb + lane;
         unsigned *out = signs + (size_t)row * WX;
-        const int f0 = rsimple ? xs0 : (int)WX, f1 = rsimple ? xs1 + 1 : (int)WX;   // direct words [f0, f1)
+        const int f0 = rface ? (int)WX : xs0, f1 = rface ? (int)WX : xs1 + 1;   // direct words [f0, f1)
         for (int xw = 0; xw < min(f0, (int)WX); xw++) {
-            const unsigned m = word_signs_slow(g, xw * 32, y, z);
+            const unsigned m = border_word(g, rb, rface, xw, lane);
             if (lane == 0) out[xw] = m;
         }
         for (int xw0 = f0; xw0 < f1; xw0 += SW) {
@@ -137,13 +149,13 @@ __global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nrows
             unsigned mine = 0;
 #pragma unroll
             for (int k = 0; k < SW; k++) {
-                const unsigned m = __ballot_sync(0xffffffffu, __fsub_rn(raw[k], g.iso) > -N2M_FLT_EPS);   // clamp maps (-eps, eps) to +eps
+                const unsigned m = __ballot_sync(0xffffffffu, __fsub_rn(raw[k], g.iso) > -N2M_FLT_EPS);
                 if (lane == k) mine = m;
             }
             if (lane < SW && xw0 + lane < f1) out[xw0 + lane] = mine;
         }
         for (int xw = max(f1, f0); xw < (int)WX; xw++) {
-            const unsigned m = word_signs_slow(g, xw * 32, y, z);
+            const unsigned m = border_word(g, rb, rface, xw, lane);
             if (lane == 0) out[xw] = m;
         }
     }
