@@ -368,16 +368,25 @@ struct BitSink {
 
 __constant__ unsigned char c_clorder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
 
-__global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restrict__ ghist, int nchunks,
+// One code for a group of G neighbouring chunks (G set per call so that the
+// groups fit one wave: each warp's tree build is a serial chain), from their
+// summed histogram; each chunk keeps its own block (header, size, stored or
+// not).  The header is written with BFINAL = 0; k_bits sets it on the last chunk.
+__global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restrict__ ghist, int nchunks, int G,
                                                         DfInfo *__restrict__ info, unsigned *__restrict__ gcodes,
                                                         unsigned *__restrict__ ghdr, unsigned *__restrict__ sizes) {
     __shared__ HuffScratch sc[DF_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int chunk = blockIdx.x * DF_WARPS + warp;
-    if (chunk >= nchunks) return;
+    const int group = blockIdx.x * DF_WARPS + warp;
+    const int c0 = group * G, c1 = min(c0 + G, nchunks);
+    if (c0 >= nchunks) return;
     HuffScratch &S = sc[warp];
-    const bool last = chunk == nchunks - 1;
-    for (int i = lane; i < DF_NSYM; i += 32) S.freq[i] = i < DF_NLIT + DF_NDIST ? ghist[(size_t)chunk * DF_NSYM + i] : 0u;
+    for (int i = lane; i < DF_NSYM; i += 32) {
+        unsigned f = 0;
+        if (i < DF_NLIT + DF_NDIST)
+            for (int c = c0; c < c1; c++) f += ghist[(size_t)c * DF_NSYM + i];
+        S.freq[i] = f;
+    }
     for (int i = lane; i < DF_HDR_WORDS; i += 32) S.hdr[i] = 0;
     __syncwarp();
     if (lane == 0) {
@@ -452,7 +461,7 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restri
         ncl = 19;
         while (ncl > 4 && !S.cll[c_clorder[ncl - 1]]) ncl--;
         BitSink b{S.hdr, 0};
-        b.put(last ? 1u : 0u, 1);
+        b.put(0u, 1);   // BFINAL (set by k_bits on the last chunk)
         b.put(2u, 2);   // BTYPE 10: dynamic Huffman codes
         b.put((unsigned)(hlit - 257), 5);
         b.put((unsigned)(hdist - 1), 5);
@@ -468,7 +477,8 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restri
         S.keys[3] = b.pos;
     }
     __syncwarp();
-    {   // coded size with the real (not phantom) frequencies, summed over the lanes
+    for (int chunk = c0; chunk < c1; chunk++) {   // each chunk's coded size with its own frequencies
+        const bool last = chunk == nchunks - 1;
         const unsigned *f = ghist + (size_t)chunk * DF_NSYM;
         unsigned long long bits = 0;
         for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) {
@@ -491,8 +501,8 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_huff(const unsigned *__restri
         }
     }
     __syncwarp();
-    for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) gcodes[(size_t)chunk * DF_NSYM + i] = S.code[i];
-    for (int i = lane; i < DF_HDR_WORDS; i += 32) ghdr[(size_t)chunk * DF_HDR_WORDS + i] = S.hdr[i];
+    for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) gcodes[(size_t)group * DF_NSYM + i] = S.code[i];
+    for (int i = lane; i < DF_HDR_WORDS; i += 32) ghdr[(size_t)group * DF_HDR_WORDS + i] = S.hdr[i];
 }
 
 // ---- bit output -------------------------------------------------------------------------------
@@ -532,7 +542,7 @@ __device__ __forceinline__ void ring_put(unsigned *ring, unsigned &bp, unsigned 
 __global__ void __launch_bounds__(32 * BITS_WARPS) k_bits(const unsigned char *__restrict__ src, const unsigned *__restrict__ tokens,
                                                         const DfInfo *__restrict__ info, const unsigned *__restrict__ gcodes,
                                                         const unsigned *__restrict__ ghdr, const unsigned *__restrict__ offs,
-                                                        int nchunks, int ch, unsigned char *__restrict__ out,
+                                                        int nchunks, int ch, int G, unsigned char *__restrict__ out,
                                                         unsigned *__restrict__ err) {
     __shared__ unsigned ring_s[BITS_WARPS][RING];
     __shared__ unsigned code_s[BITS_WARPS][DF_NLIT + DF_NDIST];
@@ -562,10 +572,11 @@ __global__ void __launch_bounds__(32 * BITS_WARPS) k_bits(const unsigned char *_
     unsigned *ring = ring_s[warp];
     unsigned *code = code_s[warp];
     for (int i = lane; i < RING; i += 32) ring[i] = 0;
-    for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) code[i] = gcodes[(size_t)chunk * DF_NSYM + i];
+    const int group = chunk / G;
+    for (int i = lane; i < DF_NLIT + DF_NDIST; i += 32) code[i] = gcodes[(size_t)group * DF_NSYM + i];
     __syncwarp();
     unsigned bp = 0, fw = 0;
-    const unsigned *hdr = ghdr + (size_t)chunk * DF_HDR_WORDS;
+    const unsigned *hdr = ghdr + (size_t)group * DF_HDR_WORDS;
     for (unsigned w0 = 0; w0 * 32 < I.hdr_bits; w0 += 32) {
         const unsigned wi = w0 + lane;
         unsigned nb = 0;
@@ -573,6 +584,7 @@ __global__ void __launch_bounds__(32 * BITS_WARPS) k_bits(const unsigned char *_
         if (wi * 32 < I.hdr_bits) {
             nb = min(32u, I.hdr_bits - wi * 32);
             v = hdr[wi] & (nb == 32 ? 0xffffffffu : ((1u << nb) - 1));
+            if (wi == 0 && last) v |= 1u;   // BFINAL
         }
         ring_put(ring, bp, fw, v, nb, dst, lim, lane);
     }
@@ -795,6 +807,8 @@ n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWor
         CK(cudaFuncSetAttribute(k_lz, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lz, 32 * LZ_WARPS, smem));
         w.lz_slots = std::max(1, sms * per_sm * LZ_WARPS);
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_huff, 32 * DF_WARPS, 0));
+        w.huff_slots = std::max(1, sms * per_sm * DF_WARPS);
         CK(cudaStreamCreateWithFlags((cudaStream_t *)&w.side, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags((cudaEvent_t *)&w.ev_in, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags((cudaEvent_t *)&w.ev_ck, cudaEventDisableTiming));
@@ -827,15 +841,18 @@ n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWor
         CKL();
         CK(cudaEventRecord((cudaEvent_t)w.ev_ck, (cudaStream_t)w.side));
     }
-    const unsigned blocks = (unsigned)((nchunks + DF_WARPS - 1) / DF_WARPS);
+    // chunks per Huffman code: the fewest that let the code builders run in one wave
+    const int G = std::max(1, (nchunks + w.huff_slots - 1) / w.huff_slots);
+    const int ngroups = (nchunks + G - 1) / G;
+    const unsigned blocks = (unsigned)((ngroups + DF_WARPS - 1) / DF_WARPS);
     CK(cudaFuncSetAttribute(k_lz, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     k_lz<<<(unsigned)((nchunks + LZ_WARPS - 1) / LZ_WARPS), 32 * LZ_WARPS, smem, s>>>(
         (const unsigned *)d_src, (long long)n, nchunks, (int)ch, w.tok.as<unsigned>(), w.info.as<DfInfo>(),
         w.hist.as<unsigned>());
     N2M_COUNT();
     CKL();
-    k_huff<<<blocks, 32 * DF_WARPS, 0, s>>>(w.hist.as<unsigned>(), nchunks, w.info.as<DfInfo>(), w.codes.as<unsigned>(),
-                                           w.hdr.as<unsigned>(), w.sizes.as<unsigned>());
+    k_huff<<<blocks, 32 * DF_WARPS, 0, s>>>(w.hist.as<unsigned>(), nchunks, G, w.info.as<DfInfo>(),
+                                           w.codes.as<unsigned>(), w.hdr.as<unsigned>(), w.sizes.as<unsigned>());
     N2M_COUNT();
     CKL();
     CKS(scan_u32(w.sizes.as<unsigned>(), (size_t)nchunks, w.sizes.as<unsigned>() + nchunks, sw, s));
@@ -849,7 +866,7 @@ n2m_status deflate_device(const void *d_src, size_t n, int container, DeflateWor
     unsigned char *out = w.out.as<unsigned char>();
     k_bits<<<(unsigned)((nchunks + BITS_WARPS - 1) / BITS_WARPS), 32 * BITS_WARPS, 0, s>>>(
         (const unsigned char *)d_src, w.tok.as<unsigned>(), w.info.as<DfInfo>(), w.codes.as<unsigned>(),
-        w.hdr.as<unsigned>(), w.sizes.as<unsigned>(), nchunks, (int)ch, out + head, (unsigned *)(acc + 2));
+        w.hdr.as<unsigned>(), w.sizes.as<unsigned>(), nchunks, (int)ch, G, out + head, (unsigned *)(acc + 2));
     N2M_COUNT();
     CKL();
     if (cksum) CK(cudaStreamWaitEvent(s, (cudaEvent_t)w.ev_ck, 0));

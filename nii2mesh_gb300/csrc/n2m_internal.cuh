@@ -120,6 +120,7 @@ n2m_status launch_cast(const void *d_raw, int datatype, float slope, float inter
 struct DeflateWork {
     DevBuf tok, info, hist, codes, hdr, sizes, misc, out;
     int lz_slots = 0;                                       // chunks the match finder keeps in flight
+    int huff_slots = 0;                                     // warps the code builder keeps in flight
     void *side = nullptr, *ev_in = nullptr, *ev_ck = nullptr;   // checksum stream and its events
 };
 size_t deflate_bound(size_t n);
