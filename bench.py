@@ -39,7 +39,7 @@ ISO = 300.0
 # DRAM bytes (read + write) per step of each stage on this workload, from one ncu capture of
 # `bench.py --profile 512` (profiles/meshify_ct512_kernels.md): smoothing = its three pass
 # kernels, count = k_signs + k_words + k_active + scans, emit = k_emit.
-NCU_TRAFFIC = {"smooth": 3414e6, "count": 966e6, "emit": 382e6, "degenerate": 346e6}
+NCU_TRAFFIC = {"smooth": 3413e6, "count": 925e6, "emit": 376e6, "degenerate": 346e6}
 # what bounds each stage (measured in the same profiles)
 STAGE_BOUND = {"smooth": "FP32 instruction issue: exact double-rounding proof per tap (~72-80 % issue active); "
                          "three streaming passes at ~8.1 B/voxel each"}
