@@ -71,3 +71,20 @@ def test_generators_deterministic():
     assert (c == 2000.0).mean() == pytest.approx(0.01, abs=0.003)
     at = synth.atlas256(n=48, labels=20)
     assert at.dtype == np.int16 and at.max() <= 20 and at.min() >= 0
+
+
+def test_mesh_format_rule_matches_reference_rule():
+    """n2m_mesh_format_of (host code of the library, no GPU call) picks the
+    format save_mesh picks (strip_ext + strstr, src/meshify.c:973-1019), as
+    restated in oracle/writers.py, on awkward names"""
+    from nii2mesh_gb300 import _lib
+    from oracle import writers as W
+    if not _lib.LIB_PATH.exists():
+        pytest.fail("libn2m_gpu.so not built (run __graft_entry__.build())")
+    L = _lib.load()
+    names = ["a.mz3", "a.gii", "a.obj", "a.OBJ", "lh.pial", "lh.inflated", "x.json", "x.off", "x.ply", "x.stl",
+             "x.vtk", "x.xyz", "x", "", ".obj", "dir.obj/file", "dir/.obj", "a.b.stl", "a.stl.gz", "a.gii.mz3",
+             "a.mz3x", "a.xmz3", "a.json5", "a.vtkx", "C:\\dir.obj\\f", "a.obj.", "a..obj", "./a.ply", "a.inflatedx",
+             "mesh.pial.gz", "m.offset", "a/b.c/d.gii"]
+    for n in names:
+        assert L.n2m_mesh_format_of(n.encode()) == W.format_of(n), n
