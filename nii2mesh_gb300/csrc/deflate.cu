@@ -15,9 +15,11 @@
 //               evaluation, walked over the tile's match-start ballot (one step
 //               per match, not per byte).  Emits 32-bit tokens and the block's
 //               symbol histogram.
-//   k_huff      per chunk: canonical Huffman codes (lengths <= 15; code-length
-//               code <= 7) from the histogram, the block header bits and the
-//               coded size; a stored block instead when that is smaller.
+//   k_huff      canonical Huffman codes (lengths <= 15; code-length code <= 7)
+//               and the block header for a group of neighbouring chunks (as few
+//               as let the groups run in one wave) from their summed histogram;
+//               each chunk's coded size from its own histogram, and a stored
+//               block instead when that is smaller.
 //   scan        chunk byte offsets (every chunk ends on a byte boundary: a
 //               non-final dynamic block is followed by an empty stored block, the
 //               "sync flush" of RFC 1951 3.2.4).
@@ -40,7 +42,7 @@ constexpr int DF_WARPS = 4;                      // chunks per CTA of k_huff
 constexpr int BITS_WARPS = 8;                    // chunks per CTA of k_bits
 constexpr int DF_MAXLEN = 258;
 constexpr int DF_NLIT = 286, DF_NDIST = 30, DF_NSYM = 320;   // histogram stride: 286 + 30, padded
-constexpr int DF_HDR_WORDS = 160;                // block header bits per chunk (<= 4498 used)
+constexpr int DF_HDR_WORDS = 160;                // block header bits per code (<= 4498 used)
 constexpr int DF_SEG = 1024;                     // checksum segment
 constexpr unsigned CRC_POLY = 0xEDB88320u;       // CRC-32, reflected
 constexpr unsigned ADLER_MOD = 65521u;
