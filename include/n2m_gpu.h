@@ -120,6 +120,14 @@ float setThreshold(float *img, int nvox, int darkMediumBright123);
  * zlib-compressed.  The file is encoded on the GPU.  Returns EXIT_SUCCESS or
  * EXIT_FAILURE (file not writable, no device). */
 int save_mesh(const char *fnm, vec3i *tris, vec3d *pts, int ntri, int npt, bool isGz);
+/* The rest of meshify.h (src/meshify.h:7-11), so that the reference's program
+ * links without meshify.o: strip_ext() cuts a file name at its extension in
+ * place (src/meshify.c:973-982), clockMsec() is a monotonic clock in
+ * milliseconds and timediff() the rounded difference of two of its readings
+ * (src/meshify.c:266-284). */
+void strip_ext(char *fname);
+double clockMsec(void);
+long timediff(double startTimeMsec, double endTimeMsec);
 /* Mirrors the USE_CLASSIC_CUBES build flag for the drop-in marchingCubes()
  * and meshify(): nonzero selects Bourke's oldcubes. Returns the old value. */
 int n2m_set_oldcubes(int enable);

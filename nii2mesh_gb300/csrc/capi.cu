@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <ctime>
 #include <condition_variable>
 #include <mutex>
 #include <thread>
@@ -1327,6 +1328,19 @@ extern "C" int marchingCubes(float *img, short dim[3], int lo[3], int hi[3], int
 
 // ---- mesh writers ------------------------------------------------------------------------------
 extern "C" int n2m_mesh_format_of(const char *fnm) { return fnm ? mesh_format_of(fnm) : -1; }
+
+// ---- the rest of meshify.h ----------------------------------------------------------------------
+extern "C" void strip_ext(char *fname) {
+    if (fname) fname[file_ext(fname) - fname] = '\0';
+}
+
+extern "C" double clockMsec(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return t.tv_sec * 1000.0 + t.tv_nsec / 1.0e6;
+}
+
+extern "C" long timediff(double startTimeMsec, double endTimeMsec) { return lround(endTimeMsec - startTimeMsec); }
 
 namespace {
 // host mesh -> context buffers (vertices after the triangles, 8-byte aligned)

@@ -137,6 +137,7 @@ struct WriterWork {
     size_t host_cap = 0;
 };
 int mesh_format_of(const char *fnm);   // N2M_FMT_*, or -1 (save_mesh appends ".mz3")
+const char *file_ext(const char *fnm);  // where strip_ext cuts the name
 n2m_status encode_mesh_device(int format, const vec3i *d_t, const vec3d *d_p, int nt, int np, bool gz, WriterWork &w,
                               ScanWork &sw, cudaStream_t s, const unsigned char **d_out, size_t *len);
 

@@ -361,12 +361,17 @@ n2m_status encode_gii(const vec3i *d_t, const vec3d *d_p, int nt, int np, bool g
 }
 }  // namespace
 
-int mesh_format_of(const char *fnm) {
-    // the extension is the text from the last '.' that is not directly after a path separator
-    // (strip_ext, src/meshify.c:973-982); the first format whose name it contains wins
+// start of a file name's extension: the last '.' that is not directly after a path separator
+// (strip_ext, src/meshify.c:973-982), or the end of the name
+const char *file_ext(const char *fnm) {
     const char *end = fnm + strlen(fnm), *dot = end;
     while (dot > fnm && *dot != '.' && *dot != '\\' && *dot != '/') --dot;
-    const char *ext = (dot > fnm && *dot == '.' && dot[-1] != '\\' && dot[-1] != '/') ? dot : end;
+    return (dot > fnm && *dot == '.' && dot[-1] != '\\' && dot[-1] != '/') ? dot : end;
+}
+
+int mesh_format_of(const char *fnm) {
+    // the first format whose name the extension contains wins (src/meshify.c:989-1013)
+    const char *ext = file_ext(fnm);
     if (strstr(ext, ".mz3")) return N2M_FMT_MZ3;
     if (strstr(ext, ".gii")) return N2M_FMT_GII;
     if (strstr(ext, ".inflated") || strstr(ext, ".pial")) return N2M_FMT_FREESURFER;

@@ -88,3 +88,36 @@ def test_mesh_format_rule_matches_reference_rule():
              "mesh.pial.gz", "m.offset", "a/b.c/d.gii"]
     for n in names:
         assert L.n2m_mesh_format_of(n.encode()) == W.format_of(n), n
+
+
+REF_SRC = Path("/root/reference/src")
+
+
+@pytest.mark.skipif(not (REF_SRC / "nii2mesh.c").exists() or shutil.which("gcc") is None,
+                    reason="needs the reference tree and gcc")
+def test_reference_program_links_against_library(tmp_path):
+    """The reference's own program (its nii2mesh.c, with quadric.c for the
+    decimation and base64.c) links against libn2m_gpu.so in place of
+    meshify.o, isolevel.o, MarchingCubes.o, bwlabel.o and radixsort.o: every
+    symbol it takes from those objects is exported with the same signature
+    (include/n2m_gpu.h).  Compiled in a temporary directory; it runs and prints
+    its usage."""
+    from nii2mesh_gb300 import _lib
+    if not _lib.LIB_PATH.exists():
+        pytest.fail("libn2m_gpu.so not built (run __graft_entry__.build())")
+    probe = subprocess.run(["gcc", "-x", "c", "-", "-lz", "-o", str(tmp_path / "z")], input="#include <zlib.h>\nint main(void){return 0;}\n",
+                           capture_output=True, text=True)
+    zl = ["-DHAVE_ZLIB"] if probe.returncode == 0 else []
+    objs = []
+    for src, extra in (("nii2mesh.c", []), ("base64.c", []), ("quadric.c", ["-Dlaplacian_smoothHC=ref_laplacian_smoothHC"])):
+        o = tmp_path / (src + ".o")
+        subprocess.run(["gcc", "-O1", "-w", "-DNII2MESH", "-DHAVE_FORMATS", *zl, *extra, "-I", str(ROOT / "include"),
+                        "-I", str(REF_SRC), "-c", str(REF_SRC / src), "-o", str(o)], check=True)
+        objs.append(str(o))
+    exe = tmp_path / "nii2mesh"
+    lib_dir = str(_lib.LIB_PATH.parent)
+    r = subprocess.run(["gcc", "-o", str(exe), *objs, "-L", lib_dir, "-ln2m_gpu", f"-Wl,-rpath,{lib_dir}", "-lm"] +
+                       (["-lz"] if zl else []), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert "Usage" in out.stdout
