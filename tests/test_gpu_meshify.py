@@ -170,3 +170,19 @@ def test_ragged_shapes_no_clustering(gpu, oracle, shape, variant):
         cubes = gpu.CLASSIC_TABLE if variant == MC_CLASSIC_TABLE else gpu.MC33
         dt, dp, nt, nv, _ = ctx.meshify_device(dv.data_ptr(), (nx, ny, nz), iso, cubes, True, False, False)
         assert (nt, nv) == (len(want[0]), len(want[1]))
+
+
+def test_ct512_full_size_bit_exact(gpu, oracle):
+    """the benchmark workload at full size (512^3 CT-like, iso 300, -p 1 -l 0
+    -b 0, Lewiner; 7.1 M triangles): the host-memory call, the caller-buffer
+    call and the oracle give the same mesh, connectivity and every vertex"""
+    vol = synth.ct512()
+    got = gpu.meshify(vol, 300.0, pre_smooth=True, only_largest=False, fill_bubbles=False)
+    want = oracle.meshify(vol, 300.0, MC33, True, False, False)
+    assert len(got[0]) > 7_000_000
+    ok, d, msg = mesh_equal(got, want, POS_TOL)
+    assert ok, msg
+    ctx = gpu.Context(0)
+    tb, pb = np.empty((len(got[0]), 3), np.int32), np.empty((len(got[1]), 3), np.float64)
+    nt, nv, _ = ctx.meshify_into(vol, tb, pb, 300.0, gpu.MC33, True, False, False)
+    assert np.array_equal(tb[:nt], got[0]) and np.array_equal(pb[:nv], got[1])
