@@ -66,3 +66,37 @@ def test_atlas_labels_touching_faces(gpu, oracle):
         ok, d, msg = mesh_equal((t, p), want, 0.0)
         assert ok, f"label {l}: {msg}"
     ctx.close()
+
+
+def test_atlas256_full_size(gpu, oracle):
+    """the benchmark workload at full size (256^3 int16, ~250 power-law labels,
+    -p 1 -l 1 -b 1 -s 5): batched equals the per-label loop on every label;
+    eight labels from the smallest to the largest against the oracle (raw
+    meshes bit for bit, HC within 1e-4 voxels)"""
+    lab = synth.atlas256()
+    ctx = gpu.Context(0)
+    kw = dict(pre_smooth=True, only_largest=True, fill_bubbles=True)
+    batched = ctx.atlas(lab, mode=gpu.ATLAS_BATCHED, post_smooth=5, **kw)
+    loop = ctx.atlas(lab, mode=gpu.ATLAS_LOOP, post_smooth=5, **kw)
+    raw = {m[0]: m for m in ctx.atlas(lab, mode=gpu.ATLAS_BATCHED, post_smooth=0, **kw)}
+    assert len(batched) == len(loop) > 200
+    for (l, sb, tb, pb), (l2, sl, tl, pl) in zip(batched, loop):
+        assert (l, sb) == (l2, sl) and np.array_equal(tb, tl) and np.array_equal(pb, pl), l
+    ids, counts = np.unique(lab[lab > 0], return_counts=True)
+    sample = [int(ids[i]) for i in np.argsort(counts)[np.linspace(0, len(ids) - 1, 8).astype(int)]]
+    img = lab.astype(np.float32)
+    by_label = {m[0]: m for m in batched}
+    for l in sample:
+        binimg, _ = oracle.binarize_label(img, l)
+        want = oracle.meshify(binimg, 0.5, 0, True, True, True)
+        _, st, t, p = by_label[l]
+        if want is None:
+            assert st != 0
+            continue
+        _, _, tr, pr = raw[l]
+        ok, d, msg = mesh_equal((tr, pr), want, 0.0)
+        assert ok, f"label {l}: {msg}"
+        ws = oracle.laplacian_smoothHC(want[1], want[0], 0.1, 0.5, 5, True)
+        ok, d, msg = smoothed_equal((tr, pr), p, want, ws, 1e-4)
+        assert ok, f"label {l} (HC): {msg}"
+    ctx.close()
