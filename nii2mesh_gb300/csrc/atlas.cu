@@ -343,23 +343,77 @@ __global__ void k_a_fill(const ABox *boxes, int nb, unsigned nch, unsigned *q, u
     });
 }
 
-__global__ void k_a_dilate(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const unsigned char *keep, float *arena,
-                           int nx, int ny, int nz) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        bool on = keep[c.i];
-        const int gx = B.o[0] + c.x, gy = B.o[1] + c.y, gz = B.o[2] + c.z;
-        if (!on && gx > 0 && gy > 0 && gz > 0 && gx < nx - 1 && gy < ny - 1 && gz < nz - 1) {
-            for (int dz = -1; dz <= 1 && !on; dz++)
-                for (int dy = -1; dy <= 1 && !on; dy++)
-                    for (int dx = -1; dx <= 1; dx++) {
-                        if ((dx | dy | dz) == 0 || (dx == -1 && dy == -1 && dz == -1)) continue;
-                        const int xx = c.x + dx, yy = c.y + dy, zz = c.z + dz;
-                        if (xx < 0 || yy < 0 || zz < 0 || xx >= B.n[0] || yy >= B.n[1] || zz >= B.n[2]) continue;
-                        if (keep[B.arena + ((long long)zz * B.n[1] + yy) * B.n[0] + xx]) { on = true; break; }
-                    }
+// Dilation + mask-out (src/meshify.c:218-264, 337-342): a voxel stays when it
+// is kept or, away from the volume faces, one of 25 neighbours is (all 26
+// except (-1,-1,-1), :252); every other voxel becomes the box minimum.  Row
+// by row, 32 voxels a word: with R3 = K(x-1)|K(x)|K(x+1) and R2 = K(x)|K(x+1)
+// of a row, the neighbourhood is R3 of rows y-1..y+1 in slices z and z+1, R3 of
+// rows y and y+1 in slice z-1, and R2 of row y-1 in slice z-1.  A chunk works on
+// the rows its voxels touch and writes only its own voxels.
+__global__ void __launch_bounds__(256) k_a_dilate(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch,
+                                                  const unsigned char *keep, float *arena, int nx, int ny, int nz) {
+    __shared__ unsigned item;
+    __shared__ int bi;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            item = atomicAdd(q, 1u);
+            bi = item < nch ? find_item(boxes, nb, item, &ABox::chunk0) : 0;
         }
-        if (!on) arena[c.i] = ord2f(B.vmin);
-    });
+        __syncthreads();
+        const unsigned it = item;
+        const int b = bi;
+        __syncthreads();
+        if (it >= nch) return;
+        const ABox &B = boxes[b];
+        const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
+        const unsigned nvb = (unsigned)n0 * (unsigned)n1 * (unsigned)n2;
+        const unsigned loc0 = (it - B.chunk0) * ch;
+        if (loc0 >= nvb) continue;
+        const unsigned loc1 = min(loc0 + ch, nvb);
+        const unsigned r0 = loc0 / (unsigned)n0, r1 = (loc1 - 1) / (unsigned)n0;   // rows (y + z n1) touched
+        const unsigned char *K = keep + B.arena;
+        const float vmin = ord2f(B.vmin);
+        const int nw = (n0 + 31) / 32;
+        for (unsigned r = r0 + (unsigned)warp; r <= r1; r += (unsigned)nwarp) {
+            const int y = (int)(r % (unsigned)n1), z = (int)(r / (unsigned)n1);
+            const int gy = B.o[1] + y, gz = B.o[2] + z;
+            const bool ryz = gy > 0 && gz > 0 && gy < ny - 1 && gz < nz - 1;
+            // 32 keep bits of row (y + dy, z + dz), word xw (zero outside the box)
+            auto word = [&](int dy, int dz, int xw) -> unsigned {
+                const int yy = y + dy, zz = z + dz, x = xw * 32 + lane;
+                const bool in = yy >= 0 && zz >= 0 && yy < n1 && zz < n2 && xw < nw && x < n0;
+                return __ballot_sync(0xffffffffu, in && K[((long long)zz * n1 + yy) * n0 + x] != 0);
+            };
+            // rows used: 0..2 = y-1..y+1 in slice z, 3..5 in slice z+1, 6 = (y, z-1), 7 = (y+1, z-1), 8 = (y-1, z-1)
+            const int DY[9] = {-1, 0, 1, -1, 0, 1, 0, 1, -1}, DZ[9] = {0, 0, 0, 1, 1, 1, -1, -1, -1};
+            unsigned prev[9], cur[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                prev[k] = 0u;
+                cur[k] = word(DY[k], DZ[k], 0);
+            }
+            for (int xw = 0; xw < nw; xw++) {
+                unsigned on = 0u;
+#pragma unroll
+                for (int k = 0; k < 9; k++) {
+                    const unsigned nxt = word(DY[k], DZ[k], xw + 1);
+                    const unsigned right = (cur[k] >> 1) | (nxt << 31);   // K(x+1)
+                    on |= cur[k] | right | (k < 8 ? (cur[k] << 1) | (prev[k] >> 31) : 0u);   // row 8: no K(x-1)
+                    prev[k] = cur[k];
+                    cur[k] = nxt;
+                }
+                const int x = xw * 32 + lane;
+                const unsigned loc = r * (unsigned)n0 + (unsigned)x;
+                if (x < n0 && loc >= loc0 && loc < loc1) {
+                    const bool kept = (prev[1] >> lane) & 1u;   // row (y, z): prev holds word xw now
+                    const int gx = B.o[0] + x;
+                    const bool interior = ryz && gx > 0 && gx < nx - 1;
+                    if (!(kept || (interior && ((on >> lane) & 1u)))) arena[B.arena + loc] = vmin;
+                }
+            }
+        }
+    }
 }
 
 // ---- S4: bbox of voxels >= iso and the range after clustering -------------------------
