@@ -261,21 +261,96 @@ __global__ void k_a_uf_init(const ABox *boxes, int nb, unsigned nch, unsigned *q
     });
 }
 
-__global__ void k_a_uf_merge(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, int *L, int nnb) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        if (L[c.i] < 0 || skip_box(B)) return;
-        // the -x neighbour (k = 0) is linked by the run start; a contact whose two
-        // left voxels also touch is implied by theirs (both pairs lie in the same runs)
-        const bool left = c.x > 0 && L[c.i - 1] >= 0;
-        for (int k = 1; k < nnb; k++) {
-            const int xx = c.x + k_half[k][0], yy = c.y + k_half[k][1], zz = c.z + k_half[k][2];
-            if (xx < 0 || yy < 0 || zz < 0 || xx >= B.n[0] || yy >= B.n[1]) continue;
-            const long long j = B.arena + ((long long)zz * B.n[1] + yy) * B.n[0] + xx;
-            const int lj = L[j];
-            if (lj < 0 || (left && xx > 0 && L[j - 1] >= 0)) continue;
-            if (lj != L[c.i]) uf::unite(L, (int)c.i, (int)j);
+// Union of each voxel of the class (m == want) with its half-neighbours of
+// k_half[1 .. NNB-1] (the -x neighbour is linked by the run start).  A contact
+// whose two left voxels also touch is implied by theirs (both pairs lie in the
+// same runs) and is skipped.  Row by row, 32 voxels a word: the class bits of
+// the row and of the rows (y-1, z), (y, z-1), (y-1, z-1), (y+1, z-1) give every
+// contact of a word by shifts; only the lanes holding one touch L.  A chunk
+// reads the rows its voxels touch and unites only its own voxels' contacts.
+template <int NNB>
+__global__ void __launch_bounds__(256) k_a_uf_merge(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch,
+                                                    const unsigned char *m, unsigned char want, int *L) {
+    static_assert(NNB == 3 || NNB == 9, "6- or 18-connectivity");
+    __shared__ unsigned item;
+    __shared__ int bi;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            item = atomicAdd(q, 1u);
+            bi = item < nch ? find_item(boxes, nb, item, &ABox::chunk0) : 0;
         }
-    });
+        __syncthreads();
+        const unsigned it = item;
+        const int b = bi;
+        __syncthreads();
+        if (it >= nch) return;
+        const ABox &B = boxes[b];
+        if (skip_box(B)) continue;
+        const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
+        const unsigned nvb = (unsigned)n0 * (unsigned)n1 * (unsigned)n2;
+        const unsigned loc0 = (it - B.chunk0) * ch;
+        if (loc0 >= nvb) continue;
+        const unsigned loc1 = min(loc0 + ch, nvb);
+        const unsigned r0 = loc0 / (unsigned)n0, r1 = (loc1 - 1) / (unsigned)n0;
+        const unsigned char *M = m + B.arena;
+        const int nw = (n0 + 31) / 32;
+        constexpr int NR = NNB == 3 ? 3 : 5;
+        // rows: 0 = (y, z), 1 = (y-1, z), 2 = (y, z-1), 3 = (y-1, z-1), 4 = (y+1, z-1)
+        const int RY[5] = {0, -1, 0, -1, 1}, RZ[5] = {0, 0, -1, -1, -1};
+        for (unsigned r = r0 + (unsigned)warp; r <= r1; r += (unsigned)nwarp) {
+            const int y = (int)(r % (unsigned)n1), z = (int)(r / (unsigned)n1);
+            auto word = [&](int dy, int dz, int xw) -> unsigned {
+                const int yy = y + dy, zz = z + dz, x = xw * 32 + lane;
+                const bool in = yy >= 0 && zz >= 0 && yy < n1 && zz < n2 && xw < nw && x < n0;
+                return __ballot_sync(0xffffffffu, in && M[((long long)zz * n1 + yy) * n0 + x] == want);
+            };
+            unsigned pw[NR], cw[NR];
+#pragma unroll
+            for (int k = 0; k < NR; k++) {
+                pw[k] = 0u;
+                cw[k] = word(RY[k], RZ[k], 0);
+            }
+            for (int xw = 0; xw < nw; xw++) {
+                unsigned nx[NR];
+#pragma unroll
+                for (int k = 0; k < NR; k++) nx[k] = word(RY[k], RZ[k], xw + 1);
+                // S(k, d): bit x = class of voxel x + d of row k (d in -2 .. 1)
+                auto S = [&](int k, int d) -> unsigned {
+                    return d == 0 ? cw[k] : d > 0 ? (cw[k] >> d) | (nx[k] << (32 - d)) : (cw[k] << -d) | (pw[k] >> (32 + d));
+                };
+                const unsigned F = cw[0], left = S(0, -1);
+                // contact masks of k_half[1 .. NNB-1]: (row, dx)
+                auto contact = [&](int k, int dx) -> unsigned { return F & S(k, dx) & ~(left & S(k, dx - 1)); };
+                // bit k-1 of this lane's set: a contact with k_half[k]
+                unsigned set = ((contact(1, 0) >> lane) & 1u) | ((contact(2, 0) >> lane) & 1u) << 1;   // (0,-1,0) (0,0,-1)
+                if constexpr (NNB == 9) {
+                    set |= ((contact(1, -1) >> lane) & 1u) << 2    // (-1, -1, 0)
+                         | ((contact(1, 1) >> lane) & 1u) << 3     // (1, -1, 0)
+                         | ((contact(2, -1) >> lane) & 1u) << 4    // (-1, 0, -1)
+                         | ((contact(2, 1) >> lane) & 1u) << 5     // (1, 0, -1)
+                         | ((contact(3, 0) >> lane) & 1u) << 6     // (0, -1, -1)
+                         | ((contact(4, 0) >> lane) & 1u) << 7;    // (0, 1, -1)
+                }
+                const int x = xw * 32 + lane;
+                const unsigned loc = r * (unsigned)n0 + (unsigned)x;
+                if (set && x < n0 && loc >= loc0 && loc < loc1) {
+                    const int i = (int)(B.arena + loc);
+                    do {
+                        const int k = __ffs(set);
+                        set &= set - 1u;
+                        const int j = i + k_half[k][0] + k_half[k][1] * n0 + k_half[k][2] * n0 * n1;
+                        if (L[j] != L[i]) uf::unite(L, i, j);
+                    } while (set);
+                }
+#pragma unroll
+                for (int k = 0; k < NR; k++) {
+                    pw[k] = cw[k];
+                    cw[k] = nx[k];
+                }
+            }
+        }
+    }
 }
 
 __global__ void k_a_uf_flatten(ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, int *L, bool fg) {
@@ -847,14 +922,14 @@ struct Segment {
             { k_a_mask<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, ar, m); N2M_COUNT(); }
             if (fill_bubbles) {
                 { k_a_uf_init<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 0, L); N2M_COUNT(); }
-                { k_a_uf_merge<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, 3); N2M_COUNT(); }
+                { k_a_uf_merge<3><<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 0, L); N2M_COUNT(); }
                 { k_a_uf_flatten<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, false); N2M_COUNT(); }
                 CK(cudaMemsetAsync(w.edge.p, 0, (size_t)arena, s));
                 { k_a_edge_roots<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.edge.as<unsigned char>()); N2M_COUNT(); }
                 { k_a_fill_bubbles<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.edge.as<unsigned char>(), m); N2M_COUNT(); }
             }
             { k_a_uf_init<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 1, L); N2M_COUNT(); }
-            { k_a_uf_merge<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, 9); N2M_COUNT(); }
+            { k_a_uf_merge<9><<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 1, L); N2M_COUNT(); }
             { k_a_uf_flatten<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, true); N2M_COUNT(); }
             if (only_largest) {
                 CK(cudaMemsetAsync(w.ucnt.p, 0, (size_t)arena * sizeof(unsigned), s));
