@@ -1,13 +1,13 @@
 // label.cu — connected-component labelling for meshify's largest-cluster and
 // bubble-fill options (src/bwlabel.c:429-543, src/meshify.c:323-342).
 //
-// GPU union-find: every foreground voxel starts as its own root; each voxel
-// unites with its already-visited half-neighbourhood (3 offsets for
-// 6-connectivity, 9 for 18, 13 for 26) by CAS-hooking the larger root under
-// the smaller one, then a flatten pass points every voxel at its root.  The
-// root of a component is therefore its first voxel in raster order, which is
-// exactly how the reference numbers labels (first appearance) and breaks
-// size ties (lowest label wins).
+// GPU union-find: every voxel of the class starts linked to the first voxel of
+// its run along x; each voxel unites with its already-visited
+// half-neighbourhood (3 offsets for 6-connectivity, 9 for 18, 13 for 26) by
+// CAS-hooking the larger root under the smaller one, then a flatten pass
+// points every voxel at its root.  The root of a component is therefore its
+// first voxel in raster order, which is exactly how the reference numbers
+// labels (first appearance) and breaks size ties (lowest label wins).
 #include "n2m_internal.cuh"
 #include "uf.cuh"
 
@@ -57,22 +57,70 @@ __constant__ signed char k_half[13][3] = {{-1, 0, 0},  {0, -1, 0}, {0, 0, -1},  
                                           {-1, 0, -1}, {1, 0, -1}, {0, -1, -1}, {0, 1, -1},  {-1, -1, -1},
                                           {1, -1, -1}, {-1, 1, -1}, {1, 1, -1}};
 
-__global__ void k_uf_merge(int *L, Dims d, int nnb) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.n; i += (long long)gridDim.x * blockDim.x) {
-        if (L[i] < 0) continue;
-        const int z = (int)(i / d.nxy);
-        const long long r = i - z * d.nxy;
-        const int y = (int)(r / d.nx), x = (int)(r - (long long)y * d.nx);
-        // the -x neighbour (k = 0) is linked by the run start; a contact whose two
-        // left voxels also touch is implied by theirs (both pairs lie in the same runs)
-        const bool left = x > 0 && L[i - 1] >= 0;
-        for (int k = 1; k < nnb; k++) {
-            const int xx = x + k_half[k][0], yy = y + k_half[k][1], zz = z + k_half[k][2];
-            if (xx < 0 || yy < 0 || zz < 0 || xx >= d.nx || yy >= d.ny) continue;
-            const long long j = zz * d.nxy + (long long)yy * d.nx + xx;
-            const int lj = L[j];
-            if (lj < 0 || (left && xx > 0 && L[j - 1] >= 0)) continue;
-            if (lj != L[i]) unite(L, (int)i, (int)j);
+// Union of each voxel of the class (m == want) with its half-neighbours of
+// k_half[1 .. NNB-1] (the -x neighbour is linked by the run start).  A contact
+// whose two left voxels also touch is implied by theirs (both pairs lie in the
+// same runs) and is skipped.  One warp per row (y, z), 32 voxels a word: the
+// class bits of the row and of the rows (y-1, z), (y, z-1), (y-1, z-1),
+// (y+1, z-1) give every contact of a word by shifts; only the lanes holding
+// one touch L.
+template <int NNB>
+__global__ void __launch_bounds__(256) k_uf_merge(const unsigned char *__restrict__ m, unsigned char want, int *L, Dims d) {
+    static_assert(NNB == 3 || NNB == 9 || NNB == 13, "6-, 18- or 26-connectivity");
+    const int lane = threadIdx.x & 31;
+    const long long nrows = (long long)d.ny * d.nz;
+    const int nw = (d.nx + 31) / 32;
+    constexpr int NR = NNB == 3 ? 3 : 5;
+    // rows: 0 = (y, z), 1 = (y-1, z), 2 = (y, z-1), 3 = (y-1, z-1), 4 = (y+1, z-1)
+    const int RY[5] = {0, -1, 0, -1, 1}, RZ[5] = {0, 0, -1, -1, -1};
+    for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < nrows;
+         r += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const int z = (int)(r / d.ny), y = (int)(r - (long long)z * d.ny);
+        auto word = [&](int dy, int dz, int xw) -> unsigned {
+            const int yy = y + dy, zz = z + dz, x = xw * 32 + lane;
+            const bool in = yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz && x < d.nx;
+            return __ballot_sync(0xffffffffu, in && m[zz * d.nxy + (long long)yy * d.nx + x] == want);
+        };
+        unsigned pw[NR], cw[NR];
+#pragma unroll
+        for (int k = 0; k < NR; k++) {
+            pw[k] = 0u;
+            cw[k] = word(RY[k], RZ[k], 0);
+        }
+        for (int xw = 0; xw < nw; xw++) {
+            unsigned nx[NR];
+#pragma unroll
+            for (int k = 0; k < NR; k++) nx[k] = word(RY[k], RZ[k], xw + 1);
+            // S(k, dx): bit x = class of voxel x + dx of row k (dx in -2 .. 1)
+            auto S = [&](int k, int dx) -> unsigned {
+                return dx == 0 ? cw[k] : dx > 0 ? (cw[k] >> dx) | (nx[k] << (32 - dx)) : (cw[k] << -dx) | (pw[k] >> (32 + dx));
+            };
+            const unsigned F = cw[0], left = S(0, -1);
+            auto contact = [&](int k, int dx) -> unsigned { return ((F & S(k, dx) & ~(left & S(k, dx - 1))) >> lane) & 1u; };
+            // bit k-1 of this lane's set: a contact with k_half[k]
+            unsigned set = contact(1, 0) | contact(2, 0) << 1;   // (0,-1,0) (0,0,-1)
+            if constexpr (NNB >= 9)
+                set |= contact(1, -1) << 2 | contact(1, 1) << 3     // (-1,-1,0) (1,-1,0)
+                     | contact(2, -1) << 4 | contact(2, 1) << 5     // (-1,0,-1) (1,0,-1)
+                     | contact(3, 0) << 6 | contact(4, 0) << 7;     // (0,-1,-1) (0,1,-1)
+            if constexpr (NNB == 13)
+                set |= contact(3, -1) << 8 | contact(3, 1) << 9     // (-1,-1,-1) (1,-1,-1)
+                     | contact(4, -1) << 10 | contact(4, 1) << 11;  // (-1,1,-1) (1,1,-1)
+            const int x = xw * 32 + lane;
+            if (set && x < d.nx) {
+                const int i = (int)(r * d.nx + x);
+                do {
+                    const int k = __ffs(set);
+                    set &= set - 1u;
+                    const int j = i + k_half[k][0] + k_half[k][1] * d.nx + k_half[k][2] * (int)d.nxy;
+                    if (L[j] != L[i]) unite(L, i, j);
+                } while (set);
+            }
+#pragma unroll
+            for (int k = 0; k < NR; k++) {
+                pw[k] = cw[k];
+                cw[k] = nx[k];
+            }
         }
     }
 }
@@ -149,24 +197,48 @@ __global__ void k_fill_iso(float *vol, long long n, const unsigned char *__restr
 }
 
 // dilate (26-neighbourhood without the (-1,-1,-1) neighbour, interior voxels
-// only; src/meshify.c:218-264) fused with the mask-out img = mn
-__global__ void k_dilate_maskout(const unsigned char *__restrict__ keep, Dims d, float *vol, float mn) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.n; i += (long long)gridDim.x * blockDim.x) {
-        bool on = keep[i];
-        if (!on) {
-            const int z = (int)(i / d.nxy);
-            const long long rr = i - z * d.nxy;
-            const int y = (int)(rr / d.nx), x = (int)(rr - (long long)y * d.nx);
-            if (x > 0 && y > 0 && z > 0 && x < d.nx - 1 && y < d.ny - 1 && z < d.nz - 1) {
-                for (int dz = -1; dz <= 1 && !on; dz++)
-                    for (int dy = -1; dy <= 1 && !on; dy++)
-                        for (int dx = -1; dx <= 1; dx++) {
-                            if ((dx | dy | dz) == 0 || (dx == -1 && dy == -1 && dz == -1)) continue;
-                            if (keep[i + dz * d.nxy + (long long)dy * d.nx + dx]) { on = true; break; }
-                        }
+// only; src/meshify.c:218-264) fused with the mask-out img = mn.  One warp per
+// row, 32 voxels a word: with R3 = K(x-1)|K(x)|K(x+1) and R2 = K(x)|K(x+1) of a
+// row, the neighbourhood is R3 of rows y-1..y+1 in slices z and z+1, R3 of rows
+// y and y+1 in slice z-1, and R2 of row y-1 in slice z-1.
+__global__ void __launch_bounds__(256) k_dilate_maskout(const unsigned char *__restrict__ keep, Dims d, float *vol, float mn) {
+    const int lane = threadIdx.x & 31;
+    const long long nrows = (long long)d.ny * d.nz;
+    const int nw = (d.nx + 31) / 32;
+    // rows used: 0..2 = y-1..y+1 in slice z, 3..5 in slice z+1, 6 = (y, z-1), 7 = (y+1, z-1), 8 = (y-1, z-1)
+    const int DY[9] = {-1, 0, 1, -1, 0, 1, 0, 1, -1}, DZ[9] = {0, 0, 0, 1, 1, 1, -1, -1, -1};
+    for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < nrows;
+         r += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const int z = (int)(r / d.ny), y = (int)(r - (long long)z * d.ny);
+        const bool ryz = y > 0 && z > 0 && y < d.ny - 1 && z < d.nz - 1;
+        auto word = [&](int dy, int dz, int xw) -> unsigned {
+            const int yy = y + dy, zz = z + dz, x = xw * 32 + lane;
+            const bool in = yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz && x < d.nx;
+            return __ballot_sync(0xffffffffu, in && keep[zz * d.nxy + (long long)yy * d.nx + x] != 0);
+        };
+        unsigned prev[9], cur[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            prev[k] = 0u;
+            cur[k] = word(DY[k], DZ[k], 0);
+        }
+        for (int xw = 0; xw < nw; xw++) {
+            unsigned on = 0u;
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                const unsigned nxt = word(DY[k], DZ[k], xw + 1);
+                const unsigned right = (cur[k] >> 1) | (nxt << 31);   // K(x+1)
+                on |= cur[k] | right | (k < 8 ? (cur[k] << 1) | (prev[k] >> 31) : 0u);   // row 8: no K(x-1)
+                prev[k] = cur[k];
+                cur[k] = nxt;
+            }
+            const int x = xw * 32 + lane;
+            if (x < d.nx) {
+                const bool kept = (prev[1] >> lane) & 1u;   // row (y, z): prev holds word xw now
+                const bool interior = ryz && x > 0 && x < d.nx - 1;
+                if (!(kept || (interior && ((on >> lane) & 1u)))) vol[r * d.nx + x] = mn;
             }
         }
-        if (!on) vol[i] = mn;
     }
 }
 
@@ -201,7 +273,11 @@ inline unsigned gsz(long long n) {
 n2m_status components(LabelWork &w, Dims d, unsigned char want, int conn, unsigned *d_nroots, cudaStream_t s) {
     int *L = w.lab.as<int>();
     { k_uf_init<<<gsz(d.n), 256, 0, s>>>(w.mask.as<unsigned char>(), d, want, L); N2M_COUNT(); }
-    { k_uf_merge<<<gsz(d.n), 256, 0, s>>>(L, d, conn == 6 ? 3 : conn == 18 ? 9 : 13); N2M_COUNT(); }
+    const unsigned gr = gsz((long long)d.ny * d.nz * 32);   // one warp per row
+    const unsigned char *m = w.mask.as<unsigned char>();
+    if (conn == 6) { k_uf_merge<3><<<gr, 256, 0, s>>>(m, want, L, d); N2M_COUNT(); }
+    else if (conn == 18) { k_uf_merge<9><<<gr, 256, 0, s>>>(m, want, L, d); N2M_COUNT(); }
+    else { k_uf_merge<13><<<gr, 256, 0, s>>>(m, want, L, d); N2M_COUNT(); }
     if (d_nroots) CK(cudaMemsetAsync(d_nroots, 0, sizeof(unsigned), s));
     { k_uf_flatten<<<gsz(d.n), 256, 0, s>>>(L, d.n, d_nroots); N2M_COUNT(); }
     CKL();
@@ -258,7 +334,7 @@ n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn
     CKL();
     CKS(label_core(w, d, 18, only_largest, fill_bubbles, s));
     if (fill_bubbles) { k_fill_iso<<<gsz(d.n), 256, 0, s>>>(vol, d.n, w.keep.as<unsigned char>(), iso); N2M_COUNT(); }
-    if (only_largest) { k_dilate_maskout<<<gsz(d.n), 256, 0, s>>>(w.keep.as<unsigned char>(), d, vol, mn); N2M_COUNT(); }
+    if (only_largest) { k_dilate_maskout<<<gsz((long long)d.ny * d.nz * 32), 256, 0, s>>>(w.keep.as<unsigned char>(), d, vol, mn); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
