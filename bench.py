@@ -487,6 +487,8 @@ def main():
     ap.add_argument("--profile", type=int, default=0, metavar="N",
                     help="profiling driver: two meshify calls on the CT-like workload at N^3 (same generator, "
                          "structure count scaled by volume), stage times printed; no bench line")
+    ap.add_argument("--largest", action="store_true", help="with --profile: keep only the largest cluster (-l 1)")
+    ap.add_argument("--bubbles", action="store_true", help="with --profile: fill bubbles (-b 1)")
     ap.add_argument("--profile-writer", type=int, default=0, metavar="N",
                     help="profiling driver: mesh the N^3 CT-like volume, then encode it twice as .mz3 gzip and once as .obj")
     ap.add_argument("--profile-atlas", action="store_true",
@@ -547,9 +549,9 @@ def main():
         d = torch.from_numpy(pv).cuda()
         ctx = n2m.Context(0)
         for _ in range(2):
-            _, _, nt, nv, rep = ctx.meshify_device(d.data_ptr(), (n, n, n), ISO, n2m.MC33, True, False, False)
+            _, _, nt, nv, rep = ctx.meshify_device(d.data_ptr(), (n, n, n), ISO, n2m.MC33, True, a.largest, a.bubbles)
         torch.cuda.synchronize()
-        print(json.dumps({"profile": n, "triangles": nt, "vertices": nv,
+        print(json.dumps({"profile": n, "largest": a.largest, "bubbles": a.bubbles, "triangles": nt, "vertices": nv,
                           "stage_ms": dict(zip(STAGE_NAMES, [round(x, 4) for x in rep["ms_stage"][:7]]))}))
         return
     rank, world, dist = dist_setup(a.gpus)

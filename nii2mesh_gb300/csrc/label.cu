@@ -41,7 +41,7 @@ __global__ void k_uf_init(const unsigned char *__restrict__ m, Dims d, unsigned 
         const unsigned act = left >= 32 ? 0xffffffffu : (1u << left) - 1u;
         const bool fg = m[i] == want;
         const bool left_fg = __shfl_up_sync(act, fg, 1);
-        const bool xpos = (i % d.nx) != 0;
+        const bool xpos = (unsigned)i % (unsigned)d.nx != 0u;   // n < 2^31
         const bool cont = fg && xpos && (lane > 0 ? left_fg : m[i - 1] == want);
         const unsigned starts = __ballot_sync(act, fg && !cont);
         int parent = -1;
@@ -125,26 +125,48 @@ __global__ void __launch_bounds__(256) k_uf_merge(const unsigned char *__restric
     }
 }
 
+// every voxel of the class points at its root; lanes sharing a parent (the
+// voxels of one run) walk its chain once
 __global__ void k_uf_flatten(int *L, long long n, unsigned *nroots) {
     unsigned c = 0;
+    const int lane = threadIdx.x & 31;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int p = L[i];
+        const unsigned grp = __match_any_sync(__activemask(), p);
+        const int lead = __ffs(grp) - 1;
+        int root = 0;
+        if (lane == lead && p >= 0) root = find_root(L, p);
+        root = __shfl_sync(grp, root, lead);
         if (p < 0) continue;
         if (p == (int)i) c++;
-        else L[i] = find_root(L, p);
+        else L[i] = root;
     }
     if (nroots && c) atomicAdd(nroots, c);
 }
 
-// background components touching a face of the volume
+// background components touching a face of the volume: one thread per face
+// voxel (slices z = 0 and z = nz-1 whole; rows y = 0 and y = ny-1 and
+// columns x = 0 and x = nx-1 of the slices between; a voxel on two faces is
+// visited twice, which writes the same flag)
 __global__ void k_edge_roots(const int *__restrict__ L, Dims d, unsigned char *edge) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.n; i += (long long)gridDim.x * blockDim.x) {
+    const long long inner = d.nz > 2 ? d.nz - 2 : 0;
+    const long long nface_z = d.nz > 1 ? 2 * d.nxy : d.nxy, nrow = inner * d.nx, ncol = inner * d.ny;
+    const long long total = nface_z + 2 * nrow + 2 * ncol;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        long long i;
+        if (t < nface_z) {
+            i = t < d.nxy ? t : (long long)(d.nz - 1) * d.nxy + (t - d.nxy);
+        } else if (t < nface_z + 2 * nrow) {
+            const long long u = t - nface_z, side = u / nrow, v = u - side * nrow;
+            const long long z = 1 + v / d.nx, x = v - (z - 1) * d.nx;
+            i = z * d.nxy + (side ? (long long)(d.ny - 1) * d.nx : 0) + x;
+        } else {
+            const long long u = t - nface_z - 2 * nrow, side = u / ncol, v = u - side * ncol;
+            const long long z = 1 + v / d.ny, y = v - (z - 1) * d.ny;
+            i = z * d.nxy + y * d.nx + (side ? d.nx - 1 : 0);
+        }
         const int r = L[i];
-        if (r < 0) continue;
-        const int z = (int)(i / d.nxy);
-        const long long rr = i - z * d.nxy;
-        const int y = (int)(rr / d.nx), x = (int)(rr - (long long)y * d.nx);
-        if (x == 0 || y == 0 || z == 0 || x == d.nx - 1 || y == d.ny - 1 || z == d.nz - 1) edge[r] = 1;
+        if (r >= 0) edge[r] = 1;
     }
 }
 
@@ -301,7 +323,7 @@ n2m_status label_core(LabelWork &w, Dims d, int conn, bool only_largest, bool fi
         CKS(w.edge.ensure((size_t)d.n));
         CKS(components(w, d, 0, 6, &misc->nbg, s));
         CK(cudaMemsetAsync(w.edge.p, 0, (size_t)d.n, s));
-        { k_edge_roots<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d, w.edge.as<unsigned char>()); N2M_COUNT(); }
+        { k_edge_roots<<<gsz(2 * d.nxy + 2 * (long long)d.nz * (d.nx + d.ny)), 256, 0, s>>>(w.lab.as<int>(), d, w.edge.as<unsigned char>()); N2M_COUNT(); }
         { k_fill_bubbles<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, w.edge.as<unsigned char>(), &misc->nbg,
                                                 w.mask.as<unsigned char>()); N2M_COUNT(); }
         CKL();
