@@ -55,15 +55,21 @@ __global__ void __launch_bounds__(NT, 2) k_smooth(const float *__restrict__ in, 
     acc.flush(st, true);
 }
 
-// range / bbox / non-finite count of an existing volume
+// range / bbox / non-finite count of an existing volume: a bounded grid whose
+// warps stride over the rows, so the block flushes (one set of atomics each)
+// stay few; every reduction is a min, max or count, so the order is free
 __global__ void __launch_bounds__(256) k_stats(const float *__restrict__ vol, int nx, int ny, int nz, float iso,
                                                VolStats *st, bool minmax) {
     Acc acc;
     acc.init();
-    const int y = blockIdx.y, z = blockIdx.z;
-    const float *row = vol + ((size_t)z * ny + y) * nx;
-    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < nx; x += gridDim.x * blockDim.x)
-        acc.add(__ldg(row + x), x, y, z, iso);
+    const long long nrows = (long long)ny * nz;
+    const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
+    for (long long r = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); r < nrows; r += (long long)gridDim.x * wpb) {
+        const int z = (int)(r / ny), y = (int)(r - (long long)z * ny);
+        const float *row = vol + r * nx;
+#pragma unroll 4
+        for (int x = lane; x < nx; x += 32) acc.add(__ldg(row + x), x, y, z, iso);
+    }
     acc.flush(st, minmax);
 }
 }  // namespace
@@ -392,7 +398,8 @@ n2m_status launch_smooth_adjoint(const float *g, float *tmp, float *out, int nx,
 
 n2m_status launch_stats(const float *vol, int nx, int ny, int nz, float iso, bool minmax, VolStats *st,
                         cudaStream_t s) {
-    dim3 grid((nx + 255) / 256 > 4 ? 4 : (nx + 255) / 256, ny, nz);
+    const long long rows = (long long)ny * nz;
+    const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((rows + 7) / 8, 152 * 8));   // 8 rows per block
     { k_stats<<<grid, 256, 0, s>>>(vol, nx, ny, nz, iso, st, minmax); N2M_COUNT(); }
     CKL();
     return N2M_OK;
