@@ -59,6 +59,20 @@ def test_selftest_known_answers(oracle):
         assert (len(v), len(t)) == (nv, nt) == (G["selftest"][str(obj)]["nvert"], G["selftest"][str(obj)]["ntri"])
 
 
+# The self-test fields written as N.nii (src/MarchingCubes.c:1355-1360) and meshed
+# through the whole nii2mesh path with -p 0 -l 0 -b 0 -r 1 -i 0.001: (triangles,
+# vertices) after the weld and the degenerate filter, per cube variant.
+KNOWN_MCTEST_CLI = {(0, MC33): (600, 302), (1, MC33): (41936, 20976), (2, MC33): (26828, 13416),
+                    (5, MC33): (50980, 25488), (8, MC33): (40368, 20186),
+                    (8, MC_CLASSIC_TABLE): (40356, 20184), (8, OLDCUBES): (40364, 20184)}
+
+
+@pytest.mark.parametrize("obj,variant", sorted(KNOWN_MCTEST_CLI))
+def test_mctest_cli_known_answers(oracle, obj, variant):
+    t, p = oracle.meshify(oracle.selftest_field(obj), 0.001, variant, False, False, False)[:2]
+    assert (len(t), len(p)) == KNOWN_MCTEST_CLI[(obj, variant)]
+
+
 def test_thresholds(oracle):
     for key, val in G["threshold"].items():
         name, mode = key.split(":")
