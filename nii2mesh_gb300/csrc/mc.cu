@@ -24,6 +24,7 @@
 #include <float.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "mc33.cuh"
 
@@ -699,13 +700,15 @@ n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, v
     const unsigned WX = (unsigned)((g.n[0] + 31) / 32);
     const unsigned nact = c.nactive;
     if (nact == 0) return N2M_OK;
-    static int resident = 0;   // CTAs of k_emit that fit the GPU at once
+    static std::atomic<int> resident_once{0};   // CTAs of k_emit that fit the GPU at once
+    int resident = resident_once.load(std::memory_order_relaxed);
     if (!resident) {
         int dev = 0, sms = 0, per_sm = 0;
         CK(cudaGetDevice(&dev));
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit, EG_WARPS * 32, 0));
         resident = sms * std::max(per_sm, 1);
+        resident_once.store(resident, std::memory_order_relaxed);
     }
     const unsigned gblocks = std::min<unsigned>(((nact + 31) / 32 + EG_WARPS - 1) / EG_WARPS, (unsigned)resident);
     CKS(w.ctr.ensure(sizeof(unsigned)));

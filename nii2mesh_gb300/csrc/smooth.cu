@@ -3,20 +3,13 @@
 //
 // The blur is three separable 5-tap passes (x, then y, then z) whose every
 // tap sum is rounded exactly as the reference's double arithmetic rounds it
-// (exact.cuh), so the output is bit-identical to quick_smooth().  Volumes
-// below 2^32 voxels run one streaming kernel per pass (k_pass_x,
-// k_pass_axis): a fast FP32 proof decides ~97 % of the taps, the rest are
-// batched per warp and recomputed in FP64 by full warps; the z pass also
-// reduces the range (min/max), the count of non-finite voxels and the bbox
-// of voxels >= iso.  Traffic: 8 B per voxel per pass, three passes.
-//
-// k_smooth (larger volumes, and the column routine the batched atlas uses):
-// one fused pass for all three blur passes.  A CTA owns a 32x16 column of
-// output voxels and streams along z over a chunk of slices: per input slice
-// it stages the raw slice (+2 halo in x and y) in shared memory, runs the x
-// pass for the 16+4 rows it needs, the y pass for its own 16 rows, and keeps
-// the last five y-pass results of each column in registers, so the z pass
-// needs no further memory traffic (4 B read + 4 B written per voxel).
+// (exact.cuh), so the output is bit-identical to quick_smooth().  One
+// streaming kernel per pass (k_pass_x, k_pass_axis): a fast FP32 proof
+// decides ~97 % of the taps, the rest are batched per warp and recomputed in
+// FP64 by full warps; the z pass also reduces the range (min/max), the count
+// of non-finite voxels and the bbox of voxels >= iso.  Traffic: 8 B per voxel
+// per pass, three passes.  (The batched atlas smooths its sub-boxes with the
+// fused column routine of smooth_core.cuh instead.)
 #include <float.h>
 
 #include <stdlib.h>
@@ -27,33 +20,6 @@
 
 namespace {
 using namespace smooth;
-
-struct VolSrc {
-    const float *in;
-    int nx;
-    size_t nxy;
-    __device__ __forceinline__ float load(int x, int y, int z) const {
-        return __ldg(in + (size_t)z * nxy + (size_t)y * nx + x);
-    }
-};
-struct VolSink {
-    float *out;
-    int nx;
-    size_t nxy;
-    __device__ __forceinline__ void put(int x, int y, int z, float v) { out[(size_t)z * nxy + (size_t)y * nx + x] = v; }
-};
-
-__global__ void __launch_bounds__(NT, 2) k_smooth(const float *__restrict__ in, float *__restrict__ out, int nx,
-                                                  int ny, int nz, float iso, VolStats *st) {
-    const size_t nxy = (size_t)nx * ny;
-    VolSrc src{in, nx, nxy};
-    VolSink sink{out, nx, nxy};
-    Acc acc;
-    acc.init();
-    const int z0 = blockIdx.z * SZC;
-    column(src, sink, acc, iso, blockIdx.x * STX, blockIdx.y * STY, z0, min(z0 + SZC, nz), nx, ny, nx, ny, nz);
-    acc.flush(st, true);
-}
 
 // range / bbox / non-finite count of an existing volume: a bounded grid whose
 // warps stride over the rows, so the block flushes (one set of atomics each)
@@ -305,62 +271,65 @@ constexpr int KRUN = 8, KSEG = 8;
 
 bool smooth_can_stage(int nx, int ny, int nz) { return (size_t)nx * ny * nz < ((size_t)1 << 32); }
 
-// nx*ny*nz < 2^32: three passes; larger volumes: the fused CTA-column kernel.
+// three passes; row and slice indices are 32-bit, so volumes stay below 2^32
+// voxels (meshify accepts at most 2^31-1)
 n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny, int nz, float iso, VolStats *st,
                          cudaStream_t s, const StagedInput *stage) {
     const size_t n = (size_t)nx * ny * nz;
-    if (n < ((size_t)1 << 32)) {
-        static int gx = 0, gx4 = 0, ga = 0, gz = 0;
-        if (!gx) {
-            gx = resident_blocks((const void *)k_pass_x, 256);
-            gx4 = resident_blocks((const void *)k_pass_x4, 256);
-            ga = resident_blocks((const void *)k_pass_axis<KRUN, KSEG, false>, 256);
-            gz = resident_blocks((const void *)k_pass_axis<KRUN, KSEG, true>, 256);
-        }
-        const unsigned nxy = (unsigned)nx * ny;
-        const Pass px{in, out, 1u, nx, ny, nxy, iso, st}, py{out, tmp, (unsigned)nx, nx, ny, nxy, iso, st},
-            pz{tmp, out, nxy, nx, ny, nxy, iso, st};
-        // 16-byte rows: the float4 x pass
-        const bool x4 = nx % 4 == 0 && ((uintptr_t)in & 15) == 0 && ((uintptr_t)out & 15) == 0;
-        auto pass_x = [&](unsigned r0, unsigned r1, unsigned g) -> n2m_status {
-            if (x4) { k_pass_x4<<<std::min<unsigned>(g, (unsigned)gx4), 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
-            else { k_pass_x<<<std::min<unsigned>(g, (unsigned)gx), 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
-            CKL();
-            return N2M_OK;
-        };
-        if (stage && stage->host) {
-            // the copy stream may only overwrite `in` once earlier work on s is done with it
-            CK(cudaEventRecord(stage->ev[N2M_STAGE_SLABS], s));
-            CK(cudaStreamWaitEvent(stage->copy, stage->ev[N2M_STAGE_SLABS], 0));
-            // per slab: x and y passes as soon as it has arrived, then the z pass of
-            // every slice whose five y-pass inputs are done
-            int zdone = 0;
-            for (int k = 0; k < N2M_STAGE_SLABS; k++) {
-                const int z0 = (int)((long long)nz * k / N2M_STAGE_SLABS), z1 = (int)((long long)nz * (k + 1) / N2M_STAGE_SLABS);
-                if (z1 <= z0) continue;
-                const size_t off = (size_t)z0 * nxy, bytes = (size_t)(z1 - z0) * nxy * sizeof(float);
-                CK(cudaMemcpyAsync((float *)in + off, stage->host + off, bytes, cudaMemcpyHostToDevice, stage->copy));
-                CK(cudaEventRecord(stage->ev[k], stage->copy));
-                CK(cudaStreamWaitEvent(s, stage->ev[k], 0));
-                const unsigned r0 = (unsigned)z0 * ny, r1 = (unsigned)z1 * ny;
-                CKS(pass_x(r0, r1, std::max<unsigned>(1u, (r1 - r0 + 7) / 8)));
-                { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, (unsigned)z0, (unsigned)(z1 - z0), 0, ny); N2M_COUNT(); }
-                const int zready = z1 == nz ? nz : z1 - 2;
-                if (zready > zdone) {
-                    { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 0u, 1u, zdone, zready); N2M_COUNT(); }
-                    zdone = zready;
-                }
-            }
-        } else {
-            CKS(pass_x(0u, (unsigned)ny * nz, 0xffffffffu));
-            { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, 0u, (unsigned)nz, 0, ny); N2M_COUNT(); }
-            { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 0u, 1u, 0, nz); N2M_COUNT(); }
-        }
+    if (n >= ((size_t)1 << 32)) {
+        n2m_set_error("smoothing supports fewer than 2^32 voxels");
+        return N2M_ERR_TOO_LARGE;
+    }
+    // resident CTAs of each pass kernel, found once; a function-local static is
+    // initialised exactly once even when threads call concurrently
+    struct PassGrids {
+        int x, x4, a, z;
+    };
+    static const PassGrids G = [] {
+        return PassGrids{resident_blocks((const void *)k_pass_x, 256), resident_blocks((const void *)k_pass_x4, 256),
+                         resident_blocks((const void *)k_pass_axis<KRUN, KSEG, false>, 256),
+                         resident_blocks((const void *)k_pass_axis<KRUN, KSEG, true>, 256)};
+    }();
+    const int gx = G.x, gx4 = G.x4, ga = G.a, gz = G.z;
+    const unsigned nxy = (unsigned)nx * ny;
+    const Pass px{in, out, 1u, nx, ny, nxy, iso, st}, py{out, tmp, (unsigned)nx, nx, ny, nxy, iso, st},
+        pz{tmp, out, nxy, nx, ny, nxy, iso, st};
+    // 16-byte rows: the float4 x pass
+    const bool x4 = nx % 4 == 0 && ((uintptr_t)in & 15) == 0 && ((uintptr_t)out & 15) == 0;
+    auto pass_x = [&](unsigned r0, unsigned r1, unsigned g) -> n2m_status {
+        if (x4) { k_pass_x4<<<std::min<unsigned>(g, (unsigned)gx4), 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
+        else { k_pass_x<<<std::min<unsigned>(g, (unsigned)gx), 256, 0, s>>>(px, r0, r1); N2M_COUNT(); }
         CKL();
         return N2M_OK;
+    };
+    if (stage && stage->host) {
+        // the copy stream may only overwrite `in` once earlier work on s is done with it
+        CK(cudaEventRecord(stage->ev[N2M_STAGE_SLABS], s));
+        CK(cudaStreamWaitEvent(stage->copy, stage->ev[N2M_STAGE_SLABS], 0));
+        // per slab: x and y passes as soon as it has arrived, then the z pass of
+        // every slice whose five y-pass inputs are done
+        int zdone = 0;
+        for (int k = 0; k < N2M_STAGE_SLABS; k++) {
+            const int z0 = (int)((long long)nz * k / N2M_STAGE_SLABS), z1 = (int)((long long)nz * (k + 1) / N2M_STAGE_SLABS);
+            if (z1 <= z0) continue;
+            const size_t off = (size_t)z0 * nxy, bytes = (size_t)(z1 - z0) * nxy * sizeof(float);
+            CK(cudaMemcpyAsync((float *)in + off, stage->host + off, bytes, cudaMemcpyHostToDevice, stage->copy));
+            CK(cudaEventRecord(stage->ev[k], stage->copy));
+            CK(cudaStreamWaitEvent(s, stage->ev[k], 0));
+            const unsigned r0 = (unsigned)z0 * ny, r1 = (unsigned)z1 * ny;
+            CKS(pass_x(r0, r1, std::max<unsigned>(1u, (r1 - r0 + 7) / 8)));
+            { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, (unsigned)z0, (unsigned)(z1 - z0), 0, ny); N2M_COUNT(); }
+            const int zready = z1 == nz ? nz : z1 - 2;
+            if (zready > zdone) {
+                { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 0u, 1u, zdone, zready); N2M_COUNT(); }
+                zdone = zready;
+            }
+        }
+    } else {
+        CKS(pass_x(0u, (unsigned)ny * nz, 0xffffffffu));
+        { k_pass_axis<KRUN, KSEG, false><<<ga, 256, 0, s>>>(py, ny, 0u, (unsigned)nz, 0, ny); N2M_COUNT(); }
+        { k_pass_axis<KRUN, KSEG, true><<<gz, 256, 0, s>>>(pz, nz, 0u, 1u, 0, nz); N2M_COUNT(); }
     }
-    dim3 grid((nx + STX - 1) / STX, (ny + STY - 1) / STY, (nz + SZC - 1) / SZC);
-    { k_smooth<<<grid, dim3(STX, STY), 0, s>>>(in, out, nx, ny, nz, iso, st); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
