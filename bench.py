@@ -144,7 +144,7 @@ def cpu_reference(vol, steps, warmup):
             times.append(t1 - t0)
     assert m is not None
     nvox = vol.size
-    return nvox / statistics.median(times) / 1e9, kind, times, len(m[0])
+    return nvox / statistics.median(times) / 1e9, kind, times, m
 
 
 def _reference_worker(path, rounds, start, done, out):
@@ -155,7 +155,7 @@ def _reference_worker(path, rounds, start, done, out):
     for _ in range(rounds):
         start.wait()
         m = impl.meshify(vol, ISO, 0, True, False, False)
-        out.put(0 if m is None else len(m[0]))
+        out.put((0, 0) if m is None else (len(m[0]), len(m[1])))
         done.wait()
 
 
@@ -189,7 +189,7 @@ def cpu_reference_parallel(vol, steps, warmup, procs):
           for _ in range(procs)]
     for w in ws:
         w.start()
-    times, ntri = [], 0
+    times, counts = [], (0, 0)
     try:
         for i in range(rounds):
             start.wait(timeout=600)
@@ -197,8 +197,8 @@ def cpu_reference_parallel(vol, steps, warmup, procs):
             res = [out.get(timeout=600) for _ in range(procs)]
             t1 = time.perf_counter()
             done.wait(timeout=600)
-            assert all(r > 0 for r in res)
-            ntri = res[0]
+            assert all(r[0] > 0 for r in res)
+            counts = res[0]
             if i >= warmup:
                 times.append(t1 - t0)
     finally:
@@ -206,7 +206,7 @@ def cpu_reference_parallel(vol, steps, warmup, procs):
             w.join(timeout=60)
         os.remove(path)
         os.rmdir(tmp)
-    return procs * vol.size / statistics.median(times) / 1e9, kind, times, ntri
+    return procs * vol.size / statistics.median(times) / 1e9, kind, times, counts
 
 
 def host_procs(bytes_per_proc=4.5e9):
@@ -225,15 +225,22 @@ def host_procs(bytes_per_proc=4.5e9):
     return max(1, min(cores, int(0.6 * avail / bytes_per_proc)))
 
 
+GD_LR = 4.0   # Adam step on the voxel intensities (the spheres are 100 on 0, iso 50)
+
+
 def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
     """fwd and fwd+bwd ms on the 128^3 differentiation workload (pre-smooth,
-    Lewiner MC, 10 HC iterations; loss = sum(|v - c| - 40)^2), and the time of
-    200 gradient-descent steps of shape fitting."""
+    Lewiner MC, 10 HC iterations; loss = sum(|v - c| - 40)^2), the gradient's
+    error against the FP64 host gradient of the same map, and 200 steps of
+    shape fitting (Adam on the voxel intensities; the mesh and its topology are
+    recomputed every step)."""
     from nii2mesh_gb300 import synth
     from nii2mesh_gb300.autograd import MeshifyFunction, sphere_loss
     ctx = n2m.Context(torch.cuda.current_device())
-    img = torch.from_numpy(synth.sphere128()).cuda()
+    host = synth.sphere128()
+    img = torch.from_numpy(host).cuda()
     center, radius = (63.5, 63.5, 63.5), 40.0
+    nvox = host.size
 
     def fwd(v):
         pts, _ = MeshifyFunction.apply(v, ctx, 50.0, 10)
@@ -256,27 +263,48 @@ def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
     def f_b():
         v = img.clone().requires_grad_(True)
         fwd(v).backward()
+        return v.grad
 
     t_f = timed(f_only, steps)
     t_fb = timed(f_b, steps)
-    v = img.clone()
+    grad = f_b().cpu().numpy()
+    _, _, nt, nv, _ = ctx.meshify_device(img.data_ptr(), (128, 128, 128), 50.0, n2m.MC33, True, False, False, 10)
+    # FP64 host gradient of the same fixed-topology map
+    from oracle.adjoint_ref import Problem
+    from oracle.oracle import Oracle
+    gh = Problem(Oracle(), host, 50.0, 10, center, radius).gradient(host)
+    rel = float(np.linalg.norm(grad - gh) / np.linalg.norm(gh))
+    # shape fitting: the loss is read back only at the first and the last step
+    v = img.clone().requires_grad_(True)
+    opt = torch.optim.Adam([v], lr=GD_LR)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     first = last = None
     for it in range(gd_steps):
-        v.requires_grad_(True)
+        opt.zero_grad(set_to_none=True)
         loss = fwd(v)
         loss.backward()
-        with torch.no_grad():
-            v = v - 0.05 * v.grad / (v.grad.abs().max() + 1e-12)
-        first = float(loss) if first is None else first
-        last = float(loss)
+        opt.step()
+        if it == 0:
+            first = loss.detach()
+        last = loss.detach()
     torch.cuda.synchronize()
     t_gd = time.perf_counter() - t0
+    first, last = float(first), float(last)
     ctx.close()
+    fb_bytes = 4.0 * nvox + 24.0 * nv + 12.0 * nt + 12.0 * nv + 4.0 * nvox
+    peak, peak_kind = peaks()
+    ach = fb_bytes / (t_fb * 1e-3) / 1e9
     return {"workload": "sphere128: 128^3 f32, spheres r 12-28, iso 50, -p 1, Lewiner, 10 HC iterations",
             "fwd_ms": round(t_f, 3), "fwd_bwd_ms": round(t_fb, 3), "ratio": round(t_fb / t_f, 3),
-            "gd200_s": round(t_gd, 3), "gd_loss_first_last": [round(first, 2), round(last, 2)],
+            "grad_rel_err_vs_fp64": rel,
+            "gd200_s": round(t_gd, 3), "gd_ms_per_step": round(1e3 * t_gd / gd_steps, 3),
+            "gd_loss_first_last": [round(first, 2), round(last, 2)],
+            "gd_loss_drop": round(1.0 - last / first, 4), "gd_optimizer": f"Adam lr {GD_LR} on the voxel values",
+            "roofline": {"bound": "hbm", "bytes": fb_bytes, "achieved": round(ach, 1), "peak": peak,
+                         "frac": round(ach / peak, 5), "peak_source": peak_kind,
+                         "formula": "fwd (4 N_vox + 24 N_vert + 12 N_tri) + bwd (12 N_vert in, 4 N_vox out) "
+                                    "per fwd+bwd wall-clock step"},
             "timing": "wall clock per step incl. host syncs (forward reads back counts)"}
 
 
@@ -289,6 +317,7 @@ def atlas_metric(n2m, torch, reps=3):
     d = torch.from_numpy(lab).cuda()
     ctx = n2m.Context(torch.cuda.current_device())
     out = {"workload": "atlas256: 256^3 int16, power-law Voronoi labels, iso 0.5, -p 1 -l 1 -b 1 -s 5, Lewiner"}
+    counts = {}
     for mode, name in ((n2m.ATLAS_BATCHED, "batched"), (n2m.ATLAS_LOOP, "loop")):
         ctx.atlas_device(d.data_ptr(), (256, 256, 256), mode=mode)
         ts = []
@@ -302,10 +331,20 @@ def atlas_metric(n2m, torch, reps=3):
         out[f"{name}_ms"] = round(1e3 * t, 2)
         out[f"{name}_meshes_per_s"] = round(ok / t, 1)
         out["meshes"] = ok
+        counts[name] = (nm, ok, nv, nt)
         if mode == n2m.ATLAS_BATCHED:
             out["batched_launches"] = rep["kernel_launches"]
             out["batched_stage_ms"] = [round(x, 3) for x in rep["ms_stage"][:5]]
+            nvox = lab.size
+            abytes = 2.0 * nvox + 24.0 * nv + 12.0 * nt
+            peak, peak_kind = peaks()
+            ach = abytes / t / 1e9
+            out["roofline"] = {"bound": "hbm", "bytes": abytes, "achieved": round(ach, 1), "peak": peak,
+                               "frac": round(ach / peak, 5), "peak_source": peak_kind,
+                               "formula": "(2 N_vox int16 labels + sum over meshes of 24 N_vert + 12 N_tri) / "
+                                          "batched wall-clock ms"}
     out["speedup_batched_vs_loop"] = round(out["batched_meshes_per_s"] / out["loop_meshes_per_s"], 2)
+    out["batched_equals_loop_counts"] = counts["batched"] == counts["loop"]
     ctx.close()
     # CPU: the reference's per-label work (binarise the whole volume, meshify, 5 HC iterations), one
     # label per host core at once as its OpenMP atlas loop runs them (src/nii2mesh.c:546-574)
@@ -335,6 +374,21 @@ def atlas_metric(n2m, torch, reps=3):
     out["cpu_baseline"] = {"meshes_per_s": round(len(labels) / tc, 4), "cores": len(labels), "kind": "port",
                            "sample": f"{len(labels)} labels (smallest to largest) through the full-volume per-label "
                                      f"path, one per host core ({tc:.1f} s)"}
+    # the same per-label work on one core, one label after another (OMP off)
+    from oracle.oracle import Oracle
+    o = Oracle()
+    img = lab.astype(np.float32)
+    one = [labels[0], labels[len(labels) // 2], labels[-1]]
+    t0 = time.perf_counter()
+    for lbl in one:
+        b, _ = o.binarize_label(img, lbl)
+        m = o.meshify(b, 0.5, 0, True, True, True)
+        if m is not None:
+            o.laplacian_smoothHC(m[1], m[0], 0.1, 0.5, 5, True)
+    t1 = time.perf_counter() - t0
+    out["cpu_baseline_1core"] = {"meshes_per_s": round(len(one) / t1, 4), "cores": 1, "kind": "port",
+                                 "sample": f"{len(one)} labels (smallest, median, largest of the sample) one after "
+                                           f"another on one core ({t1:.1f} s)"}
     return out
 
 
@@ -361,14 +415,21 @@ def brain_metric(n2m, torch, reps=5):
         out[f"e2e_{name}_ms"] = round(1e3 * statistics.median(ts), 3)
         out[f"h2d_{name}_bytes"] = int(raw.size * (1 if name == "u8" else 4))
         out["triangles"] = rep["ntri"]
+    g_raw = ctx.meshify(vol, iso, n2m.MC33, True, True, True, 0)[:2]
+    g_s = ctx.meshify(vol, iso, n2m.MC33, True, True, True, 20)[:2]
     ctx.close()
-    from oracle.oracle import Oracle
+    from oracle.oracle import Oracle, mesh_equal, smoothed_equal
     o = Oracle()
     t0 = time.perf_counter()
     m = o.meshify(vol, iso, 0, True, True, True)
-    o.laplacian_smoothHC(m[1], m[0], 0.1, 0.5, 20, True)
+    ms = o.laplacian_smoothHC(m[1], m[0], 0.1, 0.5, 20, True)
     out["cpu_ms"] = round(1e3 * (time.perf_counter() - t0), 1)
     out["cpu_kind"] = "port"
+    # parity of the same run: raw mesh bit for bit, HC positions against the oracle's FP64 HC
+    ok, _, _ = mesh_equal(g_raw, m, 0.0)
+    oks, d, _ = smoothed_equal(g_raw, g_s[1], m, ms, 1e-4)
+    out["brain182_raw_bit_exact"] = bool(ok and np.array_equal(g_raw[0], g_s[0]))
+    out["brain182_hc_max_err_vs_fp64"] = d if np.isfinite(d) else None
     return out
 
 
@@ -478,6 +539,12 @@ def writer_metric(n2m, torch, vol, reps=3):
     return out
 
 
+def bench_config(world, nt, nv):
+    """The workload description both arms print (the same dict for the same workload)."""
+    return {"workload": WORKLOAD, "l2": "inputs larger than L2 (537 MB volume)",
+            "parallelism": "replicas" if world > 1 else "single GPU", "triangles": nt, "vertices": nv}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -503,16 +570,16 @@ def main():
         if a.gpus > 1 and int(os.environ.get("RANK", "0")) != 0:
             return
         vol = synth.ct512()
-        steps = max(1, min(a.steps, 3))
         procs = host_procs()
-        gv, kind, times, nt = cpu_reference_parallel(vol, steps, 1, procs)
-        line = {"metric": METRIC, "value": round(gv, 6), "unit": "Gvox/s", "n_gpus": a.gpus, "steps": steps,
-                "warmup": 1, "ms_per_step": round(1e3 * statistics.median(times), 3), "higher_is_better": True,
+        gv, kind, times, (nt, nv) = cpu_reference_parallel(vol, a.steps, warmup, procs)
+        line = {"metric": METRIC, "value": round(gv, 6), "unit": "Gvox/s", "n_gpus": a.gpus, "steps": a.steps,
+                "warmup": warmup, "ms_per_step": round(1e3 * statistics.median(times), 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-                "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"}, "impl": "reference",
+                "config": bench_config(a.gpus, nt, nv), "impl": "reference",
                 "cpu_baseline": {"value": round(gv, 6), "unit": "Gvox/s", "cores": procs, "kind": kind,
                                  "sample": f"{procs} full 512^3 meshify calls per step, one per host core "
-                                           f"(meshify itself is single-threaded)"},
+                                           f"(meshify itself is single-threaded); median of {a.steps} steps "
+                                           f"after {warmup} warm-up steps"},
                 "e2e": {"value": round(gv, 6), "unit": "Gvox/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -589,23 +656,40 @@ def main():
     launches = sum(r["kernel_launches"] for r in reps)
     stage_ms = [statistics.mean(r["ms_stage"][i] for r in reps) for i in range(7)]
 
-    # roofline of the dominant stage (algorithmic bytes / CUDA-event duration)
+    # roofline of the dominant stage (algorithmic bytes / CUDA-event duration), every stage's
+    # figure beside it, and the whole path's: 4 B/voxel read once + 24 B/vertex + 12 B/triangle
+    # written once, over the whole step
     lo, hi = reps[-1]["lo"], reps[-1]["hi"]
     ngrid = (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1)
-    algo = {"smooth": 8.0 * nvox, "count": 4.0 * ngrid,
-            "emit": 24.0 * reps[-1]["nvert_raw"] + 12.0 * reps[-1]["ntri_raw"],
-            "degenerate": 24.0 * reps[-1]["ntri_raw"]}
+    nv_raw, nt_raw = reps[-1]["nvert_raw"], reps[-1]["ntri_raw"]
+    algo = {"smooth": 8.0 * nvox, "count": 4.0 * ngrid, "emit": 24.0 * nv_raw + 12.0 * nt_raw,
+            "weld": 24.0 * nv_raw + 24.0 * nv + 24.0 * nt_raw, "degenerate": 24.0 * nt_raw}
+    peak, peak_kind = peaks()
+    stages = {}
+    for i, nm in enumerate(STAGE_NAMES):
+        if nm not in algo or stage_ms[i] <= 0:
+            continue
+        ach = algo[nm] / (stage_ms[i] * 1e-3) / 1e9
+        st = {"ms": round(stage_ms[i], 4), "algorithmic_bytes": algo[nm], "achieved_gbs": round(ach, 1),
+              "frac": round(ach / peak, 4)}
+        if nm in NCU_TRAFFIC:
+            st["dram_bytes"] = NCU_TRAFFIC[nm]
+            st["dram_over_algorithmic"] = round(NCU_TRAFFIC[nm] / algo[nm], 2)
+        stages[nm] = st
     top = max(range(7), key=lambda i: stage_ms[i])
     name = STAGE_NAMES[top]
-    peak, peak_kind = peaks()
-    roof = None
-    if name in algo:
-        ach = algo[name] / (stage_ms[top] * 1e-3) / 1e9
-        roof = {"bound": "hbm", "kernel_stage": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                "algorithmic_bytes": algo[name], "traffic": NCU_TRAFFIC.get(name),
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels, one step",
-                "limited_by": STAGE_BOUND.get(name)}
+    whole = 4.0 * nvox + 24.0 * nv + 12.0 * nt
+    whole_gbs = whole / (ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel_stage": name, "achieved": stages.get(name, {}).get("achieved_gbs"), "peak": peak,
+            "unit": "GB/s", "frac": stages.get(name, {}).get("frac"), "peak_source": peak_kind,
+            "algorithmic_bytes": algo.get(name), "traffic": NCU_TRAFFIC.get(name),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels, one step",
+            "limited_by": STAGE_BOUND.get(name),
+            "whole_path": {"bytes": whole, "achieved": round(whole_gbs, 1), "frac": round(whole_gbs / peak, 4),
+                           "formula": "(4 N_vox + 24 N_vert + 12 N_tri) / ms_per_step / peak",
+                           "dram_bytes": sum(NCU_TRAFFIC.values()),
+                           "dram_over_algorithmic": round(sum(NCU_TRAFFIC.values()) / whole, 2)},
+            "stages": stages}
 
     # e2e through the C ABI with host buffers: the volume from pinned memory, the mesh copied back into
     # pinned arrays the caller allocates once and reuses (n2m_meshify_into); the malloc-returning
@@ -634,11 +718,18 @@ def main():
 
     if rank != 0:
         return
-    cpu = None
+    cpu, parity = None, {}
     if world == 1:
-        gv, kind, times, _ = cpu_reference(vol, 1, 0)
+        from oracle.oracle import mesh_equal
+        gv, kind, times, cmesh = cpu_reference(vol, 1, 0)
         cpu = {"value": round(gv, 6), "unit": "Gvox/s", "cores": 1, "kind": kind,
                "sample": f"one full 512^3 meshify ({times[0]:.1f} s)"}
+        # the mesh the timed calls produce (last host-memory call) against the CPU path's, outside the timed region
+        ok, d, msg = mesh_equal((tris, pts), cmesh, 0.0)
+        parity = {"ct512_bit_exact": bool(ok), "ct512_max_dpos": d if np.isfinite(d) else None,
+                  "ct512_detail": msg, "ct512_against": kind,
+                  "rule": "identical counts and canonical connectivity; positions within 0 (raw) / 1e-4 (HC) voxels"}
+        del cmesh
     adj = adjoint_metric(n2m, torch) if world == 1 else None
     atl = atlas_metric(n2m, torch) if world == 1 else None
     thr = threshold_metric(n2m, torch) if world == 1 else None
@@ -647,11 +738,16 @@ def main():
     line = {"metric": METRIC, "value": round(value, 4), "unit": "Gvox/s", "n_gpus": world, "steps": a.steps,
             "warmup": warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD, "l2": "inputs larger than L2 (537 MB volume)",
-                       "parallelism": "replicas" if world > 1 else "single GPU", "triangles": nt, "vertices": nv},
+            "config": bench_config(world, nt, nv),
             "stage_ms": {n: round(v, 4) for n, v in zip(STAGE_NAMES, stage_ms)},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck,
-            "adjoint": adj, "atlas": atl, "threshold": thr, "brain": brn, "writer": wrt}
+            "parity": parity, "adjoint": adj, "atlas": atl, "threshold": thr, "brain": brn, "writer": wrt}
+    if brn:
+        parity.update({k: brn.pop(k) for k in ("brain182_raw_bit_exact", "brain182_hc_max_err_vs_fp64")})
+    if adj:
+        parity["adjoint128_grad_rel_err_vs_fp64"] = adj.pop("grad_rel_err_vs_fp64")
+    if atl:
+        parity["atlas256_batched_equals_loop_counts"] = atl.pop("batched_equals_loop_counts")
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

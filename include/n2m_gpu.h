@@ -246,7 +246,10 @@ n2m_status n2m_save_mesh_device(n2m_context *ctx, const char *fnm, const vec3i *
 n2m_status n2m_deflate_device(n2m_context *ctx, const void *d_src, size_t nbytes, int container, unsigned char **out,
                               size_t *out_len);
 
-/* HC smoothing of device-resident meshes (d_verts updated in place). */
+/* HC smoothing of device-resident meshes (d_verts updated in place).  A
+ * triangle index outside [0, nvert) makes the call fail with N2M_ERR_BAD_ARGS
+ * and leaves d_verts unchanged (the kernels skip such triangles, so nothing is
+ * read or written out of bounds). */
 n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri,
                                 double alpha, double beta, int iter, bool lock_edges);
 
@@ -259,11 +262,15 @@ n2m_status n2m_smooth_hc_device(n2m_context *ctx, vec3d *d_verts, const vec3i *d
  * loads the library until the process exits), so meshes are limited to
  * N2M_NOALLOC_MAX_VERTS vertices and N2M_NOALLOC_MAX_TRIS triangles; larger
  * meshes fail with N2M_ERR_TOO_LARGE before any work is queued.  d_verts and
- * d_tris are device pointers; the work is queued on `stream` (a cudaStream_t,
- * NULL = legacy default stream) and the call returns without waiting.  The
- * first call on each device looks up the array's device address (make it
- * before any stream capture).  Every call shares the one array: calls whose
- * work overlaps on the GPU race and corrupt each other's results. */
+ * d_tris are device pointers; the work runs on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) and the call returns once it has finished: it
+ * reads back a 4-byte flag into host stack memory, and a triangle index
+ * outside [0, nvert) fails with N2M_ERR_BAD_ARGS with d_verts unchanged.
+ * Each call looks up the array's device address on the current device (this
+ * allocates nothing); the first call on a device may load the library's
+ * device code, so make it before any stream capture.  Every call shares the
+ * one array: calls whose work overlaps on the GPU race and corrupt each
+ * other's results. */
 #define N2M_NOALLOC_MAX_VERTS 131072
 #define N2M_NOALLOC_MAX_TRIS 262144
 n2m_status n2m_smooth_hc_noalloc(vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri, double alpha,

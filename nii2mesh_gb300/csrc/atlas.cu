@@ -1076,8 +1076,11 @@ n2m_status atlas_batched(const short *d_lab, const int dim[3], const n2m_options
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     const n2m_status cst = seg.enqueue(w, w.chunk, w.per_sm, chunks, s);
     const cudaError_t ce = cudaStreamEndCapture(s, &graph);
-    CKS(cst);
-    CK(ce);
+    if (cst != N2M_OK || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        CKS(cst);
+        CK(ce);
+    }
     cudaGraphExec_t exec = (cudaGraphExec_t)w.exec;
     bool updated = false;
     if (exec) {

@@ -1016,7 +1016,9 @@ extern "C" n2m_status n2m_smooth_hc_device(n2m_context *c, vec3d *d_verts, const
                                            double alpha, double beta, int iter, bool lock_edges) {
     if (!c) return N2M_ERR_BAD_ARGS;
     CK(cudaSetDevice(c->device));
+    if (nvert < 0 || ntri < 0) return N2M_ERR_BAD_ARGS;
     CKS(mesh_smooth_hc(d_verts, d_tris, nvert, ntri, alpha, beta, iter, lock_edges, c->hc, c->scan, c->stream));
+    CKS(mesh_smooth_hc_check(c->hc, nvert, iter, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return N2M_OK;
 }
@@ -1194,6 +1196,10 @@ extern "C" void laplacian_smoothHC(vec3d *verts, vec3i *tris, int nvert, int ntr
                                    bool lockEdges) {
     n2m_context *c;
     n2m_status s = default_ctx(&c);
+    if (s == N2M_OK && (nvert < 0 || ntri < 0 || (nvert > 0 && !verts) || (ntri > 0 && !tris))) {
+        n2m_set_error("laplacian_smoothHC: bad arguments");
+        s = N2M_ERR_BAD_ARGS;
+    }
     if (s == N2M_OK && nvert > 0 && iter > 0) {
         s = N2M_ERR_CUDA;
         if (c->hmesh.ensure((size_t)nvert * sizeof(vec3d) + (size_t)std::max(ntri, 1) * sizeof(vec3i)) == N2M_OK) {
@@ -1202,6 +1208,7 @@ extern "C" void laplacian_smoothHC(vec3d *verts, vec3i *tris, int nvert, int ntr
             if (cudaMemcpyAsync(dv, verts, (size_t)nvert * sizeof(vec3d), cudaMemcpyHostToDevice, c->stream) == cudaSuccess &&
                 cudaMemcpyAsync(dt, tris, (size_t)ntri * sizeof(vec3i), cudaMemcpyHostToDevice, c->stream) == cudaSuccess) {
                 s = mesh_smooth_hc(dv, dt, nvert, ntri, alpha, beta, iter, lockEdges, c->hc, c->scan, c->stream);
+                if (s == N2M_OK) s = mesh_smooth_hc_check(c->hc, nvert, iter, c->stream);
                 if (s == N2M_OK &&
                     (cudaMemcpyAsync(verts, dv, (size_t)nvert * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
                      cudaStreamSynchronize(c->stream) != cudaSuccess))

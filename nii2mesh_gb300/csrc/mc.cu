@@ -700,15 +700,18 @@ n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, v
     const unsigned WX = (unsigned)((g.n[0] + 31) / 32);
     const unsigned nact = c.nactive;
     if (nact == 0) return N2M_OK;
-    static std::atomic<int> resident_once{0};   // CTAs of k_emit that fit the GPU at once
-    int resident = resident_once.load(std::memory_order_relaxed);
+    // CTAs of k_emit that fit the GPU at once, per device ordinal (the emit takes
+    // its work from an atomic counter, so any grid is correct; this one is fastest)
+    static std::atomic<int> resident_of[64];
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    int resident = dev < 64 ? resident_of[dev].load(std::memory_order_relaxed) : 0;
     if (!resident) {
-        int dev = 0, sms = 0, per_sm = 0;
-        CK(cudaGetDevice(&dev));
+        int sms = 0, per_sm = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit, EG_WARPS * 32, 0));
         resident = sms * std::max(per_sm, 1);
-        resident_once.store(resident, std::memory_order_relaxed);
+        if (dev < 64) resident_of[dev].store(resident, std::memory_order_relaxed);
     }
     const unsigned gblocks = std::min<unsigned>(((nact + 31) / 32 + EG_WARPS - 1) / EG_WARPS, (unsigned)resident);
     CKS(w.ctr.ensure(sizeof(unsigned)));

@@ -10,8 +10,6 @@
 //   * apply_sform (src/meshify.c:1021-1045).
 #include <float.h>
 
-#include <mutex>
-
 #include "n2m_internal.cuh"
 
 namespace {
@@ -139,18 +137,33 @@ __global__ void __launch_bounds__(CB) k_deg_compact(const vec3i *__restrict__ t,
 }
 
 // ---- HC smoothing ----------------------------------------------------------------
-__global__ void k_degree(const vec3i *__restrict__ t, int nt, unsigned *deg) {
+// A triangle with an index outside [0, np) is skipped here and in k_fill_refs
+// (so it never enters the CSR and nothing downstream reads past the vertex
+// arrays) and raises *bad; k_hc_out then leaves every vertex untouched and the
+// entry points report N2M_ERR_BAD_ARGS.
+__device__ __forceinline__ bool tri_in_range(const vec3i &T, int np) {
+    return (unsigned)T.x < (unsigned)np && (unsigned)T.y < (unsigned)np && (unsigned)T.z < (unsigned)np;
+}
+
+__global__ void k_degree(const vec3i *__restrict__ t, int nt, int np, unsigned *deg, unsigned *bad) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
-        atomicAdd(&deg[t[i].x], 1u);
-        atomicAdd(&deg[t[i].y], 1u);
-        atomicAdd(&deg[t[i].z], 1u);
+        const vec3i T = t[i];
+        if (!tri_in_range(T, np)) {
+            *bad = 1u;
+            continue;
+        }
+        atomicAdd(&deg[T.x], 1u);
+        atomicAdd(&deg[T.y], 1u);
+        atomicAdd(&deg[T.z], 1u);
     }
 }
 
-__global__ void k_fill_refs(const vec3i *__restrict__ t, int nt, const unsigned *__restrict__ start, unsigned *fill,
-                            int *refs) {
+__global__ void k_fill_refs(const vec3i *__restrict__ t, int nt, int np, const unsigned *__restrict__ start,
+                            unsigned *fill, int *refs) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
-        const int v[3] = {t[i].x, t[i].y, t[i].z};
+        const vec3i T = t[i];
+        if (!tri_in_range(T, np)) continue;
+        const int v[3] = {T.x, T.y, T.z};
         for (int s = 0; s < 3; s++) refs[start[v[s]] + atomicAdd(&fill[v[s]], 1u)] = 3 * i + s;
     }
 }
@@ -260,7 +273,8 @@ __global__ void k_border(const vec3i *__restrict__ t, const unsigned *__restrict
 }
 
 __global__ void k_hc_out(vec3d *o, const float3 *__restrict__ P, const unsigned char *__restrict__ border, int np,
-                         bool lock) {
+                         bool lock, const unsigned *__restrict__ bad) {
+    if (*bad) return;   // a triangle index was out of range: leave the mesh as it was
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
         if (lock && border[i]) continue;
         const float3 d = P[i];
@@ -407,13 +421,15 @@ n2m_status mesh_smooth_hc(vec3d *d_pts, const vec3i *d_tris, int np, int nt, dou
     CKS(w.Lo.ensure((size_t)np * sizeof(float3)));
     CKS(w.hasnb.ensure((size_t)np));
     CKS(w.border.ensure((size_t)np));
+    CKS(w.bad.ensure(sizeof(unsigned)));
     unsigned *start = w.start.as<unsigned>();
     CK(cudaMemsetAsync(start, 0, ((size_t)np + 1) * sizeof(unsigned), s));
     CK(cudaMemsetAsync(w.fill.p, 0, (size_t)np * sizeof(unsigned), s));
-    { k_degree<<<gs(nt), 256, 0, s>>>(d_tris, nt, start); N2M_COUNT(); }
+    CK(cudaMemsetAsync(w.bad.p, 0, sizeof(unsigned), s));
+    { k_degree<<<gs(nt), 256, 0, s>>>(d_tris, nt, np, start, w.bad.as<unsigned>()); N2M_COUNT(); }
     CKL();
     CKS(scan_u32(start, (size_t)np + 1, start + np + 0, sw, s));  // start[np] receives the total as well
-    { k_fill_refs<<<gs(nt), 256, 0, s>>>(d_tris, nt, start, w.fill.as<unsigned>(), w.refs.as<int>()); N2M_COUNT(); }
+    { k_fill_refs<<<gs(nt), 256, 0, s>>>(d_tris, nt, np, start, w.fill.as<unsigned>(), w.refs.as<int>()); N2M_COUNT(); }
     { k_sort_refs<<<gs(np), 256, 0, s>>>(start, np, w.refs.as<int>()); N2M_COUNT(); }
     { k_hc_init<<<gs(np), 256, 0, s>>>(d_pts, d_tris, start, w.refs.as<int>(), np, w.Lo.as<float3>(), w.P.as<float3>(),
                                      w.hasnb.as<unsigned char>()); N2M_COUNT(); }
@@ -430,8 +446,21 @@ n2m_status mesh_smooth_hc(vec3d *d_pts, const vec3i *d_tris, int np, int nt, dou
         CK(cudaMemsetAsync(w.border.p, 0, (size_t)np, s));
         { k_border<<<gs(np), 256, 0, s>>>(d_tris, start, w.refs.as<int>(), np, w.border.as<unsigned char>()); N2M_COUNT(); }
     }
-    { k_hc_out<<<gs(np), 256, 0, s>>>(d_pts, w.P.as<float3>(), w.border.as<unsigned char>(), np, lock_edges); N2M_COUNT(); }
+    { k_hc_out<<<gs(np), 256, 0, s>>>(d_pts, w.P.as<float3>(), w.border.as<unsigned char>(), np, lock_edges,
+                                    w.bad.as<unsigned>()); N2M_COUNT(); }
     CKL();
+    return N2M_OK;
+}
+
+n2m_status mesh_smooth_hc_check(HcWork &w, int np, int iter, cudaStream_t s) {
+    if (np <= 0 || iter <= 0) return N2M_OK;
+    unsigned bad = 0;
+    CK(cudaMemcpyAsync(&bad, w.bad.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (bad) {
+        n2m_set_error("HC smoothing: a triangle index is outside [0, nvert); the vertices were left unchanged");
+        return N2M_ERR_BAD_ARGS;
+    }
     return N2M_OK;
 }
 
@@ -498,12 +527,10 @@ constexpr size_t NA_B = NA_Q + na_align(NA_V * 12);
 constexpr size_t NA_LO = NA_B + na_align(NA_V * 12);
 constexpr size_t NA_HASNB = NA_LO + na_align(NA_V * 12);
 constexpr size_t NA_BORDER = NA_HASNB + na_align(NA_V);
-constexpr size_t NA_TOTAL = NA_BORDER + na_align(NA_V);
+constexpr size_t NA_BAD = NA_BORDER + na_align(NA_V);
+constexpr size_t NA_TOTAL = NA_BAD + na_align(4);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_TOTAL];
-
-void *g_noalloc_addr[128];     // device address of g_noalloc_scratch, per device
-std::mutex g_noalloc_mu;
 
 // exclusive scan of n <= NA_V + 1 counts in one CTA (n is small by construction)
 __global__ void __launch_bounds__(1024) k_scan_small(unsigned *d, int n) {
@@ -530,8 +557,10 @@ __global__ void __launch_bounds__(1024) k_scan_small(unsigned *d, int n) {
 }
 }  // namespace
 
-// First call on each device looks up the device address of the scratch array
-// with that device current; make that first call before any stream capture.
+// Every call looks up the device address of the scratch array on the current
+// device (cudaGetSymbolAddress allocates nothing), so the address is never
+// stale, e.g. after the caller reset the device.  The first call on a device
+// may load the library's device code; make it before any stream capture.
 extern "C" n2m_status n2m_smooth_hc_noalloc(vec3d *d_verts, const vec3i *d_tris, int nvert, int ntri, double alpha,
                                             double beta, int iter, bool lock_edges, void *stream) {
     if (nvert < 0 || ntri < 0 || (nvert > 0 && !d_verts) || (ntri > 0 && !d_tris)) {
@@ -544,31 +573,22 @@ extern "C" n2m_status n2m_smooth_hc_noalloc(vec3d *d_verts, const vec3i *d_tris,
         return N2M_ERR_TOO_LARGE;
     }
     if (nvert == 0 || iter <= 0) return N2M_OK;
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 128) return N2M_ERR_BAD_ARGS;
-    unsigned char *base;
-    {
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
-            void *p = nullptr;
-            CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-            g_noalloc_addr[dev] = p;
-        }
-        base = (unsigned char *)g_noalloc_addr[dev];
-    }
+    unsigned char *base = nullptr;
+    CK(cudaGetSymbolAddress((void **)&base, g_noalloc_scratch));
     cudaStream_t s = (cudaStream_t)stream;
     unsigned *start = (unsigned *)(base + NA_START), *fill = (unsigned *)(base + NA_FILL);
     int *refs = (int *)(base + NA_REFS);
     float3 *P = (float3 *)(base + NA_P), *Q = (float3 *)(base + NA_Q), *B = (float3 *)(base + NA_B),
            *Lo = (float3 *)(base + NA_LO);
     unsigned char *hasnb = base + NA_HASNB, *border = base + NA_BORDER;
+    unsigned *bad = (unsigned *)(base + NA_BAD);
     // the array keeps the previous call's contents: clear what must start at zero
     CK(cudaMemsetAsync(start, 0, ((size_t)nvert + 1) * sizeof(unsigned), s));
     CK(cudaMemsetAsync(fill, 0, (size_t)nvert * sizeof(unsigned), s));
-    { k_degree<<<gs(ntri), 256, 0, s>>>(d_tris, ntri, start); N2M_COUNT(); }
+    CK(cudaMemsetAsync(bad, 0, sizeof(unsigned), s));
+    { k_degree<<<gs(ntri), 256, 0, s>>>(d_tris, ntri, nvert, start, bad); N2M_COUNT(); }
     { k_scan_small<<<1, 1024, 0, s>>>(start, nvert + 1); N2M_COUNT(); }
-    { k_fill_refs<<<gs(ntri), 256, 0, s>>>(d_tris, ntri, start, fill, refs); N2M_COUNT(); }
+    { k_fill_refs<<<gs(ntri), 256, 0, s>>>(d_tris, ntri, nvert, start, fill, refs); N2M_COUNT(); }
     { k_sort_refs<<<gs(nvert), 256, 0, s>>>(start, nvert, refs); N2M_COUNT(); }
     { k_hc_init<<<gs(nvert), 256, 0, s>>>(d_verts, d_tris, start, refs, nvert, Lo, P, hasnb); N2M_COUNT(); }
     const float a1 = (float)(1.0 - alpha), b = (float)beta, b1 = (float)(1.0 - beta);
@@ -580,7 +600,15 @@ extern "C" n2m_status n2m_smooth_hc_noalloc(vec3d *d_verts, const vec3i *d_tris,
         CK(cudaMemsetAsync(border, 0, (size_t)nvert, s));
         { k_border<<<gs(nvert), 256, 0, s>>>(d_tris, start, refs, nvert, border); N2M_COUNT(); }
     }
-    { k_hc_out<<<gs(nvert), 256, 0, s>>>(d_verts, P, border, nvert, lock_edges); N2M_COUNT(); }
+    { k_hc_out<<<gs(nvert), 256, 0, s>>>(d_verts, P, border, nvert, lock_edges, bad); N2M_COUNT(); }
     CKL();
+    // the validity flag comes back through pageable host memory: a plain copy, no allocation
+    unsigned h_bad = 0;
+    CK(cudaMemcpyAsync(&h_bad, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h_bad) {
+        n2m_set_error("n2m_smooth_hc_noalloc: a triangle index is outside [0, nvert); the vertices were left unchanged");
+        return N2M_ERR_BAD_ARGS;
+    }
     return N2M_OK;
 }

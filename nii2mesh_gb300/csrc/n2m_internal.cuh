@@ -188,10 +188,16 @@ struct DegWork {
 n2m_status mesh_remove_degenerate(const vec3d *d_pts, const vec3i *d_tris_in, int nt, vec3i *d_tris_out,
                                   unsigned *d_nt_out, DegWork &w, ScanWork &sw, cudaStream_t s);
 struct HcWork {
-    DevBuf start, refs, fill, P, Q, B, Lo, border, hasnb;
+    DevBuf start, refs, fill, P, Q, B, Lo, border, hasnb, bad;
 };
+// Triangles with an index outside [0, np) are skipped and flagged; the flag
+// makes the last kernel leave d_pts unchanged.  mesh_smooth_hc_check waits for
+// the stream and returns N2M_ERR_BAD_ARGS when the flag was raised (entry
+// points that take the caller's triangles call it; meshify's own meshes are
+// valid by construction).
 n2m_status mesh_smooth_hc(vec3d *d_pts, const vec3i *d_tris, int np, int nt, double alpha, double beta, int iter,
                           bool lock_edges, HcWork &w, ScanWork &sw, cudaStream_t s);
+n2m_status mesh_smooth_hc_check(HcWork &w, int np, int iter, cudaStream_t s);
 // adjoint of mesh_smooth_hc (uses the CSR and border flags the forward left in w)
 n2m_status mesh_smooth_hc_backward(const vec3i *d_tris, int np, double alpha, double beta, int iter, bool lock_edges,
                                    HcWork &w, const float3 *d_g, float3 *d_go, cudaStream_t s);

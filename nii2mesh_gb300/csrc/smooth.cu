@@ -15,6 +15,8 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "smooth_core.cuh"
 
@@ -258,15 +260,54 @@ __global__ void __launch_bounds__(256, 4) k_pass_axis(Pass P, int len, unsigned 
     if (STATS) acc.flush(P.st, true);
 }
 
+// resident CTAs of a kernel on the current device, or 0 when the query fails
 int resident_blocks(const void *fn, int threads) {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess)
-        return 152 * 4;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     return sms * std::max(per_sm, 1);
 }
 
 constexpr int KRUN = 8, KSEG = 8;
+
+// resident CTAs of each pass kernel, per device ordinal: queried on the first
+// call on that device and kept once every query succeeded (a failed query
+// gives 4 CTAs per SM of this call's device and is asked again next time)
+struct PassGrids {
+    int x, x4, a, z;
+};
+PassGrids pass_grids() {
+    static std::mutex mu;
+    static std::map<int, PassGrids> known;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) cudaGetLastError();
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = known.find(dev);
+        if (it != known.end()) return it->second;
+    }
+    PassGrids g{resident_blocks((const void *)k_pass_x, 256), resident_blocks((const void *)k_pass_x4, 256),
+                resident_blocks((const void *)k_pass_axis<KRUN, KSEG, false>, 256),
+                resident_blocks((const void *)k_pass_axis<KRUN, KSEG, true>, 256)};
+    if (g.x && g.x4 && g.a && g.z) {
+        std::lock_guard<std::mutex> lk(mu);
+        known[dev] = g;
+        return g;
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    if (!g.x) g.x = 4 * sms;
+    if (!g.x4) g.x4 = 4 * sms;
+    if (!g.a) g.a = 4 * sms;
+    if (!g.z) g.z = 4 * sms;
+    return g;
+}
 }  // namespace
 
 bool smooth_can_stage(int nx, int ny, int nz) { return (size_t)nx * ny * nz < ((size_t)1 << 32); }
@@ -280,16 +321,7 @@ n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny
         n2m_set_error("smoothing supports fewer than 2^32 voxels");
         return N2M_ERR_TOO_LARGE;
     }
-    // resident CTAs of each pass kernel, found once; a function-local static is
-    // initialised exactly once even when threads call concurrently
-    struct PassGrids {
-        int x, x4, a, z;
-    };
-    static const PassGrids G = [] {
-        return PassGrids{resident_blocks((const void *)k_pass_x, 256), resident_blocks((const void *)k_pass_x4, 256),
-                         resident_blocks((const void *)k_pass_axis<KRUN, KSEG, false>, 256),
-                         resident_blocks((const void *)k_pass_axis<KRUN, KSEG, true>, 256)};
-    }();
+    const PassGrids G = pass_grids();
     const int gx = G.x, gx4 = G.x4, ga = G.a, gz = G.z;
     const unsigned nxy = (unsigned)nx * ny;
     const Pass px{in, out, 1u, nx, ny, nxy, iso, st}, py{out, tmp, (unsigned)nx, nx, ny, nxy, iso, st},

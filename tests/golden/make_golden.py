@@ -8,12 +8,16 @@ Writes
   inputs.npz    the small seeded input volumes (stored, so that every machine
                 meshes bit-identical inputs)
   golden.json   reference results: counts and SHA-256 of canonical meshes,
-                label volumes, thresholds, self-test known answers
+                label volumes, thresholds, self-test known answers, and the
+                counts the reference's nii2mesh program writes for the
+                self-test volumes and data/bet.nii.gz (with each command)
   hc.npz        reference HC-smoothed vertices (compared with a tolerance)
 """
+import gzip
 import hashlib
 import json
 import re
+import struct
 import subprocess
 import sys
 import tempfile
@@ -28,7 +32,9 @@ sys.path.insert(0, str(ROOT))
 from nii2mesh_gb300 import synth  # noqa: E402
 from oracle.oracle import MC33, MC_CLASSIC_TABLE, OLDCUBES, Reference, canonical  # noqa: E402
 
-SRC = Path("/root/reference/src")
+from oracle.refpath import reference_src  # noqa: E402
+
+SRC = reference_src()   # N2M_REFERENCE, or a `reference` checkout beside this repository
 OPTION_SETS = [(True, True, False), (True, False, False), (False, False, False), (True, True, True),
                (False, True, True), (True, False, True)]
 
@@ -65,6 +71,25 @@ def inputs():
         "brain_small": synth.brain()[::4, ::4, ::4].astype(np.float32),
         "blobs40": blobs,
     }
+
+
+def run_cli(d, name, obj, src, variant, args):
+    """Run the reference's nii2mesh program (oracle/_ref: nii2mesh = `make lewiner`,
+    nii2mesh_classic = the default oldcubes build) and read the triangle and vertex
+    counts from the header of the .mz3 it writes (gzip, the default quality)."""
+    exe = "nii2mesh_classic" if variant == OLDCUBES else "nii2mesh"
+    opts = (["-o", "1"] if variant == MC_CLASSIC_TABLE else []) + list(args)
+    out = Path(d) / "cli_out.mz3"
+    subprocess.run([str(ROOT / "oracle" / "_ref" / exe), str(src), *opts, str(out)], check=True, cwd=d,
+                   capture_output=True)
+    raw = out.read_bytes()
+    if raw[:2] == b"\x1f\x8b":
+        raw = gzip.decompress(raw)
+    sig, _, nface, nvert, _ = struct.unpack("<HHIII", raw[:16])
+    assert sig == 23117, "not an mz3 file"
+    out.unlink()
+    return {"input": name, "object": obj, "variant": variant, "ntri": nface, "nvert": nvert,
+            "command": " ".join([exe, Path(src).name if obj is None else f"{obj}.nii", *opts, "out.mz3"])}
 
 
 def main():
@@ -125,6 +150,16 @@ def main():
             raw = (Path(d) / f"{obj}.nii").read_bytes()
             field = np.frombuffer(raw, np.float32, 60 ** 3, 352)
             g["selftest"][str(obj)] = {"nvert": counts[obj][0], "ntri": counts[obj][1], "field_sha256": raw_hash(field)}
+        # whole-program known answers: the reference's nii2mesh program run on the self-test
+        # volumes it wrote (N.nii) and on its own data/bet.nii.gz
+        g["cli"] = []
+        for obj in (0, 1, 2, 5, 8):
+            for variant in ((MC33, MC_CLASSIC_TABLE, OLDCUBES) if obj == 8 else (MC33,)):
+                g["cli"].append(run_cli(d, "selftest", obj, Path(d) / f"{obj}.nii", variant,
+                                        ["-p", "0", "-l", "0", "-b", "0", "-r", "1", "-i", "0.001"]))
+        bet = SRC.parent / "data" / "bet.nii.gz"
+        for variant in (MC33, MC_CLASSIC_TABLE, OLDCUBES):
+            g["cli"].append(run_cli(d, "bet.nii.gz", None, bet, variant, ["-r", "1"]))
     (HERE / "golden.json").write_text(json.dumps(g, indent=1))
     print("wrote", HERE / "golden.json")
 

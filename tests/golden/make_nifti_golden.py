@@ -21,7 +21,10 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-SRC = Path("/root/reference/src")
+sys.path.insert(0, str(ROOT))
+from oracle.refpath import reference_src  # noqa: E402
+
+SRC = reference_src()   # N2M_REFERENCE, or a `reference` checkout beside this repository
 DT = {np.uint8: 2, np.int16: 4, np.float32: 16, np.uint16: 512}
 
 

@@ -29,7 +29,9 @@ sys.path.insert(0, str(ROOT))
 from nii2mesh_gb300 import synth  # noqa: E402
 from oracle.oracle import Oracle  # noqa: E402
 
-SRC = Path("/root/reference/src")
+from oracle.refpath import reference_src  # noqa: E402
+
+SRC = reference_src()   # N2M_REFERENCE, or a `reference` checkout beside this repository
 EXTS = ["mz3", "gii", "inflated", "pial", "json", "off", "obj", "ply", "stl", "vtk"]
 
 

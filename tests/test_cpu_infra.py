@@ -8,6 +8,8 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from oracle.refpath import reference_src
+
 ROOT = Path(__file__).resolve().parents[1]
 
 
@@ -90,7 +92,7 @@ def test_mesh_format_rule_matches_reference_rule():
         assert L.n2m_mesh_format_of(n.encode()) == W.format_of(n), n
 
 
-REF_SRC = Path("/root/reference/src")
+REF_SRC = reference_src() or Path("/nonexistent")
 
 
 @pytest.mark.skipif(not (REF_SRC / "nii2mesh.c").exists() or shutil.which("gcc") is None,
@@ -121,3 +123,50 @@ def test_reference_program_links_against_library(tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert "Usage" in out.stdout
+
+
+# SHA-256 of the reference's marching-cubes tables (the LookUpTable.h tables in
+# process_cube's order, then oldcubes.c's edgeTable and triTable), each element
+# a little-endian int32, as tests/cpu_harness/table_check.c writes them: taken
+# from the reference's own files where they are present (the test below checks
+# it there), and compared with the packed tables everywhere.
+MC_TABLES_SHA256 = "c6dc08cd3fc42588817af879b104779dbee4e8e96aac983914f5e523203e6e94"
+
+
+def _classic_tables_inc(src_text):
+    """oldcubes.c's edgeTable / triTable declarations with their initialisers,
+    cut verbatim out of the function that holds them"""
+    out = []
+    for decl in (r"int\s+edgeTable\s*\[256\]\s*=", r"int\s+triTable\s*\[256\]\s*\[16\]\s*="):
+        i = re.search(decl, src_text).start()
+        j = src_text.index("};", i) + 2
+        out.append(src_text[i:j])
+    return "\n".join(out) + "\n"
+
+
+def test_mc_tables_match_reference(tmp_path):
+    """every entry of the packed tables (nii2mesh_gb300/csrc/mc_tables.h) equals
+    the reference's, read by the C compiler from LookUpTable.h and oldcubes.c
+    (not by the script that generated the packed copy); without the reference
+    tree, the packed tables' stream must hash to the reference's committed hash"""
+    import hashlib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("needs a C compiler")
+    csrc = ROOT / "nii2mesh_gb300" / "csrc"
+    exe = tmp_path / "tc_ours"
+    subprocess.run([cc, "-O1", "-fsigned-char", "-I", str(csrc), "-o", str(exe),
+                    str(ROOT / "tests/cpu_harness/table_check.c")], check=True)
+    ours = subprocess.run([str(exe), "ours"], check=True, capture_output=True).stdout
+    assert hashlib.sha256(ours).hexdigest() == MC_TABLES_SHA256
+    src = reference_src()
+    if src is None:
+        return
+    (tmp_path / "classic_tables.inc").write_text(_classic_tables_inc((src / "oldcubes.c").read_text()))
+    exe = tmp_path / "tc_ref"
+    subprocess.run([cc, "-O1", "-fsigned-char", "-w", "-DWITH_REFERENCE", "-I", str(csrc), "-I", str(src),
+                    "-I", str(tmp_path), "-o", str(exe), str(ROOT / "tests/cpu_harness/table_check.c")], check=True)
+    r = subprocess.run([str(exe), "ref"], capture_output=True)
+    assert r.returncode == 0, r.stderr.decode()[-2000:]
+    assert r.stdout == ours
+    assert hashlib.sha256(r.stdout).hexdigest() == MC_TABLES_SHA256

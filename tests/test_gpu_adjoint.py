@@ -44,7 +44,10 @@ def test_adjoint_vs_finite_differences(oracle, iters):
 
 def test_adjoint_128_workload(oracle):
     """the differentiation workload: 128^3, spheres r 12-28, 10 HC iterations,
-    loss to a sphere of radius 40 at the volume centre"""
+    loss to a sphere of radius 40 at the volume centre; the gradient against
+    the FP64 host gradient, and against FP64 central finite differences at 64
+    random near-surface voxels (voxels whose gradient is at least 1 % of the
+    largest: only voxels within the stencil's reach of the surface have one)"""
     img = synth.sphere128()
     center, radius = (63.5, 63.5, 63.5), 40.0
     pb = Problem(oracle, img, 50.0, 10, center, radius)
@@ -53,7 +56,7 @@ def test_adjoint_128_workload(oracle):
     assert np.linalg.norm(g - gh) / np.linalg.norm(gh) < REL
     rng = np.random.default_rng(5)
     cand = np.argwhere(np.abs(gh) > 1e-2 * np.abs(gh).max())
-    vox = cand[rng.choice(len(cand), 8, replace=False)]
+    vox = cand[rng.choice(len(cand), 64, replace=False)]
     fd = pb.central_difference(img, vox, 1e-2)
     rel = np.abs(g[tuple(vox.T)] - fd) / (np.abs(fd) + 1e-3 * np.abs(gh).max())
     assert rel.max() < REL, rel.max()

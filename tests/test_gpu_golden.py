@@ -102,3 +102,30 @@ def test_sform_golden(gpu):
     for e in G["sform"]:
         tt, pp = gpu.apply_sform(p, t, *e["rows"])
         assert raw_hash(tt.astype(np.int32), pp.astype(np.float64)) == e["sha256"]
+
+
+def test_hc_rejects_out_of_range_index(gpu):
+    """a triangle index outside [0, nvert) (past the end, or negative) fails
+    with N2M_ERR_BAD_ARGS through the device entry point and leaves the
+    vertices unchanged; the drop-in laplacian_smoothHC leaves the caller's
+    vertices unchanged; the next call on the same context is correct again"""
+    import ctypes as C
+    import torch
+    hc = np.load(GOLD / "hc.npz")
+    t, p = hc["tris"].astype(np.int32), hc["pts"]
+    L = gpu.lib()
+    ctx = gpu.Context(0)
+    for bad in (len(p), -1, 1 << 30):
+        tb = t.copy()
+        tb[len(tb) // 2, 1] = bad
+        dt = torch.from_numpy(tb).cuda()
+        dp = torch.from_numpy(p).cuda()
+        st = L.n2m_smooth_hc_device(ctx.h, C.c_void_p(dp.data_ptr()), C.c_void_p(dt.data_ptr()), len(p), len(tb),
+                                    0.1, 0.5, 3, True)
+        assert st == 4, st
+        assert b"outside" in L.n2m_last_error()
+        assert np.array_equal(dp.cpu().numpy(), p)
+        assert np.array_equal(gpu.laplacian_smoothHC(p, tb, 0.1, 0.5, 3, True), p)
+    got = gpu.laplacian_smoothHC(p, t, 0.1, 0.5, 1, True)
+    assert np.abs(got - hc["smoothed_1"]).max() <= 1e-4
+    ctx.close()

@@ -9,11 +9,12 @@ import numpy as np
 import pytest
 
 from nii2mesh_gb300 import synth
-from oracle.oracle import MC33, MC_CLASSIC_TABLE, OLDCUBES, mesh_equal
+from oracle.oracle import MC33, MC_CLASSIC_TABLE, OLDCUBES, mesh_equal, smoothed_equal
 
 pytestmark = pytest.mark.gpu
 
 POS_TOL = 0.0   # raw vertices are bit-exact (spec bar: 1e-5 voxels)
+HC_TOL = 1e-4   # HC-smoothed vertices, voxels (spec bar)
 
 
 def small_spheres(seed=10, n=48):
@@ -64,6 +65,35 @@ def test_brain_u8(gpu, oracle):
         got, want = run_both(gpu, oracle, vol, iso, variant, True, True, True)
         ok, d, msg = mesh_equal(got, want, POS_TOL)
         assert ok, msg
+
+
+@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE])
+def test_brain182_full_options(gpu, oracle, variant):
+    """the brain-sized workload with every option it names: 182x218x182 uint8
+    cast to float32, the Otsu 'medium' isolevel of the raw volume, -p 1 -l 1
+    -b 1 with the Lewiner (-o 0) and classic (-o 1) tables, then -s 20 HC
+    smoothing as nii2 runs it (alpha 0.1, beta 0.5, borders locked;
+    src/nii2mesh.c:326-331).  The isolevel and the raw mesh must equal the
+    oracle's bit for bit; the smoothed vertices, through the drop-in
+    laplacian_smoothHC and through n2m_meshify's own post-smooth, must lie
+    within 1e-4 voxels of the oracle's FP64 HC (src/quadric.c:343-394)"""
+    vol = synth.brain().astype(np.float32)
+    iso = oracle.set_threshold(vol, 2)
+    assert gpu.set_threshold(vol, 2) == iso
+    got, want = run_both(gpu, oracle, vol, iso, variant, True, True, True)
+    ok, d, msg = mesh_equal(got, want, POS_TOL)
+    assert ok, msg
+    assert len(want[0]) > 100_000
+    want_s = oracle.laplacian_smoothHC(want[1], want[0], 0.1, 0.5, 20, True)
+    got_s = gpu.laplacian_smoothHC(got[1], got[0], 0.1, 0.5, 20, True)
+    ok, d, msg = smoothed_equal(got, got_s, want, want_s, HC_TOL)
+    assert ok, msg
+    ctx = gpu.Context(0)
+    cubes = gpu.CLASSIC_TABLE if variant == MC_CLASSIC_TABLE else gpu.MC33
+    t, p, _ = ctx.meshify(vol, iso, cubes, True, True, True, post_smooth=20)
+    assert np.array_equal(t, got[0])
+    assert np.abs(p - got_s).max() <= HC_TOL
+    ctx.close()
 
 
 def test_selftest_fields_meshify(gpu, oracle):

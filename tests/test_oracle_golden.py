@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 from oracle.oracle import MC33, MC_CLASSIC_TABLE, OLDCUBES, Reference, canonical, mesh_equal, reference_available
+from oracle.refpath import reference_data
 
 GOLD = Path(__file__).resolve().parent / "golden"
 G = json.loads((GOLD / "golden.json").read_text())
@@ -60,14 +61,15 @@ def test_selftest_known_answers(oracle):
 
 
 # The self-test fields written as N.nii (src/MarchingCubes.c:1355-1360) and meshed
-# through the whole nii2mesh path with -p 0 -l 0 -b 0 -r 1 -i 0.001: (triangles,
-# vertices) after the weld and the degenerate filter, per cube variant.
-KNOWN_MCTEST_CLI = {(0, MC33): (600, 302), (1, MC33): (41936, 20976), (2, MC33): (26828, 13416),
-                    (5, MC33): (50980, 25488), (8, MC33): (40368, 20186),
-                    (8, MC_CLASSIC_TABLE): (40356, 20184), (8, OLDCUBES): (40364, 20184)}
+# by the reference's whole nii2mesh program with -p 0 -l 0 -b 0 -r 1 -i 0.001:
+# (triangles, vertices) after the weld and the degenerate filter, per cube
+# variant, read from the .mz3 files it wrote (tests/golden/make_golden.py
+# records each command beside its counts).
+KNOWN_MCTEST_CLI = {(e["object"], e["variant"]): (e["ntri"], e["nvert"]) for e in G["cli"] if e["input"] == "selftest"}
 
 
-@pytest.mark.parametrize("obj,variant", sorted(KNOWN_MCTEST_CLI))
+@pytest.mark.parametrize("obj,variant", [(0, MC33), (1, MC33), (2, MC33), (5, MC33), (8, MC33),
+                                         (8, MC_CLASSIC_TABLE), (8, OLDCUBES)])
 def test_mctest_cli_known_answers(oracle, obj, variant):
     t, p = oracle.meshify(oracle.selftest_field(obj), 0.001, variant, False, False, False)[:2]
     assert (len(t), len(p)) == KNOWN_MCTEST_CLI[(obj, variant)]
@@ -162,7 +164,7 @@ def test_writers_match_reference(case):
 
 
 
-REF_DATA = Path("/root/reference/data")
+REF_DATA = reference_data() or Path("/nonexistent")
 
 
 def _load_reference_volume(name):
@@ -186,11 +188,11 @@ def _load_reference_volume(name):
     return vol.reshape(nz, ny, nx), srow
 
 
-# bet.nii.gz with the CLI defaults (Otsu medium, -p 1 -l 1 -b 0 -r 1): triangles
-# per cube variant, as the reference prints them (Lewiner 344,400 with 172,304
-# vertices; the classic table under the Lewiner build and the oldcubes build differ)
-KNOWN_BET_TRIANGLES = {("bet.nii.gz", MC33): 344400, ("bet.nii.gz", MC_CLASSIC_TABLE): 344448,
-                       ("bet.nii.gz", OLDCUBES): 344340}
+# bet.nii.gz through the reference's nii2mesh program with its defaults (Otsu
+# medium, -p 1 -l 1 -b 0) and -r 1: (triangles, vertices) per cube variant as its
+# .mz3 output holds them (make_golden.py records the commands); the reference's
+# meshify called directly must give the same counts
+KNOWN_BET = {("bet.nii.gz", e["variant"]): (e["ntri"], e["nvert"]) for e in G["cli"] if e["input"] == "bet.nii.gz"}
 
 
 @pytest.mark.skipif(not ((REF_DATA / "bet.nii.gz").exists() and reference_available() and reference_available(True)),
@@ -211,9 +213,8 @@ def test_real_images_oracle_vs_reference(oracle, name):
         got = oracle.meshify(vol, iso, variant, True, True, False)
         ok, d, msg = mesh_equal(got, want, 0.0)
         assert ok, (name, variant, msg)
-        if (name, variant) in KNOWN_BET_TRIANGLES:
-            assert len(got[0]) == KNOWN_BET_TRIANGLES[(name, variant)]
-            assert variant != MC33 or len(got[1]) == 172304
+        if (name, variant) in KNOWN_BET:
+            assert (len(got[0]), len(got[1])) == KNOWN_BET[(name, variant)]
     want = ref.meshify(vol, iso, MC33, True, True, True)
     got = oracle.meshify(vol, iso, MC33, True, True, True)
     ok, d, msg = mesh_equal(got, want, 0.0)

@@ -58,4 +58,15 @@ def test_noalloc_matches_regular_entry_point(gpu):
     st = L.n2m_smooth_hc_noalloc(C.c_void_p(got.data_ptr()), C.c_void_p(dt.data_ptr()), 131073, len(t), 0.1, 0.5, 1,
                                  True, C.c_void_p(0))
     assert st == 8 and b"exceeds" in L.n2m_last_error()
+    # a triangle index outside [0, nvert): the kernels skip that triangle (no
+    # access out of bounds, in the scratch array or the caller's arrays), the
+    # call fails with N2M_ERR_BAD_ARGS and the vertices stay as they were
+    tb = t.astype(np.int32).copy()
+    tb[3, 2] = len(p)
+    dtb = torch.from_numpy(tb).cuda()
+    before = got.clone()
+    st = L.n2m_smooth_hc_noalloc(C.c_void_p(got.data_ptr()), C.c_void_p(dtb.data_ptr()), len(p), len(tb), 0.1, 0.5, 3,
+                                 True, C.c_void_p(0))
+    assert st == 4 and b"outside" in L.n2m_last_error()
+    assert torch.equal(got, before)
     ctx.close()
