@@ -122,3 +122,73 @@ N2M_HD bool tap5_fast(float a, float b, float c, float d, float e, float *out) {
     return false;
 }
 
+// ---- split fast path ------------------------------------------------------------
+// A cheaper exact evaluation for taps whose inputs lie within a factor 64 of
+// one another (the common case: CT air at -1000 +- 20 straddles a binade,
+// tissue values sit within a few binades).  With the /40 taken out, the tap is
+//     E = N / 5,   N = (2(a+e) + 9(b+d) + 18c) / 8,
+// and N is computed EXACTLY as NH + NL: every input is split into a high part
+// (its 12 low mantissa bits cleared) and the exact low remainder, and the
+// weighted sums of the high parts and of the low parts are each exact in FP32
+// (all terms lie on a common grid and stay below 2^24 grid steps when
+// max|x| <= 64 min|x|).  The float y ~ N/5 and the exact residual
+// R = N - 5y (also exact, see below) then say whether y, or its neighbour
+// y +- ulp, is the correctly rounded N/5: accepted only when
+// |N - 5q| < 2.5 ulp strictly, so exact ties (which the reference's double
+// rounding errors decide) and binade edges are left to tap5_fast / FP64.
+// Against the reference: its double result D lies within 10 * 2^-53 max|x| of
+// N/5, while a non-tie N/5 is at least 2^-32 max|x| / 5 from every rounding
+// boundary, so float(D) is the same q.  The test |y| >= max|x| * 2^-8 (no
+// deep cancellation) keeps the residual exact and the result normal.
+//
+// Exactness of the residual: y's ulp u >= 2^(p-31) for max|x| in [2^p,
+// 2^(p+1)); NH - 5y is a multiple of u of magnitude < 5 * 2^(p-11) + 8u, and
+// (NH - 5y) + NL a multiple of 2^(p-32) of magnitude < 8u: both fit 24 bits.
+
+// x = h + l exactly, h = x with its 12 low mantissa bits cleared
+N2M_HD void split12(float x, float &h, float &l) {
+    h = u2f(f2u(x) & 0xFFFFF000u);
+    l = FSUB(x, h);
+}
+
+// the condition under which tap5_split may be used on taps drawn from a group
+// of inputs whose magnitudes have minimum mn and maximum mx
+N2M_HD bool split_group_ok(float mn, float mx) {
+    return mn >= FMUL(mx, 0x1p-6f) && mx >= 0x1p-90f && mx < 0x1p+120f;
+}
+
+// Exact tap from split inputs.  Precondition: split_group_ok(mn, mx) for a
+// group holding all five inputs, and mth = mx * 2^-8.  Returns true (and
+// *out = the reference's float result) or false (undecided: tie, binade edge
+// or cancellation); *out is written either way.
+N2M_HD bool tap5_split(float aH, float aL, float bH, float bL, float cH, float cL, float dH, float dL, float eH,
+                       float eL, float mth, float *out) {
+    const float s1H = FADD(aH, eH), s2H = FADD(bH, dH);
+    const float NH = FFMA(cH, 2.25f, FFMA(s2H, 1.125f, FMUL(s1H, 0.25f)));
+    const float s1L = FADD(aL, eL), s2L = FADD(bL, dL);
+    const float NL = FFMA(cL, 2.25f, FFMA(s2L, 1.125f, FMUL(s1L, 0.25f)));
+    const float y = FMUL(FADD(NH, NL), 0.2f);
+    const float R2 = FADD(FFMA(-5.0f, y, NH), NL);   // N - 5y, exact
+    const uint32_t yb = f2u(y);
+    const float u = u2f((yb & 0x7F800000u) - (23u << 23));   // ulp(y) for |y| >= 2^-103
+    const float t25 = FMUL(u, 2.5f);
+    const float step = fabsf(R2) >= t25 ? u2f(f2u(u) | (f2u(R2) & 0x80000000u)) : 0.0f;
+    *out = FADD(y, step);                             // y or its neighbour towards N/5
+    const float R3 = FFMA(-5.0f, step, R2);           // N - 5q, exact
+    return fabsf(R3) < t25 && (yb & 0x7FFFFFu) != 0u && fabsf(y) >= mth;
+}
+
+// tap5_split on five raw inputs, the group being the window itself
+N2M_HD bool tap5_split_window(float a, float b, float c, float d, float e, float *out) {
+    const float mx = fmaxf(fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fabsf(c), fabsf(d))), fabsf(e));
+    const float mn = fminf(fminf(fminf(fabsf(a), fabsf(b)), fminf(fabsf(c), fabsf(d))), fabsf(e));
+    if (!split_group_ok(mn, mx)) return false;
+    float aH, aL, bH, bL, cH, cL, dH, dL, eH, eL;
+    split12(a, aH, aL);
+    split12(b, bH, bL);
+    split12(c, cH, cL);
+    split12(d, dH, dL);
+    split12(e, eH, eL);
+    return tap5_split(aH, aL, bH, bL, cH, cL, dH, dL, eH, eL, FMUL(mx, 0x1p-8f), out);
+}
+
