@@ -268,12 +268,6 @@ def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
     t_f = timed(f_only, steps)
     t_fb = timed(f_b, steps)
     grad = f_b().cpu().numpy()
-    _, _, nt, nv, _ = ctx.meshify_device(img.data_ptr(), (128, 128, 128), 50.0, n2m.MC33, True, False, False, 10)
-    # FP64 host gradient of the same fixed-topology map
-    from oracle.adjoint_ref import Problem
-    from oracle.oracle import Oracle
-    gh = Problem(Oracle(), host, 50.0, 10, center, radius).gradient(host)
-    rel = float(np.linalg.norm(grad - gh) / np.linalg.norm(gh))
     # shape fitting: the loss is read back only at the first and the last step
     v = img.clone().requires_grad_(True)
     opt = torch.optim.Adam([v], lr=GD_LR)
@@ -291,7 +285,13 @@ def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
     torch.cuda.synchronize()
     t_gd = time.perf_counter() - t0
     first, last = float(first), float(last)
+    _, _, nt, nv, _ = ctx.meshify_device(img.data_ptr(), (128, 128, 128), 50.0, n2m.MC33, True, False, False, 10)
     ctx.close()
+    # FP64 host gradient of the same fixed-topology map
+    from oracle.adjoint_ref import Problem
+    from oracle.oracle import Oracle
+    gh = Problem(Oracle(), host, 50.0, 10, center, radius).gradient(host)
+    rel = float(np.linalg.norm(grad - gh) / np.linalg.norm(gh))
     fb_bytes = 4.0 * nvox + 24.0 * nv + 12.0 * nt + 12.0 * nv + 4.0 * nvox
     peak, peak_kind = peaks()
     ach = fb_bytes / (t_fb * 1e-3) / 1e9

@@ -99,6 +99,25 @@ struct FixStage {
         if (fail) buf[n + __popc(m & ((1u << lane) - 1u))] = vox;
         n += __popc(m);
     }
+    // every lane queues the voxels base + k * step for the set bits k of fm
+    // (one warp scan of the lanes' counts instead of one ballot per output)
+    __device__ __forceinline__ void push_mask(unsigned fm, unsigned base, unsigned step, int lane) {
+        if (!__any_sync(FULL, fm != 0u)) return;
+        const int c = __popc(fm);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        int at = n + incl - c;
+        while (fm) {
+            const int k = __ffs(fm) - 1;
+            fm &= fm - 1u;
+            buf[at++] = base + (unsigned)k * step;
+        }
+        n += __shfl_sync(FULL, incl, 31);
+    }
     __device__ __forceinline__ void drain(const Pass &P, Acc &acc, int lane) {
         while (n >= 32) {
             n -= 32;
@@ -111,6 +130,44 @@ struct FixStage {
         n = 0;
     }
 };
+
+// K outputs from the K + 4 inputs w[0 .. K+3] of one lane (output k is the tap
+// sum of w[k .. k+4]).  When the K + 4 magnitudes lie within a factor 64 of one
+// another the split path decides each tap (exact.cuh: tap5_split), otherwise
+// tap5_fast; bit k of the returned mask marks an output neither could decide
+// (r[k] is then a placeholder that the FP64 fix-up overwrites).
+template <int K>
+__device__ __forceinline__ unsigned taps_run(const float (&w)[K + 4], float (&r)[K]) {
+    float mx = fabsf(w[0]), mn = fabsf(w[0]);
+#pragma unroll
+    for (int k = 1; k < K + 4; k++) {
+        mx = fmaxf(mx, fabsf(w[k]));
+        mn = fminf(mn, fabsf(w[k]));
+    }
+    unsigned fm = 0;
+    if (split_group_ok(mn, mx)) {
+        float h[K + 4], l[K + 4];
+#pragma unroll
+        for (int k = 0; k < K + 4; k++) split12(w[k], h[k], l[k]);
+        const float mth = FMUL(mx, 0x1p-8f);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            float t;
+            if (!tap5_split(h[k], l[k], h[k + 1], l[k + 1], h[k + 2], l[k + 2], h[k + 3], l[k + 3], h[k + 4], l[k + 4],
+                            mth, &t))
+                fm |= 1u << k;
+            r[k] = t;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            float t = w[k + 2];
+            if (!tap5_fast(w[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], &t)) fm |= 1u << k;
+            r[k] = t;
+        }
+    }
+    return fm;
+}
 
 // x pass: each warp takes whole rows (rows row0 .. row1-1 of the volume).
 __global__ void __launch_bounds__(256) k_pass_x(Pass P, unsigned row0, unsigned row1) {
@@ -164,19 +221,23 @@ __global__ void __launch_bounds__(256) k_pass_x4(Pass P, unsigned row0, unsigned
             const float4 A = act && q > 0 ? __ldg(r4 + q - 1) : zero;
             const float4 B = act ? __ldg(r4 + q) : zero;
             const float4 C = act && q + 1 < nq ? __ldg(r4 + q + 1) : zero;
-            const float v[12] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w, C.x, C.y, C.z, C.w};   // x0-4 .. x0+7
+            // x0-2 .. x0+5; past the row ends (only face voxels read them) stand-ins from
+            // this quad, so that the group test of the split path sees row values only
+            const float w[8] = {q > 0 ? A.z : B.x, q > 0 ? A.w : B.x, B.x, B.y, B.z, B.w,
+                                q + 1 < nq ? C.x : B.w, q + 1 < nq ? C.y : B.w};
             float o[4];
-            bool fail[4];
+            unsigned fm = 0;
+            if (act) {
+                fm = taps_run<4>(w, o);
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int x = x0 + j;
-                o[j] = v[4 + j];
-                fail[j] = act && x >= 2 && x <= nx - 3 && !tap5_fast(v[2 + j], v[3 + j], v[4 + j], v[5 + j], v[6 + j], &o[j]);
+                for (int j = 0; j < 4; j++)
+                    if (x0 + j < 2 || x0 + j > nx - 3) {   // face voxels keep their input
+                        o[j] = w[2 + j];
+                        fm &= ~(1u << j);
+                    }
+                o4[q] = make_float4(o[0], o[1], o[2], o[3]);
             }
-            if (act) o4[q] = make_float4(o[0], o[1], o[2], o[3]);
-            const unsigned base = row * (unsigned)nx + (unsigned)x0;
-#pragma unroll
-            for (int j = 0; j < 4; j++) F.push(fail[j], base + j, lane);
+            F.push_mask(fm, row * (unsigned)nx + (unsigned)x0, 1u, lane);
             F.drain(P, acc, lane);
         }
     }
@@ -193,7 +254,7 @@ __global__ void __launch_bounds__(256) k_pass_x4(Pass P, unsigned row0, unsigned
 template <int K, int SEGS, bool STATS>
 __global__ void __launch_bounds__(256, 4) k_pass_axis(Pass P, int len, unsigned outer0, unsigned nouter, int p_lo,
                                                       int p_hi) {
-    __shared__ unsigned stage_buf[8][32 * (K + 1)];   // < 32 entries between runs, + 32 per step
+    __shared__ unsigned stage_buf[8][32 * (K + 1)];   // < 32 entries between segments, + up to 32 K per segment
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     FixStage<STATS> F{stage_buf[wid], 0};
     const unsigned inner = P.stride;
@@ -220,17 +281,15 @@ __global__ void __launch_bounds__(256, 4) k_pass_axis(Pass P, int len, unsigned 
                 const float *q = P.in + base + (unsigned)(p0 - 2) * inner;
 #pragma unroll
                 for (int k = 0; k < K + 4; k++) w[k] = act ? __ldg(q + (unsigned)k * inner) : 0.f;
+                float r[K];
+                unsigned fm = 0;
+                if (act) {
+                    fm = taps_run<K>(w, r);
 #pragma unroll
-                for (int k = 0; k < K; k++) {
-                    float r;
-                    const bool fail = act && !tap5_fast(w[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], &r);
-                    const unsigned v = base + (unsigned)(p0 + k) * inner;
-                    if (act && !fail) {
-                        P.out[v] = r;
-                        if (STATS) acc.add(r, gx, gy, p0 + k, P.iso);
-                    }
-                    F.push(fail, v, lane);
+                    for (int k = 0; k < K; k++) P.out[base + (unsigned)(p0 + k) * inner] = r[k];   // placeholder where fm has bit k
+                    if (STATS) acc.add_run<K>(r, ~fm, gx, gy, p0, P.iso);
                 }
+                F.push_mask(fm, base + (unsigned)p0 * inner, inner, lane);
             } else {
 #pragma unroll
                 for (int k = 0; k < K + 4; k++) {

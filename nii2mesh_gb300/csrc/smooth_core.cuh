@@ -33,6 +33,25 @@ struct Acc {
             hi0 = max(hi0, x); hi1 = max(hi1, y); hi2 = max(hi2, z);
         }
     }
+    // the K values of one lane's run along z (x, y fixed; z = z0 + k), those
+    // whose bit is set in `take`: min/max per value, the bbox once per run
+    template <int K>
+    __device__ __forceinline__ void add_run(const float (&r)[K], unsigned take, int x, int y, int z0, float iso) {
+        unsigned ge = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if (!(take >> k & 1u)) continue;
+            const float v = r[k];
+            if (!isfinite(v)) { nf++; continue; }
+            mn = fminf(mn, v);
+            mx = fmaxf(mx, v);
+            ge |= (unsigned)(v >= iso) << k;
+        }
+        if (ge) {
+            lo0 = min(lo0, x); lo1 = min(lo1, y); lo2 = min(lo2, z0 + __ffs(ge) - 1);
+            hi0 = max(hi0, x); hi1 = max(hi1, y); hi2 = max(hi2, z0 + 31 - __clz(ge));
+        }
+    }
     // block-wide reduction, one set of atomics per CTA
     __device__ void flush(VolStats *st, bool minmax) {
         const unsigned full = 0xffffffffu;
