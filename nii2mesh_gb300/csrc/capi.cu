@@ -185,7 +185,9 @@ struct n2m_context {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evs[8] = {};   // stage boundaries of the last pipeline run
-    DevBuf in, raw, vol, stmp, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath, hmesh;
+    DevBuf in, raw, vol, stmp, stmp2, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath,
+        hmesh;
+    OdWork od;   // pre-smooth with exact rounding on demand
     McWork mc;
     ScanWork scan;
     LabelWork lab;
@@ -279,7 +281,9 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->mc.signs, &c->mc.ctr, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
-                      &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->th.buf, &c->th.table,
+                      &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->hc.bad, &c->th.buf, &c->th.table,
+                      &c->stmp2, &c->od.st, &c->od.unc, &c->od.cmin, &c->od.cmax, &c->od.need_z, &c->od.need_y,
+                      &c->od.need_x, &c->od.off, &c->od.list, &c->od.lcnt,
                       &c->wr.mt, &c->wr.mp, &c->wr.pack, &c->wr.pack2, &c->wr.lens, &c->wr.flag, &c->wr.out};
     for (DevBuf *b : bufs) b->release();
     deflate_release(c->wr.df);
@@ -454,6 +458,8 @@ struct Prep {
     const float *vol;
     float iso, mn, mnp, edge_max;
     int lo[3], hi[3];
+    bool od = false;          // vol is smoothed approximately: marching cubes makes it exact where it reads it
+    const float *src = nullptr;
 };
 
 // stages 1-3: smoothing, range, clustering, bbox
@@ -477,10 +483,24 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     }
     if (!smooth && label) CK(cudaMemcpyAsync(vol, d_src, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaEventRecord(c->evs[0], c->stream));
+    // Lewiner cubes straight after the pre-smooth (no clustering): exact rounding on
+    // demand (only where marching cubes reads values); otherwise the exact three passes
+    bool od = smooth && !label && o.cubes != N2M_CUBES_OLDCUBES && od_eligible(d_src, nx, ny, nz);
     if (smooth) {
         CKS(c->stmp.ensure(n * sizeof(float)));
-        CKS(launch_smooth(d_src, vol, c->stmp.as<float>(), nx, ny, nz, iso, dst, c->stream,
-                          c->stage.host ? &c->stage : nullptr));
+        const StagedInput *stage = c->stage.host ? &c->stage : nullptr;
+        if (od) {
+            bool fallback = false;
+            CKS(od_approx(d_src, vol, nx, ny, nz, iso, c->od, c->stream, stage));
+            CKS(od_resolve(d_src, vol, nx, ny, nz, iso, c->od, dst, c->stream, &fallback));
+            if (fallback) {   // the input is on the device by now
+                od = false;
+                CK(cudaMemcpyAsync(dst, h, sizeof(VolStats), cudaMemcpyHostToDevice, c->stream));
+                CKS(launch_smooth(d_src, vol, c->stmp.as<float>(), nx, ny, nz, iso, dst, c->stream, nullptr));
+            }
+        } else {
+            CKS(launch_smooth(d_src, vol, c->stmp.as<float>(), nx, ny, nz, iso, dst, c->stream, stage));
+        }
     }
     else CKS(launch_stats(label ? vol : d_src, nx, ny, nz, iso, true, dst, c->stream));
     CK(cudaEventRecord(c->evs[1], c->stream));
@@ -503,6 +523,10 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
         if (!g_quiet)
             printf("Suggested isolevel out of range. Intensity range %g..%g, setting isolevel to %g\n", mn, mx, iso);
         stale = true;
+        if (od) {   // the approximate pass decided signs against the old isolevel: smooth exactly
+            od = false;
+            CKS(launch_smooth(d_src, vol, c->stmp.as<float>(), nx, ny, nz, iso, dst + 1, c->stream, nullptr));
+        }
     }
     if (verbose) printf("intensity range %g..%g, isolevel %g\n", mn, mx, iso);
     VolStats s1 = s0;
@@ -527,6 +551,8 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     P.vol = v;
     P.iso = iso;
     P.mn = mn;
+    P.od = od;
+    P.src = d_src;
     for (int i = 0; i < 3; i++) {
         P.lo[i] = std::max(s1.lo[i] - 1, 0);
         P.hi[i] = std::min(s1.hi[i] + 2, dim[i]);
@@ -564,7 +590,13 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
     CKS(c->totals.ensure(sizeof(uint4)));
     uint4 *dtot = c->totals.as<uint4>();
     if (old) CKS(oc_count(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->scan, dtot, c->stream));
-    else CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream));
+    else if (P.od) {
+        const size_t n = (size_t)dim[0] * dim[1] * dim[2];
+        CKS(c->stmp2.ensure(n * sizeof(float)));
+        const OdRepair rep{P.src, c->stmp.as<float>(), c->stmp2.as<float>(), (float *)P.vol, {dim[0], dim[1], dim[2]},
+                           &c->od, &c->scan};
+        CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream, &rep));
+    } else CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream));
     CK(cudaEventRecord(c->evs[3], c->stream));
     uint4 tot;
     CKS(readback(c, &tot, dtot));

@@ -221,6 +221,51 @@ __global__ void __launch_bounds__(256) k_words(GV g, bool classic, unsigned WX, 
     }
 }
 
+// Marks for the exact pre-smooth on demand: the voxel behind every corner of
+// every cube whose corner signs differ (the only cubes whose values marching
+// cubes reads), as bits of a linear bitmap over the volume.  A grid point's
+// voxel is gval's linear index j (row wrap included); j past the volume is the
+// padding value, which needs no voxel.
+__device__ __forceinline__ void need_mark(unsigned *need, long long j, unsigned bits, long long nvox) {
+    if (j >= nvox || !bits) return;
+    if (nvox - j < 32) bits &= (1u << (unsigned)(nvox - j)) - 1u;
+    const long long w = j >> 5;
+    const int sh = (int)(j & 31);
+    const unsigned p0 = bits << sh, p1 = sh ? bits >> (32 - sh) : 0u;
+    if (p0) atomicOr(need + w, p0);
+    if (p1) atomicOr(need + w + 1, p1);
+}
+
+__global__ void __launch_bounds__(256) k_need(GV g, unsigned WX, unsigned nwords, const unsigned *__restrict__ signs,
+                                              unsigned *need) {
+    const unsigned rowstride = WX, slicestride = WX * (unsigned)g.NY;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const unsigned xw = w % WX, row = w / WX;
+        const int y = (int)(row % (unsigned)g.NY), z = (int)(row / (unsigned)g.NY);
+        if (y >= g.NY - 1 || z >= g.NZ - 1) continue;   // no cubes start on the last row / slice
+        const int x0 = (int)xw * 32;
+        const bool nx = xw + 1 < WX;
+        const unsigned hxm = x0 + 33 <= g.NX ? 0xffffffffu : (g.NX - 1 - x0 > 0 ? (1u << (g.NX - 1 - x0)) - 1u : 0u);
+        const unsigned a0 = __ldg(signs + w), b0 = __ldg(signs + w + rowstride), c0 = __ldg(signs + w + slicestride),
+                       d0 = __ldg(signs + w + slicestride + rowstride);
+        const unsigned a1 = __funnelshift_r(a0, nx ? __ldg(signs + w + 1) : 0u, 1);
+        const unsigned b1 = __funnelshift_r(b0, nx ? __ldg(signs + w + rowstride + 1) : 0u, 1);
+        const unsigned c1 = __funnelshift_r(c0, nx ? __ldg(signs + w + slicestride + 1) : 0u, 1);
+        const unsigned d1 = __funnelshift_r(d0, nx ? __ldg(signs + w + slicestride + rowstride + 1) : 0u, 1);
+        const unsigned any = a0 | a1 | b0 | b1 | c0 | c1 | d0 | d1, all = a0 & a1 & b0 & b1 & c0 & c1 & d0 & d1;
+        const unsigned mix = any & ~all & hxm;
+        if (!mix) continue;
+        const unsigned cm = mix | (mix << 1), carry = mix >> 31;   // corners x and x + 1 of each mixed cube
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const long long j = (long long)(g.lo0 + x0) + (long long)(y + (r & 1) + g.lo1) * g.dx +
+                                (long long)(z + (r >> 1) + g.lo2) * g.dxy;
+            need_mark(need, j, cm, g.nvox);
+            if (carry) need_mark(need, j + 32, 1u, g.nvox);
+        }
+    }
+}
+
 // active word list from the scanned counts (counts.w: exclusive count of
 // active words before w), in word order
 __global__ void k_active(const uint4 *__restrict__ offs, const uint4 *__restrict__ total, unsigned nwords,
@@ -662,7 +707,8 @@ GV make_gv(const McGrid &g) {
 
 // counts: per word {vertices, triangles, c-vertices, active}; after the scan,
 // exclusive offsets; totals.w = number of active words (listed in w.cand)
-n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s) {
+n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s,
+                    const OdRepair *repair) {
     const GV v = make_gv(g);
     const unsigned WX = (unsigned)((g.n[0] + 31) / 32);
     const size_t nwords = (size_t)WX * g.n[1] * g.n[2];
@@ -679,6 +725,16 @@ n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4
         const unsigned blocks = std::min<unsigned>((nrows + 7) / 8, 152u * 16u);
         k_signs<<<blocks, 256, 0, s>>>(v, WX, nrows, w.signs.as<unsigned>());
         N2M_COUNT();
+    }
+    if (repair) {   // exact smoothed values where the cubes below read them
+        const size_t nvw = (size_t)((v.nvox + 31) >> 5);
+        CKS(repair->w->need_z.ensure(nvw * sizeof(unsigned)));
+        CK(cudaMemsetAsync(repair->w->need_z.p, 0, nvw * sizeof(unsigned), s));
+        const unsigned blocks = (unsigned)std::min<size_t>((nwords + 255) / 256, 152u * 16u);
+        k_need<<<blocks, 256, 0, s>>>(v, WX, (unsigned)nwords, w.signs.as<unsigned>(), repair->w->need_z.as<unsigned>());
+        N2M_COUNT();
+        CKL();
+        CKS(od_repair(*repair, s));
     }
     {
         const unsigned blocks = (unsigned)std::min<size_t>((nwords + 255) / 256, 152u * 16u);

@@ -86,6 +86,53 @@ n2m_status launch_smooth(const float *in, float *out, float *tmp, int nx, int ny
                          cudaStream_t s, const StagedInput *stage = nullptr);
 // whether launch_smooth can take a StagedInput for this volume
 bool smooth_can_stage(int nx, int ny, int nz);
+
+// Pre-smooth with exact rounding on demand (smooth.cu): od_approx smooths the
+// whole volume approximately (one fused FP32 pass, rigorous error bound) and
+// lists the voxels whose sign against iso it cannot decide and the candidates
+// for the volume's range; od_resolve gives those their exact values and fills
+// `dst` (exact range, bbox, no non-finite count) unless *fallback (a
+// non-finite or huge input, a list overflow): then the caller runs
+// launch_smooth instead.  Marching cubes marks the corners of the cubes the
+// surface crosses in need_z (mc.cu: mc_count with an OdRepair), and od_repair
+// writes the reference's exact value at every marked voxel of `out`.
+enum : unsigned { OD_FALLBACK = 1u, OD_TIMEOUT = 2u };
+struct OdStats {
+    VolStats vs;             // bbox of decided voxels >= iso; exact range after od_resolve
+    unsigned flags;
+    unsigned cnt[3];         // undecided, min candidates, max candidates
+    int umin, lmax;          // ordered: smallest task min + B, largest task max - B
+};
+struct OdCand {              // a range candidate: voxel, approximate value, its bound
+    unsigned j;
+    float v, b;
+};
+struct OdLists {
+    unsigned *unc;
+    OdCand *cmin, *cmax;
+    unsigned *cnt;
+    unsigned cap;
+};
+struct OdWork {
+    DevBuf st, unc, cmin, cmax, need_z, need_y, need_x, off, list, lcnt;
+    unsigned cap = 0;
+};
+struct ScanWork;
+struct OdRepair {
+    const float *in;         // the raw volume
+    float *tmp1, *tmp2;      // exact x and y pass values (written at marked voxels only)
+    float *out;              // the approximately smoothed volume, exact where marked
+    int dim[3];
+    OdWork *w;
+    ScanWork *scan;
+};
+// whether the on-demand path applies: rows a multiple of 16 bytes (TMA tiles), fewer than 2^32 voxels
+bool od_eligible(const float *in, int nx, int ny, int nz);
+n2m_status od_approx(const float *in, float *out, int nx, int ny, int nz, float iso, OdWork &w, cudaStream_t s,
+                     const StagedInput *stage = nullptr);
+n2m_status od_resolve(const float *in, float *out, int nx, int ny, int nz, float iso, OdWork &w, VolStats *dst,
+                      cudaStream_t s, bool *fallback);
+n2m_status od_repair(const OdRepair &r, cudaStream_t s);
 // transposed pre-smooth: g_img = Sx^T Sy^T Sz^T g (tmp: one volume of scratch)
 n2m_status launch_smooth_adjoint(const float *g, float *tmp, float *out, int nx, int ny, int nz, cudaStream_t s);
 n2m_status launch_stats(const float *vol, int nx, int ny, int nz, float iso, bool minmax, VolStats *st,
@@ -163,7 +210,10 @@ struct McWork {
 struct McCounts {
     unsigned nv_edge, nt, nc, nactive;
 };
-n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s);
+// repair: marks the corners of the cubes with mixed signs in repair->w->need_z
+// after the sign pass and runs od_repair before any value is read (null: none)
+n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s,
+                    const OdRepair *repair = nullptr);
 n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,
                    int *d_cand, unsigned *d_ncand, int cand_cap, cudaStream_t s);
 n2m_status mc_backward(const McGrid &g, int variant, McWork &w, const McCounts &c, const float3 *d_gv, float *d_gs,

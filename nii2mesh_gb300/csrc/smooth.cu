@@ -11,8 +11,12 @@
 // per pass, three passes.  (The batched atlas smooths its sub-boxes with the
 // fused column routine of smooth_core.cuh instead.)
 #include <float.h>
-
+#include <math.h>
+#include <stddef.h>
 #include <stdlib.h>
+
+#include <cuda.h>            // CUtensorMap and its enums (the encoder comes from the driver at run time)
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <map>
@@ -461,6 +465,598 @@ n2m_status launch_stats(const float *vol, int nx, int ny, int nz, float iso, boo
     const long long rows = (long long)ny * nz;
     const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((rows + 7) / 8, 152 * 8));   // 8 rows per block
     { k_stats<<<grid, 256, 0, s>>>(vol, nx, ny, nz, iso, st, minmax); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
+}
+
+// ==== pre-smooth with exact rounding on demand ===================================
+// Marching cubes reads the smoothed volume in two ways only: the sign of every
+// grid point (value >= iso, and value - iso against the FLT_EPSILON clamp) and
+// the values at the corners of the cubes the surface crosses.  So the volume
+// is first smoothed approximately in one fused FP32 pass (pass A: one read and
+// one write per voxel), with a rigorous error bound; the few voxels whose sign
+// the bound leaves open, and the candidates for the volume's minimum and
+// maximum, are recomputed with the reference's double sequence (pass B).
+// After the sign words, the corners of every cube with mixed signs are marked
+// (mc.cu: k_need) and the exact three-pass smoothing runs on those voxels
+// only, the x and y passes on the voxels those depend on (marks dilated by +-2
+// slices, then +-2 rows), each pass one thread per marked voxel.  Every value
+// marching cubes reads is then the reference's float, bit for bit.
+//
+// Error bound of pass A: each pass evaluates the tap sum as an FP32 FMA chain
+// with the weights rounded to float: at most 7 * 2^-24 * M from the reference's
+// float of the same inputs (M = the largest input magnitude in the window; the
+// weights sum to 1, so every partial sum is below M), and the errors of earlier
+// passes carry through with total weight 1: after three passes at most
+// 21 * 2^-24 * M < 2^-19 * M, M being any bound on the input magnitudes the
+// voxel depends on.  A warp uses the largest magnitude it has read so far.
+namespace {
+constexpr int OW_Y = 8, OW_Z = 32;   // pass A warp task: 32 x 8 x 32 output voxels
+constexpr float OW0 = 0.45f, OW1 = 0.225f, OW2 = 0.05f;
+
+__device__ __forceinline__ float fma5(float a, float b, float c, float d, float e) {
+    return __fmaf_rn(e, OW2, __fmaf_rn(d, OW1, __fmaf_rn(c, OW0, __fmaf_rn(b, OW1, __fmul_rn(a, OW2)))));
+}
+
+__device__ __forceinline__ void od_flag(OdStats *st, unsigned f) { atomicOr(&st->flags, f); }
+
+// ---- TMA and mbarrier primitives (inline PTX) ----
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, unsigned long long *bar, int x, int y,
+                                            int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+// order this thread's earlier generic-proxy accesses to shared memory before later TMA writes
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Pass A: the input volume through a TMA tensor map (nx a multiple of 4, so
+// that the rows are 16-byte aligned); boxes of 40 x 12 x 1 floats, x0 - 4 ..
+// x0 + 35 and y0 - 2 .. y0 + 9 of one slice (outside the volume the copy fills
+// zeros).  A warp takes 32 x 8 columns of 32 slices (lane = x): its lane 0
+// keeps OA_S slices in flight in the warp's own ring of shared-memory stages,
+// each completing on its mbarrier; the x pass reads the stage, the y pass runs
+// over the 12 rows in registers, the z pass over a five-slice ring of the
+// eight rows' y values.  Each output is classified on the spot:
+// |v - iso| <= B + 4 eps -> listed as undecided, else v >= iso -> bbox.  At the
+// end of its task the warp lists the outputs within 2.5 B of its minimum
+// (maximum) with their value and B (range candidates) and offers min + B
+// (max - B) as a bound on the volume's exact extreme.  Waits give up after a
+// fixed number of polls (flag OD_TIMEOUT), after waiting, also bounded, for the
+// warp's copies still in flight.
+constexpr int OA_S = 4, OA_BW = 40, OA_BH = 12, OA_WARPS = 4;
+constexpr unsigned OA_BYTES = OA_BW * OA_BH * 4;
+constexpr int OA_POLLS = 1 << 22;
+struct __align__(128) OaStage {
+    float v[OA_BH][OA_BW];
+};
+
+__global__ void __launch_bounds__(OA_WARPS * 32) k_od_approx(const __grid_constant__ CUtensorMap tmap, float *out,
+                                                             int nx, int ny, int nz, int z_lo, int z_hi, float iso,
+                                                             OdStats *st, OdLists L) {
+    const unsigned FULL = 0xffffffffu;
+    __shared__ OaStage stage[OA_WARPS][OA_S];
+    __shared__ unsigned long long bars[OA_WARPS][OA_S];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    OaStage *sg = stage[wid];
+    unsigned long long *bw = bars[wid];
+    if (lane == 0) {
+        for (int k = 0; k < OA_S; k++) mbar_init(&bw[k], 1);
+        mbar_fence_init();
+    }
+    __syncwarp();
+    unsigned issued = 0, used = 0;   // loads issued / consumed by this warp (stage = n % OA_S, parity = n / OA_S)
+    const unsigned nxs = (unsigned)(nx + 31) / 32, nys = (unsigned)(ny + OW_Y - 1) / OW_Y;
+    const unsigned nzs = (unsigned)(z_hi - z_lo + OW_Z - 1) / OW_Z;
+    const unsigned ntask = nxs * nys * nzs;
+    const size_t nxy = (size_t)nx * ny;
+    bool timed_out = false;
+    for (unsigned task = blockIdx.x * OA_WARPS + wid; task < ntask && !timed_out; task += gridDim.x * OA_WARPS) {
+        const unsigned xs = task % nxs, t2 = task / nxs;
+        const int y0 = (int)(t2 % nys) * OW_Y, zs = z_lo + (int)(t2 / nys) * OW_Z, ze = min(zs + OW_Z, z_hi);
+        const int x0 = (int)xs * 32, x = x0 + lane;
+        const bool ownx = x < nx, xint = x >= 2 && x <= nx - 3;
+        // every slice zs-2 .. ze+1 is loaded (outside the volume: zeros, read only by outputs that ignore them)
+        int znext = zs - 2;
+        const int zlast = ze + 1;
+        auto issue = [&]() {
+            if (lane == 0) {
+                const unsigned k = issued % OA_S;
+                fence_proxy_async();
+                mbar_expect_tx(&bw[k], OA_BYTES);
+                tma_load_3d(&sg[k], &tmap, &bw[k], x0 - 4, y0 - 2, znext);
+            }
+            issued++;
+            znext++;
+        };
+        while (znext <= zlast && issued - used < (unsigned)OA_S) issue();
+        float zr[5][OW_Y];   // y values of slices z-2 .. z+2 (slot 4 newest)
+#pragma unroll
+        for (int a = 0; a < 5; a++)
+#pragma unroll
+            for (int k = 0; k < OW_Y; k++) zr[a][k] = 0.f;
+        float mrun = 0.f, lmin = INFINITY, lmax = -INFINITY, B = 0.f;
+        float lmin2 = INFINITY, lmax2 = -INFINITY;   // second smallest / largest
+        unsigned jmin = 0, jmax = 0;                 // where lmin / lmax are
+        int bzl = INT_MAX, bzh = INT_MIN;
+        unsigned ymask = 0;                          // rows with a decided voxel >= iso
+        float nanacc = 0.f;                          // becomes NaN if an output is NaN or infinite
+        for (int zi = zs - 2; zi <= zlast; zi++) {
+            const unsigned k = used % OA_S, par = (used / OA_S) & 1u;
+            bool ok = false;
+            for (int it = 0; it < OA_POLLS && !ok; it++) ok = mbar_try_wait(&bw[k], par);
+            if (!__all_sync(FULL, ok)) {
+                timed_out = true;
+                break;
+            }
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int kk = 0; kk < OW_Y; kk++) zr[a][kk] = zr[a + 1][kk];
+            const OaStage &S = sg[k];
+            float xv[OA_BH];
+#pragma unroll
+            for (int r = 0; r < OA_BH; r++) {
+                const float *q = &S.v[r][lane + 2];   // x - 2 .. x + 2
+                const float a = q[0], b = q[1], c = q[2], d = q[3], e = q[4];
+                mrun = fmaxf(mrun, fmaxf(fabsf(a), fabsf(e)));   // lanes together cover x0-2 .. x0+33
+                xv[r] = xint ? fma5(a, b, c, d, e) : c;
+            }
+#pragma unroll
+            for (int kk = 0; kk < OW_Y; kk++) {
+                const int yy = y0 + kk;
+                zr[4][kk] = (yy >= 2 && yy <= ny - 3) ? fma5(xv[kk], xv[kk + 1], xv[kk + 2], xv[kk + 3], xv[kk + 4])
+                                                      : xv[kk + 2];
+            }
+            __syncwarp();   // every lane is done with the stage
+            used++;
+            if (znext <= zlast) issue();
+            float m = mrun;
+            for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+            B = m * 0x1p-19f;   // bounds every output whose inputs have been read
+            const int z = zi - 2;
+            if (z >= zs && z < ze && ownx) {
+                const bool zint = z >= 2 && z <= nz - 3;
+                const float band = B + 4.0f * N2M_FLT_EPS;
+                const unsigned j0 = (unsigned)((size_t)z * nxy + (size_t)y0 * nx + x);
+                unsigned ge = 0;
+#pragma unroll
+                for (int kk = 0; kk < OW_Y; kk++) {
+                    if (y0 + kk >= ny) continue;
+                    const float zv = zint ? fma5(zr[0][kk], zr[1][kk], zr[2][kk], zr[3][kk], zr[4][kk]) : zr[2][kk];
+                    const unsigned j = j0 + (unsigned)kk * (unsigned)nx;
+                    out[j] = zv;
+                    nanacc = __fmaf_rn(zv, 0.f, nanacc);
+                    const bool lo = zv < lmin, hi = zv > lmax;
+                    lmin2 = lo ? lmin : fminf(lmin2, zv);
+                    jmin = lo ? j : jmin;
+                    lmin = fminf(lmin, zv);
+                    lmax2 = hi ? lmax : fmaxf(lmax2, zv);
+                    jmax = hi ? j : jmax;
+                    lmax = fmaxf(lmax, zv);
+                    const bool und = fabsf(__fsub_rn(zv, iso)) <= band;
+                    if (und) {
+                        const unsigned q = atomicAdd(&L.cnt[0], 1u);
+                        if (q < L.cap) L.unc[q] = j;
+                    }
+                    ge |= (unsigned)(!und && zv >= iso) << kk;
+                }
+                if (ge) {
+                    ymask |= ge;
+                    bzl = min(bzl, z);
+                    bzh = z;
+                }
+            }
+        }
+        if (timed_out) break;
+        // huge, infinite or NaN input (an unbounded B), or a non-finite output
+        const bool bad = !(B < 0x1p+120f * 0x1p-19f) || nanacc != 0.f;
+        if (__any_sync(FULL, bad)) {   // the exact three-pass path handles the volume
+            if (lane == 0) od_flag(st, OD_FALLBACK);
+            continue;
+        }
+        // bbox of the decided voxels >= iso
+        {
+            const bool any = ymask != 0u;
+            int byl = any ? y0 + __ffs(ymask) - 1 : INT_MAX, byh = any ? y0 + 31 - __clz(ymask) : INT_MIN;
+            int xl = any ? x : INT_MAX, xh = any ? x : INT_MIN;
+            for (int o = 16; o; o >>= 1) {
+                xl = min(xl, __shfl_xor_sync(FULL, xl, o)); xh = max(xh, __shfl_xor_sync(FULL, xh, o));
+                byl = min(byl, __shfl_xor_sync(FULL, byl, o)); byh = max(byh, __shfl_xor_sync(FULL, byh, o));
+                bzl = min(bzl, __shfl_xor_sync(FULL, bzl, o)); bzh = max(bzh, __shfl_xor_sync(FULL, bzh, o));
+            }
+            if (lane == 0 && xl != INT_MAX) {
+                atomicMin(&st->vs.lo[0], xl); atomicMax(&st->vs.hi[0], xh);
+                atomicMin(&st->vs.lo[1], byl); atomicMax(&st->vs.hi[1], byh);
+                atomicMin(&st->vs.lo[2], bzl); atomicMax(&st->vs.hi[2], bzh);
+            }
+        }
+        // range candidates of this task
+        float wmin = lmin, wmax = lmax;
+        for (int o = 16; o; o >>= 1) {
+            wmin = fminf(wmin, __shfl_xor_sync(FULL, wmin, o));
+            wmax = fmaxf(wmax, __shfl_xor_sync(FULL, wmax, o));
+        }
+        if (lane == 0) {
+            atomicMin(&st->umin, f2ord(__fadd_ru(wmin, B)));
+            atomicMax(&st->lmax, f2ord(__fsub_rd(wmax, B)));
+        }
+        const float cmin = __fadd_ru(wmin, 2.5f * B), cmax = __fsub_rd(wmax, 2.5f * B);
+        // a lane with one candidate lists it directly; with more (its second extreme is
+        // close too: plateaus) it re-reads its outputs
+        if (ownx && lmin <= cmin && lmin2 > cmin) {
+            const unsigned q = atomicAdd(&L.cnt[1], 1u);
+            if (q < L.cap) L.cmin[q] = OdCand{jmin, lmin, B};
+        }
+        if (ownx && lmax >= cmax && lmax2 < cmax) {
+            const unsigned q = atomicAdd(&L.cnt[2], 1u);
+            if (q < L.cap) L.cmax[q] = OdCand{jmax, lmax, B};
+        }
+        if (ownx && (lmin2 <= cmin || lmax2 >= cmax)) {
+            const bool wmn = lmin2 <= cmin, wmx = lmax2 >= cmax;
+            for (int z = zs; z < ze; z++) {
+                float v[OW_Y];
+#pragma unroll
+                for (int kk = 0; kk < OW_Y; kk++)
+                    v[kk] = y0 + kk < ny ? out[(size_t)z * nxy + (size_t)(y0 + kk) * nx + x] : 0.f;
+#pragma unroll
+                for (int kk = 0; kk < OW_Y; kk++) {
+                    if (y0 + kk >= ny) continue;
+                    const unsigned j = (unsigned)((size_t)z * nxy + (size_t)(y0 + kk) * nx + x);
+                    if (wmn && v[kk] <= cmin) {
+                        const unsigned q = atomicAdd(&L.cnt[1], 1u);
+                        if (q < L.cap) L.cmin[q] = OdCand{j, v[kk], B};
+                    }
+                    if (wmx && v[kk] >= cmax) {
+                        const unsigned q = atomicAdd(&L.cnt[2], 1u);
+                        if (q < L.cap) L.cmax[q] = OdCand{j, v[kk], B};
+                    }
+                }
+            }
+        }
+    }
+    if (timed_out) {
+        // no further copies are issued; wait (bounded) for the ones in flight before leaving
+        if (lane == 0) od_flag(st, OD_FALLBACK | OD_TIMEOUT);
+        while (used < issued) {
+            const unsigned k = used % OA_S, par = (used / OA_S) & 1u;
+            for (int it = 0; it < OA_POLLS; it++)
+                if (mbar_try_wait(&bw[k], par)) break;
+            used++;
+        }
+    }
+}
+
+// the reference's smoothed value of voxel (x, y, z), every tap in its double sequence
+__device__ float od_exact_at(const float *__restrict__ in, int x, int y, int z, int nx, int ny, int nz) {
+    const size_t nxy = (size_t)nx * ny;
+    auto X = [&](int yy, int zz) -> float {
+        const float *p = in + (size_t)zz * nxy + (size_t)yy * nx + x;
+        return (x < 2 || x > nx - 3) ? p[0] : tap5_double(p[-2], p[-1], p[0], p[1], p[2]);
+    };
+    auto Y = [&](int zz) -> float {
+        return (y < 2 || y > ny - 3) ? X(y, zz) : tap5_double(X(y - 2, zz), X(y - 1, zz), X(y, zz), X(y + 1, zz), X(y + 2, zz));
+    };
+    return (z < 2 || z > nz - 3) ? Y(z) : tap5_double(Y(z - 2), Y(z - 1), Y(z), Y(z + 1), Y(z + 2));
+}
+
+// Pass B: undecided voxels get their exact value (and join the bbox if >= iso);
+// the range is the exact extreme over the candidates that can still reach it
+// (value - B <= the smallest min + B of any task; the same for the maximum)
+__global__ void k_od_resolve(const float *__restrict__ in, float *out, int nx, int ny, int nz, float iso, OdStats *st,
+                             OdLists L, unsigned nu, unsigned nmin, unsigned nmax) {
+    const unsigned n = nu + nmin + nmax;
+    const float umin = ord2f(st->umin), lmax = ord2f(st->lmax);
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned j;
+        int which;
+        if (i < nu) {
+            which = 0;
+            j = L.unc[i];
+        } else if (i < nu + nmin) {
+            const OdCand c = L.cmin[i - nu];
+            if (__fsub_rd(c.v, c.b) > umin) continue;
+            which = 1;
+            j = c.j;
+        } else {
+            const OdCand c = L.cmax[i - nu - nmin];
+            if (__fadd_ru(c.v, c.b) < lmax) continue;
+            which = 2;
+            j = c.j;
+        }
+        const unsigned x = j % (unsigned)nx, r = j / (unsigned)nx, y = r % (unsigned)ny, z = r / (unsigned)ny;
+        const float v = od_exact_at(in, (int)x, (int)y, (int)z, nx, ny, nz);
+        if (which == 0) {
+            out[j] = v;
+            if (v >= iso) {
+                atomicMin(&st->vs.lo[0], (int)x); atomicMax(&st->vs.hi[0], (int)x);
+                atomicMin(&st->vs.lo[1], (int)y); atomicMax(&st->vs.hi[1], (int)y);
+                atomicMin(&st->vs.lo[2], (int)z); atomicMax(&st->vs.hi[2], (int)z);
+            }
+        } else if (which == 1) {
+            atomicMin(&st->vs.vmin, f2ord(v));
+        } else {
+            atomicMax(&st->vs.vmax, f2ord(v));
+        }
+    }
+}
+
+// ---- marks -> the exact passes on marked voxels ----------------------------------
+// Bitmaps are linear in the voxel index (bit j & 31 of word j >> 5).
+
+// 32 bits of `bm` starting at bit `s` (a signed voxel offset), zero outside [0, nvox)
+__device__ __forceinline__ unsigned bits_at(const unsigned *__restrict__ bm, long long s, long long nvox) {
+    if (s <= -32 || s >= nvox) return 0u;
+    const long long w = s >= 0 ? s >> 5 : -((31 - s) >> 5);
+    const int sh = (int)(s - (w << 5));
+    const long long nw = (nvox + 31) >> 5;
+    const unsigned lo = (w >= 0 && w < nw) ? __ldg(bm + w) : 0u;
+    const unsigned hi = (w + 1 >= 0 && w + 1 < nw) ? __ldg(bm + w + 1) : 0u;
+    unsigned v = __funnelshift_r(lo, hi, sh);
+    const long long end = nvox - s;   // bits at or past nvox are zero
+    if (end < 32) v &= (1u << end) - 1u;
+    if (s < 0) v &= ~0u << (unsigned)(-s);
+    return v;
+}
+
+// dst = OR over d in [-2, 2] of src shifted by d * stride voxels; per word the
+// number of set bits of dst into cnt[w].{y|z} (and of src into cnt[w].x)
+template <int FIELD>
+__global__ void k_od_dilate(const unsigned *__restrict__ src, unsigned *dst, long long nvox, long long stride,
+                            uint4 *cnt) {
+    const long long nw = (nvox + 31) >> 5;
+    for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
+        unsigned acc = 0;
+#pragma unroll
+        for (int d = -2; d <= 2; d++) acc |= bits_at(src, (w << 5) + d * stride, nvox);
+        dst[w] = acc;
+        if (FIELD == 1) {
+            cnt[w] = make_uint4((unsigned)__popc(src[w]), (unsigned)__popc(acc), 0u, 0u);
+        } else {
+            cnt[w].z = (unsigned)__popc(acc);
+        }
+    }
+}
+
+// the set bits of the three bitmaps as voxel indices, in order, at the scanned
+// word offsets (x: z marks, y: y marks, z: x marks); a warp takes 32 words and
+// writes each word's indices with one coalesced store per lane
+__device__ __forceinline__ void scatter_word(unsigned m, unsigned o, unsigned base, unsigned *list, int lane) {
+    if (m >> lane & 1u) list[o + __popc(m & ((1u << lane) - 1u))] = base + (unsigned)lane;
+}
+__global__ void k_od_scatter(const unsigned *__restrict__ bz, const unsigned *__restrict__ by,
+                             const unsigned *__restrict__ bx, const uint4 *__restrict__ off, long long nw,
+                             unsigned *lz, unsigned *ly, unsigned *lx) {
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long w0 = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; w0 < nw; w0 += nwarps * 32) {
+        const long long wl = w0 + lane;
+        const unsigned mz = wl < nw ? bz[wl] : 0u, my = wl < nw ? by[wl] : 0u, mx = wl < nw ? bx[wl] : 0u;
+        const uint4 o = wl < nw ? off[wl] : make_uint4(0u, 0u, 0u, 0u);
+        unsigned busy = __ballot_sync(0xffffffffu, (mz | my | mx) != 0u);
+        while (busy) {
+            const int k = __ffs(busy) - 1;
+            busy &= busy - 1u;
+            const unsigned base = (unsigned)((w0 + k) << 5);
+            scatter_word(__shfl_sync(0xffffffffu, mz, k), __shfl_sync(0xffffffffu, o.x, k), base, lz, lane);
+            scatter_word(__shfl_sync(0xffffffffu, my, k), __shfl_sync(0xffffffffu, o.y, k), base, ly, lane);
+            scatter_word(__shfl_sync(0xffffffffu, mx, k), __shfl_sync(0xffffffffu, o.z, k), base, lx, lane);
+        }
+    }
+}
+
+// one exact pass on the listed voxels: dst[v] = tap sum of src along the axis
+// (stride 1, nx or nx*ny; coordinate along the axis = (v / div) % len), or
+// src[v] on the two face layers; one thread per voxel, undecided taps queued
+// per warp for the FP64 fix-up
+__global__ void __launch_bounds__(256) k_od_exact(const unsigned *__restrict__ list, const unsigned *__restrict__ cnt,
+                                                  const float *__restrict__ src, float *dst, unsigned stride,
+                                                  unsigned div, unsigned len, unsigned long long mdiv,
+                                                  unsigned long long mlen) {
+    __shared__ unsigned stage_buf[8][64];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    FixStage<false> F{stage_buf[wid], 0};
+    Acc acc;   // unused
+    const Pass P{src, dst, stride, 0, 0, 0u, 0.f, nullptr};
+    const unsigned n = *cnt, nthr = gridDim.x * blockDim.x;
+    for (unsigned i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n; i0 += nthr) {   // warp-uniform
+        const unsigned i = i0 + (unsigned)lane;
+        bool fail = false;
+        unsigned v = 0;
+        if (i < n) {
+            v = __ldg(list + i);
+            const unsigned q = div == 1u ? v : (unsigned)__umul64hi(v, mdiv);   // v / div
+            const unsigned c = q - (unsigned)__umul64hi(q, mlen) * len;           // q % len
+            float r;
+            if (c >= 2u && c + 2u < len) {
+                const float *p = src + v;
+                const float a0 = __ldg(p - 2 * (size_t)stride), a1 = __ldg(p - (size_t)stride), a2 = __ldg(p),
+                            a3 = __ldg(p + stride), a4 = __ldg(p + 2 * (size_t)stride);
+                if (!tap5_split_window(a0, a1, a2, a3, a4, &r)) fail = !tap5_fast(a0, a1, a2, a3, a4, &r);
+            } else {
+                r = __ldg(src + v);
+            }
+            if (!fail) dst[v] = r;
+        }
+        F.push(fail, v, lane);
+        F.drain(P, acc, lane);
+    }
+    F.finish(P, acc, lane);
+}
+
+// floor(2^64 / d) + 1: __umul64hi(n, m) = n / d for every 32-bit n (d >= 2)
+unsigned long long od_magic(unsigned d) { return d <= 1u ? 0ull : ~0ull / d + 1ull; }
+
+int od_grid(const void *fn, int threads) {
+    int dev = 0, sms = 0, per_sm = 0, g = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) == cudaSuccess)
+        g = sms * std::max(per_sm, 1);
+    cudaGetLastError();
+    return g > 0 ? g : 152 * 4;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+        cudaGetLastError();
+    });
+    return fn;
+}
+}  // namespace
+
+bool od_eligible(const float *in, int nx, int ny, int nz) {
+    return nx % 4 == 0 && ((uintptr_t)in & 15u) == 0 && (size_t)nx * ny * nz < ((size_t)1 << 32) && nx >= 5 &&
+           ny >= 5 && nz >= 5;
+}
+
+n2m_status od_approx(const float *in, float *out, int nx, int ny, int nz, float iso, OdWork &w, cudaStream_t s,
+                     const StagedInput *stage) {
+    const size_t n = (size_t)nx * ny * nz;
+    auto encode = tensor_map_encoder();
+    if (!encode) {
+        n2m_set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return N2M_ERR_CUDA;
+    }
+    CUtensorMap tmap;
+    {
+        const cuuint64_t gdim[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+        const cuuint64_t gstride[2] = {(cuuint64_t)nx * 4u, (cuuint64_t)nx * ny * 4u};
+        const cuuint32_t box[3] = {OA_BW, OA_BH, 1}, estr[3] = {1, 1, 1};
+        const CUresult r = encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)in, gdim, gstride, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            n2m_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+            return N2M_ERR_CUDA;
+        }
+    }
+    w.cap = (unsigned)std::min<size_t>(n / 64 + 4096, 1u << 22);
+    CKS(w.st.ensure(sizeof(OdStats)));
+    CKS(w.unc.ensure((size_t)w.cap * sizeof(unsigned)));
+    CKS(w.cmin.ensure((size_t)w.cap * sizeof(OdCand)));
+    CKS(w.cmax.ensure((size_t)w.cap * sizeof(OdCand)));
+    OdStats h{};
+    stats_init_host(&h.vs);
+    h.vs.vmin = INT_MAX;   // filled by pass B from the candidates
+    h.vs.vmax = INT_MIN;
+    h.umin = INT_MAX;
+    h.lmax = INT_MIN;
+    CK(cudaMemcpyAsync(w.st.p, &h, sizeof(OdStats), cudaMemcpyHostToDevice, s));
+    OdStats *st = w.st.as<OdStats>();
+    OdLists L{w.unc.as<unsigned>(), w.cmin.as<OdCand>(), w.cmax.as<OdCand>(),
+              (unsigned *)((char *)w.st.p + offsetof(OdStats, cnt)), w.cap};
+    const int grid = od_grid((const void *)k_od_approx, OA_WARPS * 32);
+    auto launch = [&](int z_lo, int z_hi) -> n2m_status {
+        if (z_hi <= z_lo) return N2M_OK;
+        k_od_approx<<<grid, OA_WARPS * 32, 0, s>>>(tmap, out, nx, ny, nz, z_lo, z_hi, iso, st, L);
+        N2M_COUNT();
+        CKL();
+        return N2M_OK;
+    };
+    if (stage && stage->host) {
+        // the copy stream may only overwrite `in` once earlier work on s is done with it
+        CK(cudaEventRecord(stage->ev[N2M_STAGE_SLABS], s));
+        CK(cudaStreamWaitEvent(stage->copy, stage->ev[N2M_STAGE_SLABS], 0));
+        const size_t nxy = (size_t)nx * ny;
+        int zdone = 0;
+        for (int k = 0; k < N2M_STAGE_SLABS; k++) {
+            const int z0 = (int)((long long)nz * k / N2M_STAGE_SLABS), z1 = (int)((long long)nz * (k + 1) / N2M_STAGE_SLABS);
+            if (z1 <= z0) continue;
+            CK(cudaMemcpyAsync((float *)in + (size_t)z0 * nxy, stage->host + (size_t)z0 * nxy,
+                               (size_t)(z1 - z0) * nxy * sizeof(float), cudaMemcpyHostToDevice, stage->copy));
+            CK(cudaEventRecord(stage->ev[k], stage->copy));
+            CK(cudaStreamWaitEvent(s, stage->ev[k], 0));
+            const int zready = z1 == nz ? nz : z1 - 2;   // outputs whose input slices (+-2) have arrived
+            if (zready - zdone >= 32 || zready == nz) {
+                CKS(launch(zdone, zready));
+                zdone = zready;
+            }
+        }
+    } else {
+        CKS(launch(0, nz));
+    }
+    return N2M_OK;
+}
+
+n2m_status od_resolve(const float *in, float *out, int nx, int ny, int nz, float iso, OdWork &w, VolStats *dst,
+                      cudaStream_t s, bool *fallback) {
+    OdStats h;
+    CK(cudaMemcpyAsync(&h, w.st.p, sizeof(OdStats), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h.flags & OD_TIMEOUT) {
+        n2m_set_error("pre-smooth: a tile copy did not complete");
+        return N2M_ERR_TIMEOUT;
+    }
+    *fallback = (h.flags & OD_FALLBACK) != 0 || h.cnt[0] > w.cap || h.cnt[1] > w.cap || h.cnt[2] > w.cap ||
+                h.cnt[1] == 0 || h.cnt[2] == 0;
+    if (*fallback) return N2M_OK;
+    OdLists L{w.unc.as<unsigned>(), w.cmin.as<OdCand>(), w.cmax.as<OdCand>(),
+              (unsigned *)((char *)w.st.p + offsetof(OdStats, cnt)), w.cap};
+    const unsigned tot = h.cnt[0] + h.cnt[1] + h.cnt[2];
+    const unsigned blocks = std::max(1u, std::min((tot + 127) / 128, 152u * 8u));
+    k_od_resolve<<<blocks, 128, 0, s>>>(in, out, nx, ny, nz, iso, w.st.as<OdStats>(), L, h.cnt[0], h.cnt[1], h.cnt[2]);
+    N2M_COUNT();
+    CKL();
+    CK(cudaMemcpyAsync(dst, w.st.p, sizeof(VolStats), cudaMemcpyDeviceToDevice, s));   // vs is the first member
+    return N2M_OK;
+}
+
+n2m_status od_repair(const OdRepair &r, cudaStream_t s) {
+    OdWork &w = *r.w;
+    const int nx = r.dim[0], ny = r.dim[1], nz = r.dim[2];
+    const long long nvox = (long long)nx * ny * nz, nw = (nvox + 31) >> 5;
+    CKS(w.need_y.ensure((size_t)nw * sizeof(unsigned)));
+    CKS(w.need_x.ensure((size_t)nw * sizeof(unsigned)));
+    CKS(w.off.ensure((size_t)nw * sizeof(uint4)));
+    CKS(w.list.ensure((size_t)3 * nvox * sizeof(unsigned)));   // every list fits any marking
+    CKS(w.lcnt.ensure(sizeof(uint4)));
+    uint4 *off = w.off.as<uint4>();
+    unsigned *cnt = w.lcnt.as<unsigned>();   // z, y, x counts
+    unsigned *lz = w.list.as<unsigned>(), *ly = lz + nvox, *lx = ly + nvox;
+    const unsigned dblocks = (unsigned)std::min<long long>((nw + 255) / 256, 152 * 16);
+    // y values needed by marked z outputs (+-2 slices), x values by those (+-2 rows)
+    { k_od_dilate<1><<<dblocks, 256, 0, s>>>(w.need_z.as<unsigned>(), w.need_y.as<unsigned>(), nvox, (long long)nx * ny,
+                                             off); N2M_COUNT(); }
+    { k_od_dilate<2><<<dblocks, 256, 0, s>>>(w.need_y.as<unsigned>(), w.need_x.as<unsigned>(), nvox, (long long)nx,
+                                             off); N2M_COUNT(); }
+    CKL();
+    CKS(scan_uint4(off, (size_t)nw, (uint4 *)cnt, *r.scan, s));
+    { const unsigned sblocks = (unsigned)std::min<long long>((nw + 255) / 256, 152 * 16);
+      k_od_scatter<<<sblocks, 256, 0, s>>>(w.need_z.as<unsigned>(), w.need_y.as<unsigned>(), w.need_x.as<unsigned>(), off,
+                                           nw, lz, ly, lx); N2M_COUNT(); }
+    CKL();
+    const int xb = od_grid((const void *)k_od_exact, 256);
+    const unsigned uxy = (unsigned)nx * (unsigned)ny;
+    { k_od_exact<<<xb, 256, 0, s>>>(lx, cnt + 2, r.in, r.tmp1, 1u, 1u, (unsigned)nx, 0ull, od_magic((unsigned)nx)); N2M_COUNT(); }
+    { k_od_exact<<<xb, 256, 0, s>>>(ly, cnt + 1, r.tmp1, r.tmp2, (unsigned)nx, (unsigned)nx, (unsigned)ny,
+                                    od_magic((unsigned)nx), od_magic((unsigned)ny)); N2M_COUNT(); }
+    { k_od_exact<<<xb, 256, 0, s>>>(lz, cnt + 0, r.tmp2, r.out, uxy, uxy, (unsigned)nz, od_magic(uxy),
+                                    od_magic((unsigned)nz)); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
