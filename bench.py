@@ -282,6 +282,7 @@ def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
         if it == 0:
             first = loss.detach()
         last = loss.detach()
+        torch.cuda.synchronize()   # one fitting step at a time, as a loop that inspects each mesh runs
     torch.cuda.synchronize()
     t_gd = time.perf_counter() - t0
     first, last = float(first), float(last)
@@ -724,11 +725,18 @@ def main():
         gv, kind, times, cmesh = cpu_reference(vol, 1, 0)
         cpu = {"value": round(gv, 6), "unit": "Gvox/s", "cores": 1, "kind": kind,
                "sample": f"one full 512^3 meshify ({times[0]:.1f} s)"}
-        # the mesh the timed calls produce (last host-memory call) against the CPU path's, outside the timed region
+        # the meshes the timed calls produce (the device-resident step and the last host-memory
+        # call) against the CPU path's, outside the timed region
+        from nii2mesh_gb300.autograd import _DeviceView
+        tp, pp, ntd, nvd, _ = step()
+        dmesh = (torch.as_tensor(_DeviceView(tp, (ntd, 3), "<i4"), device=f"cuda:{dev}").cpu().numpy(),
+                 torch.as_tensor(_DeviceView(pp, (nvd, 3), "<f8"), device=f"cuda:{dev}").cpu().numpy())
+        okd, dd, msgd = mesh_equal(dmesh, cmesh, 0.0)
         ok, d, msg = mesh_equal((tris, pts), cmesh, 0.0)
-        parity = {"ct512_bit_exact": bool(ok), "ct512_max_dpos": d if np.isfinite(d) else None,
-                  "ct512_detail": msg, "ct512_against": kind,
+        parity = {"ct512_bit_exact": bool(ok and okd), "ct512_max_dpos": max(d, dd) if np.isfinite(max(d, dd)) else None,
+                  "ct512_detail": f"device step: {msgd}; host call: {msg}", "ct512_against": kind,
                   "rule": "identical counts and canonical connectivity; positions within 0 (raw) / 1e-4 (HC) voxels"}
+        del dmesh
         del cmesh
     adj = adjoint_metric(n2m, torch) if world == 1 else None
     atl = atlas_metric(n2m, torch) if world == 1 else None

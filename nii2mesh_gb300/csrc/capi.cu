@@ -483,9 +483,12 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     }
     if (!smooth && label) CK(cudaMemcpyAsync(vol, d_src, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaEventRecord(c->evs[0], c->stream));
-    // Lewiner cubes straight after the pre-smooth (no clustering): exact rounding on
-    // demand (only where marching cubes reads values); otherwise the exact three passes
-    bool od = smooth && !label && o.cubes != N2M_CUBES_OLDCUBES && od_eligible(d_src, nx, ny, nz);
+    // Lewiner cubes straight after the pre-smooth (no clustering), volume already in
+    // device memory: exact rounding on demand (only where marching cubes reads values).
+    // Otherwise the exact three passes; a volume arriving from host memory in slabs is
+    // smoothed while it arrives that way (the on-demand repair could only start after
+    // the last slab)
+    bool od = smooth && !label && o.cubes != N2M_CUBES_OLDCUBES && !c->stage.host && od_eligible(d_src, nx, ny, nz);
     if (smooth) {
         CKS(c->stmp.ensure(n * sizeof(float)));
         const StagedInput *stage = c->stage.host ? &c->stage : nullptr;

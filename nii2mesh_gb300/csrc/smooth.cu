@@ -865,38 +865,56 @@ __global__ void k_od_scatter(const unsigned *__restrict__ bz, const unsigned *__
 
 // one exact pass on the listed voxels: dst[v] = tap sum of src along the axis
 // (stride 1, nx or nx*ny; coordinate along the axis = (v / div) % len), or
-// src[v] on the two face layers; one thread per voxel, undecided taps queued
-// per warp for the FP64 fix-up
+// src[v] on the two face layers; one thread per voxel, OE_U list entries per
+// thread in flight at once (a warp takes OE_U runs of 32 consecutive entries),
+// undecided taps queued per warp for the FP64 fix-up
+constexpr int OE_U = 4;
 __global__ void __launch_bounds__(256) k_od_exact(const unsigned *__restrict__ list, const unsigned *__restrict__ cnt,
                                                   const float *__restrict__ src, float *dst, unsigned stride,
                                                   unsigned div, unsigned len, unsigned long long mdiv,
                                                   unsigned long long mlen) {
-    __shared__ unsigned stage_buf[8][64];
+    __shared__ unsigned stage_buf[8][32 * (OE_U + 1)];   // < 32 between drains, + 32 per entry
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     FixStage<false> F{stage_buf[wid], 0};
     Acc acc;   // unused
     const Pass P{src, dst, stride, 0, 0, 0u, 0.f, nullptr};
-    const unsigned n = *cnt, nthr = gridDim.x * blockDim.x;
-    for (unsigned i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n; i0 += nthr) {   // warp-uniform
-        const unsigned i = i0 + (unsigned)lane;
-        bool fail = false;
-        unsigned v = 0;
-        if (i < n) {
-            v = __ldg(list + i);
-            const unsigned q = div == 1u ? v : (unsigned)__umul64hi(v, mdiv);   // v / div
-            const unsigned c = q - (unsigned)__umul64hi(q, mlen) * len;           // q % len
-            float r;
-            if (c >= 2u && c + 2u < len) {
-                const float *p = src + v;
-                const float a0 = __ldg(p - 2 * (size_t)stride), a1 = __ldg(p - (size_t)stride), a2 = __ldg(p),
-                            a3 = __ldg(p + stride), a4 = __ldg(p + 2 * (size_t)stride);
-                if (!tap5_split_window(a0, a1, a2, a3, a4, &r)) fail = !tap5_fast(a0, a1, a2, a3, a4, &r);
-            } else {
-                r = __ldg(src + v);
-            }
-            if (!fail) dst[v] = r;
+    const unsigned n = *cnt;
+    const unsigned nwarps = gridDim.x * (blockDim.x >> 5), gw = blockIdx.x * (blockDim.x >> 5) + (unsigned)wid;
+    for (unsigned i0 = gw * 32u * OE_U; i0 < n; i0 += nwarps * 32u * OE_U) {   // warp-uniform
+        unsigned v[OE_U];
+        bool act[OE_U], inner[OE_U];
+        float a[OE_U][5];
+#pragma unroll
+        for (int u = 0; u < OE_U; u++) {
+            const unsigned i = i0 + (unsigned)u * 32u + (unsigned)lane;
+            act[u] = i < n;
+            v[u] = act[u] ? __ldg(list + i) : 0u;
         }
-        F.push(fail, v, lane);
+#pragma unroll
+        for (int u = 0; u < OE_U; u++) {
+            const unsigned q = div == 1u ? v[u] : (unsigned)__umul64hi(v[u], mdiv);   // v / div
+            const unsigned c = q - (unsigned)__umul64hi(q, mlen) * len;               // q % len
+            inner[u] = act[u] && c >= 2u && c + 2u < len;
+            const float *p = src + v[u];
+            if (inner[u]) {
+                a[u][0] = __ldg(p - 2 * (size_t)stride);
+                a[u][1] = __ldg(p - (size_t)stride);
+                a[u][3] = __ldg(p + stride);
+                a[u][4] = __ldg(p + 2 * (size_t)stride);
+            }
+            a[u][2] = act[u] ? __ldg(p) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < OE_U; u++) {
+            bool fail = false;
+            if (act[u]) {
+                float r = a[u][2];
+                if (inner[u] && !tap5_split_window(a[u][0], a[u][1], a[u][2], a[u][3], a[u][4], &r))
+                    fail = !tap5_fast(a[u][0], a[u][1], a[u][2], a[u][3], a[u][4], &r);
+                if (!fail) dst[v[u]] = r;
+            }
+            F.push(fail, v[u], lane);
+        }
         F.drain(P, acc, lane);
     }
     F.finish(P, acc, lane);

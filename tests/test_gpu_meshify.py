@@ -216,3 +216,42 @@ def test_ct512_full_size_bit_exact(gpu, oracle):
     tb, pb = np.empty((len(got[0]), 3), np.int32), np.empty((len(got[1]), 3), np.float64)
     nt, nv, _ = ctx.meshify_into(vol, tb, pb, 300.0, gpu.MC33, True, False, False)
     assert np.array_equal(tb[:nt], got[0]) and np.array_equal(pb[:nv], got[1])
+    # the device-resident call (pre-smooth with exact rounding on demand) gives the same mesh
+    dt, dp = device_mesh(gpu, ctx, vol, 300.0, gpu.MC33)
+    assert np.array_equal(dt, got[0]) and np.array_equal(dp, got[1])
+
+
+def device_mesh(gpu, ctx, vol, iso, cubes, largest=False, bubbles=False):
+    """n2m_meshify_device on a CUDA copy of vol; the mesh copied back to host arrays"""
+    import torch
+    from nii2mesh_gb300.autograd import _DeviceView
+    d = torch.from_numpy(vol).cuda()
+    nz, ny, nx = vol.shape
+    tp, pp, nt, nv, _ = ctx.meshify_device(d.data_ptr(), (nx, ny, nz), iso, cubes, True, largest, bubbles)
+    t = torch.as_tensor(_DeviceView(tp, (nt, 3), "<i4"), device="cuda").cpu().numpy().copy()
+    p = torch.as_tensor(_DeviceView(pp, (nv, 3), "<f8"), device="cuda").cpu().numpy().copy()
+    return t, p
+
+
+@pytest.mark.parametrize("shape", [(48, 52, 64), (96, 96, 96), (40, 33, 36), (64, 64, 128), (31, 29, 37)])
+@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE])
+def test_device_path_on_demand_smoothing(gpu, oracle, shape, variant):
+    """device-resident volumes whose rows are a multiple of 4 voxels take the
+    pre-smooth with exact rounding on demand (pass A over TMA tiles, exact
+    values only where marching cubes reads them); rows of other lengths the
+    exact three passes: either way the oracle's mesh, bit for bit, on CT-like
+    data, on spheres with noise around the isolevel and on an isolevel that
+    falls back to mid-range"""
+    ctx = gpu.Context(0)
+    nz, ny, nx = shape
+    cubes = gpu.CLASSIC_TABLE if variant == MC_CLASSIC_TABLE else gpu.MC33
+    vols = [(synth.ct512(seed=sum(shape), n=max(shape), count=10)[:nz, :ny, :nx].copy(), 300.0),
+            (synth.spheres(n=max(shape), count=6, rmin=5, rmax=12, cmin=10, cmax=max(shape) - 10, noise=20.0,
+                           seed=nx)[:nz, :ny, :nx].copy(), 50.0)]
+    vols.append((vols[1][0], 1e6))
+    for vol, iso in vols:
+        want = oracle.meshify(vol, iso, variant, True, False, False)
+        got = device_mesh(gpu, ctx, vol, iso, cubes)
+        ok, d, msg = mesh_equal(got, want, POS_TOL)
+        assert ok, (shape, iso, msg)
+    ctx.close()
