@@ -283,7 +283,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
                       &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->hc.bad, &c->th.buf, &c->th.table,
                       &c->stmp2, &c->od.st, &c->od.unc, &c->od.cmin, &c->od.cmax, &c->od.need_z, &c->od.need_y,
-                      &c->od.need_x, &c->od.off, &c->od.list, &c->od.lcnt,
+                      &c->od.need_x, &c->od.off, &c->od.list, &c->od.lcnt, &c->od.vsign,
                       &c->wr.mt, &c->wr.mp, &c->wr.pack, &c->wr.pack2, &c->wr.lens, &c->wr.flag, &c->wr.out};
     for (DevBuf *b : bufs) b->release();
     deflate_release(c->wr.df);

@@ -126,7 +126,10 @@ __device__ __forceinline__ unsigned border_word(const GV &g, long long rb, bool 
     return __ballot_sync(0xffffffffu, x < g.NX && d > -N2M_FLT_EPS);
 }
 
-__global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nrows, unsigned *signs) {
+// vsign (may be null): the volume's sign bitmap (OdWork::vsign, wv words per row,
+// nys groups of 8 rows); a direct word is then two bitmap words shifted into place
+__global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nrows, unsigned *signs,
+                                               const unsigned *__restrict__ vsign, unsigned wv, unsigned nys) {
     const int lane = threadIdx.x & 31;
     // words xw whose 32 points lie strictly inside the volume in x and inside the grid
     const int xs0 = max(0, (1 - g.lo0 + 31) / 32);
@@ -143,7 +146,16 @@ __global__ void __launch_bounds__(256) k_signs(GV g, unsigned WX, unsigned nrows
             const unsigned m = border_word(g, rb, rface, xw, lane);
             if (lane == 0) out[xw] = m;
         }
-        for (int xw0 = f0; xw0 < f1; xw0 += SW) {
+        if (vsign && f0 < f1) {   // direct words from the bitmap: lane k takes word f0 + k, f0 + 32 + k, ...
+            for (int xw = f0 + lane; xw < f1; xw += 32) {
+                const int vx0 = g.lo0 + xw * 32;   // 1 <= vx0 and vx0 + 31 <= dx - 2: both words lie in the row
+                const int sh = vx0 & 31;
+                const size_t wlo = od_vsign_word((unsigned)vx0, (unsigned)vy, (unsigned)vz, wv, nys);
+                const unsigned lo = __ldg(vsign + wlo), hi = sh ? __ldg(vsign + wlo + 8) : 0u;   // next x word: +8
+                out[xw] = __funnelshift_r(lo, hi, sh);
+            }
+        }
+        for (int xw0 = f0; xw0 < (vsign ? f0 : f1); xw0 += SW) {
             float raw[SW];
 #pragma unroll
             for (int k = 0; k < SW; k++) raw[k] = xw0 + k < f1 ? __ldg(rp + (xw0 + k) * 32) : 0.f;
@@ -723,7 +735,9 @@ n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4
     {
         const unsigned nrows = (unsigned)g.n[1] * (unsigned)g.n[2];
         const unsigned blocks = std::min<unsigned>((nrows + 7) / 8, 152u * 16u);
-        k_signs<<<blocks, 256, 0, s>>>(v, WX, nrows, w.signs.as<unsigned>());
+        k_signs<<<blocks, 256, 0, s>>>(v, WX, nrows, w.signs.as<unsigned>(),
+                                       repair ? repair->w->vsign.as<unsigned>() : nullptr,
+                                       (unsigned)(g.dim[0] + 31) / 32, (unsigned)(g.dim[1] + 7) / 8);
         N2M_COUNT();
     }
     if (repair) {   // exact smoothed values where the cubes below read them

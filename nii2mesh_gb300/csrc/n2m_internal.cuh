@@ -112,9 +112,15 @@ struct OdLists {
     OdCand *cmin, *cmax;
     unsigned *cnt;
     unsigned cap;
+    unsigned *vsign;         // sign bitmap of the smoothed volume (see OdWork)
+    unsigned wv, nys;        // its words per row, groups of 8 rows per slice
 };
 struct OdWork {
     DevBuf st, unc, cmin, cmax, need_z, need_y, need_x, off, list, lcnt;
+    // bit x & 31 of word od_vsign_word(x, y, z): the smoothed value of voxel (x, y, z)
+    // minus iso is above -FLT_EPSILON (marching cubes' sign before edge darkening),
+    // exact for every voxel once od_resolve has run
+    DevBuf vsign;
     unsigned cap = 0;
 };
 struct ScanWork;
@@ -126,6 +132,11 @@ struct OdRepair {
     OdWork *w;
     ScanWork *scan;
 };
+// the sign bitmap's word of voxel (x, y, z): the 8 row words of one 32 x 8 tile of a
+// slice are adjacent (one 32-byte sector, written at once by pass A)
+__host__ __device__ __forceinline__ size_t od_vsign_word(unsigned x, unsigned y, unsigned z, unsigned wv, unsigned nys) {
+    return (((size_t)z * nys + (y >> 3)) * wv + (x >> 5)) * 8u + (y & 7u);
+}
 // whether the on-demand path applies: rows a multiple of 16 bytes (TMA tiles), fewer than 2^32 voxels
 bool od_eligible(const float *in, int nx, int ny, int nz);
 n2m_status od_approx(const float *in, float *out, int nx, int ny, int nz, float iso, OdWork &w, cudaStream_t s,
@@ -212,6 +223,8 @@ struct McCounts {
 };
 // repair: marks the corners of the cubes with mixed signs in repair->w->need_z
 // after the sign pass and runs od_repair before any value is read (null: none)
+// (with a repair, the sign words of grid points strictly inside the volume come
+// from repair->w->vsign instead of the values)
 n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s,
                     const OdRepair *repair = nullptr);
 n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,

@@ -598,6 +598,7 @@ __global__ void __launch_bounds__(OA_WARPS * 32) k_od_approx(const __grid_consta
         unsigned jmin = 0, jmax = 0;                 // where lmin / lmax are
         int bzl = INT_MAX, bzh = INT_MIN;
         unsigned ymask = 0;                          // rows with a decided voxel >= iso
+        unsigned sgn = 0;                            // this slice's sign bits, bit kk = row y0 + kk
         float nanacc = 0.f;                          // becomes NaN if an output is NaN or infinite
         for (int zi = zs - 2; zi <= zlast; zi++) {
             const unsigned k = used % OA_S, par = (used / OA_S) & 1u;
@@ -633,6 +634,7 @@ __global__ void __launch_bounds__(OA_WARPS * 32) k_od_approx(const __grid_consta
             for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
             B = m * 0x1p-19f;   // bounds every output whose inputs have been read
             const int z = zi - 2;
+            sgn = 0;
             if (z >= zs && z < ze && ownx) {
                 const bool zint = z >= 2 && z <= nz - 3;
                 const float band = B + 4.0f * N2M_FLT_EPS;
@@ -652,7 +654,9 @@ __global__ void __launch_bounds__(OA_WARPS * 32) k_od_approx(const __grid_consta
                     lmax2 = hi ? lmax : fmaxf(lmax2, zv);
                     jmax = hi ? j : jmax;
                     lmax = fmaxf(lmax, zv);
-                    const bool und = fabsf(__fsub_rn(zv, iso)) <= band;
+                    const float dv = __fsub_rn(zv, iso);
+                    sgn |= (unsigned)(dv > -N2M_FLT_EPS) << kk;   // provisional for undecided voxels
+                    const bool und = fabsf(dv) <= band;
                     if (und) {
                         const unsigned q = atomicAdd(&L.cnt[0], 1u);
                         if (q < L.cap) L.unc[q] = j;
@@ -664,6 +668,15 @@ __global__ void __launch_bounds__(OA_WARPS * 32) k_od_approx(const __grid_consta
                     bzl = min(bzl, z);
                     bzh = z;
                 }
+            }
+            if (z >= zs && z < ze) {   // warp-uniform: the tile's 8 row words, lanes 0-7, one sector
+                unsigned mine = 0;
+#pragma unroll
+                for (int kk = 0; kk < OW_Y; kk++) {
+                    const unsigned b = __ballot_sync(FULL, (sgn >> kk) & 1u);
+                    mine = lane == kk ? b : mine;
+                }
+                if (lane < OW_Y) L.vsign[od_vsign_word((unsigned)x0, (unsigned)(y0 + lane), (unsigned)z, L.wv, L.nys)] = mine;
             }
         }
         if (timed_out) break;
@@ -786,6 +799,9 @@ __global__ void k_od_resolve(const float *__restrict__ in, float *out, int nx, i
         const float v = od_exact_at(in, (int)x, (int)y, (int)z, nx, ny, nz);
         if (which == 0) {
             out[j] = v;
+            unsigned *sw = L.vsign + od_vsign_word(x, y, z, L.wv, L.nys);
+            if (__fsub_rn(v, iso) > -N2M_FLT_EPS) atomicOr(sw, 1u << (x & 31));
+            else atomicAnd(sw, ~(1u << (x & 31)));
             if (v >= iso) {
                 atomicMin(&st->vs.lo[0], (int)x); atomicMax(&st->vs.hi[0], (int)x);
                 atomicMin(&st->vs.lo[1], (int)y); atomicMax(&st->vs.hi[1], (int)y);
@@ -823,10 +839,20 @@ template <int FIELD>
 __global__ void k_od_dilate(const unsigned *__restrict__ src, unsigned *dst, long long nvox, long long stride,
                             uint4 *cnt) {
     const long long nw = (nvox + 31) >> 5;
+    const bool aligned = (stride & 31) == 0 && (nvox & 31) == 0;   // whole-word shifts (e.g. rows of 512)
+    const long long sw = stride >> 5;
     for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
         unsigned acc = 0;
+        if (aligned) {
 #pragma unroll
-        for (int d = -2; d <= 2; d++) acc |= bits_at(src, (w << 5) + d * stride, nvox);
+            for (int d = -2; d <= 2; d++) {
+                const long long ws = w + d * sw;
+                if (ws >= 0 && ws < nw) acc |= __ldg(src + ws);
+            }
+        } else {
+#pragma unroll
+            for (int d = -2; d <= 2; d++) acc |= bits_at(src, (w << 5) + d * stride, nvox);
+        }
         dst[w] = acc;
         if (FIELD == 1) {
             cnt[w] = make_uint4((unsigned)__popc(src[w]), (unsigned)__popc(acc), 0u, 0u);
@@ -985,9 +1011,11 @@ n2m_status od_approx(const float *in, float *out, int nx, int ny, int nz, float 
     h.umin = INT_MAX;
     h.lmax = INT_MIN;
     CK(cudaMemcpyAsync(w.st.p, &h, sizeof(OdStats), cudaMemcpyHostToDevice, s));
+    const unsigned wv = (unsigned)(nx + 31) / 32, nys = (unsigned)(ny + 7) / 8;
+    CKS(w.vsign.ensure((size_t)nz * nys * wv * 8 * sizeof(unsigned)));
     OdStats *st = w.st.as<OdStats>();
     OdLists L{w.unc.as<unsigned>(), w.cmin.as<OdCand>(), w.cmax.as<OdCand>(),
-              (unsigned *)((char *)w.st.p + offsetof(OdStats, cnt)), w.cap};
+              (unsigned *)((char *)w.st.p + offsetof(OdStats, cnt)), w.cap, w.vsign.as<unsigned>(), wv, nys};
     const int grid = od_grid((const void *)k_od_approx, OA_WARPS * 32);
     auto launch = [&](int z_lo, int z_hi) -> n2m_status {
         if (z_hi <= z_lo) return N2M_OK;
@@ -1034,7 +1062,8 @@ n2m_status od_resolve(const float *in, float *out, int nx, int ny, int nz, float
                 h.cnt[1] == 0 || h.cnt[2] == 0;
     if (*fallback) return N2M_OK;
     OdLists L{w.unc.as<unsigned>(), w.cmin.as<OdCand>(), w.cmax.as<OdCand>(),
-              (unsigned *)((char *)w.st.p + offsetof(OdStats, cnt)), w.cap};
+              (unsigned *)((char *)w.st.p + offsetof(OdStats, cnt)), w.cap, w.vsign.as<unsigned>(),
+              (unsigned)(nx + 31) / 32, (unsigned)(ny + 7) / 8};
     const unsigned tot = h.cnt[0] + h.cnt[1] + h.cnt[2];
     const unsigned blocks = std::max(1u, std::min((tot + 127) / 128, 152u * 8u));
     k_od_resolve<<<blocks, 128, 0, s>>>(in, out, nx, ny, nz, iso, w.st.as<OdStats>(), L, h.cnt[0], h.cnt[1], h.cnt[2]);
