@@ -36,15 +36,20 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Gvox/s smooth+MC+weld at 512³; atlas meshes/s batched vs loop; fwd+bwd ms @128³"
 WORKLOAD = "ct512: 512^3 f32 CT-like, iso 300, -p 1 -l 0 -b 0 -o 0 -r 1 -s 0 (Lewiner MC33)"
 ISO = 300.0
-# DRAM bytes (read + write) per step of each stage on this workload, from one ncu capture of
-# `bench.py --profile 512` (profiles/meshify_ct512_kernels.md): smoothing = its three pass
-# kernels, count = k_signs + k_words + k_active + scans, emit = k_emit.
-NCU_TRAFFIC = {"smooth": 3413e6, "count": 925e6, "emit": 376e6, "degenerate": 346e6}
+# DRAM bytes (read + write) per step of each stage on this workload: one ncu capture of
+# `bench.py --profile 384` (dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels),
+# scaled by the voxel count to 512^3 (profiles/meshify_ct512_kernels.md): smooth = pass A + pass B,
+# count = signs, marks, exact passes on marked voxels, words, scans, emit = k_emit, weld, degenerate
+SCALE_384 = (512 / 384) ** 3
+NCU_TRAFFIC = {"smooth": 437.9e6 * SCALE_384, "count": 654.6e6 * SCALE_384, "emit": 138.0e6 * SCALE_384,
+               "weld": 74.0e6 * SCALE_384, "degenerate": 125.6e6 * SCALE_384}
+PASS_A_TRAFFIC = 437.6e6 * SCALE_384   # k_od_approx alone
 # what bounds each stage (measured in the same profiles)
-STAGE_BOUND = {"smooth": "FP32 instruction issue: exact double-rounding proof per tap (~72-80 % issue active); "
-                         "three streaming passes at ~8.1 B/voxel each"}
-# algorithmic bytes per stage (per unit): smooth 8 B/voxel, count 4 B/grid point,
-# emit 24 B/vertex + 12 B/triangle, degenerate 24 B/triangle
+STAGE_BOUND = {"smooth": "FP32 instruction issue in pass A (74 % issue active, ~92 instructions per voxel); "
+                         "DRAM 7.7 B/voxel, no re-reads",
+               "count": "the exact passes on the ~10 % marked voxels (issue + sector-granular gathers) and the "
+                        "sign/word passes",
+               "emit": "latency (neighbour-word and value loads) and divergent listing"}
 STAGE_NAMES = ("smooth", "cluster", "count", "emit", "weld", "degenerate", "hc")
 
 
@@ -677,20 +682,24 @@ def main():
             st["dram_bytes"] = NCU_TRAFFIC[nm]
             st["dram_over_algorithmic"] = round(NCU_TRAFFIC[nm] / algo[nm], 2)
         stages[nm] = st
-    top = max(range(7), key=lambda i: stage_ms[i])
-    name = STAGE_NAMES[top]
     whole = 4.0 * nvox + 24.0 * nv + 12.0 * nt
     whole_gbs = whole / (ms * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel_stage": name, "achieved": stages.get(name, {}).get("achieved_gbs"), "peak": peak,
-            "unit": "GB/s", "frac": stages.get(name, {}).get("frac"), "peak_source": peak_kind,
-            "algorithmic_bytes": algo.get(name), "traffic": NCU_TRAFFIC.get(name),
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels, one step",
-            "limited_by": STAGE_BOUND.get(name),
+    # the dominant kernel: pass A of the pre-smooth (k_od_approx), 4 B read + 4 B written + 1/8 B of
+    # sign bitmap per voxel, over its own CUDA-event time on the library's stream
+    pa_ms = statistics.mean(r.get("ms_smooth_pass_a", 0.0) for r in reps)
+    pa_bytes = 8.125 * nvox
+    pa_gbs = pa_bytes / (pa_ms * 1e-3) / 1e9 if pa_ms > 0 else None
+    roof = {"bound": "hbm", "kernel": "k_od_approx (pre-smooth pass A)", "achieved": round(pa_gbs, 1) if pa_gbs else None,
+            "peak": peak, "unit": "GB/s", "frac": round(pa_gbs / peak, 4) if pa_gbs else None, "peak_source": peak_kind,
+            "kernel_ms": round(pa_ms, 4), "algorithmic_bytes": pa_bytes, "traffic": PASS_A_TRAFFIC,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_od_approx launch at 384^3, "
+                              "scaled by the voxel count",
+            "limited_by": "FP32 instruction issue (74 % issue active); memory 1.9-2.4 TB/s",
             "whole_path": {"bytes": whole, "achieved": round(whole_gbs, 1), "frac": round(whole_gbs / peak, 4),
                            "formula": "(4 N_vox + 24 N_vert + 12 N_tri) / ms_per_step / peak",
-                           "dram_bytes": sum(NCU_TRAFFIC.values()),
+                           "dram_bytes": round(sum(NCU_TRAFFIC.values())),
                            "dram_over_algorithmic": round(sum(NCU_TRAFFIC.values()) / whole, 2)},
-            "stages": stages}
+            "stages": stages, "stage_bounds": STAGE_BOUND}
 
     # e2e through the C ABI with host buffers: the volume from pinned memory, the mesh copied back into
     # pinned arrays the caller allocates once and reuses (n2m_meshify_into); the malloc-returning

@@ -78,6 +78,9 @@ typedef struct {
      * (waiting for the output pages, device-to-host copy; host clock) */
     float ms_stage[8];
     int64_t kernel_launches; /* kernels this call launched */
+    float ms_smooth_pass_a;  /* device time of the fused approximate pre-smooth kernel of the
+                              * exact-on-demand path (inside ms_stage[0]); 0 when the exact
+                              * three passes ran */
 } n2m_report;
 
 /* ---- context ------------------------------------------------------------ */

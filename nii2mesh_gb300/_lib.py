@@ -46,7 +46,7 @@ class Report(C.Structure):
     _fields_ = [("isolevel_used", C.c_float), ("vmin", C.c_float), ("vmax", C.c_float), ("lo", C.c_int * 3),
                 ("hi", C.c_int * 3), ("nvert_raw", C.c_int64), ("ntri_raw", C.c_int64), ("nvert", C.c_int64),
                 ("ntri", C.c_int64), ("welded", C.c_int), ("degenerate", C.c_int), ("ms_total", C.c_float),
-                ("ms_stage", C.c_float * 8), ("kernel_launches", C.c_int64)]
+                ("ms_stage", C.c_float * 8), ("kernel_launches", C.c_int64), ("ms_smooth_pass_a", C.c_float)]
     STAGES = ("smooth", "cluster", "count", "emit", "weld", "degenerate", "hc", "unused")
 
     def as_dict(self):

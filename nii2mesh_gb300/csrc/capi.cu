@@ -185,6 +185,8 @@ struct n2m_context {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evs[8] = {};   // stage boundaries of the last pipeline run
+    cudaEvent_t eva[2] = {};   // around pass A of the exact-on-demand pre-smooth
+    bool pass_a = false;       // whether the last pipeline run used it
     DevBuf in, raw, vol, stmp, stmp2, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath,
         hmesh;
     OdWork od;   // pre-smooth with exact rounding on demand
@@ -251,7 +253,7 @@ extern "C" n2m_status n2m_context_create(n2m_context **out, int device) {
         return N2M_ERR_CUDA;
     }
     for (int i = 0; i < 8; i++)
-        if (cudaEventCreate(&c->evs[i]) != cudaSuccess) {
+        if (cudaEventCreate(&c->evs[i]) != cudaSuccess || (i < 2 && cudaEventCreate(&c->eva[i]) != cudaSuccess)) {
             n2m_set_error("event creation failed");
             return N2M_ERR_CUDA;
         }
@@ -292,6 +294,8 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
     if (c->wr.host) cudaFreeHost(c->wr.host);
     for (int i = 0; i < 8; i++)
         if (c->evs[i]) cudaEventDestroy(c->evs[i]);
+    for (int i = 0; i < 2; i++)
+        if (c->eva[i]) cudaEventDestroy(c->eva[i]);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     c->hout.discard();
@@ -470,6 +474,7 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     const bool smooth = o.pre_smooth && nx >= 5 && ny >= 5 && nz >= 5;
     const bool label = o.only_largest || o.fill_bubbles;
     float iso = o.isolevel;
+    c->pass_a = false;
     CKS(c->stats.ensure(2 * sizeof(VolStats)));
     VolStats *dst = c->stats.as<VolStats>();
     VolStats h[2];
@@ -494,7 +499,10 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
         const StagedInput *stage = c->stage.host ? &c->stage : nullptr;
         if (od) {
             bool fallback = false;
+            CK(cudaEventRecord(c->eva[0], c->stream));
             CKS(od_approx(d_src, vol, nx, ny, nz, iso, c->od, c->stream, stage));
+            CK(cudaEventRecord(c->eva[1], c->stream));
+            c->pass_a = true;
             CKS(od_resolve(d_src, vol, nx, ny, nz, iso, c->od, dst, c->stream, &fallback));
             if (fallback) {   // the input is on the device by now
                 od = false;
@@ -788,6 +796,8 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
         }
         rep->ms_stage[6] = rep->ms_stage[7] = 0.f;
         rep->kernel_launches = g_n2m_launches.load() - launches0;
+        rep->ms_smooth_pass_a = 0.f;
+        if (c->pass_a) cudaEventElapsedTime(&rep->ms_smooth_pass_a, c->eva[0], c->eva[1]);
     }
     return N2M_OK;
 }
