@@ -481,6 +481,57 @@ def threshold_metric(n2m, torch, reps=5):
     return out
 
 
+def variants_metric(n2m, torch, vol, reps=5):
+    """The same 512^3 CT volume (device-resident) with the CLI's default clustering
+    plus bubble fill (-l 1 -b 1: the clustering stage on its own) and through the
+    reference's default build, the classic marching cubes of oldcubes.c (-l 0 -b 0),
+    each checked against the CPU path on the same volume outside the timed region."""
+    from oracle.oracle import OLDCUBES, Oracle, mesh_equal
+    dev = torch.cuda.current_device()
+    d = torch.from_numpy(vol).cuda()
+    ctx = n2m.Context(dev)
+    nx = ny = nz = vol.shape[0]
+    peak, peak_kind = peaks()
+    out = {}
+    for name, cubes, largest, bubbles in (("ct512_l1_b1", n2m.MC33, True, True),
+                                          ("ct512_oldcubes", n2m.OLDCUBES, False, False)):
+        step = lambda: ctx.meshify_device(d.data_ptr(), (nx, ny, nz), ISO, cubes, True, largest, bubbles)
+        for _ in range(3):
+            step()
+        reps_ = []
+        stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            reps_.append(step()[4])
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / reps
+        r = reps_[-1]
+        st = {n: round(statistics.mean(x["ms_stage"][i] for x in reps_), 4) for i, n in enumerate(STAGE_NAMES)}
+        whole = 4.0 * vol.size + 24.0 * r["nvert"] + 12.0 * r["ntri"]
+        gbs = whole / (ms * 1e-3) / 1e9
+        out[name] = {"options": "-p 1 -l 1 -b 1 -o 0" if largest else "-p 1 -l 0 -b 0, oldcubes build",
+                     "ms_per_step": round(ms, 4), "gvox_per_s": round(vol.size / (ms * 1e-3) / 1e9, 3),
+                     "stage_ms": st, "triangles": r["ntri"], "vertices": r["nvert"],
+                     "roofline_whole_path": {"achieved": round(gbs, 1), "frac": round(gbs / peak, 4),
+                                             "peak_source": peak_kind}}
+        # parity of the timed mesh against the CPU path (one host core)
+        from nii2mesh_gb300.autograd import _DeviceView
+        tp, pp, ntd, nvd, _ = step()
+        dm = (torch.as_tensor(_DeviceView(tp, (ntd, 3), "<i4"), device=f"cuda:{dev}").cpu().numpy(),
+              torch.as_tensor(_DeviceView(pp, (nvd, 3), "<f8"), device=f"cuda:{dev}").cpu().numpy())
+        t0 = time.perf_counter()
+        want = Oracle().meshify(vol, ISO, OLDCUBES if cubes == n2m.OLDCUBES else 0, True, largest, bubbles)
+        out[name]["cpu_ms"] = round(1e3 * (time.perf_counter() - t0), 1)
+        ok, dd, _ = mesh_equal(dm, want, 0.0)
+        out[name]["bit_exact_vs_cpu"] = bool(ok)
+        del dm, want
+    ctx.close()
+    return out
+
+
 def writer_metric(n2m, torch, vol, reps=3):
     """save_mesh of the 512^3 CT mesh as nii2mesh writes it by default (.mz3
     gzip: quality 1 sets isGz, src/nii2mesh.c:350) and as OBJ text: the GPU
@@ -752,13 +803,17 @@ def main():
     thr = threshold_metric(n2m, torch) if world == 1 else None
     brn = brain_metric(n2m, torch) if world == 1 else None
     wrt = writer_metric(n2m, torch, vol) if world == 1 else None
+    var = variants_metric(n2m, torch, vol) if world == 1 else None
     line = {"metric": METRIC, "value": round(value, 4), "unit": "Gvox/s", "n_gpus": world, "steps": a.steps,
             "warmup": warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
             "config": bench_config(world, nt, nv),
             "stage_ms": {n: round(v, 4) for n, v in zip(STAGE_NAMES, stage_ms)},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": ck,
-            "parity": parity, "adjoint": adj, "atlas": atl, "threshold": thr, "brain": brn, "writer": wrt}
+            "parity": parity, "adjoint": adj, "atlas": atl, "threshold": thr, "brain": brn, "writer": wrt,
+            "variants": var}
+    if var:
+        parity.update({f"{k}_bit_exact": v.pop("bit_exact_vs_cpu") for k, v in var.items()})
     if brn:
         parity.update({k: brn.pop(k) for k in ("brain182_raw_bit_exact", "brain182_hc_max_err_vs_fp64")})
     if adj:
