@@ -273,7 +273,14 @@ def adjoint_metric(n2m, torch, steps=20, gd_steps=200):
     t_f = timed(f_only, steps)
     t_fb = timed(f_b, steps)
     grad = f_b().cpu().numpy()
-    # shape fitting: the loss is read back only at the first and the last step
+    # shape fitting: the loss is read back only at the first and the last step.  One untimed step
+    # first: the first optimizer step of a process compiles and caches torch's kernels for this GPU
+    w_ = img.clone().requires_grad_(True)
+    o_ = torch.optim.Adam([w_], lr=GD_LR)
+    fwd(w_).backward()
+    o_.step()
+    torch.cuda.synchronize()
+    del w_, o_
     v = img.clone().requires_grad_(True)
     opt = torch.optim.Adam([v], lr=GD_LR)
     torch.cuda.synchronize()
