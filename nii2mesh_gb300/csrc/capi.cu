@@ -187,8 +187,8 @@ struct n2m_context {
     cudaEvent_t evs[8] = {};   // stage boundaries of the last pipeline run
     cudaEvent_t eva[2] = {};   // around pass A of the exact-on-demand pre-smooth
     bool pass_a = false;       // whether the last pipeline run used it
-    DevBuf in, raw, vol, stmp, stmp2, stats, totals, cand, ncand, lastuse, pts_raw, tris_raw, pts, tris, ntf, weld, gath,
-        hmesh;
+    DevBuf in, raw, vol, stmp, stmp2, stats, totals, cand, ncand, lastuse, lubits, pts_raw, tris_raw, pts, tris, ntf, weld,
+        gath, hmesh;
     OdWork od;   // pre-smooth with exact rounding on demand
     McWork mc;
     ScanWork scan;
@@ -284,7 +284,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
                       &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->hc.bad, &c->th.buf, &c->th.table,
-                      &c->stmp2, &c->od.st, &c->od.unc, &c->od.cmin, &c->od.cmax, &c->od.need_z, &c->od.need_y,
+                      &c->stmp2, &c->lubits, &c->od.st, &c->od.unc, &c->od.cmin, &c->od.cmax, &c->od.need_z, &c->od.need_y,
                       &c->od.need_x, &c->od.off, &c->od.list, &c->od.lcnt, &c->od.vsign,
                       &c->wr.mt, &c->wr.mp, &c->wr.pack, &c->wr.pack2, &c->wr.lens, &c->wr.flag, &c->wr.out};
     for (DevBuf *b : bufs) b->release();
@@ -632,8 +632,7 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
         CKS(c->lastuse.ensure(nv * sizeof(long long)));
         { k_fill_ll<<<1024, 256, 0, c->stream>>>(c->lastuse.as<long long>(), nv, -1); N2M_COUNT(); }
         CKS(oc_emit(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, mcn, c->pts_raw.as<vec3d>(),
-                    c->tris_raw.as<vec3i>(), c->cand.as<int>(), c->ncand.as<unsigned>(), cap,
-                    c->lastuse.as<long long>(), c->stream));
+                    c->tris_raw.as<vec3i>(), c->cand.as<int>(), c->ncand.as<unsigned>(), cap, c->stream));
     } else {
         CKS(mc_emit(g, cubes, c->mc, mcn, c->pts_raw.as<vec3d>(), c->tris_raw.as<vec3i>(), c->cand.as<int>(),
                     c->ncand.as<unsigned>(), cap, c->stream));
@@ -643,6 +642,11 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
     if (nc[0] > (unsigned)cap || nc[1] > (unsigned)cap) {
         n2m_set_error("weld candidate overflow (%u, %u > %d)", nc[0], nc[1], cap);
         return N2M_ERR_INTERNAL;
+    }
+    if (old && nc[0]) {   // the weld orders oldcubes candidates by their last copy
+        CKS(c->lubits.ensure(((size_t)nv + 31) / 32 * sizeof(unsigned)));
+        CKS(oc_lastuse(c->tris_raw.as<vec3i>(), (int)nt, (int)nv, c->cand.as<int>(), (int)nc[0], c->lubits.as<unsigned>(),
+                       c->lastuse.as<long long>(), c->stream));
     }
     if (nc[1]) {   // c-vertex candidates: collect every vertex near them
         CK(cudaMemcpyAsync(c->cand.as<int>() + nc[0], c->cand.as<int>() + cap, nc[1] * sizeof(int),

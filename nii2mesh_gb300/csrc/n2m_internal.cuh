@@ -238,8 +238,11 @@ n2m_status mc_ccand_scan(const vec3d *d_pts, int np, const int *d_ccand, int ncc
 n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
                     McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s);
 n2m_status oc_emit(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
-                   McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris, int *d_cand, unsigned *d_ncand,
-                   int cand_cap, long long *d_lastuse, cudaStream_t s);
+                    McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris, int *d_cand, unsigned *d_ncand,
+                    int cand_cap, cudaStream_t s);
+// the last copy (3*triangle + corner) of each of the ncand weld candidates; d_bits: nv bits of scratch
+n2m_status oc_lastuse(const vec3i *d_tris, int nt, int nv, const int *d_cand, int ncand, unsigned *d_bits,
+                      long long *d_lastuse, cudaStream_t s);
 
 // mesh.cu
 n2m_status mesh_apply_weld(vec3d *d_pts, vec3i *d_tris, int np, int nt, const int *d_removed, const int *d_keep,

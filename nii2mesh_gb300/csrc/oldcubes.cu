@@ -8,9 +8,12 @@
 // and its weld keeps the position of the LAST copy (src/meshify.c:99-100).
 // Each edge here is computed once, in double, in the orientation of the last
 // cube (raster order) that uses it, so positions are the reference's
-// post-weld positions bit for bit.  d_lastuse records, per vertex, the index
-// of its last copy in the reference's pre-weld vertex list (3*triangle +
-// corner) so that near-corner clusters keep the same survivor.
+// post-weld positions bit for bit.  For the weld candidates (the few vertices
+// near a grid point), oc_lastuse records the index of the vertex's last copy in
+// the reference's pre-weld vertex list (3*triangle + corner) so that
+// near-corner clusters keep the same survivor.
+#include <algorithm>
+
 #include "mc_tables.h"
 #include "n2m_internal.cuh"
 
@@ -36,42 +39,10 @@ __device__ __forceinline__ float oval(const OV &g, int X, int Y, int Z) {
 }
 
 struct OP {
-    bool in, ex, ey, ez, cube;
+    bool ex, ey, ez;
     int X, Y, Z;         // absolute point
-    float v[8];          // corners in Bourke order: p0..p7
+    float v[5];          // p0, p1 (+x), -, p3 (+y), p4 (+z) in Bourke's corner numbering
 };
-
-__device__ __forceinline__ void oclassify(const OV &g, unsigned p, OP &q) {
-    q.in = p < g.NG;
-    q.ex = q.ey = q.ez = q.cube = false;
-    if (!q.in) return;
-    const int z = (int)(p / g.NXY);
-    const unsigned r = p - (unsigned)z * g.NXY;
-    const int y = (int)(r / (unsigned)g.NX), x = (int)(r - (unsigned)y * (unsigned)g.NX);
-    q.X = g.lo0 + x; q.Y = g.lo1 + y; q.Z = g.lo2 + z;
-    const bool hx = x < g.NX - 1, hy = y < g.NY - 1, hz = z < g.NZ - 1;
-    q.v[0] = oval(g, q.X, q.Y, q.Z);
-    q.v[1] = hx ? oval(g, q.X + 1, q.Y, q.Z) : q.v[0];
-    q.v[3] = hy ? oval(g, q.X, q.Y + 1, q.Z) : q.v[0];
-    q.v[4] = hz ? oval(g, q.X, q.Y, q.Z + 1) : q.v[0];
-    const bool b0 = q.v[0] < g.iso;
-    q.ex = hx && ((q.v[1] < g.iso) != b0);
-    q.ey = hy && ((q.v[3] < g.iso) != b0);
-    q.ez = hz && ((q.v[4] < g.iso) != b0);
-    if (hx && hy && hz) {
-        q.cube = true;
-        q.v[2] = oval(g, q.X + 1, q.Y + 1, q.Z);
-        q.v[5] = oval(g, q.X + 1, q.Y, q.Z + 1);
-        q.v[6] = oval(g, q.X + 1, q.Y + 1, q.Z + 1);
-        q.v[7] = oval(g, q.X, q.Y + 1, q.Z + 1);
-    }
-}
-
-__device__ __forceinline__ int ocube_index(const OP &q, float iso) {
-    int ci = 0;
-    for (int c = 0; c < 8; c++) ci |= (q.v[c] < iso) << c;
-    return ci;
-}
 
 __device__ __forceinline__ int ocube_ntri(int ci) {
     if (!d_edge[ci]) return 0;
@@ -80,18 +51,82 @@ __device__ __forceinline__ int ocube_ntri(int ci) {
     return n;
 }
 
-__global__ void __launch_bounds__(256) k_oc_count(OV g, uint4 *words, uint4 *counts) {
-    const unsigned p = blockIdx.x * 256u + threadIdx.x;
-    OP q;
-    oclassify(g, p, q);
-    int nt = q.cube ? ocube_ntri(ocube_index(q, g.iso)) : 0;
-    const unsigned xm = __ballot_sync(0xffffffffu, q.ex), ym = __ballot_sync(0xffffffffu, q.ey),
-                   zm = __ballot_sync(0xffffffffu, q.ez);
-    for (int o = 16; o; o >>= 1) nt += __shfl_xor_sync(0xffffffffu, nt, o);
-    const unsigned w = p >> 5;
-    if ((threadIdx.x & 31) == 0 && w * 32u < g.NG) {
-        words[w] = make_uint4(xm, ym, zm, 0u);
-        counts[w] = make_uint4(__popc(xm) + __popc(ym) + __popc(zm), (unsigned)nt, 0u, 0u);
+// Signs of the grid: bit p & 31 of word p >> 5 is set when grid point p
+// (linear in the grid) is below the isolevel, darkened value included.  The
+// count and the emit read a cube's eight corners as bits of this bitmap.
+__global__ void __launch_bounds__(256) k_oc_signs(OV g, unsigned *bits) {
+    const unsigned nw = (g.NG + 31u) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += (gridDim.x * blockDim.x) >> 5) {
+        const unsigned p = w * 32u + (unsigned)lane;
+        bool b = false;
+        if (p < g.NG) {
+            const int z = (int)(p / g.NXY);
+            const unsigned r = p - (unsigned)z * g.NXY;
+            const int y = (int)(r / (unsigned)g.NX), x = (int)(r - (unsigned)y * (unsigned)g.NX);
+            b = oval(g, g.lo0 + x, g.lo1 + y, g.lo2 + z) < g.iso;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, b);
+        if (lane == 0) bits[w] = m;
+    }
+}
+
+// 32 sign bits starting at grid point q (bits past the grid read as 0)
+__device__ __forceinline__ unsigned obits(const unsigned *__restrict__ bits, unsigned q, unsigned nw) {
+    const unsigned w = q >> 5, sh = q & 31u;
+    const unsigned lo = w < nw ? __ldg(bits + w) : 0u, hi = sh && w + 1 < nw ? __ldg(bits + w + 1) : 0u;
+    return __funnelshift_r(lo, hi, sh);
+}
+
+// a grid point's edges and cube from the sign bits; the warp's 32 consecutive
+// points p0 .. p0+31 share the eight shifted words
+struct OB {
+    bool in, ex, ey, ez, cube;
+    int x, y, z, ci;
+};
+__device__ __forceinline__ OB oc_point(const OV &g, const unsigned *__restrict__ bits, unsigned p0, int lane) {
+    const unsigned nw = (g.NG + 31u) >> 5, NX = (unsigned)g.NX, NXY = g.NXY;
+    const unsigned B0 = obits(bits, p0, nw), B1 = obits(bits, p0 + 1, nw), B3 = obits(bits, p0 + NX, nw),
+                   B2 = obits(bits, p0 + NX + 1, nw), B4 = obits(bits, p0 + NXY, nw), B5 = obits(bits, p0 + NXY + 1, nw),
+                   B7 = obits(bits, p0 + NXY + NX, nw), B6 = obits(bits, p0 + NXY + NX + 1, nw);
+    OB q;
+    const unsigned p = p0 + (unsigned)lane;
+    q.in = p < g.NG;
+    q.ex = q.ey = q.ez = q.cube = false;
+    q.ci = 0;
+    q.x = q.y = q.z = 0;
+    if (!q.in) return q;
+    q.z = (int)(p / NXY);
+    const unsigned r = p - (unsigned)q.z * NXY;
+    q.y = (int)(r / NX);
+    q.x = (int)(r - (unsigned)q.y * NX);
+    const bool hx = q.x < g.NX - 1, hy = q.y < g.NY - 1, hz = q.z < g.NZ - 1;
+    const unsigned b0 = (B0 >> lane) & 1u;
+    q.ex = hx && ((B1 >> lane) & 1u) != b0;
+    q.ey = hy && ((B3 >> lane) & 1u) != b0;
+    q.ez = hz && ((B4 >> lane) & 1u) != b0;
+    if (hx && hy && hz) {   // Bourke's corner order p0 .. p7
+        q.cube = true;
+        q.ci = (int)(b0 | ((B1 >> lane) & 1u) << 1 | ((B2 >> lane) & 1u) << 2 | ((B3 >> lane) & 1u) << 3 |
+                     ((B4 >> lane) & 1u) << 4 | ((B5 >> lane) & 1u) << 5 | ((B6 >> lane) & 1u) << 6 |
+                     ((B7 >> lane) & 1u) << 7);
+    }
+    return q;
+}
+
+__global__ void __launch_bounds__(256) k_oc_count(OV g, const unsigned *__restrict__ bits, uint4 *words, uint4 *counts) {
+    const unsigned nw = (g.NG + 31u) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += (gridDim.x * blockDim.x) >> 5) {
+        const OB q = oc_point(g, bits, w * 32u, lane);
+        int nt = q.cube ? ocube_ntri(q.ci) : 0;
+        const unsigned xm = __ballot_sync(0xffffffffu, q.ex), ym = __ballot_sync(0xffffffffu, q.ey),
+                       zm = __ballot_sync(0xffffffffu, q.ez);
+        for (int o = 16; o; o >>= 1) nt += __shfl_xor_sync(0xffffffffu, nt, o);
+        if (lane == 0) {
+            words[w] = make_uint4(xm, ym, zm, 0u);
+            counts[w] = make_uint4(__popc(xm) + __popc(ym) + __popc(zm), (unsigned)nt, 0u, 0u);
+        }
     }
 }
 
@@ -113,9 +148,9 @@ __device__ __forceinline__ double interp(double iso, double p1, double p2, doubl
     return __dadd_rn(p1, __dmul_rn(mu, __dsub_rn(p2, p1)));
 }
 
-__global__ void __launch_bounds__(256) k_oc_emit(OV g, const uint4 *__restrict__ words, const uint4 *__restrict__ offs,
-                                                 uint4 totals, vec3d *pts, vec3i *tris, int *cand, unsigned *ncand,
-                                                 int cap, long long *lastuse) {
+__global__ void __launch_bounds__(256) k_oc_emit(OV g, const unsigned *__restrict__ bits, const uint4 *__restrict__ words,
+                                                 const uint4 *__restrict__ offs, uint4 totals, vec3d *pts, vec3i *tris,
+                                                 int *cand, unsigned *ncand, int cap) {
     const unsigned p = blockIdx.x * 256u + threadIdx.x;
     const unsigned w = p >> 5, lane = threadIdx.x & 31u;
     const unsigned nwords = (g.NG + 31u) >> 5;
@@ -123,13 +158,19 @@ __global__ void __launch_bounds__(256) k_oc_emit(OV g, const uint4 *__restrict__
     const uint4 o = offs[w];
     const uint4 on = (w + 1 < nwords) ? offs[w + 1] : totals;
     const uint4 m = words[w];
-    if ((m.x | m.y | m.z) == 0u && on.y == o.y) return;
-    OP q;
-    oclassify(g, p, q);
+    if ((m.x | m.y | m.z) == 0u && on.y == o.y) return;   // warp-uniform
+    const OB b = oc_point(g, bits, w * 32u, (int)lane);
     const double iso = (double)g.iso;
-    if (q.ex | q.ey | q.ez) {
+    if (b.ex | b.ey | b.ez) {
         const unsigned lt = (1u << lane) - 1u;
         int id = (int)(o.x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt));
+        OP q;   // the values this point's edges interpolate
+        q.X = g.lo0 + b.x; q.Y = g.lo1 + b.y; q.Z = g.lo2 + b.z;
+        q.ex = b.ex; q.ey = b.ey; q.ez = b.ez;
+        q.v[0] = oval(g, q.X, q.Y, q.Z);
+        if (q.ex) q.v[1] = oval(g, q.X + 1, q.Y, q.Z);
+        if (q.ey) q.v[3] = oval(g, q.X, q.Y + 1, q.Z);
+        if (q.ez) q.v[4] = oval(g, q.X, q.Y, q.Z + 1);
         const double X = q.X, Y = q.Y, Z = q.Z;
         const double v0 = q.v[0];
         const int c0 = g.lo0, c1 = g.lo1, c2 = g.lo2, e0 = g.hi0 - 2, e1 = g.hi1 - 2, e2 = g.hi2 - 2;
@@ -163,11 +204,8 @@ __global__ void __launch_bounds__(256) k_oc_emit(OV g, const uint4 *__restrict__
             if (fabs(z - rint(z)) < 1.5e-5) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
         }
     }
-    int nt = 0, ci = 0;
-    if (q.cube) {
-        ci = ocube_index(q, g.iso);
-        nt = ocube_ntri(ci);
-    }
+    const int ci = b.ci;
+    const int nt = b.cube ? ocube_ntri(ci) : 0;
     int tb = nt;
     for (int d = 1; d < 32; d <<= 1) {
         const int a = __shfl_up_sync(0xffffffffu, tb, d);
@@ -195,8 +233,28 @@ __global__ void __launch_bounds__(256) k_oc_emit(OV g, const uint4 *__restrict__
         default: v = ovid(words, offs, p + NX, 2); break;
         }
         tv[t % 3] = v;
-        atomicMax(&lastuse[v], 3 * tri0 + t);
         if (t % 3 == 2) tris[tri0 + t / 3] = {tv[0], tv[1], tv[2]};
+    }
+}
+
+// weld candidates as a bitmap over the vertices
+__global__ void k_oc_candbits(const int *__restrict__ cand, unsigned ncand, unsigned *bits) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < ncand; i += gridDim.x * blockDim.x) {
+        const unsigned v = (unsigned)cand[i];
+        atomicOr(bits + (v >> 5), 1u << (v & 31u));
+    }
+}
+
+// last copy of every candidate vertex: the largest 3*triangle + corner that names it
+__global__ void k_oc_lastuse(const vec3i *__restrict__ tris, unsigned nt, const unsigned *__restrict__ bits,
+                             long long *lastuse) {
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+        const vec3i T = tris[t];
+        const int v[3] = {T.x, T.y, T.z};
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if ((__ldg(bits + ((unsigned)v[c] >> 5)) >> ((unsigned)v[c] & 31u)) & 1u)
+                atomicMax(&lastuse[v[c]], 3ll * t + c);
     }
 }
 
@@ -226,18 +284,30 @@ n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const i
     const size_t nwords = ((size_t)g.NG + 31) / 32;
     CKS(w.words.ensure(nwords * sizeof(uint4)));
     CKS(w.counts.ensure(nwords * sizeof(uint4)));
-    { k_oc_count<<<(unsigned)(((size_t)g.NG + 255) / 256), 256, 0, s>>>(g, w.words.as<uint4>(), w.counts.as<uint4>()); N2M_COUNT(); }
+    CKS(w.signs.ensure(nwords * sizeof(unsigned)));
+    const unsigned blocks = (unsigned)std::min<size_t>((nwords + 7) / 8, 152u * 16u);   // a warp per word
+    { k_oc_signs<<<blocks, 256, 0, s>>>(g, w.signs.as<unsigned>()); N2M_COUNT(); }
+    { k_oc_count<<<blocks, 256, 0, s>>>(g, w.signs.as<unsigned>(), w.words.as<uint4>(), w.counts.as<uint4>()); N2M_COUNT(); }
     CKL();
     return scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s);
 }
 
 n2m_status oc_emit(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
                     McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris, int *d_cand, unsigned *d_ncand,
-                    int cand_cap, long long *d_lastuse, cudaStream_t s) {
+                    int cand_cap, cudaStream_t s) {
     const OV g = make_ov(vol, dim, lo, hi, iso, edge_max);
-    { k_oc_emit<<<(unsigned)(((size_t)g.NG + 255) / 256), 256, 0, s>>>(g, w.words.as<uint4>(), w.counts.as<uint4>(),
+    { k_oc_emit<<<(unsigned)(((size_t)g.NG + 255) / 256), 256, 0, s>>>(g, w.signs.as<unsigned>(), w.words.as<uint4>(), w.counts.as<uint4>(),
                                                                      make_uint4(c.nv_edge, c.nt, 0, 0), d_pts, d_tris,
-                                                                     d_cand, d_ncand, cand_cap, d_lastuse); N2M_COUNT(); }
+                                                                     d_cand, d_ncand, cand_cap); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status oc_lastuse(const vec3i *d_tris, int nt, int nv, const int *d_cand, int ncand, unsigned *d_bits,
+                      long long *d_lastuse, cudaStream_t s) {
+    CK(cudaMemsetAsync(d_bits, 0, (size_t)(nv + 31) / 32 * sizeof(unsigned), s));
+    { k_oc_candbits<<<(unsigned)std::max(1, std::min((ncand + 255) / 256, 1024)), 256, 0, s>>>(d_cand, (unsigned)ncand, d_bits); N2M_COUNT(); }
+    { k_oc_lastuse<<<(unsigned)std::max(1, std::min((nt + 255) / 256, 152 * 16)), 256, 0, s>>>(d_tris, (unsigned)nt, d_bits, d_lastuse); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
