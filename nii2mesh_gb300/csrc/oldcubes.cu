@@ -13,6 +13,7 @@
 // the reference's pre-weld vertex list (3*triangle + corner) so that
 // near-corner clusters keep the same survivor.
 #include <algorithm>
+#include <atomic>
 
 #include "mc_tables.h"
 #include "n2m_internal.cuh"
@@ -27,7 +28,7 @@ struct OV {
     long long dxy;
     int lo0, lo1, lo2, hi0, hi1, hi2;   // cube range [lo, hi-2]
     int NX, NY, NZ;                     // grid points: hi - lo
-    unsigned NXY, NG;
+    unsigned NXY, NG, WX;   // WX: sign words per row
     float iso, edge_max;
 };
 
@@ -38,12 +39,6 @@ __device__ __forceinline__ float oval(const OV &g, int X, int Y, int Z) {
     return v;
 }
 
-struct OP {
-    bool ex, ey, ez;
-    int X, Y, Z;         // absolute point
-    float v[5];          // p0, p1 (+x), -, p3 (+y), p4 (+z) in Bourke's corner numbering
-};
-
 __device__ __forceinline__ int ocube_ntri(int ci) {
     if (!d_edge[ci]) return 0;
     int n = 0;
@@ -51,93 +46,122 @@ __device__ __forceinline__ int ocube_ntri(int ci) {
     return n;
 }
 
-// Signs of the grid: bit p & 31 of word p >> 5 is set when grid point p
-// (linear in the grid) is below the isolevel, darkened value included.  The
-// count and the emit read a cube's eight corners as bits of this bitmap.
-__global__ void __launch_bounds__(256) k_oc_signs(OV g, unsigned *bits) {
-    const unsigned nw = (g.NG + 31u) >> 5;
+// configuration of cube i of a word from its corner masks, in Bourke's corner
+// order (x,y,z) (x+1,y,z) (x+1,y+1,z) (x,y+1,z) and the same at z+1
+__device__ __forceinline__ int ocube_index(unsigned a0, unsigned a1, unsigned b0, unsigned b1, unsigned c0, unsigned c1,
+                                           unsigned d0, unsigned d1, int i) {
+    return (int)((a0 >> i) & 1u) | (int)((a1 >> i) & 1u) << 1 | (int)((b1 >> i) & 1u) << 2 | (int)((b0 >> i) & 1u) << 3 |
+           (int)((c0 >> i) & 1u) << 4 | (int)((c1 >> i) & 1u) << 5 | (int)((d1 >> i) & 1u) << 6 | (int)((d0 >> i) & 1u) << 7;
+}
+
+// ---- count pass ---------------------------------------------------------------
+// Sign words are row-aligned: bit x & 31 of signs[(z*NY + y)*WX + x/32] is set
+// when grid point (x, y, z) is below the isolevel, darkened value included
+// (points x >= NX read as 0).  Word order is raster order, so numbering by an
+// exclusive scan over words gives the raster order of the reference's cubes.
+constexpr int OS_W = 16;   // words of a row loaded at once per lane
+
+// A warp takes whole rows, OS_W words at a time with all their loads in flight.
+__global__ void __launch_bounds__(256) k_oc_signs(OV g, unsigned nrows, unsigned *signs) {
     const int lane = threadIdx.x & 31;
-    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += (gridDim.x * blockDim.x) >> 5) {
-        const unsigned p = w * 32u + (unsigned)lane;
-        bool b = false;
-        if (p < g.NG) {
-            const int z = (int)(p / g.NXY);
-            const unsigned r = p - (unsigned)z * g.NXY;
-            const int y = (int)(r / (unsigned)g.NX), x = (int)(r - (unsigned)y * (unsigned)g.NX);
-            b = oval(g, g.lo0 + x, g.lo1 + y, g.lo2 + z) < g.iso;
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, b);
-        if (lane == 0) bits[w] = m;
-    }
-}
-
-// 32 sign bits starting at grid point q (bits past the grid read as 0)
-__device__ __forceinline__ unsigned obits(const unsigned *__restrict__ bits, unsigned q, unsigned nw) {
-    const unsigned w = q >> 5, sh = q & 31u;
-    const unsigned lo = w < nw ? __ldg(bits + w) : 0u, hi = sh && w + 1 < nw ? __ldg(bits + w + 1) : 0u;
-    return __funnelshift_r(lo, hi, sh);
-}
-
-// a grid point's edges and cube from the sign bits; the warp's 32 consecutive
-// points p0 .. p0+31 share the eight shifted words
-struct OB {
-    bool in, ex, ey, ez, cube;
-    int x, y, z, ci;
-};
-__device__ __forceinline__ OB oc_point(const OV &g, const unsigned *__restrict__ bits, unsigned p0, int lane) {
-    const unsigned nw = (g.NG + 31u) >> 5, NX = (unsigned)g.NX, NXY = g.NXY;
-    const unsigned B0 = obits(bits, p0, nw), B1 = obits(bits, p0 + 1, nw), B3 = obits(bits, p0 + NX, nw),
-                   B2 = obits(bits, p0 + NX + 1, nw), B4 = obits(bits, p0 + NXY, nw), B5 = obits(bits, p0 + NXY + 1, nw),
-                   B7 = obits(bits, p0 + NXY + NX, nw), B6 = obits(bits, p0 + NXY + NX + 1, nw);
-    OB q;
-    const unsigned p = p0 + (unsigned)lane;
-    q.in = p < g.NG;
-    q.ex = q.ey = q.ez = q.cube = false;
-    q.ci = 0;
-    q.x = q.y = q.z = 0;
-    if (!q.in) return q;
-    q.z = (int)(p / NXY);
-    const unsigned r = p - (unsigned)q.z * NXY;
-    q.y = (int)(r / NX);
-    q.x = (int)(r - (unsigned)q.y * NX);
-    const bool hx = q.x < g.NX - 1, hy = q.y < g.NY - 1, hz = q.z < g.NZ - 1;
-    const unsigned b0 = (B0 >> lane) & 1u;
-    q.ex = hx && ((B1 >> lane) & 1u) != b0;
-    q.ey = hy && ((B3 >> lane) & 1u) != b0;
-    q.ez = hz && ((B4 >> lane) & 1u) != b0;
-    if (hx && hy && hz) {   // Bourke's corner order p0 .. p7
-        q.cube = true;
-        q.ci = (int)(b0 | ((B1 >> lane) & 1u) << 1 | ((B2 >> lane) & 1u) << 2 | ((B3 >> lane) & 1u) << 3 |
-                     ((B4 >> lane) & 1u) << 4 | ((B5 >> lane) & 1u) << 5 | ((B6 >> lane) & 1u) << 6 |
-                     ((B7 >> lane) & 1u) << 7);
-    }
-    return q;
-}
-
-__global__ void __launch_bounds__(256) k_oc_count(OV g, const unsigned *__restrict__ bits, uint4 *words, uint4 *counts) {
-    const unsigned nw = (g.NG + 31u) >> 5;
-    const int lane = threadIdx.x & 31;
-    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += (gridDim.x * blockDim.x) >> 5) {
-        const OB q = oc_point(g, bits, w * 32u, lane);
-        int nt = q.cube ? ocube_ntri(q.ci) : 0;
-        const unsigned xm = __ballot_sync(0xffffffffu, q.ex), ym = __ballot_sync(0xffffffffu, q.ey),
-                       zm = __ballot_sync(0xffffffffu, q.ez);
-        for (int o = 16; o; o >>= 1) nt += __shfl_xor_sync(0xffffffffu, nt, o);
-        if (lane == 0) {
-            words[w] = make_uint4(xm, ym, zm, 0u);
-            counts[w] = make_uint4(__popc(xm) + __popc(ym) + __popc(zm), (unsigned)nt, 0u, 0u);
+    const unsigned WX = g.WX;
+    for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += (gridDim.x * blockDim.x) >> 5) {
+        const int y = (int)(row % (unsigned)g.NY), z = (int)(row / (unsigned)g.NY);
+        const int vy = g.lo1 + y, vz = g.lo2 + z;
+        const bool rface = vy == 0 || vz == 0 || vy == g.dy - 1 || vz == g.dz - 1;
+        const float *rp = g.vol + (long long)vz * g.dxy + (long long)vy * g.dx + g.lo0;
+        unsigned *out = signs + (size_t)row * WX;
+        for (unsigned xw0 = 0; xw0 < WX; xw0 += OS_W) {
+            float raw[OS_W];
+#pragma unroll
+            for (int k = 0; k < OS_W; k++) {
+                const int x = (int)(xw0 + k) * 32 + lane;
+                raw[k] = xw0 + k < WX && x < g.NX ? __ldg(rp + x) : 0.f;
+            }
+            unsigned mine = 0;
+#pragma unroll
+            for (int k = 0; k < OS_W; k++) {
+                const int x = (int)(xw0 + k) * 32 + lane, vx = g.lo0 + x;
+                const float v = rface || vx == 0 || vx == g.dx - 1 ? fminf(g.edge_max, raw[k]) : raw[k];
+                const unsigned m = __ballot_sync(0xffffffffu, x < g.NX && v < g.iso);
+                if (lane == k) mine = m;
+            }
+            if (lane < OS_W && xw0 + lane < WX) out[xw0 + lane] = mine;
         }
     }
 }
 
-__device__ __forceinline__ int ovid(const uint4 *__restrict__ words, const uint4 *__restrict__ offs, unsigned q,
-                                    int axis) {
-    const unsigned w = q >> 5, l = q & 31u;
+// One thread per word, 32 grid points at a time as bit masks: corner k of the
+// word's 32 cubes is a mask of sign bits (the +x corners are the row shifted
+// down by one with bit 0 of the next word on top), edge crossings are XORs, and
+// only cubes whose corners are not all equal take a table lookup.
+// counts: {edge vertices, triangles, 0, active}.
+__global__ void __launch_bounds__(256) k_oc_words(OV g, unsigned nwords, const unsigned *__restrict__ signs,
+                                                  uint4 *words, uint4 *counts) {
+    __shared__ unsigned char ntri[256];
+    ntri[threadIdx.x] = (unsigned char)ocube_ntri(threadIdx.x);
+    __syncthreads();
+    const unsigned WX = g.WX, slice = WX * (unsigned)g.NY;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const unsigned row = w / WX, xw = w - row * WX;
+        const int z = (int)(row / (unsigned)g.NY), y = (int)(row - (unsigned)z * (unsigned)g.NY);
+        const int x0 = (int)xw * 32;
+        const bool hy = y < g.NY - 1, hz = z < g.NZ - 1, nx = xw + 1 < WX;
+        const unsigned inm = x0 + 32 <= g.NX ? 0xffffffffu : (1u << (g.NX - x0)) - 1u;   // x < NX
+        const unsigned hxm = x0 + 33 <= g.NX ? 0xffffffffu : (g.NX - 1 - x0 > 0 ? (1u << (g.NX - 1 - x0)) - 1u : 0u);
+        // a = (y, z), b = (y+1, z), c = (y, z+1), d = (y+1, z+1); "1" = the +x neighbours
+        const unsigned a0 = __ldg(signs + w), a1 = __funnelshift_r(a0, nx ? __ldg(signs + w + 1) : 0u, 1);
+        unsigned b0 = 0, b1 = 0, c0 = 0, c1 = 0, d0 = 0, d1 = 0;
+        if (hy) {
+            b0 = __ldg(signs + w + WX);
+            b1 = __funnelshift_r(b0, nx ? __ldg(signs + w + WX + 1) : 0u, 1);
+        }
+        if (hz) {
+            c0 = __ldg(signs + w + slice);
+            c1 = __funnelshift_r(c0, nx ? __ldg(signs + w + slice + 1) : 0u, 1);
+        }
+        if (hy && hz) {
+            d0 = __ldg(signs + w + slice + WX);
+            d1 = __funnelshift_r(d0, nx ? __ldg(signs + w + slice + WX + 1) : 0u, 1);
+        }
+        const unsigned xm = (a0 ^ a1) & hxm, ym = hy ? (a0 ^ b0) & inm : 0u, zm = hz ? (a0 ^ c0) & inm : 0u;
+        unsigned nt = 0;
+        if (hy && hz) {
+            unsigned mix = (a0 | a1 | b0 | b1 | c0 | c1 | d0 | d1) & ~(a0 & a1 & b0 & b1 & c0 & c1 & d0 & d1) & hxm;
+            while (mix) {
+                const int i = __ffs(mix) - 1;
+                mix &= mix - 1;
+                nt += ntri[ocube_index(a0, a1, b0, b1, c0, c1, d0, d1, i)];
+            }
+        }
+        const unsigned nv = __popc(xm) + __popc(ym) + __popc(zm);
+        words[w] = make_uint4(xm, ym, zm, 0u);
+        counts[w] = make_uint4(nv, nt, 0u, (nv | nt) ? 1u : 0u);
+    }
+}
+
+// active word list from the scanned counts (counts.w: exclusive count of active
+// words before w), in word order
+__global__ void k_oc_active(const uint4 *__restrict__ offs, const uint4 *__restrict__ total, unsigned nwords,
+                            unsigned *active) {
+    const unsigned tot = total->w;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const unsigned a = offs[w].w, b = w + 1 < nwords ? offs[w + 1].w : tot;
+        if (b != a) active[a] = w;
+    }
+}
+
+// ---- emit pass -------------------------------------------------------------------
+// id of the edge vertex owned by grid point (x, y, z) along axis ax: the word's
+// offset plus the crossings of the points before it, x then y then z at a point
+__device__ __forceinline__ int oc_vid(const uint4 *__restrict__ words, const uint4 *__restrict__ offs, unsigned WX,
+                                      unsigned NY, int x, int y, int z, int ax) {
+    const unsigned w = ((unsigned)z * NY + (unsigned)y) * WX + ((unsigned)x >> 5), l = (unsigned)x & 31u;
     const uint4 m = words[w];
     const unsigned lt = (1u << l) - 1u;
     unsigned id = offs[w].x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt);
-    if (axis >= 1) id += (m.x >> l) & 1u;
-    if (axis == 2) id += (m.y >> l) & 1u;
+    if (ax >= 1) id += (m.x >> l) & 1u;
+    if (ax == 2) id += (m.y >> l) & 1u;
     return (int)id;
 }
 
@@ -148,92 +172,159 @@ __device__ __forceinline__ double interp(double iso, double p1, double p2, doubl
     return __dadd_rn(p1, __dmul_rn(mu, __dsub_rn(p2, p1)));
 }
 
-__global__ void __launch_bounds__(256) k_oc_emit(OV g, const unsigned *__restrict__ bits, const uint4 *__restrict__ words,
-                                                 const uint4 *__restrict__ offs, uint4 totals, vec3d *pts, vec3i *tris,
-                                                 int *cand, unsigned *ncand, int cap) {
-    const unsigned p = blockIdx.x * 256u + threadIdx.x;
-    const unsigned w = p >> 5, lane = threadIdx.x & 31u;
-    const unsigned nwords = (g.NG + 31u) >> 5;
-    if (w >= nwords) return;
-    const uint4 o = offs[w];
-    const uint4 on = (w + 1 < nwords) ? offs[w + 1] : totals;
-    const uint4 m = words[w];
-    if ((m.x | m.y | m.z) == 0u && on.y == o.y) return;   // warp-uniform
-    const OB b = oc_point(g, bits, w * 32u, (int)lane);
-    const double iso = (double)g.iso;
-    if (b.ex | b.ey | b.ez) {
-        const unsigned lt = (1u << lane) - 1u;
-        int id = (int)(o.x + __popc(m.x & lt) + __popc(m.y & lt) + __popc(m.z & lt));
-        OP q;   // the values this point's edges interpolate
-        q.X = g.lo0 + b.x; q.Y = g.lo1 + b.y; q.Z = g.lo2 + b.z;
-        q.ex = b.ex; q.ey = b.ey; q.ez = b.ez;
-        q.v[0] = oval(g, q.X, q.Y, q.Z);
-        if (q.ex) q.v[1] = oval(g, q.X + 1, q.Y, q.Z);
-        if (q.ey) q.v[3] = oval(g, q.X, q.Y + 1, q.Z);
-        if (q.ez) q.v[4] = oval(g, q.X, q.Y, q.Z + 1);
-        const double X = q.X, Y = q.Y, Z = q.Z;
-        const double v0 = q.v[0];
-        const int c0 = g.lo0, c1 = g.lo1, c2 = g.lo2, e0 = g.hi0 - 2, e1 = g.hi1 - 2, e2 = g.hi2 - 2;
-        if (q.ex) {  // last user: (X,Y,Z) fwd > (X,Y-1,Z) rev > (X,Y,Z-1) fwd > (X,Y-1,Z-1) rev
-            const double v1 = q.v[1];
-            bool fwd;
-            if (q.Y <= e1 && q.Z <= e2) fwd = true;
-            else if (q.Y - 1 >= c1 && q.Z <= e2) fwd = false;
-            else if (q.Y <= e1 && q.Z - 1 >= c2) fwd = true;
-            else fwd = false;
-            const double x = fwd ? interp(iso, X, X + 1.0, v0, v1) : interp(iso, X + 1.0, X, v1, v0);
-            pts[id] = {x, Y, Z};
-            if (fabs(x - rint(x)) < 1.5e-5) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
-            id++;
-        }
-        if (q.ey) {  // (X,Y,Z) rev > (X-1,Y,Z) fwd > (X,Y,Z-1) rev > (X-1,Y,Z-1) fwd
-            const double v3 = q.v[3];
-            bool fwd;
-            if (q.X <= e0 && q.Z <= e2) fwd = false;
-            else if (q.X - 1 >= c0 && q.Z <= e2) fwd = true;
-            else if (q.X <= e0 && q.Z - 1 >= c2) fwd = false;
-            else fwd = true;
-            const double y = fwd ? interp(iso, Y, Y + 1.0, v0, v3) : interp(iso, Y + 1.0, Y, v3, v0);
-            pts[id] = {X, y, Z};
-            if (fabs(y - rint(y)) < 1.5e-5) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
-            id++;
-        }
-        if (q.ez) {  // every user lists the z edge bottom to top
-            const double z = interp(iso, Z, Z + 1.0, v0, (double)q.v[4]);
-            pts[id] = {X, Y, z};
-            if (fabs(z - rint(z)) < 1.5e-5) { unsigned k = atomicAdd(ncand, 1u); if (k < (unsigned)cap) cand[k] = id; }
-        }
+// The edge vertex of grid point (x, y, z) along axis ax, interpolated as the
+// last cube (raster order) that lists the edge orients it; a position within
+// 1.5e-5 of a grid coordinate makes the vertex a weld candidate.
+__device__ __forceinline__ void oc_vertex(const OV &g, int x, int y, int z, int ax, int id, vec3d *pts, int *cand,
+                                          unsigned *ncand, int cap) {
+    const int X = g.lo0 + x, Y = g.lo1 + y, Z = g.lo2 + z;
+    const double iso = (double)g.iso, dX = X, dY = Y, dZ = Z;
+    const double v0 = oval(g, X, Y, Z);
+    const int c0 = g.lo0, c1 = g.lo1, c2 = g.lo2, e0 = g.hi0 - 2, e1 = g.hi1 - 2, e2 = g.hi2 - 2;
+    double r;
+    vec3d P;
+    if (ax == 0) {   // last user: (X,Y,Z) fwd > (X,Y-1,Z) rev > (X,Y,Z-1) fwd > (X,Y-1,Z-1) rev
+        const double v1 = oval(g, X + 1, Y, Z);
+        bool fwd;
+        if (Y <= e1 && Z <= e2) fwd = true;
+        else if (Y - 1 >= c1 && Z <= e2) fwd = false;
+        else if (Y <= e1 && Z - 1 >= c2) fwd = true;
+        else fwd = false;
+        r = fwd ? interp(iso, dX, dX + 1.0, v0, v1) : interp(iso, dX + 1.0, dX, v1, v0);
+        P = {r, dY, dZ};
+    } else if (ax == 1) {   // (X,Y,Z) rev > (X-1,Y,Z) fwd > (X,Y,Z-1) rev > (X-1,Y,Z-1) fwd
+        const double v3 = oval(g, X, Y + 1, Z);
+        bool fwd;
+        if (X <= e0 && Z <= e2) fwd = false;
+        else if (X - 1 >= c0 && Z <= e2) fwd = true;
+        else if (X <= e0 && Z - 1 >= c2) fwd = false;
+        else fwd = true;
+        r = fwd ? interp(iso, dY, dY + 1.0, v0, v3) : interp(iso, dY + 1.0, dY, v3, v0);
+        P = {dX, r, dZ};
+    } else {   // every user lists the z edge bottom to top
+        r = interp(iso, dZ, dZ + 1.0, v0, (double)oval(g, X, Y, Z + 1));
+        P = {dX, dY, r};
     }
-    const int ci = b.ci;
-    const int nt = b.cube ? ocube_ntri(ci) : 0;
-    int tb = nt;
-    for (int d = 1; d < 32; d <<= 1) {
-        const int a = __shfl_up_sync(0xffffffffu, tb, d);
-        if ((int)lane >= d) tb += a;
+    pts[id] = P;
+    if (fabs(r - rint(r)) < 1.5e-5) {
+        const unsigned k = atomicAdd(ncand, 1u);
+        if (k < (unsigned)cap) cand[k] = id;
     }
-    tb -= nt;
-    if (nt == 0) return;
-    const unsigned NX = (unsigned)g.NX, NXY = g.NXY;
-    const long long tri0 = (long long)o.y + tb;
+}
+
+// Bourke edge 0..11 -> owning grid point offset (bit 0: +x, 1: +y, 2: +z) and axis (bits 3-4)
+__device__ __forceinline__ unsigned oc_edge(int e) {
+    constexpr unsigned long long k = (0x00ull << 0) | (0x09ull << 5) | (0x02ull << 10) | (0x08ull << 15) | (0x04ull << 20) |
+                                     (0x0dull << 25) | (0x06ull << 30) | (0x0cull << 35) | (0x10ull << 40) |
+                                     (0x11ull << 45) | (0x13ull << 50) | (0x12ull << 55);
+    return (unsigned)(k >> (5 * e)) & 31u;
+}
+
+// triangle j of configuration ci of the cube at grid point (x, y, z)
+__device__ __forceinline__ void oc_triangle(const uint4 *__restrict__ words, const uint4 *__restrict__ offs, unsigned WX,
+                                            unsigned NY, int x, int y, int z, int ci, int j, vec3i *dst) {
     int tv[3];
-    for (int t = 0; t < 3 * nt; t++) {
-        int v;
-        switch (d_tri[ci * 16 + t]) {   // Bourke edge -> owning grid point and axis
-        case 0: v = ovid(words, offs, p, 0); break;
-        case 1: v = ovid(words, offs, p + 1, 1); break;
-        case 2: v = ovid(words, offs, p + NX, 0); break;
-        case 3: v = ovid(words, offs, p, 1); break;
-        case 4: v = ovid(words, offs, p + NXY, 0); break;
-        case 5: v = ovid(words, offs, p + NXY + 1, 1); break;
-        case 6: v = ovid(words, offs, p + NXY + NX, 0); break;
-        case 7: v = ovid(words, offs, p + NXY, 1); break;
-        case 8: v = ovid(words, offs, p, 2); break;
-        case 9: v = ovid(words, offs, p + 1, 2); break;
-        case 10: v = ovid(words, offs, p + NX + 1, 2); break;
-        default: v = ovid(words, offs, p + NX, 2); break;
+#pragma unroll
+    for (int t = 0; t < 3; t++) {
+        const unsigned ec = oc_edge(d_tri[ci * 16 + 3 * j + t]);
+        tv[t] = oc_vid(words, offs, WX, NY, x + (int)(ec & 1u), y + (int)((ec >> 1) & 1u), z + (int)((ec >> 2) & 1u),
+                       (int)(ec >> 3));
+    }
+    *dst = {tv[0], tv[1], tv[2]};
+}
+
+// A warp takes 32 active words at a time (one per lane), lists their edge
+// vertices and triangles in shared memory (ids and positions are consecutive
+// within the group) and then emits the lists with all lanes busy.  Items past
+// a list's capacity are emitted by the lane that found them.
+constexpr int OE_WARPS = 4, OE_VCAP = 1024, OE_TCAP = 1024;
+
+__global__ void __launch_bounds__(OE_WARPS * 32) k_oc_emit(OV g, const unsigned *__restrict__ signs,
+                                                          const uint4 *__restrict__ words, const uint4 *__restrict__ offs,
+                                                          const unsigned *__restrict__ active, unsigned nactive,
+                                                          vec3d *pts, vec3i *tris, int *cand, unsigned *ncand, int cap,
+                                                          unsigned *next_group) {
+    __shared__ unsigned short vitem[OE_WARPS][OE_VCAP];   // lane << 7 | point << 2 | axis
+    __shared__ unsigned titem[OE_WARPS][OE_TCAP];          // lane << 27 | point << 22 | configuration << 3 | triangle
+    __shared__ unsigned char ntri[256];
+    for (int i = threadIdx.x; i < 256; i += OE_WARPS * 32) ntri[i] = (unsigned char)ocube_ntri(i);
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const unsigned WX = g.WX, NY = (unsigned)g.NY, slice = WX * NY;
+    const unsigned ngroups = (nactive + 31) / 32;
+    for (;;) {   // groups are handed out one at a time: their work varies a lot
+        unsigned grp = 0;
+        if (lane == 0) grp = atomicAdd(next_group, 1u);
+        grp = __shfl_sync(0xffffffffu, grp, 0);
+        if (grp >= ngroups) break;
+        const unsigned aw = grp * 32 + lane;
+        const bool live = aw < nactive;
+        const unsigned w = live ? active[aw] : active[nactive - 1];
+        const unsigned row = w / WX, xw = w - row * WX;
+        const int z = (int)(row / NY), y = (int)(row - (unsigned)z * NY), x0 = (int)(xw * 32u);
+        const uint4 o = offs[w];
+        const uint4 m = live ? words[w] : make_uint4(0u, 0u, 0u, 0u);
+        const unsigned vbase = __shfl_sync(0xffffffffu, o.x, 0), tbase = __shfl_sync(0xffffffffu, o.y, 0);
+        unsigned kv = o.x - vbase;   // the word's edge vertices
+        for (unsigned pm = m.x | m.y | m.z; pm; pm &= pm - 1) {
+            const int p = __ffs(pm) - 1;
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) {
+                const unsigned mk = ax == 0 ? m.x : (ax == 1 ? m.y : m.z);
+                if (!((mk >> p) & 1u)) continue;
+                if (kv < (unsigned)OE_VCAP) vitem[wid][kv] = (unsigned short)(lane << 7 | (unsigned)p << 2 | (unsigned)ax);
+                else oc_vertex(g, x0 + p, y, z, ax, (int)(vbase + kv), pts, cand, ncand, cap);
+                kv++;
+            }
         }
-        tv[t % 3] = v;
-        if (t % 3 == 2) tris[tri0 + t / 3] = {tv[0], tv[1], tv[2]};
+        unsigned kt = o.y - tbase;   // the word's triangles
+        if (live && y < g.NY - 1 && z < g.NZ - 1) {
+            const bool nx = xw + 1 < WX;
+            const unsigned a0 = __ldg(signs + w), b0 = __ldg(signs + w + WX), c0 = __ldg(signs + w + slice),
+                           d0 = __ldg(signs + w + slice + WX);
+            unsigned an = 0, bn = 0, cn = 0, dn = 0;
+            if (nx) {
+                an = __ldg(signs + w + 1); bn = __ldg(signs + w + WX + 1);
+                cn = __ldg(signs + w + slice + 1); dn = __ldg(signs + w + slice + WX + 1);
+            }
+            const unsigned a1 = __funnelshift_r(a0, an, 1), b1 = __funnelshift_r(b0, bn, 1),
+                           c1 = __funnelshift_r(c0, cn, 1), d1 = __funnelshift_r(d0, dn, 1);
+            const unsigned hxm = x0 + 33 <= g.NX ? 0xffffffffu : (g.NX - 1 - x0 > 0 ? (1u << (g.NX - 1 - x0)) - 1u : 0u);
+            for (unsigned mix = (a0 | a1 | b0 | b1 | c0 | c1 | d0 | d1) & ~(a0 & a1 & b0 & b1 & c0 & c1 & d0 & d1) & hxm; mix;
+                 mix &= mix - 1) {
+                const int p = __ffs(mix) - 1;
+                const int ci = ocube_index(a0, a1, b0, b1, c0, c1, d0, d1, p), n = ntri[ci];
+                for (int j = 0; j < n; j++, kt++) {
+                    if (kt < (unsigned)OE_TCAP) titem[wid][kt] = lane << 27 | (unsigned)p << 22 | (unsigned)ci << 3 | (unsigned)j;
+                    else oc_triangle(words, offs, WX, NY, x0 + p, y, z, ci, j, tris + tbase + kt);
+                }
+            }
+        }
+        // lanes past the last live one repeat its word with no items: the
+        // largest end is the group's end
+        const unsigned nvg = min((unsigned)OE_VCAP, __reduce_max_sync(0xffffffffu, kv));
+        const unsigned ntg = min((unsigned)OE_TCAP, __reduce_max_sync(0xffffffffu, kt));
+        __syncwarp();
+        for (unsigned b = 0; b < nvg; b += 32) {
+            const unsigned k = b + lane;
+            const unsigned e = k < nvg ? vitem[wid][k] : 0u;
+            const int l = (int)(e >> 7);
+            const int sx0 = __shfl_sync(0xffffffffu, x0, l), sy = __shfl_sync(0xffffffffu, y, l),
+                      sz = __shfl_sync(0xffffffffu, z, l);
+            if (k < nvg)
+                oc_vertex(g, sx0 + (int)((e >> 2) & 31u), sy, sz, (int)(e & 3u), (int)(vbase + k), pts, cand, ncand, cap);
+        }
+        for (unsigned b = 0; b < ntg; b += 32) {
+            const unsigned k = b + lane;
+            const unsigned e = k < ntg ? titem[wid][k] : 0u;
+            const int l = (int)(e >> 27);
+            const int sx0 = __shfl_sync(0xffffffffu, x0, l), sy = __shfl_sync(0xffffffffu, y, l),
+                      sz = __shfl_sync(0xffffffffu, z, l);
+            if (k < ntg)
+                oc_triangle(words, offs, WX, NY, sx0 + (int)((e >> 22) & 31u), sy, sz, (int)((e >> 3) & 0xffu),
+                            (int)(e & 7u), tris + tbase + k);
+        }
+        __syncwarp();   // the lists are reused by the next group
     }
 }
 
@@ -268,6 +359,7 @@ OV make_ov(const float *vol, const int dim[3], const int lo[3], const int hi[3],
     g.NX = hi[0] - lo[0]; g.NY = hi[1] - lo[1]; g.NZ = hi[2] - lo[2];
     g.NXY = (unsigned)g.NX * (unsigned)g.NY;
     g.NG = g.NXY * (unsigned)g.NZ;
+    g.WX = (unsigned)(g.NX + 31) / 32;
     g.iso = iso;
     g.edge_max = edge_max;
     return g;
@@ -281,24 +373,49 @@ n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const i
         CK(cudaMemsetAsync(d_total, 0, sizeof(uint4), s));
         return N2M_OK;
     }
-    const size_t nwords = ((size_t)g.NG + 31) / 32;
+    const size_t nwords = (size_t)g.WX * g.NY * g.NZ;
+    if (nwords >= 0xffffffffULL) {
+        n2m_set_error("grid too large");
+        return N2M_ERR_TOO_LARGE;
+    }
     CKS(w.words.ensure(nwords * sizeof(uint4)));
     CKS(w.counts.ensure(nwords * sizeof(uint4)));
     CKS(w.signs.ensure(nwords * sizeof(unsigned)));
-    const unsigned blocks = (unsigned)std::min<size_t>((nwords + 7) / 8, 152u * 16u);   // a warp per word
-    { k_oc_signs<<<blocks, 256, 0, s>>>(g, w.signs.as<unsigned>()); N2M_COUNT(); }
-    { k_oc_count<<<blocks, 256, 0, s>>>(g, w.signs.as<unsigned>(), w.words.as<uint4>(), w.counts.as<uint4>()); N2M_COUNT(); }
+    CKS(w.cand.ensure((nwords + 1) * sizeof(unsigned)));
+    const unsigned nrows = (unsigned)g.NY * (unsigned)g.NZ;
+    const unsigned wblocks = (unsigned)std::min<size_t>((nwords + 255) / 256, 152u * 16u);
+    { k_oc_signs<<<std::min<unsigned>((nrows + 7) / 8, 152u * 16u), 256, 0, s>>>(g, nrows, w.signs.as<unsigned>()); N2M_COUNT(); }
+    { k_oc_words<<<wblocks, 256, 0, s>>>(g, (unsigned)nwords, w.signs.as<unsigned>(), w.words.as<uint4>(), w.counts.as<uint4>()); N2M_COUNT(); }
     CKL();
-    return scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s);
+    CKS(scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s));
+    { k_oc_active<<<wblocks, 256, 0, s>>>(w.counts.as<uint4>(), d_total, (unsigned)nwords, w.cand.as<unsigned>()); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
 }
 
 n2m_status oc_emit(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
                     McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris, int *d_cand, unsigned *d_ncand,
                     int cand_cap, cudaStream_t s) {
     const OV g = make_ov(vol, dim, lo, hi, iso, edge_max);
-    { k_oc_emit<<<(unsigned)(((size_t)g.NG + 255) / 256), 256, 0, s>>>(g, w.signs.as<unsigned>(), w.words.as<uint4>(), w.counts.as<uint4>(),
-                                                                     make_uint4(c.nv_edge, c.nt, 0, 0), d_pts, d_tris,
-                                                                     d_cand, d_ncand, cand_cap); N2M_COUNT(); }
+    const unsigned nact = c.nactive;
+    if (nact == 0) return N2M_OK;
+    // CTAs of k_oc_emit that fit the GPU at once, per device ordinal (groups come
+    // from an atomic counter, so any grid is correct)
+    static std::atomic<int> resident_of[64];
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    int resident = dev < 64 ? resident_of[dev].load(std::memory_order_relaxed) : 0;
+    if (!resident) {
+        int sms = 0, per_sm = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_oc_emit, OE_WARPS * 32, 0));
+        resident = sms * std::max(per_sm, 1);
+        if (dev < 64) resident_of[dev].store(resident, std::memory_order_relaxed);
+    }
+    const unsigned gblocks = std::min<unsigned>(((nact + 31) / 32 + OE_WARPS - 1) / OE_WARPS, (unsigned)resident);
+    CKS(w.ctr.ensure(sizeof(unsigned)));
+    CK(cudaMemsetAsync(w.ctr.p, 0, sizeof(unsigned), s));
+    { k_oc_emit<<<gblocks, OE_WARPS * 32, 0, s>>>(g, w.signs.as<unsigned>(), w.words.as<uint4>(), w.counts.as<uint4>(), w.cand.as<unsigned>(), nact, d_pts, d_tris, d_cand, d_ncand, cand_cap, w.ctr.as<unsigned>()); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
