@@ -488,12 +488,12 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     }
     if (!smooth && label) CK(cudaMemcpyAsync(vol, d_src, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaEventRecord(c->evs[0], c->stream));
-    // Lewiner cubes straight after the pre-smooth (no clustering), volume already in
+    // Marching cubes straight after the pre-smooth (no clustering), volume already in
     // device memory: exact rounding on demand (only where marching cubes reads values).
     // Otherwise the exact three passes; a volume arriving from host memory in slabs is
     // smoothed while it arrives that way (the on-demand repair could only start after
     // the last slab)
-    bool od = smooth && !label && o.cubes != N2M_CUBES_OLDCUBES && !c->stage.host && od_eligible(d_src, nx, ny, nz);
+    bool od = smooth && !label && !c->stage.host && od_eligible(d_src, nx, ny, nz);
     if (smooth) {
         CKS(c->stmp.ensure(n * sizeof(float)));
         const StagedInput *stage = c->stage.host ? &c->stage : nullptr;
@@ -503,7 +503,7 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
             CKS(od_approx(d_src, vol, nx, ny, nz, iso, c->od, c->stream, stage));
             CK(cudaEventRecord(c->eva[1], c->stream));
             c->pass_a = true;
-            CKS(od_resolve(d_src, vol, nx, ny, nz, iso, c->od, dst, c->stream, &fallback));
+            CKS(od_resolve(d_src, vol, nx, ny, nz, iso, c->od, dst, c->stream, &fallback, o.cubes == N2M_CUBES_OLDCUBES));
             if (fallback) {   // the input is on the device by now
                 od = false;
                 CK(cudaMemcpyAsync(dst, h, sizeof(VolStats), cudaMemcpyHostToDevice, c->stream));
@@ -600,14 +600,15 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
     }
     CKS(c->totals.ensure(sizeof(uint4)));
     uint4 *dtot = c->totals.as<uint4>();
-    if (old) CKS(oc_count(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->scan, dtot, c->stream));
-    else if (P.od) {
+    if (P.od) {
         const size_t n = (size_t)dim[0] * dim[1] * dim[2];
         CKS(c->stmp2.ensure(n * sizeof(float)));
         const OdRepair rep{P.src, c->stmp.as<float>(), c->stmp2.as<float>(), (float *)P.vol, {dim[0], dim[1], dim[2]},
                            &c->od, &c->scan};
-        CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream, &rep));
-    } else CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream));
+        if (old) CKS(oc_count(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->scan, dtot, c->stream, &rep));
+        else CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream, &rep));
+    } else if (old) CKS(oc_count(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->scan, dtot, c->stream));
+    else CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream));
     CK(cudaEventRecord(c->evs[3], c->stream));
     uint4 tot;
     CKS(readback(c, &tot, dtot));

@@ -238,16 +238,6 @@ __global__ void __launch_bounds__(256) k_words(GV g, bool classic, unsigned WX, 
 // cubes reads), as bits of a linear bitmap over the volume.  A grid point's
 // voxel is gval's linear index j (row wrap included); j past the volume is the
 // padding value, which needs no voxel.
-__device__ __forceinline__ void need_mark(unsigned *need, long long j, unsigned bits, long long nvox) {
-    if (j >= nvox || !bits) return;
-    if (nvox - j < 32) bits &= (1u << (unsigned)(nvox - j)) - 1u;
-    const long long w = j >> 5;
-    const int sh = (int)(j & 31);
-    const unsigned p0 = bits << sh, p1 = sh ? bits >> (32 - sh) : 0u;
-    if (p0) atomicOr(need + w, p0);
-    if (p1) atomicOr(need + w + 1, p1);
-}
-
 __global__ void __launch_bounds__(256) k_need(GV g, unsigned WX, unsigned nwords, const unsigned *__restrict__ signs,
                                               unsigned *need) {
     const unsigned rowstride = WX, slicestride = WX * (unsigned)g.NY;
@@ -272,8 +262,8 @@ __global__ void __launch_bounds__(256) k_need(GV g, unsigned WX, unsigned nwords
         for (int r = 0; r < 4; r++) {
             const long long j = (long long)(g.lo0 + x0) + (long long)(y + (r & 1) + g.lo1) * g.dx +
                                 (long long)(z + (r >> 1) + g.lo2) * g.dxy;
-            need_mark(need, j, cm, g.nvox);
-            if (carry) need_mark(need, j + 32, 1u, g.nvox);
+            od_need_mark(need, j, cm, g.nvox);
+            if (carry) od_need_mark(need, j + 32, 1u, g.nvox);
         }
     }
 }

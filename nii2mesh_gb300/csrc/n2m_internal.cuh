@@ -118,8 +118,9 @@ struct OdLists {
 struct OdWork {
     DevBuf st, unc, cmin, cmax, need_z, need_y, need_x, off, list, lcnt;
     // bit x & 31 of word od_vsign_word(x, y, z): the smoothed value of voxel (x, y, z)
-    // minus iso is above -FLT_EPSILON (marching cubes' sign before edge darkening),
-    // exact for every voxel once od_resolve has run
+    // minus iso is above -FLT_EPSILON (Lewiner's sign before edge darkening), or with
+    // od_resolve's at_or_above, the value is >= iso (the complement of oldcubes'
+    // sign); exact for every voxel once od_resolve has run
     DevBuf vsign;
     unsigned cap = 0;
 };
@@ -137,12 +138,22 @@ struct OdRepair {
 __host__ __device__ __forceinline__ size_t od_vsign_word(unsigned x, unsigned y, unsigned z, unsigned wv, unsigned nys) {
     return (((size_t)z * nys + (y >> 3)) * wv + (x >> 5)) * 8u + (y & 7u);
 }
+// marks the voxels j .. j+31 whose bits are set in a linear bitmap over nvox voxels
+__device__ __forceinline__ void od_need_mark(unsigned *need, long long j, unsigned bits, long long nvox) {
+    if (j >= nvox || !bits) return;
+    if (nvox - j < 32) bits &= (1u << (unsigned)(nvox - j)) - 1u;
+    const long long w = j >> 5;
+    const int sh = (int)(j & 31);
+    const unsigned p0 = bits << sh, p1 = sh ? bits >> (32 - sh) : 0u;
+    if (p0) atomicOr(need + w, p0);
+    if (p1) atomicOr(need + w + 1, p1);
+}
 // whether the on-demand path applies: rows a multiple of 16 bytes (TMA tiles), fewer than 2^32 voxels
 bool od_eligible(const float *in, int nx, int ny, int nz);
 n2m_status od_approx(const float *in, float *out, int nx, int ny, int nz, float iso, OdWork &w, cudaStream_t s,
                      const StagedInput *stage = nullptr);
 n2m_status od_resolve(const float *in, float *out, int nx, int ny, int nz, float iso, OdWork &w, VolStats *dst,
-                      cudaStream_t s, bool *fallback);
+                      cudaStream_t s, bool *fallback, bool at_or_above = false);
 n2m_status od_repair(const OdRepair &r, cudaStream_t s);
 // transposed pre-smooth: g_img = Sx^T Sy^T Sz^T g (tmp: one volume of scratch)
 n2m_status launch_smooth_adjoint(const float *g, float *tmp, float *out, int nx, int ny, int nz, cudaStream_t s);
@@ -235,8 +246,9 @@ n2m_status mc_ccand_scan(const vec3d *d_pts, int np, const int *d_ccand, int ncc
                          unsigned *d_ncand, int cand_cap, cudaStream_t s);
 
 // oldcubes.cu
+// repair: as for mc_count (vsign must then hold od_resolve's at_or_above sign)
 n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
-                    McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s);
+                    McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s, const OdRepair *repair = nullptr);
 n2m_status oc_emit(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
                     McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris, int *d_cand, unsigned *d_ncand,
                     int cand_cap, cudaStream_t s);

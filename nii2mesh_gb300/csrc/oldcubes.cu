@@ -61,32 +61,92 @@ __device__ __forceinline__ int ocube_index(unsigned a0, unsigned a1, unsigned b0
 // exclusive scan over words gives the raster order of the reference's cubes.
 constexpr int OS_W = 16;   // words of a row loaded at once per lane
 
-// A warp takes whole rows, OS_W words at a time with all their loads in flight.
-__global__ void __launch_bounds__(256) k_oc_signs(OV g, unsigned nrows, unsigned *signs) {
+// Sign words from the values of row rp (grid x = 0 at rp[0]), words [xa, xb):
+// a warp takes OS_W words at a time with all their loads in flight.
+__device__ __forceinline__ void oc_value_words(const OV &g, const float *rp, bool rface, unsigned xa, unsigned xb,
+                                               unsigned *out, int lane) {
+    for (unsigned xw0 = xa; xw0 < xb; xw0 += OS_W) {
+        float raw[OS_W];
+#pragma unroll
+        for (int k = 0; k < OS_W; k++) {
+            const int x = (int)(xw0 + k) * 32 + lane;
+            raw[k] = xw0 + k < xb && x < g.NX ? __ldg(rp + x) : 0.f;
+        }
+        unsigned mine = 0;
+#pragma unroll
+        for (int k = 0; k < OS_W; k++) {
+            const int x = (int)(xw0 + k) * 32 + lane, vx = g.lo0 + x;
+            const float v = rface || vx == 0 || vx == g.dx - 1 ? fminf(g.edge_max, raw[k]) : raw[k];
+            const unsigned m = __ballot_sync(0xffffffffu, x < g.NX && v < g.iso);
+            if (lane == k) mine = m;
+        }
+        if (lane < OS_W && xw0 + lane < xb) out[xw0 + lane] = mine;
+    }
+}
+
+// A warp takes whole rows.  vsign (may be null): the volume's sign bitmap with
+// bit = value >= iso (OdWork::vsign, wv words per row, nys groups of 8 rows);
+// words whose points all lie strictly inside the volume are then the
+// complement of two bitmap words shifted into place, the rest read values.
+__global__ void __launch_bounds__(256) k_oc_signs(OV g, unsigned nrows, unsigned *signs, const unsigned *__restrict__ vsign,
+                                                  unsigned wv, unsigned nys) {
     const int lane = threadIdx.x & 31;
     const unsigned WX = g.WX;
+    // words xw whose 32 voxels lie in columns 1 .. dx-2
+    const unsigned xs0 = (unsigned)max(0, (32 - g.lo0) / 32);
+    const int xs1 = g.dx - 33 - g.lo0 >= 0 ? (g.dx - 33 - g.lo0) / 32 : -1;
     for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += (gridDim.x * blockDim.x) >> 5) {
         const int y = (int)(row % (unsigned)g.NY), z = (int)(row / (unsigned)g.NY);
         const int vy = g.lo1 + y, vz = g.lo2 + z;
         const bool rface = vy == 0 || vz == 0 || vy == g.dy - 1 || vz == g.dz - 1;
         const float *rp = g.vol + (long long)vz * g.dxy + (long long)vy * g.dx + g.lo0;
         unsigned *out = signs + (size_t)row * WX;
-        for (unsigned xw0 = 0; xw0 < WX; xw0 += OS_W) {
-            float raw[OS_W];
+        unsigned f0 = WX, f1 = WX;   // direct words [f0, f1)
+        if (vsign && !rface) {
+            f0 = min(xs0, WX);
+            f1 = max(f0, (unsigned)min(xs1 + 1, (int)WX));
+        }
+        oc_value_words(g, rp, rface, 0, f0, out, lane);
+        for (unsigned xw = f0 + lane; xw < f1; xw += 32) {
+            const int x0 = (int)xw * 32, vx0 = g.lo0 + x0, sh = vx0 & 31;
+            const size_t wlo = od_vsign_word((unsigned)vx0, (unsigned)vy, (unsigned)vz, wv, nys);
+            const unsigned lo = __ldg(vsign + wlo), hi = sh ? __ldg(vsign + wlo + 8) : 0u;   // next x word: +8
+            const unsigned inm = x0 + 32 <= g.NX ? 0xffffffffu : (1u << (g.NX - x0)) - 1u;
+            out[xw] = ~__funnelshift_r(lo, hi, sh) & inm;
+        }
+        oc_value_words(g, rp, rface, f1, WX, out, lane);
+    }
+}
+
+// Marks for the exact pre-smooth on demand: the voxel of every corner of
+// every cube whose corner signs differ (the only cubes whose values the emit
+// reads), as bits of a linear bitmap over the volume.
+__global__ void __launch_bounds__(256) k_oc_need(OV g, unsigned nwords, const unsigned *__restrict__ signs,
+                                                 unsigned *need) {
+    const unsigned WX = g.WX, slice = WX * (unsigned)g.NY;
+    const long long nvox = g.dxy * g.dz;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const unsigned row = w / WX, xw = w - row * WX;
+        const int z = (int)(row / (unsigned)g.NY), y = (int)(row - (unsigned)z * (unsigned)g.NY);
+        if (y >= g.NY - 1 || z >= g.NZ - 1) continue;   // no cubes start on the last row / slice
+        const int x0 = (int)xw * 32;
+        const bool nx = xw + 1 < WX;
+        const unsigned hxm = x0 + 33 <= g.NX ? 0xffffffffu : (g.NX - 1 - x0 > 0 ? (1u << (g.NX - 1 - x0)) - 1u : 0u);
+        const unsigned a0 = __ldg(signs + w), b0 = __ldg(signs + w + WX), c0 = __ldg(signs + w + slice),
+                       d0 = __ldg(signs + w + slice + WX);
+        const unsigned a1 = __funnelshift_r(a0, nx ? __ldg(signs + w + 1) : 0u, 1);
+        const unsigned b1 = __funnelshift_r(b0, nx ? __ldg(signs + w + WX + 1) : 0u, 1);
+        const unsigned c1 = __funnelshift_r(c0, nx ? __ldg(signs + w + slice + 1) : 0u, 1);
+        const unsigned d1 = __funnelshift_r(d0, nx ? __ldg(signs + w + slice + WX + 1) : 0u, 1);
+        const unsigned mix = (a0 | a1 | b0 | b1 | c0 | c1 | d0 | d1) & ~(a0 & a1 & b0 & b1 & c0 & c1 & d0 & d1) & hxm;
+        if (!mix) continue;
+        const unsigned cm = mix | (mix << 1), carry = mix >> 31;   // corners x and x + 1 of each mixed cube
 #pragma unroll
-            for (int k = 0; k < OS_W; k++) {
-                const int x = (int)(xw0 + k) * 32 + lane;
-                raw[k] = xw0 + k < WX && x < g.NX ? __ldg(rp + x) : 0.f;
-            }
-            unsigned mine = 0;
-#pragma unroll
-            for (int k = 0; k < OS_W; k++) {
-                const int x = (int)(xw0 + k) * 32 + lane, vx = g.lo0 + x;
-                const float v = rface || vx == 0 || vx == g.dx - 1 ? fminf(g.edge_max, raw[k]) : raw[k];
-                const unsigned m = __ballot_sync(0xffffffffu, x < g.NX && v < g.iso);
-                if (lane == k) mine = m;
-            }
-            if (lane < OS_W && xw0 + lane < WX) out[xw0 + lane] = mine;
+        for (int r = 0; r < 4; r++) {
+            const long long j = (long long)(g.lo0 + x0) + (long long)(g.lo1 + y + (r & 1)) * g.dx +
+                                (long long)(g.lo2 + z + (r >> 1)) * g.dxy;
+            od_need_mark(need, j, cm, nvox);
+            if (carry) od_need_mark(need, j + 32, 1u, nvox);
         }
     }
 }
@@ -367,7 +427,7 @@ OV make_ov(const float *vol, const int dim[3], const int lo[3], const int hi[3],
 }  // namespace
 
 n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso,
-                     float edge_max, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s) {
+                     float edge_max, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s, const OdRepair *repair) {
     const OV g = make_ov(vol, dim, lo, hi, iso, edge_max);
     if (g.NX < 2 || g.NY < 2 || g.NZ < 2) {
         CK(cudaMemsetAsync(d_total, 0, sizeof(uint4), s));
@@ -384,7 +444,15 @@ n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const i
     CKS(w.cand.ensure((nwords + 1) * sizeof(unsigned)));
     const unsigned nrows = (unsigned)g.NY * (unsigned)g.NZ;
     const unsigned wblocks = (unsigned)std::min<size_t>((nwords + 255) / 256, 152u * 16u);
-    { k_oc_signs<<<std::min<unsigned>((nrows + 7) / 8, 152u * 16u), 256, 0, s>>>(g, nrows, w.signs.as<unsigned>()); N2M_COUNT(); }
+    { k_oc_signs<<<std::min<unsigned>((nrows + 7) / 8, 152u * 16u), 256, 0, s>>>(g, nrows, w.signs.as<unsigned>(), repair ? repair->w->vsign.as<unsigned>() : nullptr, (unsigned)(dim[0] + 31) / 32, (unsigned)(dim[1] + 7) / 8); N2M_COUNT(); }
+    if (repair) {   // exact smoothed values where the emit reads them
+        const size_t nvw = ((size_t)dim[0] * dim[1] * dim[2] + 31) / 32;
+        CKS(repair->w->need_z.ensure(nvw * sizeof(unsigned)));
+        CK(cudaMemsetAsync(repair->w->need_z.p, 0, nvw * sizeof(unsigned), s));
+        { k_oc_need<<<wblocks, 256, 0, s>>>(g, (unsigned)nwords, w.signs.as<unsigned>(), repair->w->need_z.as<unsigned>()); N2M_COUNT(); }
+        CKL();
+        CKS(od_repair(*repair, s));
+    }
     { k_oc_words<<<wblocks, 256, 0, s>>>(g, (unsigned)nwords, w.signs.as<unsigned>(), w.words.as<uint4>(), w.counts.as<uint4>()); N2M_COUNT(); }
     CKL();
     CKS(scan_uint4(w.counts.as<uint4>(), nwords, d_total, sw, s));

@@ -775,7 +775,7 @@ __device__ float od_exact_at(const float *__restrict__ in, int x, int y, int z, 
 // the range is the exact extreme over the candidates that can still reach it
 // (value - B <= the smallest min + B of any task; the same for the maximum)
 __global__ void k_od_resolve(const float *__restrict__ in, float *out, int nx, int ny, int nz, float iso, OdStats *st,
-                             OdLists L, unsigned nu, unsigned nmin, unsigned nmax) {
+                             OdLists L, unsigned nu, unsigned nmin, unsigned nmax, bool at_or_above) {
     const unsigned n = nu + nmin + nmax;
     const float umin = ord2f(st->umin), lmax = ord2f(st->lmax);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -800,7 +800,7 @@ __global__ void k_od_resolve(const float *__restrict__ in, float *out, int nx, i
         if (which == 0) {
             out[j] = v;
             unsigned *sw = L.vsign + od_vsign_word(x, y, z, L.wv, L.nys);
-            if (__fsub_rn(v, iso) > -N2M_FLT_EPS) atomicOr(sw, 1u << (x & 31));
+            if (at_or_above ? v >= iso : __fsub_rn(v, iso) > -N2M_FLT_EPS) atomicOr(sw, 1u << (x & 31));
             else atomicAnd(sw, ~(1u << (x & 31)));
             if (v >= iso) {
                 atomicMin(&st->vs.lo[0], (int)x); atomicMax(&st->vs.hi[0], (int)x);
@@ -1050,7 +1050,7 @@ n2m_status od_approx(const float *in, float *out, int nx, int ny, int nz, float 
 }
 
 n2m_status od_resolve(const float *in, float *out, int nx, int ny, int nz, float iso, OdWork &w, VolStats *dst,
-                      cudaStream_t s, bool *fallback) {
+                      cudaStream_t s, bool *fallback, bool at_or_above) {
     OdStats h;
     CK(cudaMemcpyAsync(&h, w.st.p, sizeof(OdStats), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -1066,7 +1066,8 @@ n2m_status od_resolve(const float *in, float *out, int nx, int ny, int nz, float
               (unsigned)(nx + 31) / 32, (unsigned)(ny + 7) / 8};
     const unsigned tot = h.cnt[0] + h.cnt[1] + h.cnt[2];
     const unsigned blocks = std::max(1u, std::min((tot + 127) / 128, 152u * 8u));
-    k_od_resolve<<<blocks, 128, 0, s>>>(in, out, nx, ny, nz, iso, w.st.as<OdStats>(), L, h.cnt[0], h.cnt[1], h.cnt[2]);
+    k_od_resolve<<<blocks, 128, 0, s>>>(in, out, nx, ny, nz, iso, w.st.as<OdStats>(), L, h.cnt[0], h.cnt[1], h.cnt[2],
+                                        at_or_above);
     N2M_COUNT();
     CKL();
     CK(cudaMemcpyAsync(dst, w.st.p, sizeof(VolStats), cudaMemcpyDeviceToDevice, s));   // vs is the first member

@@ -48,7 +48,7 @@ def test_sphere64_config(gpu, oracle, seed):
     assert ok, msg
 
 
-@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE])
+@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE, OLDCUBES])
 def test_ct_like(gpu, oracle, variant):
     """CT-like values (negative background, salt noise), iso 300, no clustering"""
     vol = synth.ct512(seed=5, n=96, count=12)
@@ -67,11 +67,12 @@ def test_brain_u8(gpu, oracle):
         assert ok, msg
 
 
-@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE])
+@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE, OLDCUBES])
 def test_brain182_full_options(gpu, oracle, variant):
     """the brain-sized workload with every option it names: 182x218x182 uint8
     cast to float32, the Otsu 'medium' isolevel of the raw volume, -p 1 -l 1
-    -b 1 with the Lewiner (-o 0) and classic (-o 1) tables, then -s 20 HC
+    -b 1 with the Lewiner (-o 0) and classic (-o 1) tables and the classic
+    build's oldcubes, then -s 20 HC
     smoothing as nii2 runs it (alpha 0.1, beta 0.5, borders locked;
     src/nii2mesh.c:326-331).  The isolevel and the raw mesh must equal the
     oracle's bit for bit; the smoothed vertices, through the drop-in
@@ -89,7 +90,7 @@ def test_brain182_full_options(gpu, oracle, variant):
     ok, d, msg = smoothed_equal(got, got_s, want, want_s, HC_TOL)
     assert ok, msg
     ctx = gpu.Context(0)
-    cubes = gpu.CLASSIC_TABLE if variant == MC_CLASSIC_TABLE else gpu.MC33
+    cubes = {MC33: gpu.MC33, MC_CLASSIC_TABLE: gpu.CLASSIC_TABLE, OLDCUBES: gpu.OLDCUBES}[variant]
     t, p, _ = ctx.meshify(vol, iso, cubes, True, True, True, post_smooth=20)
     assert np.array_equal(t, got[0])
     assert np.abs(p - got_s).max() <= HC_TOL
@@ -234,7 +235,7 @@ def device_mesh(gpu, ctx, vol, iso, cubes, largest=False, bubbles=False):
 
 
 @pytest.mark.parametrize("shape", [(48, 52, 64), (96, 96, 96), (40, 33, 36), (64, 64, 128), (31, 29, 37)])
-@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE])
+@pytest.mark.parametrize("variant", [MC33, MC_CLASSIC_TABLE, OLDCUBES])
 def test_device_path_on_demand_smoothing(gpu, oracle, shape, variant):
     """device-resident volumes whose rows are a multiple of 4 voxels take the
     pre-smooth with exact rounding on demand (pass A over TMA tiles, exact
@@ -244,7 +245,7 @@ def test_device_path_on_demand_smoothing(gpu, oracle, shape, variant):
     falls back to mid-range"""
     ctx = gpu.Context(0)
     nz, ny, nx = shape
-    cubes = gpu.CLASSIC_TABLE if variant == MC_CLASSIC_TABLE else gpu.MC33
+    cubes = {MC33: gpu.MC33, MC_CLASSIC_TABLE: gpu.CLASSIC_TABLE, OLDCUBES: gpu.OLDCUBES}[variant]
     vols = [(synth.ct512(seed=sum(shape), n=max(shape), count=10)[:nz, :ny, :nx].copy(), 300.0),
             (synth.spheres(n=max(shape), count=6, rmin=5, rmax=12, cmin=10, cmax=max(shape) - 10, noise=20.0,
                            seed=nx)[:nz, :ny, :nx].copy(), 50.0)]
