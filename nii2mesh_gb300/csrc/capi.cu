@@ -281,7 +281,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
                       &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->raw, &c->vol, &c->stmp, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
                       &c->tris_raw, &c->pts, &c->tris, &c->ntf, &c->weld, &c->gath, &c->hmesh,
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->mc.signs, &c->mc.ctr, &c->scan.part,
-                      &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.misc,
+                      &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.rc, &c->lab.misc,
                       &c->deg.flags, &c->deg.tmp, &c->hc.start, &c->hc.refs, &c->hc.fill, &c->hc.P, &c->hc.Q,
                       &c->hc.B, &c->hc.Lo, &c->hc.border, &c->hc.hasnb, &c->hc.bad, &c->th.buf, &c->th.table,
                       &c->stmp2, &c->lubits, &c->od.st, &c->od.unc, &c->od.cmin, &c->od.cmax, &c->od.need_z, &c->od.need_y,
@@ -543,8 +543,7 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     VolStats s1 = s0;
     float min_after = mn;
     if (label) {
-        CKS(run_labelling(vol, nx, ny, nz, iso, mn, o.only_largest, o.fill_bubbles, c->lab, c->stream));
-        CKS(launch_stats(vol, nx, ny, nz, iso, true, dst + 1, c->stream));
+        CKS(run_labelling(vol, nx, ny, nz, iso, mn, o.only_largest, o.fill_bubbles, c->lab, dst + 1, c->stream));
         CKS(readback(c, &s1, dst + 1));
         min_after = ord2f(s1.vmin);
     } else if (stale) {

@@ -1,289 +1,535 @@
 // label.cu — connected-component labelling for meshify's largest-cluster and
-// bubble-fill options (src/bwlabel.c:429-543, src/meshify.c:323-342).
+// bubble-fill options (src/bwlabel.c:429-543, src/meshify.c:323-342) and the
+// drop-in bwlabel().
 //
-// GPU union-find: every voxel of the class starts linked to the first voxel of
-// its run along x; each voxel unites with its already-visited
-// half-neighbourhood (3 offsets for 6-connectivity, 9 for 18, 13 for 26) by
-// CAS-hooking the larger root under the smaller one, then a flatten pass
-// points every voxel at its root.  The root of a component is therefore its
-// first voxel in raster order, which is exactly how the reference numbers
-// labels (first appearance) and breaks size ties (lowest label wins).
+// Runs, not voxels.  The class masks are bit words (bit x & 31 of word
+// row*W + x/32, W = ceil(nx/32) words per row), and union-find links exist
+// only at the first voxel of every run along x: a run is one set of voxels
+// for any connectivity, so a component is a set of runs.  Two runs in
+// neighbouring rows are united once per overlap (the contact whose left
+// neighbours do not also touch), hooking the larger root under the smaller,
+// so the root of a component is its first voxel in raster order: that is how
+// the reference numbers labels (first appearance) and breaks size ties (lowest
+// label wins).  Flattening, face contacts, bubble filling, component sizes and
+// the kept component all work per run; only the final pass over the volume
+// (fill to iso, dilation, mask-out and the range/bbox of the result) touches
+// every voxel.
+//
+// Row kernels give each row `seg` lanes (a power of two, one word per lane,
+// rows of more than 32 words in chunks of 32): the start of the run holding a
+// word's first voxel comes from a max-scan of the last run start of the words
+// before it.
+#include <algorithm>
+
 #include "n2m_internal.cuh"
+#include "smooth_core.cuh"
 #include "uf.cuh"
 
 namespace {
 using namespace uf;
-struct Dims {
+constexpr unsigned FULL = 0xffffffffu;
+
+struct LD {
     int nx, ny, nz;
     long long nxy, n;
+    unsigned W;       // words per row
+    unsigned nrows;   // ny * nz
+    unsigned nwords;  // W * nrows
+    int seg;          // lanes per row in the row kernels
 };
 
-__global__ void k_mask(const float *__restrict__ vol, long long n, float iso, unsigned char *m) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        m[i] = vol[i] >= iso;
+__device__ __forceinline__ unsigned valid_bits(const LD &d, unsigned w) {
+    const int x0 = (int)w * 32;
+    return x0 + 32 <= d.nx ? FULL : (1u << (d.nx - x0)) - 1u;
 }
 
-__global__ void k_nonzero(const float *__restrict__ vol, long long n, unsigned char *m) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        m[i] = vol[i] != 0.0f;
+// foreground bits (want 1) or background bits (want 0) of word w of row r
+__device__ __forceinline__ unsigned class_word(const unsigned *B, const LD &d, unsigned r, unsigned w, unsigned want) {
+    const unsigned b = B[(size_t)r * d.W + w];
+    return want ? b : ~b & valid_bits(d, w);
 }
 
-// L[i] = i where m[i] == want, else -1
-// Union-find start: every voxel of the wanted class points at the start of its
-// run along x (ballot within the warp; a run entering the warp from the left
-// points at the voxel before the warp), so x links need no union; others -1.
-__global__ void k_uf_init(const unsigned char *__restrict__ m, Dims d, unsigned char want, int *L) {
-    const long long n = d.n;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int lane = threadIdx.x & 31;
-        // the lanes of this step: consecutive voxels, a prefix of the warp
-        const long long left = n - (i - lane);
-        const unsigned act = left >= 32 ? 0xffffffffu : (1u << left) - 1u;
-        const bool fg = m[i] == want;
-        const bool left_fg = __shfl_up_sync(act, fg, 1);
-        const bool xpos = (unsigned)i % (unsigned)d.nx != 0u;   // n < 2^31
-        const bool cont = fg && xpos && (lane > 0 ? left_fg : m[i - 1] == want);
-        const unsigned starts = __ballot_sync(act, fg && !cont);
-        int parent = -1;
-        if (fg) {
-            const unsigned le = starts & (lane == 31 ? 0xffffffffu : (2u << lane) - 1u);
-            parent = le ? (int)(i - (lane - (31 - __clz(le)))) : (int)(i - lane - 1);
+// x of the highest run start at or below bit b, or -1
+__device__ __forceinline__ int last_start(unsigned starts, int x0, int b) {
+    const unsigned hs = starts & (b == 31 ? FULL : (2u << b) - 1u);
+    return hs ? x0 + 31 - __clz(hs) : -1;
+}
+
+// one lane's word of a row in a row kernel: class bits, the class word before
+// it, run starts, and cs = start (x) of the run holding the voxel before the word
+struct WordRuns {
+    unsigned c, pc, starts;
+    int x0, cs;
+    __device__ __forceinline__ int start_of(int b) const {   // run of bit b (set in c)
+        const int s = last_start(starts, x0, b);
+        return s >= 0 ? s : cs;
+    }
+};
+
+// carry_start / carry_word: the row's last run start and last class word of
+// the chunks before this one (-1 / 0 before the first); all lanes call it
+__device__ __forceinline__ WordRuns word_runs(unsigned c, int x0, int li, int seg, int &carry_start,
+                                              unsigned &carry_word) {
+    WordRuns r;
+    r.c = c;
+    r.x0 = x0;
+    const unsigned up = __shfl_up_sync(FULL, c, 1, seg);
+    r.pc = li == 0 ? carry_word : up;
+    r.starts = c & ~((c << 1) | (r.pc >> 31));
+    int incl = r.starts ? x0 + 31 - __clz(r.starts) : -1;
+    for (int d = 1; d < seg; d <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, d, seg);
+        if (li >= d) incl = max(incl, t);
+    }
+    const int excl = __shfl_up_sync(FULL, incl, 1, seg);
+    r.cs = max(carry_start, li == 0 ? -1 : excl);
+    carry_start = max(carry_start, __shfl_sync(FULL, incl, seg - 1, seg));
+    carry_word = __shfl_sync(FULL, c, seg - 1, seg);
+    return r;
+}
+
+// the class word after this lane's word (0 past the row); all lanes call it
+__device__ __forceinline__ unsigned next_word(const unsigned *B, const LD &d, unsigned c, bool rowok, unsigned r,
+                                              unsigned w, int li, int seg, unsigned want) {
+    const unsigned dn = __shfl_down_sync(FULL, c, 1, seg);
+    if (li < seg - 1) return w + 1 < d.W ? dn : 0u;
+    return rowok && w + 1 < d.W ? class_word(B, d, r, w + 1, want) : 0u;
+}
+
+// bits (x mask) of the piece of a run that starts at bit b of class word rem
+__device__ __forceinline__ unsigned piece_at(unsigned rem, int b) {
+    const unsigned ones = ~(rem >> b);
+    const int len = ones ? __ffs(ones) - 1 : 32 - b;
+    return (len == 32 ? FULL : (1u << len) - 1u) << b;
+}
+
+// Class bits of the volume: value >= iso (meshify's mask), or value != 0
+// (bwlabel's).  A warp takes whole rows, 16 words at a time in flight.
+__global__ void __launch_bounds__(256) k_lab_bits(const float *__restrict__ vol, LD d, float iso, bool nonzero,
+                                                  unsigned *B) {
+    constexpr int K = 16;
+    const int lane = threadIdx.x & 31;
+    for (unsigned r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < d.nrows; r += (gridDim.x * blockDim.x) >> 5) {
+        const float *rp = vol + (long long)r * d.nx;
+        unsigned *out = B + (size_t)r * d.W;
+        for (unsigned w0 = 0; w0 < d.W; w0 += K) {
+            float v[K];
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const int x = (int)(w0 + k) * 32 + lane;
+                v[k] = w0 + k < d.W && x < d.nx ? __ldg(rp + x) : 0.f;
+            }
+            unsigned mine = 0;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const int x = (int)(w0 + k) * 32 + lane;
+                const unsigned m = __ballot_sync(FULL, x < d.nx && (nonzero ? v[k] != 0.0f : v[k] >= iso));
+                if (lane == k) mine = m;
+            }
+            if (lane < K && w0 + lane < d.W) out[w0 + lane] = mine;
         }
-        L[i] = parent;
     }
 }
 
-__constant__ signed char k_half[13][3] = {{-1, 0, 0},  {0, -1, 0}, {0, 0, -1},  {-1, -1, 0}, {1, -1, 0},
-                                          {-1, 0, -1}, {1, 0, -1}, {0, -1, -1}, {0, 1, -1},  {-1, -1, -1},
-                                          {1, -1, -1}, {-1, 1, -1}, {1, 1, -1}};
+// every run start of the class links to itself; z8 / z32 (may be null) are
+// zeroed at the run starts (the edge flags and sizes the roots will carry)
+__global__ void k_run_init(const unsigned *__restrict__ B, LD d, unsigned want, int *L, unsigned char *z8,
+                           unsigned *z32) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nwords; i += gridDim.x * blockDim.x) {
+        const unsigned r = i / d.W, w = i - r * d.W;
+        const unsigned c = class_word(B, d, r, w, want), pc = w ? class_word(B, d, r, w - 1, want) : 0u;
+        const long long base = (long long)r * d.nx + (long long)w * 32;
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
+            const int s = (int)(base + __ffs(st) - 1);
+            L[s] = s;
+            if (z8) z8[s] = 0;
+            if (z32) z32[s] = 0;
+        }
+    }
+}
 
-// Union of each voxel of the class (m == want) with its half-neighbours of
-// k_half[1 .. NNB-1] (the -x neighbour is linked by the run start).  A contact
-// whose two left voxels also touch is implied by theirs (both pairs lie in the
-// same runs) and is skipped.  One warp per row (y, z), 32 voxels a word: the
-// class bits of the row and of the rows (y-1, z), (y, z-1), (y-1, z-1),
-// (y+1, z-1) give every contact of a word by shifts; only the lanes holding
-// one touch L.
+// Union of the runs of the class with those of the rows before them: rows
+// (y-1, z) and (y, z-1) for 6-connectivity, with x offsets -1..1 for 18 and
+// rows (y-1, z-1), (y+1, z-1) for 18 (x offset 0) and 26 (-1..1).  A contact
+// of voxel x with voxel x+dx of row k counts only if voxels x-1 and x+dx-1
+// do not also touch: one union per overlap of two runs.
 template <int NNB>
-__global__ void __launch_bounds__(256) k_uf_merge(const unsigned char *__restrict__ m, unsigned char want, int *L, Dims d) {
+__global__ void __launch_bounds__(256) k_run_merge(const unsigned *__restrict__ B, LD d, unsigned want, int *L) {
     static_assert(NNB == 3 || NNB == 9 || NNB == 13, "6-, 18- or 26-connectivity");
-    const int lane = threadIdx.x & 31;
-    const long long nrows = (long long)d.ny * d.nz;
-    const int nw = (d.nx + 31) / 32;
     constexpr int NR = NNB == 3 ? 3 : 5;
-    // rows: 0 = (y, z), 1 = (y-1, z), 2 = (y, z-1), 3 = (y-1, z-1), 4 = (y+1, z-1)
     const int RY[5] = {0, -1, 0, -1, 1}, RZ[5] = {0, 0, -1, -1, -1};
-    for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < nrows;
-         r += ((long long)gridDim.x * blockDim.x) >> 5) {
-        const int z = (int)(r / d.ny), y = (int)(r - (long long)z * d.ny);
-        auto word = [&](int dy, int dz, int xw) -> unsigned {
-            const int yy = y + dy, zz = z + dz, x = xw * 32 + lane;
-            const bool in = yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz && x < d.nx;
-            return __ballot_sync(0xffffffffu, in && m[zz * d.nxy + (long long)yy * d.nx + x] == want);
-        };
-        unsigned pw[NR], cw[NR];
+    const int lane = threadIdx.x & 31, seg = d.seg, li = lane & (seg - 1);
+    const unsigned rpw = 32u / (unsigned)seg, rsub = (unsigned)lane / (unsigned)seg;
+    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < d.nrows; rb += nw * rpw) {
+        const unsigned r = rb + rsub;
+        const bool rowok = r < d.nrows;
+        const int z = rowok ? (int)(r / (unsigned)d.ny) : 0, y = rowok ? (int)(r - (unsigned)z * (unsigned)d.ny) : 0;
+        bool kok[NR];
+        unsigned rk[NR];
 #pragma unroll
         for (int k = 0; k < NR; k++) {
-            pw[k] = 0u;
-            cw[k] = word(RY[k], RZ[k], 0);
+            const int yy = y + RY[k], zz = z + RZ[k];
+            kok[k] = rowok && yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz;
+            rk[k] = kok[k] ? (unsigned)zz * (unsigned)d.ny + (unsigned)yy : 0u;
         }
-        for (int xw = 0; xw < nw; xw++) {
-            unsigned nx[NR];
+        int cst[NR];
+        unsigned cwd[NR];
 #pragma unroll
-            for (int k = 0; k < NR; k++) nx[k] = word(RY[k], RZ[k], xw + 1);
-            // S(k, dx): bit x = class of voxel x + dx of row k (dx in -2 .. 1)
-            auto S = [&](int k, int dx) -> unsigned {
-                return dx == 0 ? cw[k] : dx > 0 ? (cw[k] >> dx) | (nx[k] << (32 - dx)) : (cw[k] << -dx) | (pw[k] >> (32 + dx));
-            };
-            const unsigned F = cw[0], left = S(0, -1);
-            auto contact = [&](int k, int dx) -> unsigned { return ((F & S(k, dx) & ~(left & S(k, dx - 1))) >> lane) & 1u; };
-            // bit k-1 of this lane's set: a contact with k_half[k]
-            unsigned set = contact(1, 0) | contact(2, 0) << 1;   // (0,-1,0) (0,0,-1)
-            if constexpr (NNB >= 9)
-                set |= contact(1, -1) << 2 | contact(1, 1) << 3     // (-1,-1,0) (1,-1,0)
-                     | contact(2, -1) << 4 | contact(2, 1) << 5     // (-1,0,-1) (1,0,-1)
-                     | contact(3, 0) << 6 | contact(4, 0) << 7;     // (0,-1,-1) (0,1,-1)
-            if constexpr (NNB == 13)
-                set |= contact(3, -1) << 8 | contact(3, 1) << 9     // (-1,-1,-1) (1,-1,-1)
-                     | contact(4, -1) << 10 | contact(4, 1) << 11;  // (-1,1,-1) (1,1,-1)
-            const int x = xw * 32 + lane;
-            if (set && x < d.nx) {
-                const int i = (int)(r * d.nx + x);
-                do {
-                    const int k = __ffs(set);
-                    set &= set - 1u;
-                    const int j = i + k_half[k][0] + k_half[k][1] * d.nx + k_half[k][2] * (int)d.nxy;
-                    if (L[j] != L[i]) unite(L, i, j);
-                } while (set);
-            }
+        for (int k = 0; k < NR; k++) { cst[k] = -1; cwd[k] = 0u; }
+        for (unsigned c0 = 0; c0 < d.W; c0 += (unsigned)seg) {
+            const unsigned w = c0 + (unsigned)li;
+            const bool ok = w < d.W;
+            const int x0 = (int)w * 32;
+            WordRuns R[NR];
+            unsigned nk[NR];
 #pragma unroll
             for (int k = 0; k < NR; k++) {
-                pw[k] = cw[k];
-                cw[k] = nx[k];
+                const unsigned c = ok && kok[k] ? class_word(B, d, rk[k], w, want) : 0u;
+                R[k] = word_runs(c, x0, li, seg, cst[k], cwd[k]);
+                nk[k] = next_word(B, d, c, kok[k], rk[k], w, li, seg, want);
+            }
+            const unsigned F = R[0].c;
+            if (!F) continue;
+            const unsigned left = (F << 1) | (R[0].pc >> 31);
+            auto S = [&](int k, int dx) -> unsigned {
+                const WordRuns &q = R[k];
+                return dx == 0 ? q.c : dx == 1 ? (q.c >> 1) | (nk[k] << 31)
+                                     : dx == -1 ? (q.c << 1) | (q.pc >> 31) : (q.c << 2) | (q.pc >> 30);
+            };
+            const long long base0 = (long long)r * d.nx;
+            auto link = [&](int k, int dx) {
+                unsigned m = F & S(k, dx) & ~(left & S(k, dx - 1));
+                if (!m) return;
+                const WordRuns &q = R[k];
+                const long long basek = (long long)rk[k] * d.nx;
+                for (; m; m &= m - 1) {
+                    const int b = __ffs(m) - 1, xx = b + dx;
+                    const int sk = xx < 0 ? q.cs : xx > 31 ? ((q.c >> 31) & 1u ? q.start_of(31) : x0 + 32) : q.start_of(xx);
+                    const int i = (int)(base0 + R[0].start_of(b)), j = (int)(basek + sk);
+                    if (L[i] != L[j]) unite(L, i, j);
+                }
+            };
+            link(1, 0);
+            link(2, 0);
+            if constexpr (NNB >= 9) {
+                link(1, -1); link(1, 1); link(2, -1); link(2, 1); link(3, 0); link(4, 0);
+            }
+            if constexpr (NNB == 13) {
+                link(3, -1); link(3, 1); link(4, -1); link(4, 1);
             }
         }
     }
 }
 
-// every voxel of the class points at its root; lanes sharing a parent (the
-// voxels of one run) walk its chain once
-__global__ void k_uf_flatten(int *L, long long n, unsigned *nroots) {
-    unsigned c = 0;
-    const int lane = threadIdx.x & 31;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int p = L[i];
-        const unsigned grp = __match_any_sync(__activemask(), p);
-        const int lead = __ffs(grp) - 1;
-        int root = 0;
-        if (lane == lead && p >= 0) root = find_root(L, p);
-        root = __shfl_sync(grp, root, lead);
-        if (p < 0) continue;
-        if (p == (int)i) c++;
-        else L[i] = root;
+// every run start of the class points at its root; roots are counted
+__global__ void k_run_flatten(const unsigned *__restrict__ B, LD d, unsigned want, int *L, unsigned *nroots) {
+    unsigned cnt = 0;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nwords; i += gridDim.x * blockDim.x) {
+        const unsigned r = i / d.W, w = i - r * d.W;
+        const unsigned c = class_word(B, d, r, w, want), pc = w ? class_word(B, d, r, w - 1, want) : 0u;
+        const long long base = (long long)r * d.nx + (long long)w * 32;
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
+            const int s = (int)(base + __ffs(st) - 1);
+            const int root = find_halve(L, s);
+            if (root == s) cnt++;
+            else L[s] = root;
+        }
     }
-    if (nroots && c) atomicAdd(nroots, c);
+    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULL, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(nroots, cnt);
 }
 
-// background components touching a face of the volume: one thread per face
-// voxel (slices z = 0 and z = nz-1 whole; rows y = 0 and y = ny-1 and
-// columns x = 0 and x = nx-1 of the slices between; a voxel on two faces is
-// visited twice, which writes the same flag)
-__global__ void k_edge_roots(const int *__restrict__ L, Dims d, unsigned char *edge) {
-    const long long inner = d.nz > 2 ? d.nz - 2 : 0;
-    const long long nface_z = d.nz > 1 ? 2 * d.nxy : d.nxy, nrow = inner * d.nx, ncol = inner * d.ny;
-    const long long total = nface_z + 2 * nrow + 2 * ncol;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
-        long long i;
-        if (t < nface_z) {
-            i = t < d.nxy ? t : (long long)(d.nz - 1) * d.nxy + (t - d.nxy);
-        } else if (t < nface_z + 2 * nrow) {
-            const long long u = t - nface_z, side = u / nrow, v = u - side * nrow;
-            const long long z = 1 + v / d.nx, x = v - (z - 1) * d.nx;
-            i = z * d.nxy + (side ? (long long)(d.ny - 1) * d.nx : 0) + x;
-        } else {
-            const long long u = t - nface_z - 2 * nrow, side = u / ncol, v = u - side * ncol;
-            const long long z = 1 + v / d.ny, y = v - (z - 1) * d.ny;
-            i = z * d.nxy + y * d.nx + (side ? d.nx - 1 : 0);
+// Background components touching a face of the volume: every run of a row on
+// a y or z face, and the runs holding x = 0 and x = nx-1 of every row, flag
+// their root.
+__global__ void __launch_bounds__(256) k_run_edges(const unsigned *__restrict__ B, LD d, const int *__restrict__ L,
+                                                   unsigned char *edge) {
+    const int lane = threadIdx.x & 31, seg = d.seg, li = lane & (seg - 1);
+    const unsigned rpw = 32u / (unsigned)seg, rsub = (unsigned)lane / (unsigned)seg;
+    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < d.nrows; rb += nw * rpw) {
+        const unsigned r = rb + rsub;
+        const bool rowok = r < d.nrows;
+        const int z = rowok ? (int)(r / (unsigned)d.ny) : 0, y = rowok ? (int)(r - (unsigned)z * (unsigned)d.ny) : 0;
+        const bool face = y == 0 || z == 0 || y == d.ny - 1 || z == d.nz - 1;
+        const long long base = (long long)r * d.nx;
+        int cst = -1;
+        unsigned cwd = 0;
+        for (unsigned c0 = 0; c0 < d.W; c0 += (unsigned)seg) {
+            const unsigned w = c0 + (unsigned)li;
+            const unsigned c = rowok && w < d.W ? class_word(B, d, r, w, 0u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, li, seg, cst, cwd);
+            if (!c) continue;
+            if (face)
+                for (unsigned st = R.starts; st; st &= st - 1) edge[L[base + R.x0 + __ffs(st) - 1]] = 1;
+            else if (w == 0 && (c & 1u))
+                edge[L[base]] = 1;
+            if (!face && w == d.W - 1) {
+                const int b = (d.nx - 1) & 31;
+                if ((c >> b) & 1u) edge[L[base + R.start_of(b)]] = 1;
+            }
         }
-        const int r = L[i];
-        if (r >= 0) edge[r] = 1;
     }
 }
 
 // bubbles (background components away from every face) become foreground,
 // only when the background has at least two components (src/bwlabel.c:488-491)
-__global__ void k_fill_bubbles(const int *__restrict__ L, long long n, const unsigned char *__restrict__ edge,
-                               const unsigned *__restrict__ ncomp, unsigned char *m) {
-    if (*ncomp <= 1) return;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int r = L[i];
-        if (r >= 0 && !edge[r]) m[i] = 1;
+__global__ void __launch_bounds__(256) k_run_fill(unsigned *B, LD d, const int *__restrict__ L,
+                                                  const unsigned char *__restrict__ edge, const unsigned *__restrict__ nbg) {
+    if (*nbg <= 1) return;
+    const int lane = threadIdx.x & 31, seg = d.seg, li = lane & (seg - 1);
+    const unsigned rpw = 32u / (unsigned)seg, rsub = (unsigned)lane / (unsigned)seg;
+    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < d.nrows; rb += nw * rpw) {
+        const unsigned r = rb + rsub;
+        const bool rowok = r < d.nrows;
+        const long long base = (long long)r * d.nx;
+        int cst = -1;
+        unsigned cwd = 0;
+        for (unsigned c0 = 0; c0 < d.W; c0 += (unsigned)seg) {
+            const unsigned w = c0 + (unsigned)li;
+            const unsigned c = rowok && w < d.W ? class_word(B, d, r, w, 0u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, li, seg, cst, cwd);
+            unsigned fill = 0;
+            for (unsigned rem = c; rem;) {   // the word's pieces of runs
+                const int b = __ffs(rem) - 1;
+                const unsigned pm = piece_at(rem, b);
+                rem &= ~pm;
+                if (!edge[L[base + R.start_of(b)]]) fill |= pm;
+            }
+            // every lane has read its neighbours' words (word_runs) before any write
+            if (fill) B[(size_t)r * d.W + w] |= fill;
+        }
     }
 }
 
-__global__ void k_sizes(const int *__restrict__ L, long long n, unsigned *cnt) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int r = L[i];
-        const unsigned grp = __match_any_sync(__activemask(), r);   // lanes sharing a root add together
-        if (r >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&cnt[r], __popc(grp));
+// component sizes: every run adds its length to its root (at the run's end)
+__global__ void __launch_bounds__(256) k_run_sizes(const unsigned *__restrict__ B, LD d, const int *__restrict__ L,
+                                                   unsigned *cnt) {
+    const int lane = threadIdx.x & 31, seg = d.seg, li = lane & (seg - 1);
+    const unsigned rpw = 32u / (unsigned)seg, rsub = (unsigned)lane / (unsigned)seg;
+    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < d.nrows; rb += nw * rpw) {
+        const unsigned r = rb + rsub;
+        const bool rowok = r < d.nrows;
+        const long long base = (long long)r * d.nx;
+        int cst = -1;
+        unsigned cwd = 0;
+        for (unsigned c0 = 0; c0 < d.W; c0 += (unsigned)seg) {
+            const unsigned w = c0 + (unsigned)li;
+            const unsigned c = rowok && w < d.W ? class_word(B, d, r, w, 1u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, li, seg, cst, cwd);
+            const unsigned nxt = next_word(B, d, c, rowok, r, w, li, seg, 1u);
+            for (unsigned ends = c & ~((c >> 1) | (nxt << 31)); ends; ends &= ends - 1) {
+                const int e = __ffs(ends) - 1, s = R.start_of(e);
+                atomicAdd(&cnt[L[base + s]], (unsigned)(R.x0 + e - s + 1));
+            }
+        }
     }
 }
 
 // largest component; ties go to the smallest root (first in raster order)
-__global__ void k_best(const int *__restrict__ L, const unsigned *__restrict__ cnt, long long n,
-                       unsigned long long *best) {
+__global__ void k_run_best(const unsigned *__restrict__ B, LD d, const int *__restrict__ L,
+                           const unsigned *__restrict__ cnt, unsigned long long *best) {
     unsigned long long b = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        if (L[i] == (int)i) {
-            const unsigned long long k = ((unsigned long long)cnt[i] << 32) | (0xffffffffu - (unsigned)i);
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nwords; i += gridDim.x * blockDim.x) {
+        const unsigned r = i / d.W, w = i - r * d.W;
+        const unsigned c = class_word(B, d, r, w, 1u), pc = w ? class_word(B, d, r, w - 1, 1u) : 0u;
+        const long long base = (long long)r * d.nx + (long long)w * 32;
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
+            const int s = (int)(base + __ffs(st) - 1);
+            if (L[s] != s) continue;
+            const unsigned long long k = ((unsigned long long)cnt[s] << 32) | (0xffffffffu - (unsigned)s);
             b = k > b ? k : b;
         }
+    }
     for (int o = 16; o; o >>= 1) {
-        const unsigned long long t = __shfl_xor_sync(0xffffffffu, b, o);
+        const unsigned long long t = __shfl_xor_sync(FULL, b, o);
         b = t > b ? t : b;
     }
     if ((threadIdx.x & 31) == 0 && b) atomicMax(best, b);
 }
 
-__global__ void k_keep_best(const int *__restrict__ L, long long n, const unsigned long long *__restrict__ best,
-                            unsigned char *keep) {
-    const unsigned long long b = *best;
-    const int root = b ? (int)(0xffffffffu - (unsigned)(b & 0xffffffffu)) : -2;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        keep[i] = L[i] == root;
+// bits of the voxels of the largest component
+__global__ void __launch_bounds__(256) k_run_keep(const unsigned *__restrict__ B, LD d, const int *__restrict__ L,
+                                                  const unsigned long long *__restrict__ best, unsigned *K) {
+    const unsigned long long bk = *best;
+    const int root = bk ? (int)(0xffffffffu - (unsigned)(bk & 0xffffffffu)) : -2;
+    const int lane = threadIdx.x & 31, seg = d.seg, li = lane & (seg - 1);
+    const unsigned rpw = 32u / (unsigned)seg, rsub = (unsigned)lane / (unsigned)seg;
+    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < d.nrows; rb += nw * rpw) {
+        const unsigned r = rb + rsub;
+        const bool rowok = r < d.nrows;
+        const long long base = (long long)r * d.nx;
+        int cst = -1;
+        unsigned cwd = 0;
+        for (unsigned c0 = 0; c0 < d.W; c0 += (unsigned)seg) {
+            const unsigned w = c0 + (unsigned)li;
+            const unsigned c = rowok && w < d.W ? class_word(B, d, r, w, 1u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, li, seg, cst, cwd);
+            unsigned keep = 0;
+            for (unsigned rem = c; rem;) {
+                const int b = __ffs(rem) - 1;
+                const unsigned pm = piece_at(rem, b);
+                rem &= ~pm;
+                if (L[base + R.start_of(b)] == root) keep |= pm;
+            }
+            if (rowok && w < d.W) K[(size_t)r * d.W + w] = keep;
+        }
+    }
 }
 
-__global__ void k_fill_iso(float *vol, long long n, const unsigned char *__restrict__ keep, float iso) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        if (keep[i]) vol[i] = fmaxf(vol[i], iso);
+__global__ void k_nl_from(const unsigned *nroots, bool only_largest, int *nl) {
+    *nl = only_largest ? (*nroots > 0 ? 1 : 0) : (int)*nroots;
 }
 
-// dilate (26-neighbourhood without the (-1,-1,-1) neighbour, interior voxels
-// only; src/meshify.c:218-264) fused with the mask-out img = mn.  One warp per
-// row, 32 voxels a word: with R3 = K(x-1)|K(x)|K(x+1) and R2 = K(x)|K(x+1) of a
-// row, the neighbourhood is R3 of rows y-1..y+1 in slices z and z+1, R3 of rows
-// y and y+1 in slice z-1, and R2 of row y-1 in slice z-1.
-__global__ void __launch_bounds__(256) k_dilate_maskout(const unsigned char *__restrict__ keep, Dims d, float *vol, float mn) {
+// The labelled volume, one warp per row, 32 voxels a word, with the range and
+// bbox of the result.  Kept voxels (K) are raised to iso when FILL; with
+// LARGEST, voxels neither kept nor in the dilation of the kept set (the
+// 26-neighbourhood without (-1,-1,-1), interior voxels only;
+// src/meshify.c:218-264) become mn and are not read.  With R3 = K(x-1) | K(x) |
+// K(x+1) and R2 = K(x) | K(x+1) of a row, the dilation is R3 of rows y-1..y+1
+// in slices z and z+1, R3 of rows y and y+1 in slice z-1, and R2 of row y-1 in
+// slice z-1.
+template <bool LARGEST, bool FILL>
+__global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ K, LD d, float *vol, float iso, float mn,
+                                                   VolStats *st) {
+    smooth::Acc acc;
+    acc.init();
     const int lane = threadIdx.x & 31;
-    const long long nrows = (long long)d.ny * d.nz;
-    const int nw = (d.nx + 31) / 32;
     // rows used: 0..2 = y-1..y+1 in slice z, 3..5 in slice z+1, 6 = (y, z-1), 7 = (y+1, z-1), 8 = (y-1, z-1)
     const int DY[9] = {-1, 0, 1, -1, 0, 1, 0, 1, -1}, DZ[9] = {0, 0, 0, 1, 1, 1, -1, -1, -1};
-    for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < nrows;
-         r += ((long long)gridDim.x * blockDim.x) >> 5) {
-        const int z = (int)(r / d.ny), y = (int)(r - (long long)z * d.ny);
+    for (unsigned r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < d.nrows; r += (gridDim.x * blockDim.x) >> 5) {
+        const int z = (int)(r / (unsigned)d.ny), y = (int)(r - (unsigned)z * (unsigned)d.ny);
+        float *row = vol + (long long)r * d.nx;
+        if (!LARGEST) {
+            const unsigned *K0 = K + (size_t)r * d.W;
+            for (unsigned w = 0; w < d.W; w++) {
+                const unsigned kw = K0[w];
+                const int x = (int)w * 32 + lane;
+                if (x >= d.nx) continue;
+                float v = row[x];
+                if (FILL && ((kw >> lane) & 1u)) {
+                    v = fmaxf(v, iso);
+                    row[x] = v;
+                }
+                acc.add(v, x, y, z, iso);
+            }
+            continue;
+        }
         const bool ryz = y > 0 && z > 0 && y < d.ny - 1 && z < d.nz - 1;
-        auto word = [&](int dy, int dz, int xw) -> unsigned {
-            const int yy = y + dy, zz = z + dz, x = xw * 32 + lane;
-            const bool in = yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz && x < d.nx;
-            return __ballot_sync(0xffffffffu, in && keep[zz * d.nxy + (long long)yy * d.nx + x] != 0);
-        };
+        const unsigned *Kr[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int yy = y + DY[k], zz = z + DZ[k];
+            Kr[k] = yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz ? K + ((size_t)zz * d.ny + yy) * d.W : nullptr;
+        }
         unsigned prev[9], cur[9];
 #pragma unroll
         for (int k = 0; k < 9; k++) {
             prev[k] = 0u;
-            cur[k] = word(DY[k], DZ[k], 0);
+            cur[k] = Kr[k] ? Kr[k][0] : 0u;
         }
-        for (int xw = 0; xw < nw; xw++) {
+        for (unsigned w = 0; w < d.W; w++) {
             unsigned on = 0u;
 #pragma unroll
             for (int k = 0; k < 9; k++) {
-                const unsigned nxt = word(DY[k], DZ[k], xw + 1);
+                const unsigned nxt = Kr[k] && w + 1 < d.W ? Kr[k][w + 1] : 0u;
                 const unsigned right = (cur[k] >> 1) | (nxt << 31);   // K(x+1)
                 on |= cur[k] | right | (k < 8 ? (cur[k] << 1) | (prev[k] >> 31) : 0u);   // row 8: no K(x-1)
                 prev[k] = cur[k];
                 cur[k] = nxt;
             }
-            const int x = xw * 32 + lane;
-            if (x < d.nx) {
-                const bool kept = (prev[1] >> lane) & 1u;   // row (y, z): prev holds word xw now
-                const bool interior = ryz && x > 0 && x < d.nx - 1;
-                if (!(kept || (interior && ((on >> lane) & 1u)))) vol[r * d.nx + x] = mn;
+            const int x = (int)w * 32 + lane;
+            if (x >= d.nx) continue;
+            const bool kept = (prev[1] >> lane) & 1u;   // row (y, z): prev holds word w now
+            const bool interior = ryz && x > 0 && x < d.nx - 1;
+            float v;
+            if (!(kept || (interior && ((on >> lane) & 1u)))) {
+                v = mn;
+                row[x] = v;
+            } else {
+                v = row[x];
+                if (FILL && kept) {
+                    v = fmaxf(v, iso);
+                    row[x] = v;
+                }
             }
+            acc.add(v, x, y, z, iso);
+        }
+    }
+    acc.flush(st, true);
+}
+
+// bwlabel() output: 0/1 of the kept set
+__global__ void __launch_bounds__(256) k_write_keep(const unsigned *__restrict__ K, LD d, float *vol) {
+    const int lane = threadIdx.x & 31;
+    for (unsigned r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < d.nrows; r += (gridDim.x * blockDim.x) >> 5) {
+        float *row = vol + (long long)r * d.nx;
+        for (unsigned w = 0; w < d.W; w++) {
+            const unsigned kw = K[(size_t)r * d.W + w];
+            const int x = (int)w * 32 + lane;
+            if (x < d.nx) row[x] = (kw >> lane) & 1u ? 1.0f : 0.0f;
         }
     }
 }
 
-// bwlabel() output: label = 1 + rank of the component's root among roots
-__global__ void k_root_flags(const int *__restrict__ L, long long n, unsigned *flag) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        flag[i] = L[i] == (int)i;
-}
-
-__global__ void k_write_labels(const int *__restrict__ L, long long n, const unsigned *__restrict__ rank, float *vol) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int r = L[i];
-        vol[i] = r < 0 ? 0.0f : (float)(rank[r] + 1u);
+// bwlabel() labels: 1 + rank of the component's root among the roots in
+// raster order.  Roots per word, then (after a scan) each root's rank.
+__global__ void k_root_count(const unsigned *__restrict__ B, LD d, const int *__restrict__ L, unsigned *rc) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nwords; i += gridDim.x * blockDim.x) {
+        const unsigned r = i / d.W, w = i - r * d.W;
+        const unsigned c = class_word(B, d, r, w, 1u), pc = w ? class_word(B, d, r, w - 1, 1u) : 0u;
+        const long long base = (long long)r * d.nx + (long long)w * 32;
+        unsigned n = 0;
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
+            const int s = (int)(base + __ffs(st) - 1);
+            n += L[s] == s;
+        }
+        rc[i] = n;
     }
 }
 
-__global__ void k_write_keep(const unsigned char *__restrict__ keep, long long n, float *vol) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        vol[i] = keep[i] ? 1.0f : 0.0f;
+__global__ void k_root_rank(const unsigned *__restrict__ B, LD d, const int *__restrict__ L,
+                            const unsigned *__restrict__ rc, unsigned *rank) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nwords; i += gridDim.x * blockDim.x) {
+        const unsigned r = i / d.W, w = i - r * d.W;
+        const unsigned c = class_word(B, d, r, w, 1u), pc = w ? class_word(B, d, r, w - 1, 1u) : 0u;
+        const long long base = (long long)r * d.nx + (long long)w * 32;
+        unsigned k = rc[i];
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
+            const int s = (int)(base + __ffs(st) - 1);
+            if (L[s] == s) rank[s] = k++;
+        }
+    }
 }
 
-__global__ void k_nl_from(const unsigned *nroots, const unsigned long long *best, bool only_largest, int *nl) {
-    *nl = only_largest ? (*nroots > 0 ? 1 : 0) : (int)*nroots;
+__global__ void __launch_bounds__(256) k_write_labels(const unsigned *__restrict__ B, LD d, const int *__restrict__ L,
+                                                      const unsigned *__restrict__ rank, float *vol) {
+    const int lane = threadIdx.x & 31;
+    for (unsigned r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < d.nrows; r += (gridDim.x * blockDim.x) >> 5) {
+        float *row = vol + (long long)r * d.nx;
+        const long long base = (long long)r * d.nx;
+        int carry = -1;   // last run start of the words before
+        unsigned pc = 0;
+        for (unsigned w = 0; w < d.W; w++) {
+            const unsigned c = B[(size_t)r * d.W + w];
+            const unsigned starts = c & ~((c << 1) | (pc >> 31));
+            const int x0 = (int)w * 32, x = x0 + lane;
+            if (x < d.nx) {
+                float v = 0.0f;
+                if ((c >> lane) & 1u) {
+                    const int s0 = last_start(starts, x0, lane);
+                    v = (float)(rank[L[base + (s0 >= 0 ? s0 : carry)]] + 1u);
+                }
+                row[x] = v;
+            }
+            if (starts) carry = x0 + 31 - __clz(starts);
+            pc = c;
+        }
+    }
 }
 
 inline unsigned gsz(long long n) {
@@ -291,97 +537,124 @@ inline unsigned gsz(long long n) {
     if (b > 152 * 64) b = 152 * 64;
     return b ? (unsigned)b : 1u;
 }
+// row kernels: one warp per 32/seg rows
+inline unsigned rgrid(const LD &d) {
+    const long long warps = ((long long)d.nrows * d.seg + 31) / 32;
+    return (unsigned)std::max<long long>(1, std::min<long long>((warps + 7) / 8, 152 * 16));
+}
+// one warp per row
+inline unsigned wgrid(const LD &d) {
+    return (unsigned)std::max<long long>(1, std::min<long long>(((long long)d.nrows + 7) / 8, 152 * 16));
+}
 
-n2m_status components(LabelWork &w, Dims d, unsigned char want, int conn, unsigned *d_nroots, cudaStream_t s) {
+LD make_ld(int nx, int ny, int nz) {
+    LD d;
+    d.nx = nx; d.ny = ny; d.nz = nz;
+    d.nxy = (long long)nx * ny;
+    d.n = d.nxy * nz;
+    d.W = (unsigned)(nx + 31) / 32;
+    d.nrows = (unsigned)ny * (unsigned)nz;
+    d.nwords = d.W * d.nrows;
+    d.seg = 1;
+    while (d.seg < 32 && (unsigned)d.seg < d.W) d.seg <<= 1;
+    return d;
+}
+
+n2m_status components(LabelWork &w, const LD &d, unsigned want, int conn, unsigned *d_nroots, unsigned char *z8,
+                      unsigned *z32, cudaStream_t s) {
     int *L = w.lab.as<int>();
-    { k_uf_init<<<gsz(d.n), 256, 0, s>>>(w.mask.as<unsigned char>(), d, want, L); N2M_COUNT(); }
-    const unsigned gr = gsz((long long)d.ny * d.nz * 32);   // one warp per row
-    const unsigned char *m = w.mask.as<unsigned char>();
-    if (conn == 6) { k_uf_merge<3><<<gr, 256, 0, s>>>(m, want, L, d); N2M_COUNT(); }
-    else if (conn == 18) { k_uf_merge<9><<<gr, 256, 0, s>>>(m, want, L, d); N2M_COUNT(); }
-    else { k_uf_merge<13><<<gr, 256, 0, s>>>(m, want, L, d); N2M_COUNT(); }
-    if (d_nroots) CK(cudaMemsetAsync(d_nroots, 0, sizeof(unsigned), s));
-    { k_uf_flatten<<<gsz(d.n), 256, 0, s>>>(L, d.n, d_nroots); N2M_COUNT(); }
+    const unsigned *B = w.mask.as<unsigned>();
+    { k_run_init<<<gsz(d.nwords), 256, 0, s>>>(B, d, want, L, z8, z32); N2M_COUNT(); }
+    if (conn == 6) { k_run_merge<3><<<rgrid(d), 256, 0, s>>>(B, d, want, L); N2M_COUNT(); }
+    else if (conn == 18) { k_run_merge<9><<<rgrid(d), 256, 0, s>>>(B, d, want, L); N2M_COUNT(); }
+    else { k_run_merge<13><<<rgrid(d), 256, 0, s>>>(B, d, want, L); N2M_COUNT(); }
+    { k_run_flatten<<<gsz(d.nwords), 256, 0, s>>>(B, d, want, L, d_nroots); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
 
-// misc layout: [0] nroots bg, [1] nroots fg, [2..3] best (u64), [4] nl
 struct Misc {
     unsigned nbg, nfg;
     unsigned long long best;
     int nl, pad;
 };
 
-n2m_status label_core(LabelWork &w, Dims d, int conn, bool only_largest, bool fill_bubbles, cudaStream_t s) {
+// the class bits in w.mask on entry; *keep: the kept voxels' bits on return
+// (the foreground after filling, or its largest component)
+n2m_status label_core(LabelWork &w, const LD &d, int conn, bool only_largest, bool fill_bubbles, cudaStream_t s,
+                      const unsigned **keep) {
     CKS(w.lab.ensure((size_t)d.n * sizeof(int)));
-    CKS(w.keep.ensure((size_t)d.n));
     CKS(w.misc.ensure(sizeof(Misc)));
     Misc *misc = w.misc.as<Misc>();
     CK(cudaMemsetAsync(misc, 0, sizeof(Misc), s));
+    unsigned *B = w.mask.as<unsigned>();
     if (fill_bubbles) {
         CKS(w.edge.ensure((size_t)d.n));
-        CKS(components(w, d, 0, 6, &misc->nbg, s));
-        CK(cudaMemsetAsync(w.edge.p, 0, (size_t)d.n, s));
-        { k_edge_roots<<<gsz(2 * d.nxy + 2 * (long long)d.nz * (d.nx + d.ny)), 256, 0, s>>>(w.lab.as<int>(), d, w.edge.as<unsigned char>()); N2M_COUNT(); }
-        { k_fill_bubbles<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, w.edge.as<unsigned char>(), &misc->nbg,
-                                                w.mask.as<unsigned char>()); N2M_COUNT(); }
+        CKS(components(w, d, 0u, 6, &misc->nbg, w.edge.as<unsigned char>(), nullptr, s));
+        { k_run_edges<<<rgrid(d), 256, 0, s>>>(B, d, w.lab.as<int>(), w.edge.as<unsigned char>()); N2M_COUNT(); }
+        { k_run_fill<<<rgrid(d), 256, 0, s>>>(B, d, w.lab.as<int>(), w.edge.as<unsigned char>(), &misc->nbg); N2M_COUNT(); }
         CKL();
     }
-    CKS(components(w, d, 1, conn, &misc->nfg, s));
+    if (only_largest) CKS(w.cnt.ensure((size_t)d.n * sizeof(unsigned)));
+    CKS(components(w, d, 1u, conn, &misc->nfg, nullptr, only_largest ? w.cnt.as<unsigned>() : nullptr, s));
+    *keep = B;
     if (only_largest) {
-        CKS(w.cnt.ensure((size_t)d.n * sizeof(unsigned)));
-        CK(cudaMemsetAsync(w.cnt.p, 0, (size_t)d.n * sizeof(unsigned), s));
-        { k_sizes<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, w.cnt.as<unsigned>()); N2M_COUNT(); }
-        { k_best<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), w.cnt.as<unsigned>(), d.n, &misc->best); N2M_COUNT(); }
-        { k_keep_best<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, &misc->best, w.keep.as<unsigned char>()); N2M_COUNT(); }
-    } else {
-        CK(cudaMemcpyAsync(w.keep.p, w.mask.p, (size_t)d.n, cudaMemcpyDeviceToDevice, s));
+        CKS(w.keep.ensure((size_t)d.nwords * sizeof(unsigned)));
+        { k_run_sizes<<<rgrid(d), 256, 0, s>>>(B, d, w.lab.as<int>(), w.cnt.as<unsigned>()); N2M_COUNT(); }
+        { k_run_best<<<gsz(d.nwords), 256, 0, s>>>(B, d, w.lab.as<int>(), w.cnt.as<unsigned>(), &misc->best); N2M_COUNT(); }
+        { k_run_keep<<<rgrid(d), 256, 0, s>>>(B, d, w.lab.as<int>(), &misc->best, w.keep.as<unsigned>()); N2M_COUNT(); }
+        *keep = w.keep.as<unsigned>();
     }
-    { k_nl_from<<<1, 1, 0, s>>>(&misc->nfg, &misc->best, only_largest, &misc->nl); N2M_COUNT(); }
+    { k_nl_from<<<1, 1, 0, s>>>(&misc->nfg, only_largest, &misc->nl); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status class_bits(LabelWork &w, const LD &d, const float *vol, float iso, bool nonzero, cudaStream_t s) {
+    if (d.n > 0x7fffffffLL) {
+        n2m_set_error("labelling supports at most 2^31-1 voxels");
+        return N2M_ERR_TOO_LARGE;
+    }
+    CKS(w.mask.ensure((size_t)d.nwords * sizeof(unsigned)));
+    { k_lab_bits<<<wgrid(d), 256, 0, s>>>(vol, d, iso, nonzero, w.mask.as<unsigned>()); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
 }  // namespace
 
 n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn, bool only_largest,
-                         bool fill_bubbles, LabelWork &w, cudaStream_t s) {
-    Dims d{nx, ny, nz, (long long)nx * ny, (long long)nx * ny * nz};
-    if (d.n > 0x7fffffffLL) {
-        n2m_set_error("labelling supports at most 2^31-1 voxels");
-        return N2M_ERR_TOO_LARGE;
-    }
-    CKS(w.mask.ensure((size_t)d.n));
-    { k_mask<<<gsz(d.n), 256, 0, s>>>(vol, d.n, iso, w.mask.as<unsigned char>()); N2M_COUNT(); }
-    CKL();
-    CKS(label_core(w, d, 18, only_largest, fill_bubbles, s));
-    if (fill_bubbles) { k_fill_iso<<<gsz(d.n), 256, 0, s>>>(vol, d.n, w.keep.as<unsigned char>(), iso); N2M_COUNT(); }
-    if (only_largest) { k_dilate_maskout<<<gsz((long long)d.ny * d.nz * 32), 256, 0, s>>>(w.keep.as<unsigned char>(), d, vol, mn); N2M_COUNT(); }
+                         bool fill_bubbles, LabelWork &w, VolStats *st, cudaStream_t s) {
+    const LD d = make_ld(nx, ny, nz);
+    CKS(class_bits(w, d, vol, iso, false, s));
+    const unsigned *K;
+    CKS(label_core(w, d, 18, only_largest, fill_bubbles, s, &K));
+    const unsigned g = wgrid(d);
+    if (only_largest && fill_bubbles) { k_lab_final<true, true><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
+    else if (only_largest) { k_lab_final<true, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
+    else if (fill_bubbles) { k_lab_final<false, true><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
+    else { k_lab_final<false, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }
 
 n2m_status run_bwlabel(float *vol, int nx, int ny, int nz, int conn, bool only_largest, bool fill_bubbles,
                        LabelWork &w, ScanWork &sw, int *d_nl, cudaStream_t s) {
-    Dims d{nx, ny, nz, (long long)nx * ny, (long long)nx * ny * nz};
-    if (d.n > 0x7fffffffLL) {
-        n2m_set_error("labelling supports at most 2^31-1 voxels");
-        return N2M_ERR_TOO_LARGE;
-    }
-    CKS(w.mask.ensure((size_t)d.n));
-    { k_nonzero<<<gsz(d.n), 256, 0, s>>>(vol, d.n, w.mask.as<unsigned char>()); N2M_COUNT(); }
-    CKL();
-    CKS(label_core(w, d, conn, only_largest, fill_bubbles, s));
+    const LD d = make_ld(nx, ny, nz);
+    CKS(class_bits(w, d, vol, 0.0f, true, s));
+    const unsigned *K;
+    CKS(label_core(w, d, conn, only_largest, fill_bubbles, s, &K));
     if (only_largest) {
-        { k_write_keep<<<gsz(d.n), 256, 0, s>>>(w.keep.as<unsigned char>(), d.n, vol); N2M_COUNT(); }
+        { k_write_keep<<<wgrid(d), 256, 0, s>>>(K, d, vol); N2M_COUNT(); }
     } else {
-        CKS(w.cnt.ensure(((size_t)d.n + 1) * sizeof(unsigned)));
-        unsigned *rank = w.cnt.as<unsigned>();
-        CK(cudaMemsetAsync(rank + d.n, 0, sizeof(unsigned), s));
-        { k_root_flags<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, rank); N2M_COUNT(); }
+        CKS(w.rc.ensure(((size_t)d.nwords + 1) * sizeof(unsigned)));
+        CKS(w.cnt.ensure((size_t)d.n * sizeof(unsigned)));
+        unsigned *rc = w.rc.as<unsigned>();
+        CK(cudaMemsetAsync(rc + d.nwords, 0, sizeof(unsigned), s));
+        { k_root_count<<<gsz(d.nwords), 256, 0, s>>>(K, d, w.lab.as<int>(), rc); N2M_COUNT(); }
         CKL();
-        CKS(scan_u32(rank, (size_t)d.n + 1, rank + d.n, sw, s));
-        { k_write_labels<<<gsz(d.n), 256, 0, s>>>(w.lab.as<int>(), d.n, rank, vol); N2M_COUNT(); }
+        CKS(scan_u32(rc, (size_t)d.nwords + 1, rc + d.nwords, sw, s));
+        { k_root_rank<<<gsz(d.nwords), 256, 0, s>>>(K, d, w.lab.as<int>(), rc, w.cnt.as<unsigned>()); N2M_COUNT(); }
+        { k_write_labels<<<wgrid(d), 256, 0, s>>>(K, d, w.lab.as<int>(), w.cnt.as<unsigned>(), vol); N2M_COUNT(); }
     }
     CK(cudaMemcpyAsync(d_nl, &w.misc.as<Misc>()->nl, sizeof(int), cudaMemcpyDeviceToDevice, s));
     CKL();

@@ -170,10 +170,12 @@ n2m_status scan_u32(unsigned *d, size_t n, unsigned *d_total, ScanWork &w, cudaS
 
 // label.cu
 struct LabelWork {
-    DevBuf lab, mask, keep, cnt, edge, misc;
+    DevBuf lab, mask, keep, cnt, edge, rc, misc;
 };
+// meshify's labelling of vol in place; st: the range and bbox of the result
+// (accumulated into, like launch_stats)
 n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn, bool only_largest,
-                         bool fill_bubbles, LabelWork &w, cudaStream_t s);
+                         bool fill_bubbles, LabelWork &w, VolStats *st, cudaStream_t s);
 // bwlabel() semantics on a float volume (nonzero = foreground); *d_nl gets the label count
 n2m_status run_bwlabel(float *vol, int nx, int ny, int nz, int conn, bool only_largest, bool fill_bubbles,
                        LabelWork &w, ScanWork &sw, int *d_nl, cudaStream_t s);
