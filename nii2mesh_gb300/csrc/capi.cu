@@ -23,6 +23,7 @@
 #include <condition_variable>
 #include <mutex>
 #include <thread>
+#include <unordered_set>
 #include <vector>
 
 #include "n2m_internal.cuh"
@@ -187,7 +188,7 @@ struct n2m_context {
     cudaEvent_t evs[8] = {};   // stage boundaries of the last pipeline run
     cudaEvent_t eva[2] = {};   // around pass A of the exact-on-demand pre-smooth
     bool pass_a = false;       // whether the last pipeline run used it
-    DevBuf in, raw, vol, stmp, stmp2, stats, totals, cand, ncand, lastuse, lubits, pts_raw, tris_raw, pts, tris, ntf, weld,
+    DevBuf in, raw, vol, stmp, stmp2, stats, totals, cand, ncand, ocq, lubits, pts_raw, tris_raw, pts, tris, ntf, weld,
         gath, hmesh;
     OdWork od;   // pre-smooth with exact rounding on demand
     McWork mc;
@@ -278,7 +279,7 @@ extern "C" void n2m_context_destroy(n2m_context *c) {
     DevBuf *bufs[] = {&c->aw.cnt, &c->aw.bb, &c->aw.boxes, &c->aw.queue, &c->aw.arena, &c->aw.mask, &c->aw.keep,
                       &c->aw.lab, &c->aw.edge, &c->aw.ucnt, &c->aw.words, &c->aw.counts, &c->aw.active, &c->aw.tot,
                       &c->aw.pts, &c->aw.pts2, &c->aw.tris, &c->aw.tris2, &c->aw.cand, &c->aw.gath, &c->aw.weld,
-                      &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->raw, &c->vol, &c->stmp, &c->stats, &c->totals, &c->cand, &c->ncand, &c->lastuse, &c->pts_raw,
+                      &c->aw.ranges, &c->alab, &c->lpts, &c->ltris, &c->gA, &c->gB, &c->gs, &c->gtmp, &c->in, &c->raw, &c->vol, &c->stmp, &c->stats, &c->totals, &c->cand, &c->ncand, &c->ocq, &c->pts_raw,
                       &c->tris_raw, &c->pts, &c->tris, &c->ntf, &c->weld, &c->gath, &c->hmesh,
                       &c->mc.words, &c->mc.counts, &c->mc.cand, &c->mc.verts_tmp, &c->mc.tris_tmp, &c->mc.signs, &c->mc.ctr, &c->scan.part,
                       &c->lab.lab, &c->lab.mask, &c->lab.keep, &c->lab.cnt, &c->lab.edge, &c->lab.rc, &c->lab.misc,
@@ -337,17 +338,19 @@ template <class T> n2m_status readback(n2m_context *c, T *dst, const void *dsrc,
     return N2M_OK;
 }
 
-__global__ void k_gather(const vec3d *__restrict__ p, const int *__restrict__ ids, int n, vec3d *out,
-                         const long long *__restrict__ lastuse, long long *lout) {
+__global__ void k_gather(const vec3d *__restrict__ p, const int *__restrict__ ids, int n, vec3d *out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        out[i] = p[ids[i]];
-        if (lastuse) lout[i] = lastuse[ids[i]];
-    }
+    if (i < n) out[i] = p[ids[i]];
 }
 
-__global__ void k_fill_ll(long long *p, size_t n, long long v) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+// corner q = 3*t + c of the triangle list takes vertex v, for n (q, v) pairs
+__global__ void k_set_corners(vec3i *tris, const int2 *__restrict__ qv, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const int t = qv[i].x / 3, c = qv[i].x - 3 * t;
+        int *T = &tris[t].x;
+        T[c] = qv[i].y;
+    }
 }
 
 double dist3(const vec3d &a, const vec3d &b) {
@@ -361,37 +364,21 @@ uint32_t key_bits(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-// Host side of the weld (src/meshify.c:45-106) restricted to the candidates:
-// only vertices within the tolerance of another vertex can merge, and every
-// such vertex is a candidate, so the greedy grouping in key order over the
-// candidates makes exactly the reference's merges.  Outputs the removed ids
-// (sorted), the id each merges into, and position overrides (the group's
-// last writer in the reference's vertex order).
-n2m_status weld_candidates(n2m_context *c, int nv, int ncand, bool oldcubes, std::vector<int> &removed,
-                           std::vector<int> &keep, std::vector<int> &ov_id, std::vector<vec3d> &ov_pos,
-                           std::vector<int> &ov_src, vec3d v0) {
-    std::vector<int> ids(ncand);
-    CK(cudaMemcpyAsync(ids.data(), c->cand.p, ncand * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    std::sort(ids.begin(), ids.end());
-    ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
-    const int n = (int)ids.size();
-    CKS(c->gath.ensure((size_t)n * (sizeof(vec3d) + sizeof(int) + sizeof(long long))));
-    vec3d *dpos = c->gath.as<vec3d>();
-    int *dids = (int *)(dpos + n);
-    long long *dlu = (long long *)(dids + n + (n & 1));
-    CK(cudaMemcpyAsync(dids, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    { k_gather<<<(n + 255) / 256, 256, 0, c->stream>>>(c->pts_raw.as<vec3d>(), dids, n, dpos,
-                                                     oldcubes ? c->lastuse.as<long long>() : nullptr, dlu); N2M_COUNT(); }
-    CKL();
-    std::vector<vec3d> pos(n);
-    std::vector<long long> order(n);
-    CK(cudaMemcpyAsync(pos.data(), dpos, n * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream));
-    if (oldcubes) CK(cudaMemcpyAsync(order.data(), dlu, n * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (!oldcubes)
-        for (int i = 0; i < n; i++) order[i] = ids[i];
-    // sort by (float key, reference order) = the reference's stable radix sort
+struct Prep {
+    const float *vol;
+    float iso, mn, mnp, edge_max;
+    int lo[3], hi[3];
+    bool od = false;          // vol is smoothed approximately: marching cubes makes it exact where it reads it
+    const float *src = nullptr;
+};
+
+// The reference's greedy grouping (src/meshify.c:62-78) over elements with
+// positions pos and reference order `order`: sorted by (float distance to v0,
+// order) as its stable radix sort leaves them, each element not yet in a group
+// seeds a new one that takes every later element within the tolerance, even
+// one already in an earlier group.  Returns the group of every element.
+std::vector<int> weld_groups(const std::vector<vec3d> &pos, const std::vector<long long> &order, vec3d v0, int *ng_out) {
+    const int n = (int)pos.size();
     std::vector<float> key(n);
     std::vector<int> srt(n);
     for (int i = 0; i < n; i++) {
@@ -412,6 +399,58 @@ n2m_status weld_candidates(n2m_context *c, int nv, int ncand, bool oldcubes, std
             if (dist3(pos[a], pos[srt[j]]) < tol) grp[srt[j]] = ng;
         ng++;
     }
+    *ng_out = ng;
+    return grp;
+}
+
+// removed ids (with the id each merges into) and position overrides, sorted by id
+void sort_weld_lists(std::vector<int> &removed, std::vector<int> &keep, std::vector<int> &ov_id,
+                     std::vector<vec3d> &ov_pos, std::vector<int> &ov_src) {
+    std::vector<int> ri(removed.size());
+    for (size_t i = 0; i < ri.size(); i++) ri[i] = (int)i;
+    std::sort(ri.begin(), ri.end(), [&](int a, int b) { return removed[a] < removed[b]; });
+    std::vector<int> r2, k2;
+    for (int i : ri) { r2.push_back(removed[i]); k2.push_back(keep[i]); }
+    removed.swap(r2);
+    keep.swap(k2);
+    std::vector<int> oi(ov_id.size());
+    for (size_t i = 0; i < oi.size(); i++) oi[i] = (int)i;
+    std::sort(oi.begin(), oi.end(), [&](int a, int b) { return ov_id[a] < ov_id[b]; });
+    std::vector<int> o2, s2;
+    std::vector<vec3d> p2;
+    for (int i : oi) { o2.push_back(ov_id[i]); p2.push_back(ov_pos[i]); s2.push_back(ov_src[i]); }
+    ov_id.swap(o2);
+    ov_pos.swap(p2);
+    ov_src.swap(s2);
+}
+
+// Host side of the weld (src/meshify.c:45-106) restricted to the candidates:
+// only vertices within the tolerance of another vertex can merge, and every
+// such vertex is a candidate, so the greedy grouping over the candidates makes
+// exactly the reference's merges.  Lewiner's vertices are shared already, so
+// each is one element in the reference's vertex order.  Outputs the removed
+// ids (sorted), the id each merges into, and position overrides (the group's
+// last writer in the reference's vertex order).
+n2m_status weld_candidates(n2m_context *c, int nv, int ncand, std::vector<int> &removed, std::vector<int> &keep,
+                           std::vector<int> &ov_id, std::vector<vec3d> &ov_pos, std::vector<int> &ov_src, vec3d v0) {
+    std::vector<int> ids(ncand);
+    CK(cudaMemcpyAsync(ids.data(), c->cand.p, ncand * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::sort(ids.begin(), ids.end());
+    ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+    const int n = (int)ids.size();
+    CKS(c->gath.ensure((size_t)n * (sizeof(vec3d) + sizeof(int))));
+    vec3d *dpos = c->gath.as<vec3d>();
+    int *dids = (int *)(dpos + n);
+    CK(cudaMemcpyAsync(dids, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    { k_gather<<<(n + 255) / 256, 256, 0, c->stream>>>(c->pts_raw.as<vec3d>(), dids, n, dpos); N2M_COUNT(); }
+    CKL();
+    std::vector<vec3d> pos(n);
+    CK(cudaMemcpyAsync(pos.data(), dpos, n * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const std::vector<long long> order(ids.begin(), ids.end());   // the reference's vertex order
+    int ng = 0;
+    const std::vector<int> grp = weld_groups(pos, order, v0, &ng);
     // per group: keep the smallest id, position of the last writer
     std::vector<int> gkeep(ng, INT32_MAX), glast(ng, -1), gsize(ng, 0);
     for (int i = 0; i < n; i++) {
@@ -432,24 +471,92 @@ n2m_status weld_candidates(n2m_context *c, int nv, int ncand, bool oldcubes, std
             ov_src.push_back(ids[glast[g]]);
         }
     }
-    // sort removed (with keep) and overrides by id
-    std::vector<int> ri(removed.size());
-    for (size_t i = 0; i < ri.size(); i++) ri[i] = (int)i;
-    std::sort(ri.begin(), ri.end(), [&](int a, int b) { return removed[a] < removed[b]; });
-    std::vector<int> r2, k2;
-    for (int i : ri) { r2.push_back(removed[i]); k2.push_back(keep[i]); }
-    removed.swap(r2);
-    keep.swap(k2);
-    std::vector<int> oi(ov_id.size());
-    for (size_t i = 0; i < oi.size(); i++) oi[i] = (int)i;
-    std::sort(oi.begin(), oi.end(), [&](int a, int b) { return ov_id[a] < ov_id[b]; });
-    std::vector<int> o2, s2;
-    std::vector<vec3d> p2;
-    for (int i : oi) { o2.push_back(ov_id[i]); p2.push_back(ov_pos[i]); s2.push_back(ov_src[i]); }
-    ov_id.swap(o2);
-    ov_pos.swap(p2);
-    ov_src.swap(s2);
+    sort_weld_lists(removed, keep, ov_id, ov_pos, ov_src);
     (void)nv;
+    return N2M_OK;
+}
+
+// The oldcubes weld.  The reference welds a triangle soup: every triangle
+// corner is its own copy of a vertex, at the position the emitting cube's
+// VertexInterp gives (the edge's orientation in that cube), with its own key
+// and its order 3*t + c; the soup's first copy is the origin of the keys.  So
+// the copies of the candidates are the elements here, and a vertex whose
+// copies land in different groups is split: every candidate corner gets its
+// group's vertex (corners: (3*t + c, vertex) pairs), the group's vertex is
+// the smallest member not already another group's, at the position of the
+// group's last copy; members that are no group's vertex are removed.
+n2m_status weld_oc(n2m_context *c, const Prep &P, const int dim[3], int nv, int nt, int ncand, std::vector<int> &removed,
+                   std::vector<int> &keep, std::vector<int> &ov_id, std::vector<vec3d> &ov_pos, std::vector<int> &ov_src,
+                   std::vector<int2> &corners) {
+    const unsigned cap = (unsigned)std::min<long long>(32LL * ncand + 1024, 3LL * nt);
+    CKS(c->lubits.ensure(((size_t)nv + 31) / 32 * sizeof(unsigned)));
+    CKS(c->ocq.ensure(((size_t)cap + 2) * sizeof(unsigned)));
+    unsigned *dq = c->ocq.as<unsigned>(), *dcount = dq + cap + 1;
+    CKS(oc_copies(c->tris_raw.as<vec3i>(), nt, nv, c->cand.as<int>(), ncand, c->lubits.as<unsigned>(), dq, dcount, cap,
+                  c->stream));
+    unsigned ncopy = 0;
+    CKS(readback(c, &ncopy, dcount));
+    if (ncopy > cap) {
+        n2m_set_error("weld copy overflow (%u > %u)", ncopy, cap);
+        return N2M_ERR_INTERNAL;
+    }
+    CK(cudaMemsetAsync(dq + ncopy, 0, sizeof(unsigned), c->stream));   // q = 0: the soup's first copy, the origin
+    const int n = (int)ncopy + 1;
+    CKS(c->gath.ensure((size_t)n * (sizeof(vec3d) + sizeof(int))));
+    vec3d *dpos = c->gath.as<vec3d>();
+    int *dvid = (int *)(dpos + n);
+    CKS(oc_copy_positions(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->tris_raw.as<vec3i>(), dq, n, dvid, dpos,
+                          c->stream));
+    std::vector<unsigned> q(n);
+    std::vector<int> vid(n);
+    std::vector<vec3d> pos(n);
+    CK(cudaMemcpyAsync(q.data(), dq, n * sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(vid.data(), dvid, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(pos.data(), dpos, n * sizeof(vec3d), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const vec3d v0 = pos[ncopy];
+    q.pop_back();
+    vid.pop_back();
+    pos.pop_back();
+    const std::vector<long long> order(q.begin(), q.end());
+    int ng = 0;
+    const std::vector<int> grp = weld_groups(pos, order, v0, &ng);
+    std::vector<int> glast(ng, -1);
+    std::vector<std::vector<int>> gv(ng);   // member vertices of each group
+    for (int i = 0; i < (int)ncopy; i++) {
+        const int g = grp[i];
+        if (glast[g] < 0 || q[i] > q[glast[g]]) glast[g] = i;
+        gv[g].push_back(vid[i]);
+    }
+    std::vector<int> rep(ng, -1);
+    std::unordered_set<int> taken;
+    for (int g = 0; g < ng; g++) {
+        if (glast[g] < 0) continue;   // every member moved on to a later group
+        std::sort(gv[g].begin(), gv[g].end());
+        for (int v : gv[g])
+            if (!taken.count(v)) {
+                rep[g] = v;
+                break;
+            }
+        if (rep[g] < 0) {
+            n2m_set_error("weld: a group with no vertex of its own");
+            return N2M_ERR_INTERNAL;
+        }
+        taken.insert(rep[g]);
+        ov_id.push_back(rep[g]);
+        ov_pos.push_back(pos[glast[g]]);
+        ov_src.push_back(rep[g]);
+    }
+    std::unordered_set<int> seen;
+    for (int i = 0; i < (int)ncopy; i++) {
+        const int r = rep[grp[i]];
+        if (vid[i] != r) corners.push_back(make_int2((int)q[i], r));
+        if (!taken.count(vid[i]) && seen.insert(vid[i]).second) {
+            removed.push_back(vid[i]);
+            keep.push_back(r);
+        }
+    }
+    sort_weld_lists(removed, keep, ov_id, ov_pos, ov_src);
     return N2M_OK;
 }
 
@@ -458,13 +565,6 @@ float half_sum(float a, float b) {   // (float)(0.5 * (a + b)) with a float sum,
     return (float)(0.5 * (double)s);
 }
 
-struct Prep {
-    const float *vol;
-    float iso, mn, mnp, edge_max;
-    int lo[3], hi[3];
-    bool od = false;          // vol is smoothed approximately: marching cubes makes it exact where it reads it
-    const float *src = nullptr;
-};
 
 // stages 1-3: smoothing, range, clustering, bbox
 n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n2m_options &o, bool verbose,
@@ -629,8 +729,6 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
     CK(cudaMemsetAsync(c->ncand.p, 0, 2 * sizeof(unsigned), c->stream));
     McCounts mcn{tot.x, tot.y, tot.z, tot.w};
     if (old) {
-        CKS(c->lastuse.ensure(nv * sizeof(long long)));
-        { k_fill_ll<<<1024, 256, 0, c->stream>>>(c->lastuse.as<long long>(), nv, -1); N2M_COUNT(); }
         CKS(oc_emit(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, mcn, c->pts_raw.as<vec3d>(),
                     c->tris_raw.as<vec3i>(), c->cand.as<int>(), c->ncand.as<unsigned>(), cap, c->stream));
     } else {
@@ -642,11 +740,6 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
     if (nc[0] > (unsigned)cap || nc[1] > (unsigned)cap) {
         n2m_set_error("weld candidate overflow (%u, %u > %d)", nc[0], nc[1], cap);
         return N2M_ERR_INTERNAL;
-    }
-    if (old && nc[0]) {   // the weld orders oldcubes candidates by their last copy
-        CKS(c->lubits.ensure(((size_t)nv + 31) / 32 * sizeof(unsigned)));
-        CKS(oc_lastuse(c->tris_raw.as<vec3i>(), (int)nt, (int)nv, c->cand.as<int>(), (int)nc[0], c->lubits.as<unsigned>(),
-                       c->lastuse.as<long long>(), c->stream));
     }
     if (nc[1]) {   // c-vertex candidates: collect every vertex near them
         CK(cudaMemcpyAsync(c->cand.as<int>() + nc[0], c->cand.as<int>() + cap, nc[1] * sizeof(int),
@@ -704,28 +797,34 @@ n2m_status pipeline(n2m_context *c, const float *d_src, const int dim[3], const 
     int welded = 0;
     c->fwd.nrem = c->fwd.nov = 0;
     if (ncand > 0) {
-        vec3d v0;
-        if (o.cubes == N2M_CUBES_OLDCUBES) {
-            vec3i t0;
-            CKS(readback(c, &t0, c->tris_raw.p));
-            CKS(readback(c, &v0, pts + t0.x));
-        } else {
-            CKS(readback(c, &v0, pts));
-        }
         std::vector<int> removed, keep, ov_id, ov_src;
         std::vector<vec3d> ov_pos;
-        CKS(weld_candidates(c, nv, ncand, o.cubes == N2M_CUBES_OLDCUBES, removed, keep, ov_id, ov_pos, ov_src, v0));
-        if (!removed.empty()) {
-            const int nr = (int)removed.size(), no = (int)ov_id.size();
-            CKS(c->weld.ensure((size_t)(2 * nr + 2 * no + 2) * sizeof(int) + (size_t)(no + 1) * sizeof(vec3d)));
+        std::vector<int2> corners;
+        if (o.cubes == N2M_CUBES_OLDCUBES) {
+            CKS(weld_oc(c, P, dim, nv, nt, ncand, removed, keep, ov_id, ov_pos, ov_src, corners));
+        } else {
+            vec3d v0;
+            CKS(readback(c, &v0, pts));
+            CKS(weld_candidates(c, nv, ncand, removed, keep, ov_id, ov_pos, ov_src, v0));
+        }
+        if (!removed.empty() || !ov_id.empty()) {
+            const int nr = (int)removed.size(), no = (int)ov_id.size(), ncr = (int)corners.size();
+            CKS(c->weld.ensure((size_t)(2 * nr + 2 * no + 2) * sizeof(int) + (size_t)(no + 1) * sizeof(vec3d) +
+                               (size_t)(ncr + 1) * sizeof(int2)));
             vec3d *dov = c->weld.as<vec3d>();
-            int *drem = (int *)(dov + no + 1);
+            int2 *dcr = (int2 *)(dov + no + 1);
+            int *drem = (int *)(dcr + ncr + 1);
             int *dkeep = drem + nr, *dovid = dkeep + nr, *dovsrc = dovid + no + 1;
             if (no) CK(cudaMemcpyAsync(dov, ov_pos.data(), no * sizeof(vec3d), cudaMemcpyHostToDevice, c->stream));
-            CK(cudaMemcpyAsync(drem, removed.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-            CK(cudaMemcpyAsync(dkeep, keep.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            if (nr) CK(cudaMemcpyAsync(drem, removed.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            if (nr) CK(cudaMemcpyAsync(dkeep, keep.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
             if (no) CK(cudaMemcpyAsync(dovid, ov_id.data(), no * sizeof(int), cudaMemcpyHostToDevice, c->stream));
             if (no) CK(cudaMemcpyAsync(dovsrc, ov_src.data(), no * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            if (ncr) {   // split vertices: corners take their copy's group vertex before the renumbering
+                CK(cudaMemcpyAsync(dcr, corners.data(), ncr * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+                { k_set_corners<<<(ncr + 255) / 256, 256, 0, c->stream>>>(c->tris_raw.as<vec3i>(), dcr, ncr); N2M_COUNT(); }
+                CKL();
+            }
             c->fwd.removed = drem;
             c->fwd.ov_id = dovid;
             c->fwd.ov_src = dovsrc;

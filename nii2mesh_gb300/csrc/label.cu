@@ -222,7 +222,10 @@ __global__ void __launch_bounds__(256) k_run_merge(const unsigned *__restrict__ 
     }
 }
 
-// every run start of the class points at its root; roots are counted
+// every run start of the class points at its root; roots are counted.  The
+// root search only reads: the one store of this kernel is a start's final
+// root (a path-halving store could overwrite a root another thread has just
+// stored with a lower ancestor).
 __global__ void k_run_flatten(const unsigned *__restrict__ B, LD d, unsigned want, int *L, unsigned *nroots) {
     unsigned cnt = 0;
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nwords; i += gridDim.x * blockDim.x) {
@@ -231,7 +234,7 @@ __global__ void k_run_flatten(const unsigned *__restrict__ B, LD d, unsigned wan
         const long long base = (long long)r * d.nx + (long long)w * 32;
         for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
             const int s = (int)(base + __ffs(st) - 1);
-            const int root = find_halve(L, s);
+            const int root = find_root(L, s);
             if (root == s) cnt++;
             else L[s] = root;
         }
@@ -240,36 +243,52 @@ __global__ void k_run_flatten(const unsigned *__restrict__ B, LD d, unsigned wan
     if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(nroots, cnt);
 }
 
-// Background components touching a face of the volume: every run of a row on
-// a y or z face, and the runs holding x = 0 and x = nx-1 of every row, flag
-// their root.
-__global__ void __launch_bounds__(256) k_run_edges(const unsigned *__restrict__ B, LD d, const int *__restrict__ L,
-                                                   unsigned char *edge) {
-    const int lane = threadIdx.x & 31, seg = d.seg, li = lane & (seg - 1);
-    const unsigned rpw = 32u / (unsigned)seg, rsub = (unsigned)lane / (unsigned)seg;
-    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
-    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < d.nrows; rb += nw * rpw) {
-        const unsigned r = rb + rsub;
-        const bool rowok = r < d.nrows;
-        const int z = rowok ? (int)(r / (unsigned)d.ny) : 0, y = rowok ? (int)(r - (unsigned)z * (unsigned)d.ny) : 0;
-        const bool face = y == 0 || z == 0 || y == d.ny - 1 || z == d.nz - 1;
-        const long long base = (long long)r * d.nx;
-        int cst = -1;
-        unsigned cwd = 0;
-        for (unsigned c0 = 0; c0 < d.W; c0 += (unsigned)seg) {
-            const unsigned w = c0 + (unsigned)li;
-            const unsigned c = rowok && w < d.W ? class_word(B, d, r, w, 0u) : 0u;
-            const WordRuns R = word_runs(c, (int)w * 32, li, seg, cst, cwd);
-            if (!c) continue;
-            if (face)
-                for (unsigned st = R.starts; st; st &= st - 1) edge[L[base + R.x0 + __ffs(st) - 1]] = 1;
-            else if (w == 0 && (c & 1u))
-                edge[L[base]] = 1;
-            if (!face && w == d.W - 1) {
-                const int b = (d.nx - 1) & 31;
-                if ((c >> b) & 1u) edge[L[base + R.start_of(b)]] = 1;
+// Background components touching a face of the volume flag their root:
+// items [0, nrows) take the runs holding x = 0 and x = nx-1 of a row, the items
+// after them one word each of the rows on a y or z face (every run in it).  A
+// flag is stored only if it is not set yet (most items name the same root).
+__global__ void k_run_edges(const unsigned *__restrict__ B, LD d, const int *__restrict__ L, unsigned char *edge) {
+    const unsigned nzf = d.nz > 1 ? 2u : 1u, nyf = d.ny > 1 ? 2u : 1u;
+    const unsigned zrows = nzf * (unsigned)d.ny, yrows = d.nz > 2 ? nyf * (unsigned)(d.nz - 2) : 0u;
+    const unsigned total = d.nrows + (zrows + yrows) * d.W;
+    auto mark = [&](long long j) {
+        const int root = L[j];
+        if (!edge[root]) edge[root] = 1;
+    };
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        if (t < d.nrows) {
+            const unsigned r = t;
+            const long long base = (long long)r * d.nx;
+            if (class_word(B, d, r, 0, 0u) & 1u) mark(base);
+            unsigned w = d.W - 1;
+            int b = (d.nx - 1) & 31;
+            unsigned c = class_word(B, d, r, w, 0u);
+            if (!((c >> b) & 1u)) continue;
+            for (;;) {   // back to the run's start (x = 0 of a background run is one)
+                const unsigned pc = w ? class_word(B, d, r, w - 1, 0u) : 0u;
+                const int ls = last_start(c & ~((c << 1) | (pc >> 31)), (int)w * 32, b);
+                if (ls >= 0) {
+                    mark(base + ls);
+                    break;
+                }
+                w--;
+                b = 31;
+                c = pc;
             }
+            continue;
         }
+        const unsigned u = t - d.nrows, fr = u / d.W, w = u - fr * d.W;
+        unsigned r;
+        if (fr < zrows) {   // slices z = 0 and z = nz-1
+            const unsigned side = fr / (unsigned)d.ny, y = fr - side * (unsigned)d.ny;
+            r = (side ? (unsigned)(d.nz - 1) * (unsigned)d.ny : 0u) + y;
+        } else {            // rows y = 0 and y = ny-1 of the slices between
+            const unsigned v = fr - zrows, side = v / (unsigned)(d.nz - 2), z = 1 + v - side * (unsigned)(d.nz - 2);
+            r = z * (unsigned)d.ny + (side ? (unsigned)(d.ny - 1) : 0u);
+        }
+        const unsigned c = class_word(B, d, r, w, 0u), pc = w ? class_word(B, d, r, w - 1, 0u) : 0u;
+        const long long base = (long long)r * d.nx + (long long)w * 32;
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) mark(base + __ffs(st) - 1);
     }
 }
 
@@ -392,7 +411,9 @@ __global__ void k_nl_from(const unsigned *nroots, bool only_largest, int *nl) {
 // src/meshify.c:218-264) become mn and are not read.  With R3 = K(x-1) | K(x) |
 // K(x+1) and R2 = K(x) | K(x+1) of a row, the dilation is R3 of rows y-1..y+1
 // in slices z and z+1, R3 of rows y and y+1 in slice z-1, and R2 of row y-1 in
-// slice z-1.
+// slice z-1.  The keep words of a row are loaded 32 at a time (lane l holds
+// word c0 + l) and broadcast; 32 words with no kept voxel within reach are
+// written without being read.
 template <bool LARGEST, bool FILL>
 __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ K, LD d, float *vol, float iso, float mn,
                                                    VolStats *st) {
@@ -406,16 +427,21 @@ __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ 
         float *row = vol + (long long)r * d.nx;
         if (!LARGEST) {
             const unsigned *K0 = K + (size_t)r * d.W;
-            for (unsigned w = 0; w < d.W; w++) {
-                const unsigned kw = K0[w];
-                const int x = (int)w * 32 + lane;
-                if (x >= d.nx) continue;
-                float v = row[x];
-                if (FILL && ((kw >> lane) & 1u)) {
-                    v = fmaxf(v, iso);
-                    row[x] = v;
+            for (unsigned c0 = 0; c0 < d.W; c0 += 32) {
+                const unsigned kk = c0 + lane < d.W ? K0[c0 + lane] : 0u;
+                const unsigned wend = min(d.W, c0 + 32);
+#pragma unroll 4
+                for (unsigned w = c0; w < wend; w++) {
+                    const unsigned kw = __shfl_sync(FULL, kk, (int)(w - c0));
+                    const int x = (int)w * 32 + lane;
+                    if (x >= d.nx) continue;
+                    float v = row[x];
+                    if (FILL && ((kw >> lane) & 1u)) {
+                        v = fmaxf(v, iso);
+                        row[x] = v;
+                    }
+                    acc.add(v, x, y, z, iso);
                 }
-                acc.add(v, x, y, z, iso);
             }
             continue;
         }
@@ -426,38 +452,58 @@ __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ 
             const int yy = y + DY[k], zz = z + DZ[k];
             Kr[k] = yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz ? K + ((size_t)zz * d.ny + yy) * d.W : nullptr;
         }
-        unsigned prev[9], cur[9];
+        unsigned carry[9];   // word c0 - 1 of each row
 #pragma unroll
-        for (int k = 0; k < 9; k++) {
-            prev[k] = 0u;
-            cur[k] = Kr[k] ? Kr[k][0] : 0u;
-        }
-        for (unsigned w = 0; w < d.W; w++) {
-            unsigned on = 0u;
+        for (int k = 0; k < 9; k++) carry[k] = 0u;
+        for (unsigned c0 = 0; c0 < d.W; c0 += 32) {
+            unsigned kk[9], nk[9];
+            unsigned any = 0u, edge = 0u;
 #pragma unroll
             for (int k = 0; k < 9; k++) {
-                const unsigned nxt = Kr[k] && w + 1 < d.W ? Kr[k][w + 1] : 0u;
-                const unsigned right = (cur[k] >> 1) | (nxt << 31);   // K(x+1)
-                on |= cur[k] | right | (k < 8 ? (cur[k] << 1) | (prev[k] >> 31) : 0u);   // row 8: no K(x-1)
-                prev[k] = cur[k];
-                cur[k] = nxt;
+                kk[k] = Kr[k] && c0 + lane < d.W ? Kr[k][c0 + lane] : 0u;
+                nk[k] = Kr[k] && c0 + 32 < d.W ? Kr[k][c0 + 32] : 0u;   // the word after the chunk
+                any |= kk[k];
+                edge |= (carry[k] >> 31) | (nk[k] & 1u);
             }
-            const int x = (int)w * 32 + lane;
-            if (x >= d.nx) continue;
-            const bool kept = (prev[1] >> lane) & 1u;   // row (y, z): prev holds word w now
-            const bool interior = ryz && x > 0 && x < d.nx - 1;
-            float v;
-            if (!(kept || (interior && ((on >> lane) & 1u)))) {
-                v = mn;
-                row[x] = v;
+            const unsigned wend = min(d.W, c0 + 32);
+            if (!__any_sync(FULL, any != 0u) && !edge) {   // nothing kept within reach: all mn
+                const int xe = min(d.nx, (int)wend * 32);
+                for (int x = (int)c0 * 32 + lane; x < xe; x += 32) row[x] = mn;
+                acc.mn = fminf(acc.mn, mn);
+                acc.mx = fmaxf(acc.mx, mn);
             } else {
-                v = row[x];
-                if (FILL && kept) {
-                    v = fmaxf(v, iso);
-                    row[x] = v;
+                for (unsigned w = c0; w < wend; w++) {
+                    const int l = (int)(w - c0);
+                    unsigned on = 0u, kept0 = 0u;
+#pragma unroll
+                    for (int k = 0; k < 9; k++) {
+                        const unsigned cur = __shfl_sync(FULL, kk[k], l);
+                        const unsigned prv = l ? __shfl_sync(FULL, kk[k], l - 1) : carry[k];
+                        const unsigned nxt = l < 31 ? __shfl_sync(FULL, kk[k], l + 1) : nk[k];
+                        const unsigned right = (cur >> 1) | (nxt << 31);   // K(x+1)
+                        on |= cur | right | (k < 8 ? (cur << 1) | (prv >> 31) : 0u);   // row 8: no K(x-1)
+                        if (k == 1) kept0 = cur;
+                    }
+                    const int x = (int)w * 32 + lane;
+                    if (x >= d.nx) continue;
+                    const bool kept = (kept0 >> lane) & 1u;
+                    const bool interior = ryz && x > 0 && x < d.nx - 1;
+                    float v;
+                    if (!(kept || (interior && ((on >> lane) & 1u)))) {
+                        v = mn;
+                        row[x] = v;
+                    } else {
+                        v = row[x];
+                        if (FILL && kept) {
+                            v = fmaxf(v, iso);
+                            row[x] = v;
+                        }
+                    }
+                    acc.add(v, x, y, z, iso);
                 }
             }
-            acc.add(v, x, y, z, iso);
+#pragma unroll
+            for (int k = 0; k < 9; k++) carry[k] = __shfl_sync(FULL, kk[k], 31);
         }
     }
     acc.flush(st, true);
@@ -591,7 +637,7 @@ n2m_status label_core(LabelWork &w, const LD &d, int conn, bool only_largest, bo
     if (fill_bubbles) {
         CKS(w.edge.ensure((size_t)d.n));
         CKS(components(w, d, 0u, 6, &misc->nbg, w.edge.as<unsigned char>(), nullptr, s));
-        { k_run_edges<<<rgrid(d), 256, 0, s>>>(B, d, w.lab.as<int>(), w.edge.as<unsigned char>()); N2M_COUNT(); }
+        { k_run_edges<<<gsz((long long)d.nrows + 4ll * (d.nx + d.ny + d.nz) * d.W), 256, 0, s>>>(B, d, w.lab.as<int>(), w.edge.as<unsigned char>()); N2M_COUNT(); }
         { k_run_fill<<<rgrid(d), 256, 0, s>>>(B, d, w.lab.as<int>(), w.edge.as<unsigned char>(), &misc->nbg); N2M_COUNT(); }
         CKL();
     }

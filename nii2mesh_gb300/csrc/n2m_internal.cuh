@@ -254,9 +254,16 @@ n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const i
 n2m_status oc_emit(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso, float edge_max,
                     McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris, int *d_cand, unsigned *d_ncand,
                     int cand_cap, cudaStream_t s);
-// the last copy (3*triangle + corner) of each of the ncand weld candidates; d_bits: nv bits of scratch
-n2m_status oc_lastuse(const vec3i *d_tris, int nt, int nv, const int *d_cand, int ncand, unsigned *d_bits,
-                      long long *d_lastuse, cudaStream_t s);
+// the copies of the ncand weld candidates in the reference's triangle soup: every
+// corner 3*t + c naming one, into d_out (at most cap; *d_count = how many there
+// are); d_bits: nv bits of scratch
+n2m_status oc_copies(const vec3i *d_tris, int nt, int nv, const int *d_cand, int ncand, unsigned *d_bits,
+                     unsigned *d_out, unsigned *d_count, unsigned cap, cudaStream_t s);
+// the vertex id each listed corner names and the position the cube that emitted
+// its triangle interpolates for it (needs oc_count's words of the same grid)
+n2m_status oc_copy_positions(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso,
+                             float edge_max, const McWork &w, const vec3i *d_tris, const unsigned *d_q, int n, int *d_vid,
+                             vec3d *d_pos, cudaStream_t s);
 
 // mesh.cu
 n2m_status mesh_apply_weld(vec3d *d_pts, vec3i *d_tris, int np, int nt, const int *d_removed, const int *d_keep,

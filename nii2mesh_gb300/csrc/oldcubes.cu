@@ -396,16 +396,76 @@ __global__ void k_oc_candbits(const int *__restrict__ cand, unsigned ncand, unsi
     }
 }
 
-// last copy of every candidate vertex: the largest 3*triangle + corner that names it
-__global__ void k_oc_lastuse(const vec3i *__restrict__ tris, unsigned nt, const unsigned *__restrict__ bits,
-                             long long *lastuse) {
+// every triangle corner (3*t + c) that names a weld candidate (bit set)
+__global__ void k_oc_copies(const vec3i *__restrict__ tris, unsigned nt, const unsigned *__restrict__ bits,
+                            unsigned *out, unsigned *count, unsigned cap) {
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
         const vec3i T = tris[t];
         const int v[3] = {T.x, T.y, T.z};
 #pragma unroll
         for (int c = 0; c < 3; c++)
-            if ((__ldg(bits + ((unsigned)v[c] >> 5)) >> ((unsigned)v[c] & 31u)) & 1u)
-                atomicMax(&lastuse[v[c]], 3ll * t + c);
+            if ((__ldg(bits + ((unsigned)v[c] >> 5)) >> ((unsigned)v[c] & 31u)) & 1u) {
+                const unsigned k = atomicAdd(count, 1u);
+                if (k < cap) out[k] = 3u * t + (unsigned)c;
+            }
+    }
+}
+
+// Bourke's corners (bit 0: +x, 1: +y, 2: +z) and each edge's two corners, in
+// the order VertexInterp takes them (src/oldcubes.c:418-441)
+__constant__ unsigned char c_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+__constant__ unsigned char c_edge_ab[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                               {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+// The copy of a vertex that corner q = 3t + c holds in the reference's
+// triangle soup: the cube that emitted triangle t (the word whose triangle
+// range holds t, then the cube within it) and the position that cube's
+// VertexInterp gives, in the edge's orientation within that cube.
+__global__ void k_oc_copy_pos(OV g, const unsigned *__restrict__ signs, const uint4 *__restrict__ offs, unsigned nwords,
+                              const vec3i *__restrict__ tris, const unsigned *__restrict__ qs, unsigned n, int *vid,
+                              vec3d *pos) {
+    const unsigned WX = g.WX, slice = WX * (unsigned)g.NY;
+    const double iso = (double)g.iso;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned q = qs[i], t = q / 3u, c = q - 3u * t;
+        unsigned lo = 0, hi = nwords - 1;   // the last word whose first triangle is <= t
+        while (lo < hi) {
+            const unsigned mid = lo + (hi - lo + 1) / 2;
+            if (offs[mid].y <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const unsigned w = lo, row = w / WX, xw = w - row * WX;
+        const int z = (int)(row / (unsigned)g.NY), y = (int)(row - (unsigned)z * (unsigned)g.NY), x0 = (int)xw * 32;
+        const bool nx = xw + 1 < WX;
+        const unsigned hxm = x0 + 33 <= g.NX ? 0xffffffffu : (g.NX - 1 - x0 > 0 ? (1u << (g.NX - 1 - x0)) - 1u : 0u);
+        const unsigned a0 = signs[w], b0 = signs[w + WX], c0 = signs[w + slice], d0 = signs[w + slice + WX];
+        const unsigned a1 = __funnelshift_r(a0, nx ? signs[w + 1] : 0u, 1), b1 = __funnelshift_r(b0, nx ? signs[w + WX + 1] : 0u, 1),
+                       c1 = __funnelshift_r(c0, nx ? signs[w + slice + 1] : 0u, 1),
+                       d1 = __funnelshift_r(d0, nx ? signs[w + slice + WX + 1] : 0u, 1);
+        unsigned k = t - offs[w].y;
+        int p = 0, ci = 0;
+        for (unsigned mix = (a0 | a1 | b0 | b1 | c0 | c1 | d0 | d1) & ~(a0 & a1 & b0 & b1 & c0 & c1 & d0 & d1) & hxm; mix;
+             mix &= mix - 1) {
+            p = __ffs(mix) - 1;
+            ci = ocube_index(a0, a1, b0, b1, c0, c1, d0, d1, p);
+            const unsigned nc = (unsigned)ocube_ntri(ci);
+            if (k < nc) break;
+            k -= nc;
+        }
+        const int e = d_tri[ci * 16 + 3 * (int)k + (int)c];
+        const unsigned ca = c_corner[c_edge_ab[e][0]], cb = c_corner[c_edge_ab[e][1]];
+        const int X = g.lo0 + x0 + p, Y = g.lo1 + y, Z = g.lo2 + z;
+        const int ax = X + (int)(ca & 1u), ay = Y + (int)((ca >> 1) & 1u), az = Z + (int)(ca >> 2);
+        const int bx = X + (int)(cb & 1u), by = Y + (int)((cb >> 1) & 1u), bz = Z + (int)(cb >> 2);
+        const double va = oval(g, ax, ay, az), vb = oval(g, bx, by, bz);
+        const double mu = __ddiv_rn(__dsub_rn(iso, va), __dsub_rn(vb, va));
+        vec3d P = {(double)ax, (double)ay, (double)az};
+        if (ax != bx) P.x = __dadd_rn(P.x, __dmul_rn(mu, (double)(bx - ax)));
+        if (ay != by) P.y = __dadd_rn(P.y, __dmul_rn(mu, (double)(by - ay)));
+        if (az != bz) P.z = __dadd_rn(P.z, __dmul_rn(mu, (double)(bz - az)));
+        const vec3i T = tris[t];
+        vid[i] = c == 0 ? T.x : (c == 1 ? T.y : T.z);
+        pos[i] = P;
     }
 }
 
@@ -488,11 +548,23 @@ n2m_status oc_emit(const float *vol, const int dim[3], const int lo[3], const in
     return N2M_OK;
 }
 
-n2m_status oc_lastuse(const vec3i *d_tris, int nt, int nv, const int *d_cand, int ncand, unsigned *d_bits,
-                      long long *d_lastuse, cudaStream_t s) {
+n2m_status oc_copies(const vec3i *d_tris, int nt, int nv, const int *d_cand, int ncand, unsigned *d_bits,
+                     unsigned *d_out, unsigned *d_count, unsigned cap, cudaStream_t s) {
     CK(cudaMemsetAsync(d_bits, 0, (size_t)(nv + 31) / 32 * sizeof(unsigned), s));
+    CK(cudaMemsetAsync(d_count, 0, sizeof(unsigned), s));
     { k_oc_candbits<<<(unsigned)std::max(1, std::min((ncand + 255) / 256, 1024)), 256, 0, s>>>(d_cand, (unsigned)ncand, d_bits); N2M_COUNT(); }
-    { k_oc_lastuse<<<(unsigned)std::max(1, std::min((nt + 255) / 256, 152 * 16)), 256, 0, s>>>(d_tris, (unsigned)nt, d_bits, d_lastuse); N2M_COUNT(); }
+    { k_oc_copies<<<(unsigned)std::max(1, std::min((nt + 255) / 256, 152 * 16)), 256, 0, s>>>(d_tris, (unsigned)nt, d_bits, d_out, d_count, cap); N2M_COUNT(); }
+    CKL();
+    return N2M_OK;
+}
+
+n2m_status oc_copy_positions(const float *vol, const int dim[3], const int lo[3], const int hi[3], float iso,
+                             float edge_max, const McWork &w, const vec3i *d_tris, const unsigned *d_q, int n, int *d_vid,
+                             vec3d *d_pos, cudaStream_t s) {
+    const OV g = make_ov(vol, dim, lo, hi, iso, edge_max);
+    const size_t nwords = (size_t)g.WX * g.NY * g.NZ;
+    if (n <= 0 || nwords == 0) return N2M_OK;
+    { k_oc_copy_pos<<<(unsigned)std::min((n + 127) / 128, 1024), 128, 0, s>>>(g, w.signs.as<unsigned>(), w.counts.as<uint4>(), (unsigned)nwords, d_tris, d_q, (unsigned)n, d_vid, d_pos); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

@@ -74,6 +74,21 @@ def test_bwlabel_vs_oracle_random(gpu, oracle):
                 assert na == nb and np.array_equal(a, b), (shape, conn, ol, fb)
 
 
+def test_bwlabel_vs_oracle_ct_mask(gpu, oracle):
+    """a 200^3 CT-like mask (hundreds of thousands of components, one
+    background component spanning the volume, rows of 7 words): every
+    connectivity and option set equals the oracle, on repeated calls (a race
+    in the labelling would show as a few voxels that differ between calls)"""
+    from nii2mesh_gb300 import synth
+    img = (synth.ct512(n=200) >= 300.0).astype(np.float32)
+    for conn in (6, 18, 26):
+        for ol, fb in ((False, False), (True, False), (False, True), (True, True)):
+            b, nb = oracle.bwlabel(img, conn, ol, fb)
+            for _ in range(2):
+                a, na = gpu.bwlabel(img, conn, ol, fb)
+                assert na == nb and np.array_equal(a, b), (conn, ol, fb, int((a != b).sum()))
+
+
 def test_hc_golden(gpu):
     hc = np.load(GOLD / "hc.npz")
     t, p = hc["tris"], hc["pts"]

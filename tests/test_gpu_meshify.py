@@ -97,6 +97,21 @@ def test_brain182_full_options(gpu, oracle, variant):
     ctx.close()
 
 
+@pytest.mark.parametrize("variant", [MC33, OLDCUBES])
+def test_ct_labelling_256(gpu, oracle, variant):
+    """-p 1 -l 1 -b 1 on a 256^3 CT-like volume through the device entry
+    point, three calls in a row: the oracle's mesh every time"""
+    vol = synth.ct512(n=256)
+    want = oracle.meshify(vol, 300.0, variant, True, True, True)
+    ctx = gpu.Context(0)
+    cubes = gpu.OLDCUBES if variant == OLDCUBES else gpu.MC33
+    for _ in range(3):
+        got = device_mesh(gpu, ctx, vol, 300.0, cubes, True, True)
+        ok, d, msg = mesh_equal(got, want, POS_TOL)
+        assert ok, msg
+    ctx.close()
+
+
 def test_selftest_fields_meshify(gpu, oracle):
     """the reference's analytic self-test fields through the whole pipeline"""
     for obj in range(10):
