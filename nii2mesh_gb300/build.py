@@ -19,8 +19,12 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libn2m_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
          "-I", str(CSRC), "-I", str(PKG.parent / "include")]
+# units with bit-exact floating-point duties: smoothing, marching cubes (both
+# builds), the weld and degenerate filter, sform, Otsu, the NIfTI cast, the
+# batched atlas, the text writers and the host-side glue
+EXACT = {"smooth", "mc", "oldcubes", "mesh", "isolevel", "decode", "atlas", "writers", "capi"}
 
 
 def nvcc():
@@ -44,7 +48,8 @@ def build(verbose=False, force=False, extra=()):
 
     def compile_one(src):
         obj = OUT / (src.stem + ".o")
-        cmd = [cc, *ARCH, *FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+        fmad = ["--fmad=false"] if src.stem in EXACT else []
+        cmd = [cc, *ARCH, *FLAGS, *fmad, *extra, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stderr}")
