@@ -194,6 +194,7 @@ struct n2m_context {
     McWork mc;
     ScanWork scan;
     LabelWork lab;
+    LabelPost lpost{};
     DegWork deg;
     HcWork hc;
     ThresholdWork th;
@@ -370,6 +371,7 @@ struct Prep {
     int lo[3], hi[3];
     bool od = false;          // vol is smoothed approximately: marching cubes makes it exact where it reads it
     const float *src = nullptr;
+    const LabelPost *post = nullptr;   // with od: what the clustering did to vol
 };
 
 // The reference's greedy grouping (src/meshify.c:62-78) over elements with
@@ -588,12 +590,13 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     }
     if (!smooth && label) CK(cudaMemcpyAsync(vol, d_src, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaEventRecord(c->evs[0], c->stream));
-    // Marching cubes straight after the pre-smooth (no clustering), volume already in
-    // device memory: exact rounding on demand (only where marching cubes reads values).
+    // Volume already in device memory: exact rounding on demand (only where marching
+    // cubes reads values), also under -l 1 clustering, whose mask is pass A's sign
+    // bitmap and whose result's minimum is the volume's once any voxel is masked out.
     // Otherwise the exact three passes; a volume arriving from host memory in slabs is
     // smoothed while it arrives that way (the on-demand repair could only start after
     // the last slab)
-    bool od = smooth && !label && !c->stage.host && od_eligible(d_src, nx, ny, nz);
+    bool od = smooth && (!label || o.only_largest) && !c->stage.host && od_eligible(d_src, nx, ny, nz);
     if (smooth) {
         CKS(c->stmp.ensure(n * sizeof(float)));
         const StagedInput *stage = c->stage.host ? &c->stage : nullptr;
@@ -603,7 +606,7 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
             CKS(od_approx(d_src, vol, nx, ny, nz, iso, c->od, c->stream, stage));
             CK(cudaEventRecord(c->eva[1], c->stream));
             c->pass_a = true;
-            CKS(od_resolve(d_src, vol, nx, ny, nz, iso, c->od, dst, c->stream, &fallback, o.cubes == N2M_CUBES_OLDCUBES));
+            CKS(od_resolve(d_src, vol, nx, ny, nz, iso, c->od, dst, c->stream, &fallback, label || o.cubes == N2M_CUBES_OLDCUBES));
             if (fallback) {   // the input is on the device by now
                 od = false;
                 CK(cudaMemcpyAsync(dst, h, sizeof(VolStats), cudaMemcpyHostToDevice, c->stream));
@@ -643,9 +646,19 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     VolStats s1 = s0;
     float min_after = mn;
     if (label) {
-        CKS(run_labelling(vol, nx, ny, nz, iso, mn, o.only_largest, o.fill_bubbles, c->lab, dst + 1, c->stream));
+        // (a stale isolevel's exact smoothing above left its statistics there)
+        CK(cudaMemcpyAsync(dst + 1, &h[1], sizeof(VolStats), cudaMemcpyHostToDevice, c->stream));
+        CKS(run_labelling(vol, nx, ny, nz, iso, mn, o.only_largest, o.fill_bubbles, c->lab, dst + 1, c->stream,
+                          od ? c->od.vsign.as<unsigned>() : nullptr, &c->lpost));
         CKS(readback(c, &s1, dst + 1));
-        min_after = ord2f(s1.vmin);
+        if (od && s1.masked == 0) {   // nothing masked out: the minimum is the labelled values': smooth exactly
+            od = false;
+            CK(cudaMemcpyAsync(dst, h, 2 * sizeof(VolStats), cudaMemcpyHostToDevice, c->stream));
+            CKS(launch_smooth(d_src, vol, c->stmp.as<float>(), nx, ny, nz, iso, dst, c->stream, nullptr));
+            CKS(run_labelling(vol, nx, ny, nz, iso, mn, o.only_largest, o.fill_bubbles, c->lab, dst + 1, c->stream));
+            CKS(readback(c, &s1, dst + 1));
+        }
+        min_after = od ? mn : ord2f(s1.vmin);   // masked voxels hold mn, every exact value is >= mn
     } else if (stale) {
         CKS(launch_stats(v, nx, ny, nz, iso, false, dst + 1, c->stream));
         CKS(readback(c, &s1, dst + 1));
@@ -663,6 +676,7 @@ n2m_status prepare(n2m_context *c, const float *d_src, const int dim[3], const n
     P.mn = mn;
     P.od = od;
     P.src = d_src;
+    P.post = od && label ? &c->lpost : nullptr;
     for (int i = 0; i < 3; i++) {
         P.lo[i] = std::max(s1.lo[i] - 1, 0);
         P.hi[i] = std::min(s1.hi[i] + 2, dim[i]);
@@ -703,7 +717,7 @@ n2m_status march(n2m_context *c, const Prep &P, const int dim[3], int cubes, int
         const size_t n = (size_t)dim[0] * dim[1] * dim[2];
         CKS(c->stmp2.ensure(n * sizeof(float)));
         const OdRepair rep{P.src, c->stmp.as<float>(), c->stmp2.as<float>(), (float *)P.vol, {dim[0], dim[1], dim[2]},
-                           &c->od, &c->scan};
+                           &c->od, &c->scan, P.post};
         if (old) CKS(oc_count(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->scan, dtot, c->stream, &rep));
         else CKS(mc_count(g, cubes, c->mc, c->scan, dtot, c->stream, &rep));
     } else if (old) CKS(oc_count(P.vol, dim, P.lo, P.hi, P.iso, P.edge_max, c->mc, c->scan, dtot, c->stream));

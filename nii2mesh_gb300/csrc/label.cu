@@ -131,6 +131,15 @@ __global__ void __launch_bounds__(256) k_lab_bits(const float *__restrict__ vol,
     }
 }
 
+// Class bits from a sign bitmap (bit = value >= iso; OdWork::vsign layout:
+// wv = W words per row, the 8 row words of a 32 x 8 tile of a slice adjacent)
+__global__ void k_lab_bits_vsign(const unsigned *__restrict__ vsign, LD d, unsigned nys, unsigned *B) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nwords; i += gridDim.x * blockDim.x) {
+        const unsigned r = i / d.W, w = i - r * d.W, z = r / (unsigned)d.ny, y = r - z * (unsigned)d.ny;
+        B[i] = __ldg(vsign + od_vsign_word(w * 32u, y, z, d.W, nys)) & valid_bits(d, w);
+    }
+}
+
 // every run start of the class links to itself; z8 / z32 (may be null) are
 // zeroed at the run starts (the edge flags and sizes the roots will carry)
 __global__ void k_run_init(const unsigned *__restrict__ B, LD d, unsigned want, int *L, unsigned char *z8,
@@ -419,6 +428,7 @@ __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ 
                                                    VolStats *st) {
     smooth::Acc acc;
     acc.init();
+    unsigned masked = 0;
     const int lane = threadIdx.x & 31;
     // rows used: 0..2 = y-1..y+1 in slice z, 3..5 in slice z+1, 6 = (y, z-1), 7 = (y+1, z-1), 8 = (y-1, z-1)
     const int DY[9] = {-1, 0, 1, -1, 0, 1, 0, 1, -1}, DZ[9] = {0, 0, 0, 1, 1, 1, -1, -1, -1};
@@ -468,7 +478,10 @@ __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ 
             const unsigned wend = min(d.W, c0 + 32);
             if (!__any_sync(FULL, any != 0u) && !edge) {   // nothing kept within reach: all mn
                 const int xe = min(d.nx, (int)wend * 32);
-                for (int x = (int)c0 * 32 + lane; x < xe; x += 32) row[x] = mn;
+                for (int x = (int)c0 * 32 + lane; x < xe; x += 32) {
+                    row[x] = mn;
+                    masked++;
+                }
                 acc.mn = fminf(acc.mn, mn);
                 acc.mx = fmaxf(acc.mx, mn);
             } else {
@@ -492,6 +505,7 @@ __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ 
                     if (!(kept || (interior && ((on >> lane) & 1u)))) {
                         v = mn;
                         row[x] = v;
+                        masked++;
                     } else {
                         v = row[x];
                         if (FILL && kept) {
@@ -506,6 +520,8 @@ __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ 
             for (int k = 0; k < 9; k++) carry[k] = __shfl_sync(FULL, kk[k], 31);
         }
     }
+    for (int o = 16; o; o >>= 1) masked += __shfl_xor_sync(FULL, masked, o);
+    if (lane == 0 && masked) atomicAdd(&st->masked, masked);
     acc.flush(st, true);
 }
 
@@ -669,11 +685,23 @@ n2m_status class_bits(LabelWork &w, const LD &d, const float *vol, float iso, bo
 }  // namespace
 
 n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn, bool only_largest,
-                         bool fill_bubbles, LabelWork &w, VolStats *st, cudaStream_t s) {
+                         bool fill_bubbles, LabelWork &w, VolStats *st, cudaStream_t s, const unsigned *vsign,
+                         LabelPost *post) {
     const LD d = make_ld(nx, ny, nz);
-    CKS(class_bits(w, d, vol, iso, false, s));
+    if (vsign) {
+        if (d.n > 0x7fffffffLL) {
+            n2m_set_error("labelling supports at most 2^31-1 voxels");
+            return N2M_ERR_TOO_LARGE;
+        }
+        CKS(w.mask.ensure((size_t)d.nwords * sizeof(unsigned)));
+        { k_lab_bits_vsign<<<gsz(d.nwords), 256, 0, s>>>(vsign, d, (unsigned)(ny + 7) / 8, w.mask.as<unsigned>()); N2M_COUNT(); }
+        CKL();
+    } else {
+        CKS(class_bits(w, d, vol, iso, false, s));
+    }
     const unsigned *K;
     CKS(label_core(w, d, 18, only_largest, fill_bubbles, s, &K));
+    if (post) *post = LabelPost{K, d.W, mn, iso, fill_bubbles, only_largest};
     const unsigned g = wgrid(d);
     if (only_largest && fill_bubbles) { k_lab_final<true, true><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
     else if (only_largest) { k_lab_final<true, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }

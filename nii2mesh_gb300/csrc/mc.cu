@@ -726,7 +726,7 @@ n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4
         const unsigned nrows = (unsigned)g.n[1] * (unsigned)g.n[2];
         const unsigned blocks = std::min<unsigned>((nrows + 7) / 8, 152u * 16u);
         k_signs<<<blocks, 256, 0, s>>>(v, WX, nrows, w.signs.as<unsigned>(),
-                                       repair ? repair->w->vsign.as<unsigned>() : nullptr,
+                                       repair && !repair->post ? repair->w->vsign.as<unsigned>() : nullptr,
                                        (unsigned)(g.dim[0] + 31) / 32, (unsigned)(g.dim[1] + 7) / 8);
         N2M_COUNT();
     }

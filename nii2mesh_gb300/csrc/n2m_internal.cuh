@@ -68,7 +68,7 @@ struct VolStats {
     int vmin, vmax;          // ordered-int min/max of the volume
     int lo[3], hi[3];        // bbox of voxels >= iso (unpadded, inclusive)
     unsigned nonfinite;      // NaN/Inf voxels
-    unsigned pad;
+    unsigned masked;         // voxels the labelling set to the minimum (run_labelling)
 };
 
 // ---- kernels' host launchers (stream-ordered, no syncs) ----------------------
@@ -125,6 +125,16 @@ struct OdWork {
     unsigned cap = 0;
 };
 struct ScanWork;
+// What meshify's labelling did to each voxel (src/meshify.c:330-342), for the
+// exact values the repair writes afterwards: voxels of K (bit x & 31 of word
+// (z*ny + y)*W + x/32) are raised to iso when fill; with largest, voxels
+// neither in K nor in its dilation are the minimum mn.
+struct LabelPost {
+    const unsigned *K;
+    unsigned W;
+    float mn, iso;
+    bool fill, largest;
+};
 struct OdRepair {
     const float *in;         // the raw volume
     float *tmp1, *tmp2;      // exact x and y pass values (written at marked voxels only)
@@ -132,6 +142,7 @@ struct OdRepair {
     int dim[3];
     OdWork *w;
     ScanWork *scan;
+    const LabelPost *post = nullptr;   // the volume was labelled: the repaired values get the same treatment
 };
 // the sign bitmap's word of voxel (x, y, z): the 8 row words of one 32 x 8 tile of a
 // slice are adjacent (one 32-byte sector, written at once by pass A)
@@ -173,9 +184,13 @@ struct LabelWork {
     DevBuf lab, mask, keep, cnt, edge, rc, misc;
 };
 // meshify's labelling of vol in place; st: the range and bbox of the result
-// (accumulated into, like launch_stats)
+// (accumulated into, like launch_stats) and the count of masked voxels.
+// vsign (may be null): a sign bitmap (OdWork::vsign with od_resolve's
+// at_or_above) to take the mask from instead of vol; post (may be null): what
+// the labelling did, for values computed later
 n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn, bool only_largest,
-                         bool fill_bubbles, LabelWork &w, VolStats *st, cudaStream_t s);
+                         bool fill_bubbles, LabelWork &w, VolStats *st, cudaStream_t s, const unsigned *vsign = nullptr,
+                         LabelPost *post = nullptr);
 // bwlabel() semantics on a float volume (nonzero = foreground); *d_nl gets the label count
 n2m_status run_bwlabel(float *vol, int nx, int ny, int nz, int conn, bool only_largest, bool fill_bubbles,
                        LabelWork &w, ScanWork &sw, int *d_nl, cudaStream_t s);
@@ -236,8 +251,8 @@ struct McCounts {
 };
 // repair: marks the corners of the cubes with mixed signs in repair->w->need_z
 // after the sign pass and runs od_repair before any value is read (null: none)
-// (with a repair, the sign words of grid points strictly inside the volume come
-// from repair->w->vsign instead of the values)
+// (with a repair and no labelling, the sign words of grid points strictly inside
+// the volume come from repair->w->vsign instead of the values)
 n2m_status mc_count(const McGrid &g, int variant, McWork &w, ScanWork &sw, uint4 *d_total, cudaStream_t s,
                     const OdRepair *repair = nullptr);
 n2m_status mc_emit(const McGrid &g, int variant, McWork &w, const McCounts &c, vec3d *d_pts, vec3i *d_tris,

@@ -504,7 +504,7 @@ n2m_status oc_count(const float *vol, const int dim[3], const int lo[3], const i
     CKS(w.cand.ensure((nwords + 1) * sizeof(unsigned)));
     const unsigned nrows = (unsigned)g.NY * (unsigned)g.NZ;
     const unsigned wblocks = (unsigned)std::min<size_t>((nwords + 255) / 256, 152u * 16u);
-    { k_oc_signs<<<std::min<unsigned>((nrows + 7) / 8, 152u * 16u), 256, 0, s>>>(g, nrows, w.signs.as<unsigned>(), repair ? repair->w->vsign.as<unsigned>() : nullptr, (unsigned)(dim[0] + 31) / 32, (unsigned)(dim[1] + 7) / 8); N2M_COUNT(); }
+    { k_oc_signs<<<std::min<unsigned>((nrows + 7) / 8, 152u * 16u), 256, 0, s>>>(g, nrows, w.signs.as<unsigned>(), repair && !repair->post ? repair->w->vsign.as<unsigned>() : nullptr, (unsigned)(dim[0] + 31) / 32, (unsigned)(dim[1] + 7) / 8); N2M_COUNT(); }
     if (repair) {   // exact smoothed values where the emit reads them
         const size_t nvw = ((size_t)dim[0] * dim[1] * dim[2] + 31) / 32;
         CKS(repair->w->need_z.ensure(nvw * sizeof(unsigned)));

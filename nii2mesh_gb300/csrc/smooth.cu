@@ -51,7 +51,7 @@ void stats_init_host(VolStats *h) {
     h->vmax = INT_MIN;
     for (int i = 0; i < 3; i++) { h->lo[i] = INT_MAX; h->hi[i] = INT_MIN; }
     h->nonfinite = 0;
-    h->pad = 0;
+    h->masked = 0;
 }
 
 // ---- three separable passes with batched exact fix-ups -------------------------
@@ -946,6 +946,35 @@ __global__ void __launch_bounds__(256) k_od_exact(const unsigned *__restrict__ l
     F.finish(P, acc, lane);
 }
 
+// The labelling's effect on the exact values the z pass just wrote at the
+// listed voxels (src/meshify.c:330-342): kept voxels raised to iso (fill);
+// with largest, voxels neither kept nor in the kept set's dilation (the
+// 26-neighbourhood without (-1,-1,-1), interior voxels; src/meshify.c:218-264)
+// are the minimum.
+__global__ void k_od_post(const unsigned *__restrict__ list, const unsigned *__restrict__ cnt, float *out, LabelPost L,
+                          int nx, int ny, int nz) {
+    const unsigned n = *cnt;
+    auto bit = [&](int x, int y, int z) -> unsigned {
+        return (__ldg(L.K + ((size_t)z * ny + y) * L.W + ((unsigned)x >> 5)) >> (x & 31)) & 1u;
+    };
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned j = list[i], x = j % (unsigned)nx, r = j / (unsigned)nx, y = r % (unsigned)ny, z = r / (unsigned)ny;
+        if (bit(x, y, z)) {
+            if (L.fill) out[j] = fmaxf(out[j], L.iso);
+            continue;
+        }
+        if (!L.largest) continue;
+        bool on = false;
+        if (x > 0 && y > 0 && z > 0 && x + 1 < (unsigned)nx && y + 1 < (unsigned)ny && z + 1 < (unsigned)nz) {
+            for (int dz = -1; dz <= 1 && !on; dz++)
+                for (int dy = -1; dy <= 1 && !on; dy++)
+                    for (int dx = -1; dx <= 1 && !on; dx++)
+                        if (!(dx == -1 && dy == -1 && dz == -1)) on = bit((int)x + dx, (int)y + dy, (int)z + dz);
+        }
+        if (!on) out[j] = L.mn;
+    }
+}
+
 // floor(2^64 / d) + 1: __umul64hi(n, m) = n / d for every 32-bit n (d >= 2)
 unsigned long long od_magic(unsigned d) { return d <= 1u ? 0ull : ~0ull / d + 1ull; }
 
@@ -1105,6 +1134,7 @@ n2m_status od_repair(const OdRepair &r, cudaStream_t s) {
                                     od_magic((unsigned)nx), od_magic((unsigned)ny)); N2M_COUNT(); }
     { k_od_exact<<<xb, 256, 0, s>>>(lz, cnt + 0, r.tmp2, r.out, uxy, uxy, (unsigned)nz, od_magic(uxy),
                                     od_magic((unsigned)nz)); N2M_COUNT(); }
+    if (r.post) { k_od_post<<<xb, 256, 0, s>>>(lz, cnt + 0, r.out, *r.post, nx, ny, nz); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

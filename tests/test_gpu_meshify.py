@@ -170,6 +170,33 @@ def test_bbox_touches_volume_faces(gpu, oracle):
         assert ok, msg
 
 
+@pytest.mark.parametrize("shape", [(48, 52, 64), (96, 96, 96), (40, 33, 36), (64, 64, 128)])
+@pytest.mark.parametrize("variant", [MC33, OLDCUBES])
+@pytest.mark.parametrize("bubbles", [False, True])
+def test_device_path_on_demand_labelling(gpu, oracle, shape, variant, bubbles):
+    """-l 1 (with and without -b 1) on device-resident volumes whose rows
+    allow the on-demand pre-smooth: the mask is pass A's sign bitmap, the
+    exact values at the marching cubes' corners get the clustering's fill and
+    mask-out; equal to the oracle bit for bit.  The last volume masks nothing
+    out (its one component's dilation covers it), which takes the exact
+    three passes instead"""
+    ctx = gpu.Context(0)
+    nz, ny, nx = shape
+    cubes = gpu.OLDCUBES if variant == OLDCUBES else gpu.MC33
+    full = np.full(shape, 100.0, np.float32) + synth.spheres(n=max(shape), count=3, seed=3)[:nz, :ny, :nx]
+    full[nz // 2 - 1:nz // 2 + 2, ny // 2 - 1:ny // 2 + 2, nx // 2 - 1:nx // 2 + 2] = 0.0
+    vols = [(synth.ct512(seed=sum(shape), n=max(shape), count=10)[:nz, :ny, :nx].copy(), 300.0),
+            (synth.spheres(n=max(shape), count=6, rmin=5, rmax=12, cmin=10, cmax=max(shape) - 10, noise=20.0,
+                           seed=nx)[:nz, :ny, :nx].copy(), 50.0),
+            (full, 50.0)]
+    for vol, iso in vols:
+        want = oracle.meshify(vol, iso, variant, True, True, bubbles)
+        got = device_mesh(gpu, ctx, vol, iso, cubes, True, bubbles)
+        ok, d, msg = mesh_equal(got, want, POS_TOL)
+        assert ok, (shape, iso, msg)
+    ctx.close()
+
+
 def test_meshify_into_caller_buffers(gpu):
     """n2m_meshify_into writes the same mesh as n2m_meshify into reused caller
     arrays (pageable and pinned), staged and unstaged uploads, with and without
