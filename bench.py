@@ -620,6 +620,7 @@ def main():
                          "structure count scaled by volume), stage times printed; no bench line")
     ap.add_argument("--largest", action="store_true", help="with --profile: keep only the largest cluster (-l 1)")
     ap.add_argument("--bubbles", action="store_true", help="with --profile: fill bubbles (-b 1)")
+    ap.add_argument("--oldcubes", action="store_true", help="with --profile: the classic build's oldcubes marching cubes")
     ap.add_argument("--profile-writer", type=int, default=0, metavar="N",
                     help="profiling driver: mesh the N^3 CT-like volume, then encode it twice as .mz3 gzip and once as .obj")
     ap.add_argument("--profile-atlas", action="store_true",
@@ -680,9 +681,11 @@ def main():
         d = torch.from_numpy(pv).cuda()
         ctx = n2m.Context(0)
         for _ in range(2):
-            _, _, nt, nv, rep = ctx.meshify_device(d.data_ptr(), (n, n, n), ISO, n2m.MC33, True, a.largest, a.bubbles)
+            _, _, nt, nv, rep = ctx.meshify_device(d.data_ptr(), (n, n, n), ISO, n2m.OLDCUBES if a.oldcubes else n2m.MC33,
+                                                   True, a.largest, a.bubbles)
         torch.cuda.synchronize()
-        print(json.dumps({"profile": n, "largest": a.largest, "bubbles": a.bubbles, "triangles": nt, "vertices": nv,
+        print(json.dumps({"profile": n, "largest": a.largest, "bubbles": a.bubbles, "oldcubes": a.oldcubes,
+                          "triangles": nt, "vertices": nv,
                           "stage_ms": dict(zip(STAGE_NAMES, [round(x, 4) for x in rep["ms_stage"][:7]]))}))
         return
     rank, world, dist = dist_setup(a.gpus)

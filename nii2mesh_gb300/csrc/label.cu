@@ -423,9 +423,9 @@ __global__ void k_nl_from(const unsigned *nroots, bool only_largest, int *nl) {
 // slice z-1.  The keep words of a row are loaded 32 at a time (lane l holds
 // word c0 + l) and broadcast; 32 words with no kept voxel within reach are
 // written without being read.
-template <bool LARGEST, bool FILL>
+template <bool LARGEST, bool FILL, bool ONE>   // ONE: rows of at most 32 words
 __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ K, LD d, float *vol, float iso, float mn,
-                                                   VolStats *st) {
+                                                   VolStats *st, bool vec4) {
     smooth::Acc acc;
     acc.init();
     unsigned masked = 0;
@@ -456,68 +456,65 @@ __global__ void __launch_bounds__(256) k_lab_final(const unsigned *__restrict__ 
             continue;
         }
         const bool ryz = y > 0 && z > 0 && y < d.ny - 1 && z < d.nz - 1;
-        const unsigned *Kr[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) {
-            const int yy = y + DY[k], zz = z + DZ[k];
-            Kr[k] = yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz ? K + ((size_t)zz * d.ny + yy) * d.W : nullptr;
-        }
         unsigned carry[9];   // word c0 - 1 of each row
 #pragma unroll
         for (int k = 0; k < 9; k++) carry[k] = 0u;
         for (unsigned c0 = 0; c0 < d.W; c0 += 32) {
-            unsigned kk[9], nk[9];
-            unsigned any = 0u, edge = 0u;
+            // lane l: word c0 + l of the kept set and of its dilation (the row's own word for
+            // `kept`); the words next to it come from the neighbouring lanes
+            unsigned on = 0u, kept = 0u;
 #pragma unroll
             for (int k = 0; k < 9; k++) {
-                kk[k] = Kr[k] && c0 + lane < d.W ? Kr[k][c0 + lane] : 0u;
-                nk[k] = Kr[k] && c0 + 32 < d.W ? Kr[k][c0 + 32] : 0u;   // the word after the chunk
-                any |= kk[k];
-                edge |= (carry[k] >> 31) | (nk[k] & 1u);
+                const int yy = y + DY[k], zz = z + DZ[k];
+                const bool in = yy >= 0 && zz >= 0 && yy < d.ny && zz < d.nz;
+                const unsigned *Kk = K + ((size_t)(in ? zz : 0) * d.ny + (in ? yy : 0)) * d.W;
+                const unsigned cur = in && c0 + lane < d.W ? Kk[c0 + lane] : 0u;
+                unsigned prv = __shfl_up_sync(FULL, cur, 1), nxt = __shfl_down_sync(FULL, cur, 1);
+                if (lane == 0) prv = carry[k];
+                if (lane == 31) nxt = !ONE && in && c0 + 32 < d.W ? Kk[c0 + 32] : 0u;
+                if (!ONE) carry[k] = __shfl_sync(FULL, cur, 31);
+                on |= cur | (cur >> 1) | (nxt << 31) | (k < 8 ? (cur << 1) | (prv >> 31) : 0u);   // row 8: no K(x-1)
+                if (k == 1) kept = cur;
             }
             const unsigned wend = min(d.W, c0 + 32);
-            if (!__any_sync(FULL, any != 0u) && !edge) {   // nothing kept within reach: all mn
-                const int xe = min(d.nx, (int)wend * 32);
-                for (int x = (int)c0 * 32 + lane; x < xe; x += 32) {
-                    row[x] = mn;
-                    masked++;
+            if (!__any_sync(FULL, on != 0u)) {   // nothing kept within reach: all mn
+                const int xb = (int)c0 * 32, xe = min(d.nx, (int)wend * 32);
+                if (vec4) {   // rows of a multiple of 4 voxels on 16-byte boundaries
+                    float4 *r4 = (float4 *)(row + xb);
+                    for (int q = lane; q < (xe - xb) >> 2; q += 32) {
+                        r4[q] = make_float4(mn, mn, mn, mn);
+                        masked += 4;
+                    }
+                } else {
+                    for (int x = xb + lane; x < xe; x += 32) {
+                        row[x] = mn;
+                        masked++;
+                    }
                 }
                 acc.mn = fminf(acc.mn, mn);
                 acc.mx = fmaxf(acc.mx, mn);
-            } else {
-                for (unsigned w = c0; w < wend; w++) {
-                    const int l = (int)(w - c0);
-                    unsigned on = 0u, kept0 = 0u;
-#pragma unroll
-                    for (int k = 0; k < 9; k++) {
-                        const unsigned cur = __shfl_sync(FULL, kk[k], l);
-                        const unsigned prv = l ? __shfl_sync(FULL, kk[k], l - 1) : carry[k];
-                        const unsigned nxt = l < 31 ? __shfl_sync(FULL, kk[k], l + 1) : nk[k];
-                        const unsigned right = (cur >> 1) | (nxt << 31);   // K(x+1)
-                        on |= cur | right | (k < 8 ? (cur << 1) | (prv >> 31) : 0u);   // row 8: no K(x-1)
-                        if (k == 1) kept0 = cur;
-                    }
-                    const int x = (int)w * 32 + lane;
-                    if (x >= d.nx) continue;
-                    const bool kept = (kept0 >> lane) & 1u;
-                    const bool interior = ryz && x > 0 && x < d.nx - 1;
-                    float v;
-                    if (!(kept || (interior && ((on >> lane) & 1u)))) {
-                        v = mn;
-                        row[x] = v;
-                        masked++;
-                    } else {
-                        v = row[x];
-                        if (FILL && kept) {
-                            v = fmaxf(v, iso);
-                            row[x] = v;
-                        }
-                    }
-                    acc.add(v, x, y, z, iso);
-                }
+                continue;
             }
-#pragma unroll
-            for (int k = 0; k < 9; k++) carry[k] = __shfl_sync(FULL, kk[k], 31);
+            for (unsigned w = c0; w < wend; w++) {
+                const unsigned onw = __shfl_sync(FULL, on, (int)(w - c0)), kw = __shfl_sync(FULL, kept, (int)(w - c0));
+                const int x = (int)w * 32 + lane;
+                if (x >= d.nx) continue;
+                const bool kp = (kw >> lane) & 1u;
+                const bool interior = ryz && x > 0 && x < d.nx - 1;
+                float v;
+                if (!(kp || (interior && ((onw >> lane) & 1u)))) {
+                    v = mn;
+                    row[x] = v;
+                    masked++;
+                } else {
+                    v = row[x];
+                    if (FILL && kp) {
+                        v = fmaxf(v, iso);
+                        row[x] = v;
+                    }
+                }
+                acc.add(v, x, y, z, iso);
+            }
         }
     }
     for (int o = 16; o; o >>= 1) masked += __shfl_xor_sync(FULL, masked, o);
@@ -703,10 +700,13 @@ n2m_status run_labelling(float *vol, int nx, int ny, int nz, float iso, float mn
     CKS(label_core(w, d, 18, only_largest, fill_bubbles, s, &K));
     if (post) *post = LabelPost{K, d.W, mn, iso, fill_bubbles, only_largest};
     const unsigned g = wgrid(d);
-    if (only_largest && fill_bubbles) { k_lab_final<true, true><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
-    else if (only_largest) { k_lab_final<true, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
-    else if (fill_bubbles) { k_lab_final<false, true><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
-    else { k_lab_final<false, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st); N2M_COUNT(); }
+    const bool v4 = nx % 4 == 0 && ((uintptr_t)vol & 15) == 0, one = d.W <= 32;
+    if (only_largest && fill_bubbles && one) { k_lab_final<true, true, true><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st, v4); N2M_COUNT(); }
+    else if (only_largest && fill_bubbles) { k_lab_final<true, true, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st, v4); N2M_COUNT(); }
+    else if (only_largest && one) { k_lab_final<true, false, true><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st, v4); N2M_COUNT(); }
+    else if (only_largest) { k_lab_final<true, false, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st, v4); N2M_COUNT(); }
+    else if (fill_bubbles) { k_lab_final<false, true, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st, v4); N2M_COUNT(); }
+    else { k_lab_final<false, false, false><<<g, 256, 0, s>>>(K, d, vol, iso, mn, st, v4); N2M_COUNT(); }
     CKL();
     return N2M_OK;
 }

@@ -65,6 +65,16 @@ constexpr int OS_W = 16;   // words of a row loaded at once per lane
 // a warp takes OS_W words at a time with all their loads in flight.
 __device__ __forceinline__ void oc_value_words(const OV &g, const float *rp, bool rface, unsigned xa, unsigned xb,
                                                unsigned *out, int lane) {
+    if (xb - xa <= 2u) {   // the border words around the bitmap's: one at a time
+        for (unsigned xw = xa; xw < xb; xw++) {
+            const int x = (int)xw * 32 + lane, vx = g.lo0 + x;
+            float v = x < g.NX ? __ldg(rp + x) : 0.f;
+            if (rface || vx == 0 || vx == g.dx - 1) v = fminf(g.edge_max, v);
+            const unsigned m = __ballot_sync(0xffffffffu, x < g.NX && v < g.iso);
+            if (lane == 0) out[xw] = m;
+        }
+        return;
+    }
     for (unsigned xw0 = xa; xw0 < xb; xw0 += OS_W) {
         float raw[OS_W];
 #pragma unroll
