@@ -8,10 +8,12 @@
 // and its weld keeps the position of the LAST copy (src/meshify.c:99-100).
 // Each edge here is computed once, in double, in the orientation of the last
 // cube (raster order) that uses it, so positions are the reference's
-// post-weld positions bit for bit.  For the weld candidates (the few vertices
-// near a grid point), oc_lastuse records the index of the vertex's last copy in
-// the reference's pre-weld vertex list (3*triangle + corner) so that
-// near-corner clusters keep the same survivor.
+// post-weld positions bit for bit.  The weld candidates (the few vertices near
+// a grid point) can merge with vertices of other edges; the reference merges
+// copies, so oc_copies / oc_copy_positions list every triangle corner that
+// names a candidate (3*triangle + corner, its order in the reference's
+// triangle soup) with the position the emitting cube gives that copy, and the
+// host weld groups the copies as the reference does.
 #include <algorithm>
 #include <atomic>
 
