@@ -163,7 +163,7 @@ __global__ void k_run_init(const unsigned *__restrict__ B, LD d, unsigned want, 
 // of voxel x with voxel x+dx of row k counts only if voxels x-1 and x+dx-1
 // do not also touch: one union per overlap of two runs.
 template <int NNB>
-__global__ void __launch_bounds__(256) k_run_merge(const unsigned *__restrict__ B, LD d, unsigned want, int *L) {
+__global__ void __launch_bounds__(256, 6) k_run_merge(const unsigned *__restrict__ B, LD d, unsigned want, int *L) {
     static_assert(NNB == 3 || NNB == 9 || NNB == 13, "6-, 18- or 26-connectivity");
     constexpr int NR = NNB == 3 ? 3 : 5;
     const int RY[5] = {0, -1, 0, -1, 1}, RZ[5] = {0, 0, -1, -1, -1};
