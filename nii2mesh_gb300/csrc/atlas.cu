@@ -23,11 +23,13 @@
 #include <vector>
 
 #include "mc33.cuh"
+#include "runs.cuh"
 #include "smooth_core.cuh"
 #include "uf.cuh"
 
 namespace {
 using namespace mc33;
+using namespace runs;
 
 struct ABox {
     int label;
@@ -46,6 +48,8 @@ struct ABox {
     // marching-cubes grid (global origin lo, size gn), filled by the host
     int glo[3], gn[3];
     unsigned WX, word0, ctile0;
+    // clustering on x-runs: bit words per row, first row and first bit word across the boxes
+    unsigned W, row0, bw0;
 };
 
 struct AtlasVol {
@@ -226,266 +230,349 @@ __device__ __forceinline__ void for_chunks(const ABox *boxes, int nb, unsigned n
     }
 }
 
-__constant__ signed char k_half[13][3] = {{-1, 0, 0},  {0, -1, 0}, {0, 0, -1},  {-1, -1, 0}, {1, -1, 0},
-                                          {-1, 0, -1}, {1, 0, -1}, {0, -1, -1}, {0, 1, -1},  {-1, -1, -1},
-                                          {1, -1, -1}, {-1, 1, -1}, {1, 1, -1}};
-
+// The clustering of label.cu on every sub-box: class masks as bit words per
+// box (bit x & 31 of word B.bw0 + (z*n1 + y)*B.W + x/32, local coordinates),
+// union-find parents in L (arena-indexed) at the first voxel of each x-run
+// only, boxes independent of one another.  A row kernel takes one row of one
+// box per warp (lanes over its words, 32 at a time); rows and words are
+// numbered across the boxes (B.row0, B.bw0).  The background's face contacts
+// are the box's faces (src/meshify.c:332-336 on the binarised sub-box).
 __device__ __forceinline__ bool skip_box(const ABox &B) { return B.fail != 0; }
 
-__global__ void k_a_mask(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const float *arena, unsigned char *m) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) { m[c.i] = arena[c.i] >= B.iso; });
+__device__ __forceinline__ unsigned ab_valid(const ABox &B, unsigned w) {
+    const int x0 = (int)w * 32;
+    return x0 + 32 <= B.n[0] ? FULL : (1u << (B.n[0] - x0)) - 1u;
+}
+// foreground (want 1) or background (want 0) bits of word w of local row lr
+__device__ __forceinline__ unsigned ab_class(const unsigned *Bits, const ABox &B, unsigned lr, unsigned w, unsigned want) {
+    const unsigned b = Bits[B.bw0 + lr * B.W + w];
+    return want ? b : ~b & ab_valid(B, w);
 }
 
-// Union-find start: every voxel of the wanted class points at the start of its
-// run along x (found with a ballot within the warp; a run that enters the
-// warp from the left points at the voxel before the warp), so the x links
-// never need a union.  Other voxels get -1.  Parents are smaller indices of
-// the same component, as the hooking rule requires.
-__global__ void k_a_uf_init(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const unsigned char *m,
-                            unsigned char want, int *L) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        const int lane = threadIdx.x & 31;
-        // the lanes of this step: consecutive voxels, a prefix of the warp
-        const long long left_in_box = (long long)B.n[0] * B.n[1] * B.n[2] - (c.i - B.arena - lane);
-        const unsigned act = left_in_box >= 32 ? 0xffffffffu : (1u << left_in_box) - 1u;
-        const bool fg = m[c.i] == want;
-        const bool left_fg = __shfl_up_sync(act, fg, 1);
-        const bool cont = fg && c.x > 0 && (lane > 0 ? left_fg : m[c.i - 1] == want);
-        const unsigned starts = __ballot_sync(act, fg && !cont);
-        int parent = -1;
-        if (fg) {
-            const unsigned le = starts & (lane == 31 ? 0xffffffffu : (2u << lane) - 1u);
-            parent = le ? (int)(c.i - (lane - (31 - __clz(le)))) : (int)(c.i - lane - 1);
+// class bits: smoothed value >= the box's isolevel
+__global__ void __launch_bounds__(256) k_ab_bits(const ABox *boxes, int nb, unsigned nrows, const float *arena,
+                                                 unsigned *Bits) {
+    const int lane = threadIdx.x & 31;
+    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
+        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
+        const unsigned lr = gr - B.row0;
+        const float *rp = arena + B.arena + (long long)lr * B.n[0];
+        for (unsigned w = 0; w < B.W; w++) {
+            const int x = (int)w * 32 + lane;
+            const unsigned m = __ballot_sync(FULL, x < B.n[0] && rp[x] >= B.iso);
+            if (lane == 0) Bits[B.bw0 + lr * B.W + w] = m;
         }
-        L[c.i] = parent;
-    });
+    }
 }
 
-// Union of each voxel of the class (m == want) with its half-neighbours of
-// k_half[1 .. NNB-1] (the -x neighbour is linked by the run start).  A contact
-// whose two left voxels also touch is implied by theirs (both pairs lie in the
-// same runs) and is skipped.  Row by row, 32 voxels a word: the class bits of
-// the row and of the rows (y-1, z), (y, z-1), (y-1, z-1), (y+1, z-1) give every
-// contact of a word by shifts; only the lanes holding one touch L.  A chunk
-// reads the rows its voxels touch and unites only its own voxels' contacts.
+// every run start of the class links to itself; z8 / z32 (may be null) zeroed there
+__global__ void k_ab_init(const ABox *boxes, int nb, unsigned nbw, const unsigned *__restrict__ Bits, unsigned want,
+                          int *L, unsigned char *z8, unsigned *z32) {
+    for (unsigned gw = blockIdx.x * blockDim.x + threadIdx.x; gw < nbw; gw += gridDim.x * blockDim.x) {
+        const ABox &B = boxes[find_item(boxes, nb, gw, &ABox::bw0)];
+        const unsigned lw = gw - B.bw0, lr = lw / B.W, w = lw - lr * B.W;
+        const unsigned c = ab_class(Bits, B, lr, w, want), pc = w ? ab_class(Bits, B, lr, w - 1, want) : 0u;
+        const long long base = B.arena + (long long)lr * B.n[0] + (long long)w * 32;
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
+            const int s = (int)(base + __ffs(st) - 1);
+            L[s] = s;
+            if (z8) z8[s] = 0;
+            if (z32) z32[s] = 0;
+        }
+    }
+}
+
+// union of touching runs with the rows before them in the box (rows (y-1, z),
+// (y, z-1), and for 18-connectivity x offsets -1..1 and rows (y-1, z-1),
+// (y+1, z-1)); a contact counts where the voxels before it do not also touch
 template <int NNB>
-__global__ void __launch_bounds__(256) k_a_uf_merge(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch,
-                                                    const unsigned char *m, unsigned char want, int *L) {
+__global__ void __launch_bounds__(256) k_ab_merge(const ABox *boxes, int nb, unsigned nrows,
+                                                  const unsigned *__restrict__ Bits, unsigned want, int *L) {
     static_assert(NNB == 3 || NNB == 9, "6- or 18-connectivity");
-    __shared__ unsigned item;
-    __shared__ int bi;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            item = atomicAdd(q, 1u);
-            bi = item < nch ? find_item(boxes, nb, item, &ABox::chunk0) : 0;
-        }
-        __syncthreads();
-        const unsigned it = item;
-        const int b = bi;
-        __syncthreads();
-        if (it >= nch) return;
-        const ABox &B = boxes[b];
+    constexpr int NR = NNB == 3 ? 3 : 5;
+    const int RY[5] = {0, -1, 0, -1, 1}, RZ[5] = {0, 0, -1, -1, -1};
+    const int lane = threadIdx.x & 31;
+    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
+        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
         if (skip_box(B)) continue;
         const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
-        const unsigned nvb = (unsigned)n0 * (unsigned)n1 * (unsigned)n2;
-        const unsigned loc0 = (it - B.chunk0) * ch;
-        if (loc0 >= nvb) continue;
-        const unsigned loc1 = min(loc0 + ch, nvb);
-        const unsigned r0 = loc0 / (unsigned)n0, r1 = (loc1 - 1) / (unsigned)n0;
-        const unsigned char *M = m + B.arena;
-        const int nw = (n0 + 31) / 32;
-        constexpr int NR = NNB == 3 ? 3 : 5;
-        // rows: 0 = (y, z), 1 = (y-1, z), 2 = (y, z-1), 3 = (y-1, z-1), 4 = (y+1, z-1)
-        const int RY[5] = {0, -1, 0, -1, 1}, RZ[5] = {0, 0, -1, -1, -1};
-        for (unsigned r = r0 + (unsigned)warp; r <= r1; r += (unsigned)nwarp) {
-            const int y = (int)(r % (unsigned)n1), z = (int)(r / (unsigned)n1);
-            auto word = [&](int dy, int dz, int xw) -> unsigned {
-                const int yy = y + dy, zz = z + dz, x = xw * 32 + lane;
-                const bool in = yy >= 0 && zz >= 0 && yy < n1 && zz < n2 && xw < nw && x < n0;
-                return __ballot_sync(0xffffffffu, in && M[((long long)zz * n1 + yy) * n0 + x] == want);
-            };
-            unsigned pw[NR], cw[NR];
+        const unsigned lr = gr - B.row0, W = B.W;
+        const int z = (int)(lr / (unsigned)n1), y = (int)(lr - (unsigned)z * (unsigned)n1);
+        bool kok[NR];
+        unsigned rk[NR];
+#pragma unroll
+        for (int k = 0; k < NR; k++) {
+            const int yy = y + RY[k], zz = z + RZ[k];
+            kok[k] = yy >= 0 && zz >= 0 && yy < n1 && zz < n2;
+            rk[k] = kok[k] ? (unsigned)zz * (unsigned)n1 + (unsigned)yy : 0u;
+        }
+        int cst[NR];
+        unsigned cwd[NR];
+#pragma unroll
+        for (int k = 0; k < NR; k++) { cst[k] = -1; cwd[k] = 0u; }
+        for (unsigned c0 = 0; c0 < W; c0 += 32) {
+            const unsigned w = c0 + (unsigned)lane;
+            const bool ok = w < W;
+            const int x0 = (int)w * 32;
+            WordRuns R[NR];
+            unsigned nk[NR];
 #pragma unroll
             for (int k = 0; k < NR; k++) {
-                pw[k] = 0u;
-                cw[k] = word(RY[k], RZ[k], 0);
+                const unsigned c = ok && kok[k] ? ab_class(Bits, B, rk[k], w, want) : 0u;
+                R[k] = word_runs(c, x0, lane, 32, cst[k], cwd[k]);
+                const unsigned dn = __shfl_down_sync(FULL, c, 1);
+                nk[k] = lane < 31 ? (w + 1 < W ? dn : 0u) : (kok[k] && w + 1 < W ? ab_class(Bits, B, rk[k], w + 1, want) : 0u);
             }
-            for (int xw = 0; xw < nw; xw++) {
-                unsigned nx[NR];
-#pragma unroll
-                for (int k = 0; k < NR; k++) nx[k] = word(RY[k], RZ[k], xw + 1);
-                // S(k, d): bit x = class of voxel x + d of row k (d in -2 .. 1)
-                auto S = [&](int k, int d) -> unsigned {
-                    return d == 0 ? cw[k] : d > 0 ? (cw[k] >> d) | (nx[k] << (32 - d)) : (cw[k] << -d) | (pw[k] >> (32 + d));
-                };
-                const unsigned F = cw[0], left = S(0, -1);
-                // contact masks of k_half[1 .. NNB-1]: (row, dx)
-                auto contact = [&](int k, int dx) -> unsigned { return F & S(k, dx) & ~(left & S(k, dx - 1)); };
-                // bit k-1 of this lane's set: a contact with k_half[k]
-                unsigned set = ((contact(1, 0) >> lane) & 1u) | ((contact(2, 0) >> lane) & 1u) << 1;   // (0,-1,0) (0,0,-1)
-                if constexpr (NNB == 9) {
-                    set |= ((contact(1, -1) >> lane) & 1u) << 2    // (-1, -1, 0)
-                         | ((contact(1, 1) >> lane) & 1u) << 3     // (1, -1, 0)
-                         | ((contact(2, -1) >> lane) & 1u) << 4    // (-1, 0, -1)
-                         | ((contact(2, 1) >> lane) & 1u) << 5     // (1, 0, -1)
-                         | ((contact(3, 0) >> lane) & 1u) << 6     // (0, -1, -1)
-                         | ((contact(4, 0) >> lane) & 1u) << 7;    // (0, 1, -1)
+            const unsigned F = R[0].c;
+            if (!F) continue;
+            const unsigned left = (F << 1) | (R[0].pc >> 31);
+            auto S = [&](int k, int dx) -> unsigned {
+                const WordRuns &q = R[k];
+                return dx == 0 ? q.c : dx == 1 ? (q.c >> 1) | (nk[k] << 31)
+                                     : dx == -1 ? (q.c << 1) | (q.pc >> 31) : (q.c << 2) | (q.pc >> 30);
+            };
+            const long long base0 = B.arena + (long long)lr * n0;
+            auto link = [&](int k, int dx) {
+                unsigned m = F & S(k, dx) & ~(left & S(k, dx - 1));
+                if (!m) return;
+                const WordRuns &q = R[k];
+                const long long basek = B.arena + (long long)rk[k] * n0;
+                for (; m; m &= m - 1) {
+                    const int b = __ffs(m) - 1, xx = b + dx;
+                    const int sk = xx < 0 ? q.cs : xx > 31 ? ((q.c >> 31) & 1u ? q.start_of(31) : x0 + 32) : q.start_of(xx);
+                    const int i = (int)(base0 + R[0].start_of(b)), j = (int)(basek + sk);
+                    if (L[i] != L[j]) uf::unite(L, i, j);
                 }
-                const int x = xw * 32 + lane;
-                const unsigned loc = r * (unsigned)n0 + (unsigned)x;
-                if (set && x < n0 && loc >= loc0 && loc < loc1) {
-                    const int i = (int)(B.arena + loc);
-                    do {
-                        const int k = __ffs(set);
-                        set &= set - 1u;
-                        const int j = i + k_half[k][0] + k_half[k][1] * n0 + k_half[k][2] * n0 * n1;
-                        if (L[j] != L[i]) uf::unite(L, i, j);
-                    } while (set);
-                }
-#pragma unroll
-                for (int k = 0; k < NR; k++) {
-                    pw[k] = cw[k];
-                    cw[k] = nx[k];
-                }
+            };
+            link(1, 0);
+            link(2, 0);
+            if constexpr (NNB == 9) {
+                link(1, -1); link(1, 1); link(2, -1); link(2, 1); link(3, 0); link(4, 0);
             }
         }
     }
 }
 
-__global__ void k_a_uf_flatten(ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, int *L, bool fg) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        const int p = L[c.i];
-        if (p < 0) return;
-        if (p == (int)c.i) atomicAdd(fg ? &boxes[c.b].nfg : &boxes[c.b].nbg, 1u);
-        else L[c.i] = uf::find_root(L, p);
-    });
-}
-
-// background components touching the sub-box boundary reach a face of the volume
-__global__ void k_a_edge_roots(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L, unsigned char *edge) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        const int r = L[c.i];
-        if (r < 0) return;
-        if (c.x == 0 || c.y == 0 || c.z == 0 || c.x == B.n[0] - 1 || c.y == B.n[1] - 1 || c.z == B.n[2] - 1) edge[r] = 1;
-    });
-}
-
-__global__ void k_a_fill_bubbles(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L,
-                                 const unsigned char *edge, unsigned char *m) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        if (B.nbg <= 1) return;
-        const int r = L[c.i];
-        if (r >= 0 && !edge[r]) m[c.i] = 1;
-    });
-}
-
-// component sizes; lanes of a warp that share a root add together
-__global__ void k_a_sizes(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L, unsigned *cnt) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        const int r = L[c.i];
-        const unsigned grp = __match_any_sync(__activemask(), r);
-        if (r >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&cnt[r], __popc(grp));
-    });
-}
-
-__global__ void k_a_best(ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L, const unsigned *cnt) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        if (L[c.i] == (int)c.i) {
-            const unsigned loc = (unsigned)(c.i - B.arena);
-            atomicMax(&boxes[c.b].best, ((unsigned long long)cnt[c.i] << 32) | (0xffffffffu - loc));
-        }
-    });
-}
-
-__global__ void k_a_keep(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const int *L, const unsigned char *m,
-                         bool only_largest, unsigned char *keep) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        if (only_largest) {
-            const long long root = B.best ? B.arena + (0xffffffffu - (unsigned)(B.best & 0xffffffffu)) : -2;
-            keep[c.i] = L[c.i] == root;
-        } else {
-            keep[c.i] = m[c.i];
-        }
-    });
-}
-
-// fill (img = max(img, iso) where kept), then dilate (interior voxels of the
-// volume, 25 neighbours) + mask-out (img = mn) — src/meshify.c:332-342
-__global__ void k_a_fill(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch, const unsigned char *keep, float *arena) {
-    for_chunks(boxes, nb, nch, q, ch, [&](VoxCtx c, const ABox &B) {
-        if (keep[c.i]) arena[c.i] = fmaxf(arena[c.i], B.iso);
-    });
-}
-
-// Dilation + mask-out (src/meshify.c:218-264, 337-342): a voxel stays when it
-// is kept or, away from the volume faces, one of 25 neighbours is (all 26
-// except (-1,-1,-1), :252); every other voxel becomes the box minimum.  Row
-// by row, 32 voxels a word: with R3 = K(x-1)|K(x)|K(x+1) and R2 = K(x)|K(x+1)
-// of a row, the neighbourhood is R3 of rows y-1..y+1 in slices z and z+1, R3 of
-// rows y and y+1 in slice z-1, and R2 of row y-1 in slice z-1.  A chunk works on
-// the rows its voxels touch and writes only its own voxels.
-__global__ void __launch_bounds__(256) k_a_dilate(const ABox *boxes, int nb, unsigned nch, unsigned *q, unsigned ch,
-                                                  const unsigned char *keep, float *arena, int nx, int ny, int nz) {
-    __shared__ unsigned item;
-    __shared__ int bi;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            item = atomicAdd(q, 1u);
-            bi = item < nch ? find_item(boxes, nb, item, &ABox::chunk0) : 0;
-        }
-        __syncthreads();
-        const unsigned it = item;
-        const int b = bi;
-        __syncthreads();
-        if (it >= nch) return;
+// every run start points at its root (read-only root search: the one store is
+// the final root); roots are counted per box
+__global__ void k_ab_flatten(ABox *boxes, int nb, unsigned nbw, const unsigned *__restrict__ Bits, unsigned want, int *L,
+                             bool fg) {
+    for (unsigned gw = blockIdx.x * blockDim.x + threadIdx.x; gw < nbw; gw += gridDim.x * blockDim.x) {
+        const int b = find_item(boxes, nb, gw, &ABox::bw0);
         const ABox &B = boxes[b];
+        const unsigned lw = gw - B.bw0, lr = lw / B.W, w = lw - lr * B.W;
+        const unsigned c = ab_class(Bits, B, lr, w, want), pc = w ? ab_class(Bits, B, lr, w - 1, want) : 0u;
+        const long long base = B.arena + (long long)lr * B.n[0] + (long long)w * 32;
+        unsigned nroots = 0;
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
+            const int s = (int)(base + __ffs(st) - 1);
+            const int root = uf::find_root(L, s);
+            if (root == s) nroots++;
+            else L[s] = root;
+        }
+        if (nroots) atomicAdd(fg ? &boxes[b].nfg : &boxes[b].nbg, nroots);
+    }
+}
+
+// background components touching a face of the box flag their root: every run
+// of a row on a y or z face, the runs holding x = 0 and x = n0-1 of the others
+__global__ void k_ab_edges(const ABox *boxes, int nb, unsigned nbw, const unsigned *__restrict__ Bits, const int *L,
+                           unsigned char *edge) {
+    for (unsigned gw = blockIdx.x * blockDim.x + threadIdx.x; gw < nbw; gw += gridDim.x * blockDim.x) {
+        const ABox &B = boxes[find_item(boxes, nb, gw, &ABox::bw0)];
         const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
-        const unsigned nvb = (unsigned)n0 * (unsigned)n1 * (unsigned)n2;
-        const unsigned loc0 = (it - B.chunk0) * ch;
-        if (loc0 >= nvb) continue;
-        const unsigned loc1 = min(loc0 + ch, nvb);
-        const unsigned r0 = loc0 / (unsigned)n0, r1 = (loc1 - 1) / (unsigned)n0;   // rows (y + z n1) touched
-        const unsigned char *K = keep + B.arena;
+        const unsigned lw = gw - B.bw0, lr = lw / B.W, w = lw - lr * B.W;
+        const int z = (int)(lr / (unsigned)n1), y = (int)(lr - (unsigned)z * (unsigned)n1);
+        const unsigned c = ab_class(Bits, B, lr, w, 0u);
+        if (!c) continue;
+        const long long base = B.arena + (long long)lr * n0;
+        auto mark = [&](long long j) {
+            const int r = L[j];
+            if (!edge[r]) edge[r] = 1;
+        };
+        if (y == 0 || z == 0 || y == n1 - 1 || z == n2 - 1) {
+            const unsigned pc = w ? ab_class(Bits, B, lr, w - 1, 0u) : 0u;
+            for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) mark(base + w * 32 + __ffs(st) - 1);
+            continue;
+        }
+        if (w == 0 && (c & 1u)) mark(base);
+        if (w == B.W - 1) {
+            int b = (n0 - 1) & 31;
+            if (!((c >> b) & 1u)) continue;
+            unsigned ww = w, cc = c;
+            for (;;) {   // back to the run's start (x = 0 of a background run is one)
+                const unsigned pc = ww ? ab_class(Bits, B, lr, ww - 1, 0u) : 0u;
+                const int ls = last_start(cc & ~((cc << 1) | (pc >> 31)), (int)ww * 32, b);
+                if (ls >= 0) {
+                    mark(base + ls);
+                    break;
+                }
+                ww--;
+                b = 31;
+                cc = pc;
+            }
+        }
+    }
+}
+
+// bubbles (background components away from the box faces) become foreground,
+// when the box's background has at least two components (src/bwlabel.c:488-491)
+__global__ void __launch_bounds__(256) k_ab_fill(const ABox *boxes, int nb, unsigned nrows, unsigned *Bits, const int *L,
+                                                 const unsigned char *__restrict__ edge) {
+    const int lane = threadIdx.x & 31;
+    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
+        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
+        if (B.nbg <= 1) continue;
+        const unsigned lr = gr - B.row0;
+        const long long base = B.arena + (long long)lr * B.n[0];
+        int cst = -1;
+        unsigned cwd = 0;
+        for (unsigned c0 = 0; c0 < B.W; c0 += 32) {
+            const unsigned w = c0 + (unsigned)lane;
+            const unsigned c = w < B.W ? ab_class(Bits, B, lr, w, 0u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, lane, 32, cst, cwd);
+            unsigned fill = 0;
+            for (unsigned rem = c; rem;) {
+                const int b = __ffs(rem) - 1;
+                const unsigned pm = piece_at(rem, b);
+                rem &= ~pm;
+                if (!edge[L[base + R.start_of(b)]]) fill |= pm;
+            }
+            // every lane has read its neighbours' words (word_runs) before any write
+            if (fill) Bits[B.bw0 + lr * B.W + w] |= fill;
+        }
+    }
+}
+
+// component sizes at the roots (each run adds its length at its end)
+__global__ void __launch_bounds__(256) k_ab_sizes(const ABox *boxes, int nb, unsigned nrows,
+                                                  const unsigned *__restrict__ Bits, const int *L, unsigned *cnt) {
+    const int lane = threadIdx.x & 31;
+    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
+        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
+        const unsigned lr = gr - B.row0;
+        const long long base = B.arena + (long long)lr * B.n[0];
+        int cst = -1;
+        unsigned cwd = 0;
+        for (unsigned c0 = 0; c0 < B.W; c0 += 32) {
+            const unsigned w = c0 + (unsigned)lane;
+            const unsigned c = w < B.W ? ab_class(Bits, B, lr, w, 1u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, lane, 32, cst, cwd);
+            const unsigned dn = __shfl_down_sync(FULL, c, 1);
+            const unsigned nxt = lane < 31 ? (w + 1 < B.W ? dn : 0u) : (w + 1 < B.W ? ab_class(Bits, B, lr, w + 1, 1u) : 0u);
+            for (unsigned ends = c & ~((c >> 1) | (nxt << 31)); ends; ends &= ends - 1) {
+                const int e = __ffs(ends) - 1, st = R.start_of(e);
+                atomicAdd(&cnt[L[base + st]], (unsigned)(R.x0 + e - st + 1));
+            }
+        }
+    }
+}
+
+// largest component per box; ties go to the smallest root (first in raster order)
+__global__ void k_ab_best(ABox *boxes, int nb, unsigned nbw, const unsigned *__restrict__ Bits, const int *L,
+                          const unsigned *__restrict__ cnt) {
+    for (unsigned gw = blockIdx.x * blockDim.x + threadIdx.x; gw < nbw; gw += gridDim.x * blockDim.x) {
+        const int b = find_item(boxes, nb, gw, &ABox::bw0);
+        const ABox &B = boxes[b];
+        const unsigned lw = gw - B.bw0, lr = lw / B.W, w = lw - lr * B.W;
+        const unsigned c = ab_class(Bits, B, lr, w, 1u), pc = w ? ab_class(Bits, B, lr, w - 1, 1u) : 0u;
+        const long long base = B.arena + (long long)lr * B.n[0] + (long long)w * 32;
+        for (unsigned st = c & ~((c << 1) | (pc >> 31)); st; st &= st - 1) {
+            const int s = (int)(base + __ffs(st) - 1);
+            if (L[s] != s) continue;
+            const unsigned loc = (unsigned)(s - B.arena);
+            atomicMax(&boxes[b].best, ((unsigned long long)cnt[s] << 32) | (0xffffffffu - loc));
+        }
+    }
+}
+
+// bits of the voxels of each box's largest component
+__global__ void __launch_bounds__(256) k_ab_keep(const ABox *boxes, int nb, unsigned nrows, const unsigned *__restrict__ Bits,
+                                                 const int *L, unsigned *K) {
+    const int lane = threadIdx.x & 31;
+    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
+        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
+        const long long root = B.best ? B.arena + (long long)(0xffffffffu - (unsigned)(B.best & 0xffffffffu)) : -2;
+        const unsigned lr = gr - B.row0;
+        const long long base = B.arena + (long long)lr * B.n[0];
+        int cst = -1;
+        unsigned cwd = 0;
+        for (unsigned c0 = 0; c0 < B.W; c0 += 32) {
+            const unsigned w = c0 + (unsigned)lane;
+            const unsigned c = w < B.W ? ab_class(Bits, B, lr, w, 1u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, lane, 32, cst, cwd);
+            unsigned keep = 0;
+            for (unsigned rem = c; rem;) {
+                const int b = __ffs(rem) - 1;
+                const unsigned pm = piece_at(rem, b);
+                rem &= ~pm;
+                if ((long long)L[base + R.start_of(b)] == root) keep |= pm;
+            }
+            if (w < B.W) K[B.bw0 + lr * B.W + w] = keep;
+        }
+    }
+}
+
+// The clustered sub-box (src/meshify.c:332-342): kept voxels (K) raised to the
+// box's isolevel when FILL; with LARGEST, a voxel neither kept nor, away from
+// the volume faces, next to a kept voxel (all 26 neighbours except
+// (-1,-1,-1), src/meshify.c:252) becomes the box minimum.  A warp per row; the
+// dilation bits of 32 words at a time lane-parallel (lane l: word c0 + l).
+template <bool LARGEST, bool FILL>
+__global__ void __launch_bounds__(256) k_ab_final(const ABox *boxes, int nb, unsigned nrows, const unsigned *__restrict__ K,
+                                                  float *arena, int nx, int ny, int nz) {
+    const int lane = threadIdx.x & 31;
+    const int DY[9] = {-1, 0, 1, -1, 0, 1, 0, 1, -1}, DZ[9] = {0, 0, 0, 1, 1, 1, -1, -1, -1};
+    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
+        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
+        const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
+        const unsigned lr = gr - B.row0, W = B.W;
+        const int z = (int)(lr / (unsigned)n1), y = (int)(lr - (unsigned)z * (unsigned)n1);
+        float *row = arena + B.arena + (long long)lr * n0;
+        const unsigned *K0 = K + B.bw0;
+        if (!LARGEST) {
+            for (unsigned w = 0; w < W; w++) {
+                const unsigned kw = K0[lr * W + w];
+                const int x = (int)w * 32 + lane;
+                if (x < n0 && ((kw >> lane) & 1u)) row[x] = fmaxf(row[x], B.iso);
+            }
+            continue;
+        }
         const float vmin = ord2f(B.vmin);
-        const int nw = (n0 + 31) / 32;
-        for (unsigned r = r0 + (unsigned)warp; r <= r1; r += (unsigned)nwarp) {
-            const int y = (int)(r % (unsigned)n1), z = (int)(r / (unsigned)n1);
-            const int gy = B.o[1] + y, gz = B.o[2] + z;
-            const bool ryz = gy > 0 && gz > 0 && gy < ny - 1 && gz < nz - 1;
-            // 32 keep bits of row (y + dy, z + dz), word xw (zero outside the box)
-            auto word = [&](int dy, int dz, int xw) -> unsigned {
-                const int yy = y + dy, zz = z + dz, x = xw * 32 + lane;
-                const bool in = yy >= 0 && zz >= 0 && yy < n1 && zz < n2 && xw < nw && x < n0;
-                return __ballot_sync(0xffffffffu, in && K[((long long)zz * n1 + yy) * n0 + x] != 0);
-            };
-            // rows used: 0..2 = y-1..y+1 in slice z, 3..5 in slice z+1, 6 = (y, z-1), 7 = (y+1, z-1), 8 = (y-1, z-1)
-            const int DY[9] = {-1, 0, 1, -1, 0, 1, 0, 1, -1}, DZ[9] = {0, 0, 0, 1, 1, 1, -1, -1, -1};
-            unsigned prev[9], cur[9];
+        const int gy = B.o[1] + y, gz = B.o[2] + z;
+        const bool ryz = gy > 0 && gz > 0 && gy < ny - 1 && gz < nz - 1;
+        unsigned carry[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) carry[k] = 0u;
+        for (unsigned c0 = 0; c0 < W; c0 += 32) {
+            unsigned on = 0u, kept = 0u;
 #pragma unroll
             for (int k = 0; k < 9; k++) {
-                prev[k] = 0u;
-                cur[k] = word(DY[k], DZ[k], 0);
+                const int yy = y + DY[k], zz = z + DZ[k];
+                const bool in = yy >= 0 && zz >= 0 && yy < n1 && zz < n2;
+                const unsigned rb = in ? ((unsigned)zz * (unsigned)n1 + (unsigned)yy) * W : 0u;
+                const unsigned cur = in && c0 + lane < W ? K0[rb + c0 + lane] : 0u;
+                unsigned prv = __shfl_up_sync(FULL, cur, 1), nxt = __shfl_down_sync(FULL, cur, 1);
+                if (lane == 0) prv = carry[k];
+                if (lane == 31) nxt = in && c0 + 32 < W ? K0[rb + c0 + 32] : 0u;
+                carry[k] = __shfl_sync(FULL, cur, 31);
+                on |= cur | (cur >> 1) | (nxt << 31) | (k < 8 ? (cur << 1) | (prv >> 31) : 0u);   // row 8: no K(x-1)
+                if (k == 1) kept = cur;
             }
-            for (int xw = 0; xw < nw; xw++) {
-                unsigned on = 0u;
-#pragma unroll
-                for (int k = 0; k < 9; k++) {
-                    const unsigned nxt = word(DY[k], DZ[k], xw + 1);
-                    const unsigned right = (cur[k] >> 1) | (nxt << 31);   // K(x+1)
-                    on |= cur[k] | right | (k < 8 ? (cur[k] << 1) | (prev[k] >> 31) : 0u);   // row 8: no K(x-1)
-                    prev[k] = cur[k];
-                    cur[k] = nxt;
-                }
-                const int x = xw * 32 + lane;
-                const unsigned loc = r * (unsigned)n0 + (unsigned)x;
-                if (x < n0 && loc >= loc0 && loc < loc1) {
-                    const bool kept = (prev[1] >> lane) & 1u;   // row (y, z): prev holds word xw now
-                    const int gx = B.o[0] + x;
-                    const bool interior = ryz && gx > 0 && gx < nx - 1;
-                    if (!(kept || (interior && ((on >> lane) & 1u)))) arena[B.arena + loc] = vmin;
-                }
+            const unsigned wend = min(W, c0 + 32);
+            if (!__any_sync(FULL, on != 0u)) {   // nothing kept within reach
+                for (int x = (int)c0 * 32 + lane; x < min(n0, (int)wend * 32); x += 32) row[x] = vmin;
+                continue;
+            }
+            for (unsigned w = c0; w < wend; w++) {
+                const unsigned onw = __shfl_sync(FULL, on, (int)(w - c0)), kw = __shfl_sync(FULL, kept, (int)(w - c0));
+                const int x = (int)w * 32 + lane;
+                if (x >= n0) continue;
+                const bool kp = (kw >> lane) & 1u;
+                const int gx = B.o[0] + x;
+                const bool interior = ryz && gx > 0 && gx < nx - 1;
+                if (!(kp || (interior && ((onw >> lane) & 1u)))) row[x] = vmin;
+                else if (FILL && kp) row[x] = fmaxf(row[x], B.iso);
             }
         }
     }
@@ -898,11 +985,12 @@ struct Segment {
     int nx, ny, nz;
     unsigned *q;
     long long arena;
+    unsigned nrows, nbw;   // rows and bit words of all the boxes
 
     n2m_status ensure(AtlasWork &w) {
         if (only_largest || fill_bubbles) {
-            CKS(w.mask.ensure((size_t)arena));
-            CKS(w.keep.ensure((size_t)arena));
+            CKS(w.mask.ensure((size_t)nbw * sizeof(unsigned)));
+            if (only_largest) CKS(w.keep.ensure((size_t)nbw * sizeof(unsigned)));
             CKS(w.lab.ensure((size_t)arena * sizeof(int)));
             if (fill_bubbles) CKS(w.edge.ensure((size_t)arena));
             if (only_largest) CKS(w.ucnt.ensure((size_t)arena * sizeof(unsigned)));
@@ -917,28 +1005,34 @@ struct Segment {
         { k_a_iso<<<(nb + 127) / 128, 128, 0, s>>>(db, nb); N2M_COUNT(); }
         const unsigned g = pgrid(chunks, per_sm);
         if (only_largest || fill_bubbles) {
-            unsigned char *m = w.mask.as<unsigned char>(), *keep = w.keep.as<unsigned char>();
+            unsigned *Bm = w.mask.as<unsigned>();
             int *L = w.lab.as<int>();
-            { k_a_mask<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, ar, m); N2M_COUNT(); }
+            const unsigned rg = std::max(1u, std::min((nrows + 7) / 8, 152u * 16u));     // a warp per row
+            const unsigned wg = std::max(1u, std::min((nbw + 255) / 256, 152u * 16u));   // a thread per word
+            { k_ab_bits<<<rg, 256, 0, s>>>(db, nb, nrows, ar, Bm); N2M_COUNT(); }
             if (fill_bubbles) {
-                { k_a_uf_init<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 0, L); N2M_COUNT(); }
-                { k_a_uf_merge<3><<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 0, L); N2M_COUNT(); }
-                { k_a_uf_flatten<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, false); N2M_COUNT(); }
-                CK(cudaMemsetAsync(w.edge.p, 0, (size_t)arena, s));
-                { k_a_edge_roots<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.edge.as<unsigned char>()); N2M_COUNT(); }
-                { k_a_fill_bubbles<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.edge.as<unsigned char>(), m); N2M_COUNT(); }
+                unsigned char *edge = w.edge.as<unsigned char>();
+                { k_ab_init<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, 0u, L, edge, nullptr); N2M_COUNT(); }
+                { k_ab_merge<3><<<rg, 256, 0, s>>>(db, nb, nrows, Bm, 0u, L); N2M_COUNT(); }
+                { k_ab_flatten<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, 0u, L, false); N2M_COUNT(); }
+                { k_ab_edges<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, L, edge); N2M_COUNT(); }
+                { k_ab_fill<<<rg, 256, 0, s>>>(db, nb, nrows, Bm, L, edge); N2M_COUNT(); }
             }
-            { k_a_uf_init<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 1, L); N2M_COUNT(); }
-            { k_a_uf_merge<9><<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, m, 1, L); N2M_COUNT(); }
-            { k_a_uf_flatten<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, true); N2M_COUNT(); }
+            unsigned *cnt = only_largest ? w.ucnt.as<unsigned>() : nullptr;
+            { k_ab_init<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, 1u, L, nullptr, cnt); N2M_COUNT(); }
+            { k_ab_merge<9><<<rg, 256, 0, s>>>(db, nb, nrows, Bm, 1u, L); N2M_COUNT(); }
+            { k_ab_flatten<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, 1u, L, true); N2M_COUNT(); }
+            const unsigned *K = Bm;
             if (only_largest) {
-                CK(cudaMemsetAsync(w.ucnt.p, 0, (size_t)arena * sizeof(unsigned), s));
-                { k_a_sizes<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.ucnt.as<unsigned>()); N2M_COUNT(); }
-                { k_a_best<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, w.ucnt.as<unsigned>()); N2M_COUNT(); }
+                unsigned *Kb = w.keep.as<unsigned>();
+                { k_ab_sizes<<<rg, 256, 0, s>>>(db, nb, nrows, Bm, L, cnt); N2M_COUNT(); }
+                { k_ab_best<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, L, cnt); N2M_COUNT(); }
+                { k_ab_keep<<<rg, 256, 0, s>>>(db, nb, nrows, Bm, L, Kb); N2M_COUNT(); }
+                K = Kb;
             }
-            { k_a_keep<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, L, m, only_largest, keep); N2M_COUNT(); }
-            if (fill_bubbles) { k_a_fill<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, keep, ar); N2M_COUNT(); }
-            if (only_largest) { k_a_dilate<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, keep, ar, nx, ny, nz); N2M_COUNT(); }
+            if (only_largest && fill_bubbles) { k_ab_final<true, true><<<rg, 256, 0, s>>>(db, nb, nrows, K, ar, nx, ny, nz); N2M_COUNT(); }
+            else if (only_largest) { k_ab_final<true, false><<<rg, 256, 0, s>>>(db, nb, nrows, K, ar, nx, ny, nz); N2M_COUNT(); }
+            else { k_ab_final<false, true><<<rg, 256, 0, s>>>(db, nb, nrows, K, ar, nx, ny, nz); N2M_COUNT(); }
         }
         { k_a_stats<<<g, 256, 0, s>>>(db, nb, chunks, q + qi++, ch, ar); N2M_COUNT(); }
         { k_a_pad<<<(nb + 127) / 128, 128, 0, s>>>(db, nb); N2M_COUNT(); }
@@ -1009,6 +1103,7 @@ n2m_status atlas_batched(const short *d_lab, const int dim[3], const n2m_options
     std::vector<ABox> boxes;
     long long arena = 0;
     unsigned tiles = 0;
+    unsigned long long rows = 0, bwords = 0;
     for (int l = 1; l <= maxlab; l++) {
         if (!cnt[l]) continue;
         ABox B;
@@ -1028,6 +1123,11 @@ n2m_status atlas_batched(const short *d_lab, const int dim[3], const n2m_options
         tiles += (unsigned)(((B.n[0] + smooth::STX - 1) / smooth::STX) * ((B.n[1] + smooth::STY - 1) / smooth::STY) *
                             ((B.n[2] + smooth::SZC - 1) / smooth::SZC));
         B.chunk0 = 0;   // set per chunk size below
+        B.W = (unsigned)(B.n[0] + 31) / 32;
+        B.row0 = rows;
+        B.bw0 = bwords;
+        rows += (unsigned long long)B.n[1] * B.n[2];
+        bwords += (unsigned long long)B.W * B.n[1] * B.n[2];
         B.vmin = INT_MAX;
         B.vmax = INT_MIN;
         for (int a = 0; a < 3; a++) { B.blo[a] = INT_MAX; B.bhi[a] = INT_MIN; }
@@ -1047,7 +1147,8 @@ n2m_status atlas_batched(const short *d_lab, const int dim[3], const n2m_options
     CK(cudaMemsetAsync(q, 0, 96 * sizeof(unsigned), s));
     float *ar = w.arena.as<float>();
     const bool smooth_on = o.pre_smooth && dim[0] >= 5 && dim[1] >= 5 && dim[2] >= 5;
-    Segment seg{v, db, nb, tiles, ar, smooth_on, o.only_largest, o.fill_bubbles, dim[0], dim[1], dim[2], q, arena};
+    Segment seg{v, db, nb, tiles, ar, smooth_on, o.only_largest, o.fill_bubbles, dim[0], dim[1], dim[2], q, arena,
+                (unsigned)rows, (unsigned)bwords};
     CKS(seg.ensure(w));
     // pick chunk size and persistent-grid width once per context (autotuner)
     if (!w.tuned) {

@@ -22,12 +22,13 @@
 #include <algorithm>
 
 #include "n2m_internal.cuh"
+#include "runs.cuh"
 #include "smooth_core.cuh"
 #include "uf.cuh"
 
 namespace {
 using namespace uf;
-constexpr unsigned FULL = 0xffffffffu;
+using namespace runs;
 
 struct LD {
     int nx, ny, nz;
@@ -49,58 +50,12 @@ __device__ __forceinline__ unsigned class_word(const unsigned *B, const LD &d, u
     return want ? b : ~b & valid_bits(d, w);
 }
 
-// x of the highest run start at or below bit b, or -1
-__device__ __forceinline__ int last_start(unsigned starts, int x0, int b) {
-    const unsigned hs = starts & (b == 31 ? FULL : (2u << b) - 1u);
-    return hs ? x0 + 31 - __clz(hs) : -1;
-}
-
-// one lane's word of a row in a row kernel: class bits, the class word before
-// it, run starts, and cs = start (x) of the run holding the voxel before the word
-struct WordRuns {
-    unsigned c, pc, starts;
-    int x0, cs;
-    __device__ __forceinline__ int start_of(int b) const {   // run of bit b (set in c)
-        const int s = last_start(starts, x0, b);
-        return s >= 0 ? s : cs;
-    }
-};
-
-// carry_start / carry_word: the row's last run start and last class word of
-// the chunks before this one (-1 / 0 before the first); all lanes call it
-__device__ __forceinline__ WordRuns word_runs(unsigned c, int x0, int li, int seg, int &carry_start,
-                                              unsigned &carry_word) {
-    WordRuns r;
-    r.c = c;
-    r.x0 = x0;
-    const unsigned up = __shfl_up_sync(FULL, c, 1, seg);
-    r.pc = li == 0 ? carry_word : up;
-    r.starts = c & ~((c << 1) | (r.pc >> 31));
-    int incl = r.starts ? x0 + 31 - __clz(r.starts) : -1;
-    for (int d = 1; d < seg; d <<= 1) {
-        const int t = __shfl_up_sync(FULL, incl, d, seg);
-        if (li >= d) incl = max(incl, t);
-    }
-    const int excl = __shfl_up_sync(FULL, incl, 1, seg);
-    r.cs = max(carry_start, li == 0 ? -1 : excl);
-    carry_start = max(carry_start, __shfl_sync(FULL, incl, seg - 1, seg));
-    carry_word = __shfl_sync(FULL, c, seg - 1, seg);
-    return r;
-}
-
 // the class word after this lane's word (0 past the row); all lanes call it
 __device__ __forceinline__ unsigned next_word(const unsigned *B, const LD &d, unsigned c, bool rowok, unsigned r,
                                               unsigned w, int li, int seg, unsigned want) {
     const unsigned dn = __shfl_down_sync(FULL, c, 1, seg);
     if (li < seg - 1) return w + 1 < d.W ? dn : 0u;
     return rowok && w + 1 < d.W ? class_word(B, d, r, w + 1, want) : 0u;
-}
-
-// bits (x mask) of the piece of a run that starts at bit b of class word rem
-__device__ __forceinline__ unsigned piece_at(unsigned rem, int b) {
-    const unsigned ones = ~(rem >> b);
-    const int len = ones ? __ffs(ones) - 1 : 32 - b;
-    return (len == 32 ? FULL : (1u << len) - 1u) << b;
 }
 
 // Class bits of the volume: value >= iso (meshify's mask), or value != 0
