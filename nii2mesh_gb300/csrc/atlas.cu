@@ -285,33 +285,40 @@ __global__ void k_ab_init(const ABox *boxes, int nb, unsigned nbw, const unsigne
 // union of touching runs with the rows before them in the box (rows (y-1, z),
 // (y, z-1), and for 18-connectivity x offsets -1..1 and rows (y-1, z-1),
 // (y+1, z-1)); a contact counts where the voxels before it do not also touch
+// A row kernel's rows: AB_SEG lanes per row (one word per lane, wider rows in
+// chunks), 32 / AB_SEG rows per warp, each with its own box
+constexpr int AB_SEG = 4;
+
 template <int NNB>
 __global__ void __launch_bounds__(256) k_ab_merge(const ABox *boxes, int nb, unsigned nrows,
                                                   const unsigned *__restrict__ Bits, unsigned want, int *L) {
     static_assert(NNB == 3 || NNB == 9, "6- or 18-connectivity");
     constexpr int NR = NNB == 3 ? 3 : 5;
     const int RY[5] = {0, -1, 0, -1, 1}, RZ[5] = {0, 0, -1, -1, -1};
-    const int lane = threadIdx.x & 31;
-    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
-        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
-        if (skip_box(B)) continue;
+    const int lane = threadIdx.x & 31, li = lane & (AB_SEG - 1);
+    const unsigned rpw = 32u / AB_SEG, rsub = (unsigned)lane / AB_SEG, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < nrows; rb += nwarps * rpw) {
+        const unsigned gr = rb + rsub;
+        const ABox &B = boxes[gr < nrows ? find_item(boxes, nb, gr, &ABox::row0) : 0];
+        const bool rowok = gr < nrows && !skip_box(B);
         const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
-        const unsigned lr = gr - B.row0, W = B.W;
+        const unsigned lr = rowok ? gr - B.row0 : 0u, W = rowok ? B.W : 0u;
         const int z = (int)(lr / (unsigned)n1), y = (int)(lr - (unsigned)z * (unsigned)n1);
         bool kok[NR];
         unsigned rk[NR];
 #pragma unroll
         for (int k = 0; k < NR; k++) {
             const int yy = y + RY[k], zz = z + RZ[k];
-            kok[k] = yy >= 0 && zz >= 0 && yy < n1 && zz < n2;
+            kok[k] = rowok && yy >= 0 && zz >= 0 && yy < n1 && zz < n2;
             rk[k] = kok[k] ? (unsigned)zz * (unsigned)n1 + (unsigned)yy : 0u;
         }
         int cst[NR];
         unsigned cwd[NR];
 #pragma unroll
         for (int k = 0; k < NR; k++) { cst[k] = -1; cwd[k] = 0u; }
-        for (unsigned c0 = 0; c0 < W; c0 += 32) {
-            const unsigned w = c0 + (unsigned)lane;
+        const unsigned wmax = __reduce_max_sync(FULL, W);
+        for (unsigned c0 = 0; c0 < wmax; c0 += AB_SEG) {
+            const unsigned w = c0 + (unsigned)li;
             const bool ok = w < W;
             const int x0 = (int)w * 32;
             WordRuns R[NR];
@@ -319,9 +326,10 @@ __global__ void __launch_bounds__(256) k_ab_merge(const ABox *boxes, int nb, uns
 #pragma unroll
             for (int k = 0; k < NR; k++) {
                 const unsigned c = ok && kok[k] ? ab_class(Bits, B, rk[k], w, want) : 0u;
-                R[k] = word_runs(c, x0, lane, 32, cst[k], cwd[k]);
-                const unsigned dn = __shfl_down_sync(FULL, c, 1);
-                nk[k] = lane < 31 ? (w + 1 < W ? dn : 0u) : (kok[k] && w + 1 < W ? ab_class(Bits, B, rk[k], w + 1, want) : 0u);
+                R[k] = word_runs(c, x0, li, AB_SEG, cst[k], cwd[k]);
+                const unsigned dn = __shfl_down_sync(FULL, c, 1, AB_SEG);
+                nk[k] = li < AB_SEG - 1 ? (w + 1 < W ? dn : 0u)
+                                        : (kok[k] && w + 1 < W ? ab_class(Bits, B, rk[k], w + 1, want) : 0u);
             }
             const unsigned F = R[0].c;
             if (!F) continue;
@@ -419,18 +427,21 @@ __global__ void k_ab_edges(const ABox *boxes, int nb, unsigned nbw, const unsign
 // when the box's background has at least two components (src/bwlabel.c:488-491)
 __global__ void __launch_bounds__(256) k_ab_fill(const ABox *boxes, int nb, unsigned nrows, unsigned *Bits, const int *L,
                                                  const unsigned char *__restrict__ edge) {
-    const int lane = threadIdx.x & 31;
-    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
-        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
-        if (B.nbg <= 1) continue;
-        const unsigned lr = gr - B.row0;
+    const int lane = threadIdx.x & 31, li = lane & (AB_SEG - 1);
+    const unsigned rpw = 32u / AB_SEG, rsub = (unsigned)lane / AB_SEG, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < nrows; rb += nwarps * rpw) {
+        const unsigned gr = rb + rsub;
+        const ABox &B = boxes[gr < nrows ? find_item(boxes, nb, gr, &ABox::row0) : 0];
+        const bool rowok = gr < nrows && B.nbg > 1;
+        const unsigned lr = rowok ? gr - B.row0 : 0u, W = rowok ? B.W : 0u;
         const long long base = B.arena + (long long)lr * B.n[0];
         int cst = -1;
         unsigned cwd = 0;
-        for (unsigned c0 = 0; c0 < B.W; c0 += 32) {
-            const unsigned w = c0 + (unsigned)lane;
-            const unsigned c = w < B.W ? ab_class(Bits, B, lr, w, 0u) : 0u;
-            const WordRuns R = word_runs(c, (int)w * 32, lane, 32, cst, cwd);
+        const unsigned wmax = __reduce_max_sync(FULL, W);
+        for (unsigned c0 = 0; c0 < wmax; c0 += AB_SEG) {
+            const unsigned w = c0 + (unsigned)li;
+            const unsigned c = w < W ? ab_class(Bits, B, lr, w, 0u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, li, AB_SEG, cst, cwd);
             unsigned fill = 0;
             for (unsigned rem = c; rem;) {
                 const int b = __ffs(rem) - 1;
@@ -447,19 +458,23 @@ __global__ void __launch_bounds__(256) k_ab_fill(const ABox *boxes, int nb, unsi
 // component sizes at the roots (each run adds its length at its end)
 __global__ void __launch_bounds__(256) k_ab_sizes(const ABox *boxes, int nb, unsigned nrows,
                                                   const unsigned *__restrict__ Bits, const int *L, unsigned *cnt) {
-    const int lane = threadIdx.x & 31;
-    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
-        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
-        const unsigned lr = gr - B.row0;
+    const int lane = threadIdx.x & 31, li = lane & (AB_SEG - 1);
+    const unsigned rpw = 32u / AB_SEG, rsub = (unsigned)lane / AB_SEG, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < nrows; rb += nwarps * rpw) {
+        const unsigned gr = rb + rsub;
+        const ABox &B = boxes[gr < nrows ? find_item(boxes, nb, gr, &ABox::row0) : 0];
+        const bool rowok = gr < nrows;
+        const unsigned lr = rowok ? gr - B.row0 : 0u, W = rowok ? B.W : 0u;
         const long long base = B.arena + (long long)lr * B.n[0];
         int cst = -1;
         unsigned cwd = 0;
-        for (unsigned c0 = 0; c0 < B.W; c0 += 32) {
-            const unsigned w = c0 + (unsigned)lane;
-            const unsigned c = w < B.W ? ab_class(Bits, B, lr, w, 1u) : 0u;
-            const WordRuns R = word_runs(c, (int)w * 32, lane, 32, cst, cwd);
-            const unsigned dn = __shfl_down_sync(FULL, c, 1);
-            const unsigned nxt = lane < 31 ? (w + 1 < B.W ? dn : 0u) : (w + 1 < B.W ? ab_class(Bits, B, lr, w + 1, 1u) : 0u);
+        const unsigned wmax = __reduce_max_sync(FULL, W);
+        for (unsigned c0 = 0; c0 < wmax; c0 += AB_SEG) {
+            const unsigned w = c0 + (unsigned)li;
+            const unsigned c = w < W ? ab_class(Bits, B, lr, w, 1u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, li, AB_SEG, cst, cwd);
+            const unsigned dn = __shfl_down_sync(FULL, c, 1, AB_SEG);
+            const unsigned nxt = li < AB_SEG - 1 ? (w + 1 < W ? dn : 0u) : (w + 1 < W ? ab_class(Bits, B, lr, w + 1, 1u) : 0u);
             for (unsigned ends = c & ~((c >> 1) | (nxt << 31)); ends; ends &= ends - 1) {
                 const int e = __ffs(ends) - 1, st = R.start_of(e);
                 atomicAdd(&cnt[L[base + st]], (unsigned)(R.x0 + e - st + 1));
@@ -489,18 +504,22 @@ __global__ void k_ab_best(ABox *boxes, int nb, unsigned nbw, const unsigned *__r
 // bits of the voxels of each box's largest component
 __global__ void __launch_bounds__(256) k_ab_keep(const ABox *boxes, int nb, unsigned nrows, const unsigned *__restrict__ Bits,
                                                  const int *L, unsigned *K) {
-    const int lane = threadIdx.x & 31;
-    for (unsigned gr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nrows; gr += (gridDim.x * blockDim.x) >> 5) {
-        const ABox &B = boxes[find_item(boxes, nb, gr, &ABox::row0)];
+    const int lane = threadIdx.x & 31, li = lane & (AB_SEG - 1);
+    const unsigned rpw = 32u / AB_SEG, rsub = (unsigned)lane / AB_SEG, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned rb = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rpw; rb < nrows; rb += nwarps * rpw) {
+        const unsigned gr = rb + rsub;
+        const ABox &B = boxes[gr < nrows ? find_item(boxes, nb, gr, &ABox::row0) : 0];
+        const bool rowok = gr < nrows;
         const long long root = B.best ? B.arena + (long long)(0xffffffffu - (unsigned)(B.best & 0xffffffffu)) : -2;
-        const unsigned lr = gr - B.row0;
+        const unsigned lr = rowok ? gr - B.row0 : 0u, W = rowok ? B.W : 0u;
         const long long base = B.arena + (long long)lr * B.n[0];
         int cst = -1;
         unsigned cwd = 0;
-        for (unsigned c0 = 0; c0 < B.W; c0 += 32) {
-            const unsigned w = c0 + (unsigned)lane;
-            const unsigned c = w < B.W ? ab_class(Bits, B, lr, w, 1u) : 0u;
-            const WordRuns R = word_runs(c, (int)w * 32, lane, 32, cst, cwd);
+        const unsigned wmax = __reduce_max_sync(FULL, W);
+        for (unsigned c0 = 0; c0 < wmax; c0 += AB_SEG) {
+            const unsigned w = c0 + (unsigned)li;
+            const unsigned c = w < W ? ab_class(Bits, B, lr, w, 1u) : 0u;
+            const WordRuns R = word_runs(c, (int)w * 32, li, AB_SEG, cst, cwd);
             unsigned keep = 0;
             for (unsigned rem = c; rem;) {
                 const int b = __ffs(rem) - 1;
@@ -508,7 +527,7 @@ __global__ void __launch_bounds__(256) k_ab_keep(const ABox *boxes, int nb, unsi
                 rem &= ~pm;
                 if ((long long)L[base + R.start_of(b)] == root) keep |= pm;
             }
-            if (w < B.W) K[B.bw0 + lr * B.W + w] = keep;
+            if (w < W) K[B.bw0 + lr * B.W + w] = keep;
         }
     }
 }
@@ -1008,26 +1027,27 @@ struct Segment {
             unsigned *Bm = w.mask.as<unsigned>();
             int *L = w.lab.as<int>();
             const unsigned rg = std::max(1u, std::min((nrows + 7) / 8, 152u * 16u));     // a warp per row
+            const unsigned sg = std::max(1u, std::min((nrows * AB_SEG / 32 + 8) / 8, 152u * 16u));   // AB_SEG lanes per row
             const unsigned wg = std::max(1u, std::min((nbw + 255) / 256, 152u * 16u));   // a thread per word
             { k_ab_bits<<<rg, 256, 0, s>>>(db, nb, nrows, ar, Bm); N2M_COUNT(); }
             if (fill_bubbles) {
                 unsigned char *edge = w.edge.as<unsigned char>();
                 { k_ab_init<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, 0u, L, edge, nullptr); N2M_COUNT(); }
-                { k_ab_merge<3><<<rg, 256, 0, s>>>(db, nb, nrows, Bm, 0u, L); N2M_COUNT(); }
+                { k_ab_merge<3><<<sg, 256, 0, s>>>(db, nb, nrows, Bm, 0u, L); N2M_COUNT(); }
                 { k_ab_flatten<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, 0u, L, false); N2M_COUNT(); }
                 { k_ab_edges<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, L, edge); N2M_COUNT(); }
-                { k_ab_fill<<<rg, 256, 0, s>>>(db, nb, nrows, Bm, L, edge); N2M_COUNT(); }
+                { k_ab_fill<<<sg, 256, 0, s>>>(db, nb, nrows, Bm, L, edge); N2M_COUNT(); }
             }
             unsigned *cnt = only_largest ? w.ucnt.as<unsigned>() : nullptr;
             { k_ab_init<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, 1u, L, nullptr, cnt); N2M_COUNT(); }
-            { k_ab_merge<9><<<rg, 256, 0, s>>>(db, nb, nrows, Bm, 1u, L); N2M_COUNT(); }
+            { k_ab_merge<9><<<sg, 256, 0, s>>>(db, nb, nrows, Bm, 1u, L); N2M_COUNT(); }
             { k_ab_flatten<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, 1u, L, true); N2M_COUNT(); }
             const unsigned *K = Bm;
             if (only_largest) {
                 unsigned *Kb = w.keep.as<unsigned>();
-                { k_ab_sizes<<<rg, 256, 0, s>>>(db, nb, nrows, Bm, L, cnt); N2M_COUNT(); }
+                { k_ab_sizes<<<sg, 256, 0, s>>>(db, nb, nrows, Bm, L, cnt); N2M_COUNT(); }
                 { k_ab_best<<<wg, 256, 0, s>>>(db, nb, nbw, Bm, L, cnt); N2M_COUNT(); }
-                { k_ab_keep<<<rg, 256, 0, s>>>(db, nb, nrows, Bm, L, Kb); N2M_COUNT(); }
+                { k_ab_keep<<<sg, 256, 0, s>>>(db, nb, nrows, Bm, L, Kb); N2M_COUNT(); }
                 K = Kb;
             }
             if (only_largest && fill_bubbles) { k_ab_final<true, true><<<rg, 256, 0, s>>>(db, nb, nrows, K, ar, nx, ny, nz); N2M_COUNT(); }
