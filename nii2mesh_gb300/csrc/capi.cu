@@ -490,14 +490,19 @@ n2m_status weld_candidates(n2m_context *c, int nv, int ncand, std::vector<int> &
 n2m_status weld_oc(n2m_context *c, const Prep &P, const int dim[3], int nv, int nt, int ncand, std::vector<int> &removed,
                    std::vector<int> &keep, std::vector<int> &ov_id, std::vector<vec3d> &ov_pos, std::vector<int> &ov_src,
                    std::vector<int2> &corners) {
-    const unsigned cap = (unsigned)std::min<long long>(32LL * ncand + 1024, 3LL * nt);
     CKS(c->lubits.ensure(((size_t)nv + 31) / 32 * sizeof(unsigned)));
-    CKS(c->ocq.ensure(((size_t)cap + 2) * sizeof(unsigned)));
-    unsigned *dq = c->ocq.as<unsigned>(), *dcount = dq + cap + 1;
-    CKS(oc_copies(c->tris_raw.as<vec3i>(), nt, nv, c->cand.as<int>(), ncand, c->lubits.as<unsigned>(), dq, dcount, cap,
-                  c->stream));
-    unsigned ncopy = 0;
-    CKS(readback(c, &ncopy, dcount));
+    unsigned cap = (unsigned)std::min<long long>(32LL * ncand + 1024, 3LL * nt), ncopy = 0;
+    unsigned *dq = nullptr, *dcount = nullptr;
+    for (int pass = 0; pass < 2; pass++) {   // a second pass with room for every copy the first one counted
+        CKS(c->ocq.ensure(((size_t)cap + 2) * sizeof(unsigned)));
+        dq = c->ocq.as<unsigned>();
+        dcount = dq + cap + 1;
+        CKS(oc_copies(c->tris_raw.as<vec3i>(), nt, nv, c->cand.as<int>(), ncand, c->lubits.as<unsigned>(), dq, dcount,
+                      cap, c->stream));
+        CKS(readback(c, &ncopy, dcount));
+        if (ncopy <= cap) break;
+        cap = ncopy;
+    }
     if (ncopy > cap) {
         n2m_set_error("weld copy overflow (%u > %u)", ncopy, cap);
         return N2M_ERR_INTERNAL;
